@@ -1,0 +1,191 @@
+/*
+ * schnelgpu.h -- C ABI of the GB300 (sm_103a) streaming LFMM2 engine.
+ *
+ * Drop-in boundary for the hot path of schnelLFMM v0.3.2.  Every entry point
+ * takes plain pointers and sizes, returns an int status (0 = OK, negative =
+ * error) and leaves a human-readable message in slfmm_last_error().  There is
+ * no CPU fallback: when no sm_103a device is present the calls fail with
+ * SLFMM_ERR_CUDA.
+ *
+ * Layout conventions (all host arrays):
+ *   - packed genotypes: the .bed payload AFTER the 3-byte magic, SNP-major,
+ *     ceil(n_physical/4) bytes per SNP (src/bed.rs:137-145);
+ *   - dense matrices are row-major: X is n x d, U_hat is n x K, per-SNP
+ *     outputs are p x d (SNP-major rows);
+ *   - index arrays are uint64_t.
+ *
+ * Threading: a context is bound to one device and one CUDA stream and is not
+ * thread-safe; use one context per host thread.  Calls are blocking (results
+ * are in host memory when the call returns) unless documented otherwise.
+ */
+#ifndef SCHNELGPU_H
+#define SCHNELGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define SLFMM_OK                  0
+#define SLFMM_ERR_BAD_ARG        -1   /* invalid argument / shape            */
+#define SLFMM_ERR_BAD_BED        -2   /* magic or size mismatch, parse error */
+#define SLFMM_ERR_SINGULAR       -3   /* inversion failed even regularised   */
+#define SLFMM_ERR_DF_NONPOSITIVE -4   /* n <= 1 + d + K                      */
+#define SLFMM_ERR_CUDA           -5   /* CUDA runtime / launch failure       */
+#define SLFMM_ERR_DEVICE_TIMEOUT -6   /* a bounded device wait expired       */
+#define SLFMM_ERR_IO             -7   /* file open/read/write failure        */
+#define SLFMM_ERR_NOMEM          -8   /* device or host allocation failed    */
+
+/* ---- enums ------------------------------------------------------------- */
+#define SLFMM_NORM_CENTER_ONLY 0      /* SnpNorm::CenterOnly (src/bed.rs:19-26) */
+#define SLFMM_NORM_EIGENSTRAT  1      /* SnpNorm::Eigenstrat                     */
+
+#define SLFMM_PREC_FP32        0      /* plain FP32 SIMT contractions            */
+#define SLFMM_PREC_SPLIT_BF16  1      /* tcgen05 tensor cores, exact BF16
+                                         genotypes x hi+lo BF16 operand          */
+
+#define SLFMM_IMPUTE_MEAN      0      /* ImputeStrategy::Mean (src/lib.rs:39-44) */
+#define SLFMM_IMPUTE_NMF       1      /* ImputeStrategy::Nmf                     */
+
+#define SLFMM_SUBSET_ALL       0      /* SubsetSpec::All     (src/bed.rs:50-57)  */
+#define SLFMM_SUBSET_RATE      1      /* SubsetSpec::Rate(r)                     */
+#define SLFMM_SUBSET_INDICES   2      /* SubsetSpec::Indices(v)                  */
+
+typedef struct slfmm_ctx  slfmm_ctx;   /* one per device+stream              */
+typedef struct slfmm_geno slfmm_geno;  /* device-resident packed genotypes   */
+
+typedef struct {
+    int   precision;   /* SLFMM_PREC_*                                     */
+    int   verbose;     /* progress/diagnostics on stderr                   */
+    void* stream;      /* optional cudaStream_t to run on (NULL = own)     */
+} slfmm_opts;
+
+typedef struct {
+    int             kind;      /* SLFMM_SUBSET_*                      */
+    double          rate;      /* for RATE: step = ceil(1/rate)       */
+    const uint64_t* indices;   /* for INDICES                         */
+    uint64_t        n_indices;
+} slfmm_subset;
+
+/* Mirrors Lfmm2Config (src/lib.rs:47-98) and NmfConfig (src/nmf.rs:15-50). */
+typedef struct {
+    uint32_t k;             /* latent factors K                           */
+    double   lambda;        /* ridge penalty, must be > 0                 */
+    uint32_t chunk_size;    /* SNPs per streaming chunk (CV streams)      */
+    uint32_t oversampling;  /* RSVD oversampling (l = K + oversampling)   */
+    uint32_t n_power_iter;  /* RSVD power iterations q                    */
+    uint64_t seed;          /* RNG seed                                   */
+    int      norm;          /* SLFMM_NORM_*                               */
+    int      scale_cov;     /* divide covariates by sd after centring     */
+    int      impute;        /* SLFMM_IMPUTE_*                             */
+    uint32_t nmf_k;         /* NMF rank (0 = K)                           */
+    uint32_t nmf_iter;      /* multiplicative-update iterations           */
+    double   nmf_eps;       /* denominator/clamp epsilon (1e-16)          */
+    double   nmf_cv_rate;   /* CV hold-out rate                           */
+} slfmm_config;
+
+/* Mirrors TestResults (src/testing.rs:76-93) plus the per-SNP columns the
+ * reference writes to <out>.tsv.  All arrays are CALLER-allocated; a NULL
+ * pointer skips that output. */
+typedef struct {
+    double*  u_hat;          /* n x K                                       */
+    double*  beta;           /* p x d  ridge effect sizes                   */
+    double*  tstat;          /* p x d                                       */
+    double*  pvalue;         /* p x d  GIF-calibrated                       */
+    double*  r2;             /* p x 3  r2_cov, r2_latent, r2_resid          */
+    double*  gif_per_trait;  /* d      clamped >= 1, used for calibration   */
+    double   gif;            /* mean of the unclamped per-trait GIFs        */
+    double*  nmf_cv;         /* nmf_iter per-iteration CV MAE (NMF only)    */
+    double   nmf_cv_mean;    /* mean-imputation CV MAE on the last mask     */
+    double   nmf_gwas_cv_mae;
+    double   nmf_gwas_cv_mean_mae;
+    uint64_t nmf_gwas_cv_count;
+} slfmm_results;
+
+/* ---- context ------------------------------------------------------------ */
+/* Replaces the thread pool set-up of parallel_stream (src/parallel.rs:156-199)
+ * and openblas_set_num_threads (src/lib.rs:23-35). */
+int         slfmm_create(int device, const slfmm_opts* opts, slfmm_ctx** out);
+void        slfmm_destroy(slfmm_ctx* ctx);
+const char* slfmm_last_error(const slfmm_ctx* ctx);
+/* Number of kernels this context launched since creation. */
+uint64_t    slfmm_launch_count(const slfmm_ctx* ctx);
+/* Opaque cudaStream_t the context runs on. */
+void*       slfmm_stream(const slfmm_ctx* ctx);
+
+/* ---- .bed ingest --------------------------------------------------------- */
+/* BedFile::open validation (src/bed.rs:78-135): magic 6C 1B 01 and size
+ * 3 + ceil(n/4)*p.  Reads the payload into a caller buffer of
+ * ceil(n/4)*p bytes (pass NULL to only validate). */
+int slfmm_bed_validate(const char* bed_path, uint64_t n_samples, uint64_t n_snps,
+                       uint8_t* payload_out, char* err, size_t err_len);
+
+/* Upload a packed payload to the device (pinned ring, double-buffered H2D),
+ * applying the sample subset (BedFile::subset_samples, src/bed.rs:155-159)
+ * and the SNP subset (subset_indices, src/parallel.rs:113-122; copy_raw_chunk
+ * :129-146).  Builds the per-SNP allele counts and missing-call lists once;
+ * every later pass reads the resident copy. */
+int slfmm_geno_upload(slfmm_ctx* ctx, const uint8_t* packed, uint64_t n_physical,
+                      uint64_t n_snps, const uint64_t* sample_keep, uint64_t n_keep,
+                      const slfmm_subset* snps, slfmm_geno** out);
+int slfmm_geno_free(slfmm_ctx* ctx, slfmm_geno* g);
+uint64_t slfmm_geno_n_samples(const slfmm_geno* g);
+uint64_t slfmm_geno_n_snps(const slfmm_geno* g);
+
+/* ---- parity hooks for stage (a) ----------------------------------------- */
+/* Per-SNP allele counts c0,c1,c2,cmiss (int32, p x 4), mean over observed
+ * calls, scale (src/bed.rs:382-395) and TSS of the standardised column.
+ * counts/mean/scale are bit-exact with decode_single_snp
+ * (src/bed.rs:300-379).  Any output may be NULL. */
+int slfmm_decode_stats(slfmm_ctx* ctx, const slfmm_geno* g, int norm,
+                       int32_t* counts4, double* mean, double* scale, double* tss);
+/* Standardised decode of SNPs [snp0, snp0+ncols) into out (n x ncols,
+ * row-major), mean imputation: decode_bed_chunk_into (src/bed.rs:211-235). */
+int slfmm_decode_chunk(slfmm_ctx* ctx, const slfmm_geno* g, uint64_t snp0,
+                       uint64_t ncols, int norm, double* out);
+
+/* ---- library API (src/lib.rs) ------------------------------------------- */
+/* center_covariates (src/lib.rs:102-117). x, out: n x d row-major. */
+int slfmm_center_covariates(slfmm_ctx* ctx, const double* x, uint64_t n, uint32_t d,
+                            int scale, double* out);
+/* Random sketch Omega (n x l) the engine uses for a given seed. */
+int slfmm_generate_omega(slfmm_ctx* ctx, uint64_t seed, uint64_t n, uint32_t l,
+                         double* out);
+/* estimate_factors (src/lib.rs:127-136): Step 0 + RSVD of M Y_est.
+ * omega: n x (K+oversampling) or NULL (engine RNG).  u_hat: n x K. */
+int slfmm_estimate_factors(slfmm_ctx* ctx, const slfmm_geno* y_est, const double* x,
+                           uint32_t d, const slfmm_config* cfg, const double* omega,
+                           double* u_hat);
+/* test_associations (src/lib.rs:144-154) with a given U_hat (n x K). */
+int slfmm_test_associations(slfmm_ctx* ctx, const slfmm_geno* y_full, const double* x,
+                            uint32_t d, const double* u_hat, const slfmm_config* cfg,
+                            slfmm_results* res);
+/* fit_lfmm2 (src/lib.rs:162-263) on resident genotypes. */
+int slfmm_fit(slfmm_ctx* ctx, const slfmm_geno* y_est, const slfmm_geno* y_full,
+              const double* x, uint32_t d, const slfmm_config* cfg, const double* omega,
+              slfmm_results* res);
+/* fit_lfmm2 from HOST buffers: uploads (H2D inside), fits, copies results
+ * back, frees the device copy.  est == NULL or kind ALL uses y_full. */
+int slfmm_fit_host(slfmm_ctx* ctx, const uint8_t* packed, uint64_t n_physical,
+                   uint64_t n_snps, const uint64_t* sample_keep, uint64_t n_keep,
+                   const slfmm_subset* est, const double* x, uint32_t d,
+                   const slfmm_config* cfg, const double* omega, slfmm_results* res);
+
+/* ---- output (src/testing.rs:740-801) ------------------------------------ */
+/* Write <out>.tsv: header chr pos snp_id {p_,beta_,t_}xcov r2_cov r2_latent
+ * r2_resid, numbers in Rust "{:.6e}" form.  chrom/snp_id are arrays of p
+ * C strings, cov_names d C strings.  Formatting runs on n_threads host
+ * threads (0 = all). */
+int slfmm_write_tsv(const char* path, uint64_t p, uint32_t d, const char* const* chrom,
+                    const uint64_t* pos, const char* const* snp_id,
+                    const char* const* cov_names, const slfmm_results* res, int n_threads);
+/* Format one value like Rust "{:.6e}"; returns the length written. */
+int slfmm_format_exp6(double v, char* buf, size_t buf_len);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SCHNELGPU_H */

@@ -1,0 +1,607 @@
+"""schnellfmm_gb300 -- GB300-native streaming LFMM2 (host mirror of schnelLFMM).
+
+The compute runs in ``libschnelgpu.so`` (sm_103a CUDA kernels behind the C
+ABI declared in ``include/schnelgpu.h``).  This module is a thin ctypes host
+layer that mirrors the reference crate's library surface:
+
+=============================  ============================================
+reference (src/lib.rs, ...)    here
+=============================  ============================================
+``BedFile::open``              :meth:`BedFile.open`  (src/bed.rs:78-135)
+``BedFile::subset_samples``    :meth:`BedFile.subset_samples` (:155-159)
+``SubsetSpec``                 :class:`SubsetSpec`   (src/bed.rs:50-57)
+``SnpNorm``                    :class:`SnpNorm`      (src/bed.rs:19-26)
+``Lfmm2Config`` / ``NmfConfig``:class:`Lfmm2Config` / :class:`NmfConfig`
+``center_covariates``          :func:`center_covariates` (src/lib.rs:102-117)
+``estimate_factors``           :func:`estimate_factors`  (src/lib.rs:127-136)
+``test_associations``          :func:`test_associations` (src/lib.rs:144-154)
+``fit_lfmm2``                  :func:`fit_lfmm2`         (src/lib.rs:162-263)
+``TestResults``                :class:`TestResults`  (src/testing.rs:76-93)
+=============================  ============================================
+
+There is no CPU fallback: without the built library or an sm_103a device
+every call raises :class:`SchnelGpuError`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import enum
+import math
+import os
+from dataclasses import dataclass, field
+from pathlib import Path
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "libschnelgpu.so"
+
+OK = 0
+ERR_BAD_ARG = -1
+ERR_BAD_BED = -2
+ERR_SINGULAR = -3
+ERR_DF_NONPOSITIVE = -4
+ERR_CUDA = -5
+ERR_DEVICE_TIMEOUT = -6
+ERR_IO = -7
+ERR_NOMEM = -8
+
+
+class SchnelGpuError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(message)
+        self.code = code
+
+
+class SnpNorm(enum.IntEnum):
+    CENTER_ONLY = 0   # library default (src/bed.rs:22-23)
+    EIGENSTRAT = 1    # CLI default (src/main.rs:79-80)
+
+
+class ImputeStrategy(enum.IntEnum):
+    MEAN = 0
+    NMF = 1
+
+
+class Precision(enum.IntEnum):
+    FP32 = 0
+    SPLIT_BF16 = 1
+
+
+# ---------------------------------------------------------------------------
+# ctypes declarations (must match include/schnelgpu.h)
+# ---------------------------------------------------------------------------
+class _Opts(C.Structure):
+    _fields_ = [("precision", C.c_int), ("verbose", C.c_int), ("stream", C.c_void_p)]
+
+
+class _Subset(C.Structure):
+    _fields_ = [("kind", C.c_int), ("rate", C.c_double), ("indices", C.POINTER(C.c_uint64)),
+                ("n_indices", C.c_uint64)]
+
+
+class _Config(C.Structure):
+    _fields_ = [("k", C.c_uint32), ("lambda_", C.c_double), ("chunk_size", C.c_uint32),
+                ("oversampling", C.c_uint32), ("n_power_iter", C.c_uint32), ("seed", C.c_uint64),
+                ("norm", C.c_int), ("scale_cov", C.c_int), ("impute", C.c_int), ("nmf_k", C.c_uint32),
+                ("nmf_iter", C.c_uint32), ("nmf_eps", C.c_double), ("nmf_cv_rate", C.c_double)]
+
+
+_dp = C.POINTER(C.c_double)
+
+
+class _Results(C.Structure):
+    _fields_ = [("u_hat", _dp), ("beta", _dp), ("tstat", _dp), ("pvalue", _dp), ("r2", _dp),
+                ("gif_per_trait", _dp), ("gif", C.c_double), ("nmf_cv", _dp), ("nmf_cv_mean", C.c_double),
+                ("nmf_gwas_cv_mae", C.c_double), ("nmf_gwas_cv_mean_mae", C.c_double),
+                ("nmf_gwas_cv_count", C.c_uint64)]
+
+
+EXPORTED_SYMBOLS = (
+    "slfmm_create", "slfmm_destroy", "slfmm_last_error", "slfmm_launch_count", "slfmm_stream",
+    "slfmm_bed_validate", "slfmm_geno_upload", "slfmm_geno_free", "slfmm_geno_n_samples",
+    "slfmm_geno_n_snps", "slfmm_decode_stats", "slfmm_decode_chunk", "slfmm_center_covariates",
+    "slfmm_generate_omega", "slfmm_estimate_factors", "slfmm_test_associations", "slfmm_fit",
+    "slfmm_fit_host", "slfmm_write_tsv", "slfmm_format_exp6",
+)
+
+_lib_handle = None
+
+
+def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
+    """Load the C-ABI library (raises if it was never built)."""
+    global _lib_handle
+    if _lib_handle is not None and path is None:
+        return _lib_handle
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise SchnelGpuError(ERR_CUDA, f"{p} is not built; run `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(str(p))
+    vp, u64, i32, u32 = C.c_void_p, C.c_uint64, C.c_int, C.c_uint32
+    sig = {
+        "slfmm_create": (i32, [i32, C.POINTER(_Opts), C.POINTER(vp)]),
+        "slfmm_destroy": (None, [vp]),
+        "slfmm_last_error": (C.c_char_p, [vp]),
+        "slfmm_launch_count": (u64, [vp]),
+        "slfmm_stream": (vp, [vp]),
+        "slfmm_bed_validate": (i32, [C.c_char_p, u64, u64, vp, C.c_char_p, C.c_size_t]),
+        "slfmm_geno_upload": (i32, [vp, vp, u64, u64, C.POINTER(u64), u64, C.POINTER(_Subset), C.POINTER(vp)]),
+        "slfmm_geno_free": (i32, [vp, vp]),
+        "slfmm_geno_n_samples": (u64, [vp]),
+        "slfmm_geno_n_snps": (u64, [vp]),
+        "slfmm_decode_stats": (i32, [vp, vp, i32, vp, vp, vp, vp]),
+        "slfmm_decode_chunk": (i32, [vp, vp, u64, u64, i32, vp]),
+        "slfmm_center_covariates": (i32, [vp, vp, u64, u32, i32, vp]),
+        "slfmm_generate_omega": (i32, [vp, u64, u64, u32, vp]),
+        "slfmm_estimate_factors": (i32, [vp, vp, vp, u32, C.POINTER(_Config), vp, vp]),
+        "slfmm_test_associations": (i32, [vp, vp, vp, u32, vp, C.POINTER(_Config), C.POINTER(_Results)]),
+        "slfmm_fit": (i32, [vp, vp, vp, vp, u32, C.POINTER(_Config), vp, C.POINTER(_Results)]),
+        "slfmm_fit_host": (i32, [vp, vp, u64, u64, C.POINTER(u64), u64, C.POINTER(_Subset), vp, u32,
+                                 C.POINTER(_Config), vp, C.POINTER(_Results)]),
+        "slfmm_write_tsv": (i32, [C.c_char_p, u64, u32, C.POINTER(C.c_char_p), C.POINTER(u64),
+                                  C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.POINTER(_Results), i32]),
+        "slfmm_format_exp6": (i32, [C.c_double, C.c_char_p, C.c_size_t]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib_handle = lib
+    return lib
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _dptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+# ---------------------------------------------------------------------------
+# configuration mirrors
+# ---------------------------------------------------------------------------
+@dataclass
+class NmfConfig:
+    """src/nmf.rs:15-50."""
+    k: int = 5
+    n_iter: int = 10
+    eps: float = 1e-16
+    cv_rate: float = 0.0005
+    chunk_size: int = 10_000
+    n_workers: int = 0
+    progress: bool = False
+    seed: int = 42
+
+
+@dataclass
+class Lfmm2Config:
+    """src/lib.rs:47-98 (norm defaults to CenterOnly like the library)."""
+    k: int = 5
+    lambda_: float = 1e-5
+    chunk_size: int = 10_000
+    oversampling: int = 10
+    n_power_iter: int = 2
+    seed: int = 42
+    n_workers: int = 0
+    progress: bool = False
+    norm: SnpNorm = SnpNorm.CENTER_ONLY
+    scale_cov: bool = False
+    impute: ImputeStrategy = ImputeStrategy.MEAN
+    nmf: Optional[NmfConfig] = None
+
+    def _c(self) -> _Config:
+        nmf = self.nmf or NmfConfig(k=self.k)
+        return _Config(self.k, self.lambda_, self.chunk_size, self.oversampling, self.n_power_iter,
+                       self.seed & 0xFFFFFFFFFFFFFFFF, int(self.norm), int(self.scale_cov), int(self.impute),
+                       nmf.k, nmf.n_iter, nmf.eps, nmf.cv_rate)
+
+
+@dataclass
+class SubsetSpec:
+    """All / Rate(r) / Indices(v) (src/bed.rs:50-57)."""
+    kind: str = "all"
+    rate: float = 1.0
+    indices: Optional[np.ndarray] = None
+
+    @staticmethod
+    def all() -> "SubsetSpec":
+        return SubsetSpec("all")
+
+    @staticmethod
+    def from_rate(rate: float) -> "SubsetSpec":
+        return SubsetSpec("rate", rate=rate)
+
+    @staticmethod
+    def from_indices(idx: Sequence[int]) -> "SubsetSpec":
+        return SubsetSpec("indices", indices=np.ascontiguousarray(idx, dtype=np.uint64))
+
+    def _c(self) -> _Subset:
+        if self.kind == "all":
+            return _Subset(0, 1.0, None, 0)
+        if self.kind == "rate":
+            return _Subset(1, float(self.rate), None, 0)
+        idx = self.indices
+        return _Subset(2, 1.0, idx.ctypes.data_as(C.POINTER(C.c_uint64)), len(idx))
+
+    def count(self, n_snps: int) -> int:
+        """subset_snp_count (src/bed.rs:162-171)."""
+        if self.kind == "all":
+            return n_snps
+        if self.kind == "rate":
+            step = math.ceil(1.0 / self.rate)
+            return (n_snps + step - 1) // step
+        return len(self.indices)
+
+
+@dataclass
+class TestResults:
+    """src/testing.rs:76-93 plus the per-SNP columns of <out>.tsv."""
+    u_hat: np.ndarray
+    gif: float
+    gif_per_trait: np.ndarray
+    beta: np.ndarray
+    tstat: np.ndarray
+    pvalue: np.ndarray
+    r2: np.ndarray
+    nmf_cv: Optional[List[float]] = None
+    nmf_cv_mean: Optional[float] = None
+    nmf_gwas_cv_mae: Optional[float] = None
+    nmf_gwas_cv_mean_mae: Optional[float] = None
+    nmf_gwas_cv_count: Optional[int] = None
+
+    __test__ = False  # not a pytest class
+
+
+# ---------------------------------------------------------------------------
+# engine + resident genotypes
+# ---------------------------------------------------------------------------
+class Engine:
+    """One CUDA context + stream on one device (replaces the worker pool)."""
+
+    def __init__(self, device: int = 0, precision: Precision = Precision.SPLIT_BF16, stream: Optional[int] = None,
+                 verbose: bool = False):
+        self.lib = load_library()
+        opts = _Opts(int(precision), int(verbose), C.c_void_p(stream) if stream else None)
+        h = C.c_void_p()
+        rc = self.lib.slfmm_create(device, C.byref(opts), C.byref(h))
+        if rc != OK:
+            raise SchnelGpuError(rc, f"slfmm_create failed ({rc})")
+        self.h = h
+        self.precision = Precision(precision)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.slfmm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def check(self, rc: int):
+        if rc != OK:
+            msg = self.lib.slfmm_last_error(self.h)
+            raise SchnelGpuError(rc, msg.decode() if msg else f"error {rc}")
+
+    @property
+    def launches(self) -> int:
+        return int(self.lib.slfmm_launch_count(self.h))
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.slfmm_stream(self.h) or 0)
+
+    def upload(self, packed: np.ndarray, n_physical: int, sample_keep: Optional[Sequence[int]] = None,
+               snps: Optional[SubsetSpec] = None) -> "Genotypes":
+        packed = np.ascontiguousarray(packed, dtype=np.uint8)
+        bps = (n_physical + 3) // 4
+        n_snps = packed.size // bps if bps else 0
+        if packed.size != n_snps * bps:
+            raise SchnelGpuError(ERR_BAD_BED, "payload size is not a multiple of ceil(n/4)")
+        keep = None if sample_keep is None else np.ascontiguousarray(sample_keep, dtype=np.uint64)
+        sub = (snps or SubsetSpec.all())._c()
+        h = C.c_void_p()
+        self.check(self.lib.slfmm_geno_upload(
+            self.h, _ptr(packed), n_physical, n_snps,
+            None if keep is None else keep.ctypes.data_as(C.POINTER(C.c_uint64)),
+            0 if keep is None else len(keep), C.byref(sub), C.byref(h)))
+        return Genotypes(self, h)
+
+    def generate_omega(self, seed: int, n: int, l: int) -> np.ndarray:
+        out = np.empty((n, l))
+        self.check(self.lib.slfmm_generate_omega(self.h, seed & 0xFFFFFFFFFFFFFFFF, n, l, _ptr(out)))
+        return out
+
+    def center_covariates(self, x: np.ndarray, scale: bool) -> np.ndarray:
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        out = np.empty_like(x)
+        self.check(self.lib.slfmm_center_covariates(self.h, _ptr(x), x.shape[0], x.shape[1], int(scale), _ptr(out)))
+        return out
+
+
+class Genotypes:
+    """Device-resident packed genotype matrix (slfmm_geno)."""
+
+    def __init__(self, eng: Engine, h: C.c_void_p):
+        self.eng = eng
+        self.h = h
+
+    @property
+    def n_samples(self) -> int:
+        return int(self.eng.lib.slfmm_geno_n_samples(self.h))
+
+    @property
+    def n_snps(self) -> int:
+        return int(self.eng.lib.slfmm_geno_n_snps(self.h))
+
+    def free(self):
+        if self.h:
+            self.eng.lib.slfmm_geno_free(self.eng.h, self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    def decode_stats(self, norm: SnpNorm):
+        p = self.n_snps
+        counts = np.empty((p, 4), dtype=np.int32)
+        mean, scale, tss = np.empty(p), np.empty(p), np.empty(p)
+        self.eng.check(self.eng.lib.slfmm_decode_stats(self.eng.h, self.h, int(norm), _ptr(counts), _ptr(mean),
+                                                       _ptr(scale), _ptr(tss)))
+        return counts, mean, scale, tss
+
+    def decode_chunk(self, snp0: int, ncols: int, norm: SnpNorm) -> np.ndarray:
+        out = np.empty((self.n_samples, ncols))
+        self.eng.check(self.eng.lib.slfmm_decode_chunk(self.eng.h, self.h, snp0, ncols, int(norm), _ptr(out)))
+        return out
+
+
+# ---------------------------------------------------------------------------
+# PLINK triplet (src/bed.rs)
+# ---------------------------------------------------------------------------
+@dataclass
+class BimRecord:
+    chrom: str
+    snp_id: str
+    cm: float
+    pos: int
+    allele1: str
+    allele2: str
+
+
+@dataclass
+class FamRecord:
+    fid: str
+    iid: str
+    father: str
+    mother: str
+    sex: int
+    pheno: str
+
+
+def _parse_fam(path: Path) -> List[FamRecord]:
+    out = []
+    with open(path) as f:
+        for i, line in enumerate(f):
+            fs = line.split()
+            if len(fs) < 6:
+                raise SchnelGpuError(ERR_BAD_BED, f"FAM line {i + 1} has {len(fs)} fields, expected 6")
+            try:
+                sex = int(fs[4])
+            except ValueError:
+                raise SchnelGpuError(ERR_BAD_BED, f"FAM line {i + 1}: invalid sex '{fs[4]}'")
+            out.append(FamRecord(fs[0], fs[1], fs[2], fs[3], sex, fs[5]))
+    return out
+
+
+def _parse_bim(path: Path) -> List[BimRecord]:
+    out = []
+    with open(path) as f:
+        for i, line in enumerate(f):
+            fs = line.split()
+            if len(fs) < 6:
+                raise SchnelGpuError(ERR_BAD_BED, f"BIM line {i + 1} has {len(fs)} fields, expected 6")
+            try:
+                cm = float(fs[2])
+            except ValueError:
+                raise SchnelGpuError(ERR_BAD_BED, f"BIM line {i + 1}: invalid cM '{fs[2]}'")
+            try:
+                pos = int(fs[3])
+            except ValueError:
+                raise SchnelGpuError(ERR_BAD_BED, f"BIM line {i + 1}: invalid position '{fs[3]}'")
+            out.append(BimRecord(fs[0], fs[1], cm, pos, fs[4], fs[5]))
+    return out
+
+
+class BedFile:
+    """PLINK .bed/.bim/.fam triplet (src/bed.rs:60-171)."""
+
+    def __init__(self, bed_path: Path, fam: List[FamRecord], bim: List[BimRecord], payload: np.ndarray):
+        self.bed_path = bed_path
+        self.fam_records = fam
+        self.bim_records = bim
+        self.n_physical_samples = len(fam)
+        self.n_samples = len(fam)
+        self.n_snps = len(bim)
+        self.payload = payload          # bytes after the magic, SNP-major
+        self.sample_keep: Optional[np.ndarray] = None
+
+    @staticmethod
+    def open(bed_path: os.PathLike) -> "BedFile":
+        bed_path = Path(bed_path)
+        stem = bed_path.with_suffix("")
+        fam_path, bim_path = stem.with_suffix(".fam"), stem.with_suffix(".bim")
+        try:
+            fam = _parse_fam(fam_path)
+        except FileNotFoundError:
+            raise SchnelGpuError(ERR_IO, f"Failed to parse {fam_path}")
+        try:
+            bim = _parse_bim(bim_path)
+        except FileNotFoundError:
+            raise SchnelGpuError(ERR_IO, f"Failed to parse {bim_path}")
+        lib = load_library()
+        err = C.create_string_buffer(512)
+        rc = lib.slfmm_bed_validate(str(bed_path).encode(), len(fam), len(bim), None, err, 512)
+        if rc != OK:
+            raise SchnelGpuError(rc, err.value.decode())
+        payload = np.memmap(bed_path, dtype=np.uint8, mode="r", offset=3) if len(bim) else np.zeros(0, np.uint8)
+        return BedFile(bed_path, fam, bim, payload)
+
+    def bytes_per_snp(self) -> int:
+        return (self.n_physical_samples + 3) // 4
+
+    def subset_samples(self, indices: Sequence[int]) -> None:
+        """src/bed.rs:155-159."""
+        idx = np.asarray(indices, dtype=np.uint64)
+        self.fam_records = [self.fam_records[int(i)] for i in idx]
+        self.n_samples = len(idx)
+        self.sample_keep = idx
+
+    def subset_snp_count(self, subset: SubsetSpec) -> int:
+        return subset.count(self.n_snps)
+
+    def upload(self, eng: Engine, snps: Optional[SubsetSpec] = None) -> Genotypes:
+        return eng.upload(np.asarray(self.payload), self.n_physical_samples, self.sample_keep, snps)
+
+
+# ---------------------------------------------------------------------------
+# library API (src/lib.rs)
+# ---------------------------------------------------------------------------
+_default_engine: Optional[Engine] = None
+
+
+def default_engine() -> Engine:
+    global _default_engine
+    if _default_engine is None:
+        _default_engine = Engine()
+    return _default_engine
+
+
+def center_covariates(x: np.ndarray, scale: bool, engine: Optional[Engine] = None) -> np.ndarray:
+    return (engine or default_engine()).center_covariates(x, scale)
+
+
+def _as_geno(y, eng: Engine, subset: Optional[SubsetSpec] = None) -> Genotypes:
+    if isinstance(y, Genotypes):
+        if subset is not None and subset.kind != "all":
+            raise SchnelGpuError(ERR_BAD_ARG, "apply SNP subsets at upload time for resident genotypes")
+        return y
+    return y.upload(eng, subset)
+
+
+def estimate_factors(y_est, subset: SubsetSpec, x: np.ndarray, config: Lfmm2Config,
+                     omega: Optional[np.ndarray] = None, engine: Optional[Engine] = None) -> np.ndarray:
+    eng = engine or default_engine()
+    g = _as_geno(y_est, eng, subset)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    u = np.empty((g.n_samples, config.k))
+    om = None if omega is None else np.ascontiguousarray(omega, dtype=np.float64)
+    cfg = config._c()
+    eng.check(eng.lib.slfmm_estimate_factors(eng.h, g.h, _ptr(x), x.shape[1], C.byref(cfg), _ptr(om), _ptr(u)))
+    return u
+
+
+def _alloc_results(n: int, p: int, d: int, k: int, nmf_iter: int):
+    arr = dict(u_hat=np.empty((n, k)), beta=np.empty((p, d)), tstat=np.empty((p, d)), pvalue=np.empty((p, d)),
+               r2=np.empty((p, 3)), gif_per_trait=np.empty(d), nmf_cv=np.empty(max(nmf_iter, 1)))
+    r = _Results(_dptr(arr["u_hat"]), _dptr(arr["beta"]), _dptr(arr["tstat"]), _dptr(arr["pvalue"]),
+                 _dptr(arr["r2"]), _dptr(arr["gif_per_trait"]), 0.0, _dptr(arr["nmf_cv"]), 0.0, 0.0, 0.0, 0)
+    return r, arr
+
+
+def _to_results(r: _Results, arr, config: Lfmm2Config) -> TestResults:
+    out = TestResults(arr["u_hat"], r.gif, arr["gif_per_trait"], arr["beta"], arr["tstat"], arr["pvalue"], arr["r2"])
+    if config.impute == ImputeStrategy.NMF:
+        nmf = config.nmf or NmfConfig(k=config.k)
+        out.nmf_cv = list(arr["nmf_cv"][:nmf.n_iter])
+        out.nmf_cv_mean = r.nmf_cv_mean
+        out.nmf_gwas_cv_mae = r.nmf_gwas_cv_mae
+        out.nmf_gwas_cv_mean_mae = r.nmf_gwas_cv_mean_mae
+        out.nmf_gwas_cv_count = int(r.nmf_gwas_cv_count)
+    return out
+
+
+def test_associations(y_full, x: np.ndarray, u_hat: np.ndarray, config: Lfmm2Config,
+                      engine: Optional[Engine] = None) -> TestResults:
+    eng = engine or default_engine()
+    g = _as_geno(y_full, eng)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    u_hat = np.ascontiguousarray(u_hat, dtype=np.float64)
+    r, arr = _alloc_results(g.n_samples, g.n_snps, x.shape[1], config.k, 0)
+    cfg = config._c()
+    eng.check(eng.lib.slfmm_test_associations(eng.h, g.h, _ptr(x), x.shape[1], _ptr(u_hat), C.byref(cfg),
+                                              C.byref(r)))
+    return _to_results(r, arr, config)
+
+
+test_associations.__test__ = False  # keep pytest from collecting the API function
+
+
+@dataclass
+class OutputConfig:
+    """src/testing.rs:68-73 (TSV only)."""
+    path: Path
+    bim: Sequence[BimRecord]
+    cov_names: Sequence[str]
+
+
+def write_tsv(path: os.PathLike, bim: Sequence[BimRecord], cov_names: Sequence[str], res: TestResults,
+              n_threads: int = 0) -> None:
+    lib = load_library()
+    p, d = res.beta.shape
+    enc = lambda xs: (C.c_char_p * len(xs))(*[s.encode() for s in xs])
+    chrom = enc([b.chrom for b in bim])
+    sid = enc([b.snp_id for b in bim])
+    pos = np.ascontiguousarray([b.pos for b in bim], dtype=np.uint64)
+    names = enc(list(cov_names))
+    r = _Results(None, _dptr(res.beta), _dptr(res.tstat), _dptr(res.pvalue), _dptr(res.r2), None, res.gif, None,
+                 0.0, 0.0, 0.0, 0)
+    rc = lib.slfmm_write_tsv(str(path).encode(), p, d, chrom, pos.ctypes.data_as(C.POINTER(C.c_uint64)), sid,
+                             names, C.byref(r), n_threads)
+    if rc != OK:
+        raise SchnelGpuError(rc, f"Failed to create {path}")
+
+
+def fit_lfmm2(y_est, est_subset: SubsetSpec, y_full, x: np.ndarray, config: Lfmm2Config,
+              output: Optional[OutputConfig] = None, omega: Optional[np.ndarray] = None,
+              engine: Optional[Engine] = None) -> TestResults:
+    """fit_lfmm2 (src/lib.rs:162-263): estimate U_hat on y_est (subset), test
+    every SNP of y_full, calibrate, optionally write <out>.tsv."""
+    eng = engine or default_engine()
+    gf = _as_geno(y_full, eng)
+    if y_est is y_full and (est_subset is None or est_subset.kind == "all"):
+        ge = gf
+    else:
+        ge = _as_geno(y_est, eng, est_subset)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    nmf_iter = (config.nmf.n_iter if config.nmf else 0) if config.impute == ImputeStrategy.NMF else 0
+    r, arr = _alloc_results(gf.n_samples, gf.n_snps, x.shape[1], config.k, nmf_iter)
+    om = None if omega is None else np.ascontiguousarray(omega, dtype=np.float64)
+    cfg = config._c()
+    eng.check(eng.lib.slfmm_fit(eng.h, ge.h, gf.h, _ptr(x), x.shape[1], C.byref(cfg), _ptr(om), C.byref(r)))
+    res = _to_results(r, arr, config)
+    if output is not None:
+        write_tsv(output.path, output.bim, output.cov_names, res)
+    return res
+
+
+def format_exp6(v: float) -> str:
+    """Rust ``{:.6e}`` as produced by the C ABI."""
+    lib = load_library()
+    buf = C.create_string_buffer(64)
+    n = lib.slfmm_format_exp6(float(v), buf, 64)
+    return buf.value[:n].decode()

@@ -1,0 +1,889 @@
+// C ABI and host orchestration of the GB300 streaming LFMM2 engine.
+//
+// Mirrors the library surface of schnelLFMM (src/lib.rs:102-263) and the
+// stage drivers estimate_factors_streaming (src/rsvd.rs:26-177) and
+// test_associations_fused (src/testing.rs:252-528).  The reference streams
+// the memory-mapped .bed through a thread pool for every pass; here the
+// packed matrix is uploaded once (pinned staging ring, double-buffered) and
+// every pass is a kernel over the resident copy.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <memory>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "slfmm_internal.h"
+
+struct slfmm_ctx : slfmm::Ctx {};
+struct slfmm_geno : slfmm::Geno {};
+
+namespace slfmm {
+
+void after_launch(Ctx& c, const char* name) {
+    ++c.launches;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess)
+        throw Error(SLFMM_ERR_CUDA, std::string("launch of ") + name + " failed: " + cudaGetErrorString(e));
+}
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// small host <-> device helpers
+// ---------------------------------------------------------------------------
+template <typename T>
+void h2d(Ctx& c, T* dst, const T* src, size_t count) {
+    if (count) SLFMM_CUDA(cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyHostToDevice, c.stream));
+}
+template <typename T>
+void d2h(Ctx& c, T* dst, const T* src, size_t count) {
+    if (count) SLFMM_CUDA(cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyDeviceToHost, c.stream));
+}
+void sync(Ctx& c) { SLFMM_CUDA(cudaStreamSynchronize(c.stream)); }
+
+template <typename T>
+std::vector<T> fetch(Ctx& c, const T* src, size_t count) {
+    std::vector<T> v(count);
+    d2h(c, v.data(), src, count);
+    sync(c);
+    return v;
+}
+template <typename T>
+DBuf<T> upload(Ctx& c, const T* src, size_t count) {
+    DBuf<T> b(count, c.stream);
+    h2d(c, b.get(), src, count);
+    return b;
+}
+
+void log(Ctx& c, const std::string& s) {
+    if (c.verbose) fprintf(stderr, "[schnelgpu] %s\n", s.c_str());
+}
+
+// ---------------------------------------------------------------------------
+// SNP subset expansion (src/parallel.rs:113-122, src/bed.rs:162-171)
+// ---------------------------------------------------------------------------
+std::vector<uint64_t> subset_indices(const slfmm_subset* s, uint64_t n_snps) {
+    std::vector<uint64_t> idx;
+    if (s == nullptr || s->kind == SLFMM_SUBSET_ALL) {
+        idx.resize(n_snps);
+        for (uint64_t i = 0; i < n_snps; ++i) idx[i] = i;
+    } else if (s->kind == SLFMM_SUBSET_RATE) {
+        SLFMM_REQUIRE(s->rate > 0.0 && s->rate <= 1.0, SLFMM_ERR_BAD_ARG,
+                      "--est-rate must be in (0.0, 1.0], got " + std::to_string(s->rate));
+        const uint64_t step = (uint64_t)std::ceil(1.0 / s->rate);
+        for (uint64_t i = 0; i < n_snps; i += step) idx.push_back(i);
+    } else if (s->kind == SLFMM_SUBSET_INDICES) {
+        SLFMM_REQUIRE(s->indices != nullptr || s->n_indices == 0, SLFMM_ERR_BAD_ARG, "null index list");
+        idx.assign(s->indices, s->indices + s->n_indices);
+        for (uint64_t v : idx)
+            SLFMM_REQUIRE(v < n_snps, SLFMM_ERR_BAD_ARG, "SNP index out of range: " + std::to_string(v));
+    } else {
+        throw Error(SLFMM_ERR_BAD_ARG, "unknown subset kind");
+    }
+    return idx;
+}
+
+bool is_pinned(const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+}
+
+// ---------------------------------------------------------------------------
+// ingest: host payload -> resident packed matrix
+// ---------------------------------------------------------------------------
+void upload_geno(Ctx& c, Geno& g, const uint8_t* packed, uint64_t n_phys, uint64_t n_snps,
+                 const uint64_t* keep, uint64_t n_keep, const std::vector<uint64_t>& snps) {
+    SLFMM_REQUIRE(packed != nullptr || n_snps == 0, SLFMM_ERR_BAD_ARG, "null genotype payload");
+    SLFMM_REQUIRE(n_phys > 0, SLFMM_ERR_BAD_ARG, "no samples");
+    const uint64_t bps = ceil_div(n_phys, 4);
+    g.n = keep ? n_keep : n_phys;
+    g.p = snps.size();
+    SLFMM_REQUIRE(g.n > 0, SLFMM_ERR_BAD_ARG, "empty sample subset");
+    SLFMM_REQUIRE(g.n < (1ull << 31), SLFMM_ERR_BAD_ARG, "too many samples");
+    g.stride = round_up(ceil_div(g.n, 4), 128);
+    g.packed.alloc(std::max<uint64_t>(g.p, 1) * g.stride, c.stream);
+    g.counts.alloc(std::max<uint64_t>(g.p, 1) * 4, c.stream);
+    DBuf<uint32_t> keep_d;
+    if (keep) {
+        std::vector<uint32_t> k32(n_keep);
+        for (uint64_t i = 0; i < n_keep; ++i) {
+            SLFMM_REQUIRE(keep[i] < n_phys, SLFMM_ERR_BAD_ARG, "sample index out of range");
+            k32[i] = (uint32_t)keep[i];
+        }
+        keep_d = upload(c, k32.data(), n_keep);
+        sync(c);
+    }
+    if (g.p) {
+        // staging: ~64 MiB per chunk, two device buffers, two pinned buffers
+        const uint64_t rows_per = std::max<uint64_t>(1, std::min<uint64_t>(g.p, (64ull << 20) / bps));
+        const bool direct = is_pinned(packed);
+        DBuf<uint8_t> dstage[2];
+        dstage[0].alloc(rows_per * bps, c.stream);
+        dstage[1].alloc(rows_per * bps, c.stream);
+        uint8_t* hstage[2] = {nullptr, nullptr};
+        cudaEvent_t copied[2], consumed[2];
+        for (int b = 0; b < 2; ++b) {
+            SLFMM_CUDA(cudaEventCreateWithFlags(&copied[b], cudaEventDisableTiming));
+            SLFMM_CUDA(cudaEventCreateWithFlags(&consumed[b], cudaEventDisableTiming));
+            SLFMM_CUDA(cudaEventRecord(consumed[b], c.stream));
+        }
+        struct Cleanup {
+            uint8_t** h; cudaEvent_t* a; cudaEvent_t* b;
+            ~Cleanup() {
+                for (int i = 0; i < 2; ++i) {
+                    if (h[i]) cudaFreeHost(h[i]);
+                    cudaEventDestroy(a[i]);
+                    cudaEventDestroy(b[i]);
+                }
+            }
+        } cleanup{hstage, copied, consumed};
+        if (!direct)
+            for (int b = 0; b < 2; ++b) SLFMM_CUDA(cudaMallocHost(&hstage[b], rows_per * bps));
+        SLFMM_CUDA(cudaStreamSynchronize(c.stream));
+        const uint64_t nchunks = ceil_div(g.p, rows_per);
+        for (uint64_t ch = 0; ch < nchunks; ++ch) {
+            const int b = (int)(ch & 1);
+            const uint64_t r0 = ch * rows_per, r1 = std::min(g.p, r0 + rows_per), rows = r1 - r0;
+            bool contiguous = true;  // one copy when the rows are consecutive (src/parallel.rs:129-146)
+            for (uint64_t r = r0 + 1; r < r1 && contiguous; ++r) contiguous = snps[r] == snps[r - 1] + 1;
+            // wait until the repack that last used buffer b is done
+            SLFMM_CUDA(cudaStreamWaitEvent(c.copy_stream, consumed[b], 0));
+            if (direct && contiguous) {
+                SLFMM_CUDA(cudaMemcpyAsync(dstage[b].get(), packed + snps[r0] * bps, rows * bps,
+                                           cudaMemcpyHostToDevice, c.copy_stream));
+            } else if (direct) {
+                for (uint64_t r = r0; r < r1; ++r)
+                    SLFMM_CUDA(cudaMemcpyAsync(dstage[b].get() + (r - r0) * bps, packed + snps[r] * bps, bps,
+                                               cudaMemcpyHostToDevice, c.copy_stream));
+            } else {
+                // the pinned buffer b is reused only after its previous H2D finished
+                SLFMM_CUDA(cudaEventSynchronize(copied[b]));
+                if (contiguous) {
+                    std::memcpy(hstage[b], packed + snps[r0] * bps, rows * bps);
+                } else {
+                    for (uint64_t r = r0; r < r1; ++r)
+                        std::memcpy(hstage[b] + (r - r0) * bps, packed + snps[r] * bps, bps);
+                }
+                SLFMM_CUDA(cudaMemcpyAsync(dstage[b].get(), hstage[b], rows * bps, cudaMemcpyHostToDevice,
+                                           c.copy_stream));
+            }
+            SLFMM_CUDA(cudaEventRecord(copied[b], c.copy_stream));
+            SLFMM_CUDA(cudaStreamWaitEvent(c.stream, copied[b], 0));
+            launch_repack(c, dstage[b].get(), rows, bps, n_phys, keep_d.get(), g.n,
+                          g.packed.get() + r0 * g.stride, g.stride);
+            SLFMM_CUDA(cudaEventRecord(consumed[b], c.stream));
+        }
+        SLFMM_CUDA(cudaStreamSynchronize(c.stream));
+        SLFMM_CUDA(cudaStreamSynchronize(c.copy_stream));
+    }
+    launch_snp_counts(c, g, nullptr);
+    sync(c);
+}
+
+// ---------------------------------------------------------------------------
+// per-SNP standardisation state of one genotype matrix
+// ---------------------------------------------------------------------------
+struct SnpStd {
+    DBuf<double> mean, scale, tss;
+    DBuf<uint8_t> zero_var;
+    DBuf<float> lut;  // p x 4
+};
+
+void std_mean(Ctx& c, const Geno& g, int norm, SnpStd& s) {
+    const uint64_t p = std::max<uint64_t>(g.p, 1);
+    s.mean.alloc(p, c.stream);
+    s.scale.alloc(p, c.stream);
+    s.tss.alloc(p, c.stream);
+    s.zero_var.alloc(p, c.stream);
+    s.lut.alloc(p * 4, c.stream);
+    launch_stats_mean(c, g, norm, s.mean.get(), s.scale.get(), s.tss.get(), s.zero_var.get());
+    launch_lut_std(c, g.p, s.mean.get(), s.scale.get(), s.lut.get());
+}
+
+// ---------------------------------------------------------------------------
+// contractions over the resident genotypes
+// ---------------------------------------------------------------------------
+int pad16(int w) { return (int)round_up((uint64_t)w, 16); }
+
+// out (p x wp, FP32) = Y_hat^T W, W = n x w FP64 (leading dim ldw)
+void row_contract(Ctx& c, const Geno& g, const SnpStd& s, const double* W, int w, int ldw,
+                  DBuf<float>& out, int& wp) {
+    wp = pad16(w);
+    SLFMM_REQUIRE(wp <= kMaxW, SLFMM_ERR_BAD_ARG, "operand wider than 128 columns");
+    const uint64_t n_pad = round_up(g.n, 128);
+    DBuf<float> W32(n_pad * wp, c.stream);
+    launch_f64_to_f32_pad(c, W, g.n, w, ldw, W32.get(), n_pad, wp);
+    out.alloc(std::max<uint64_t>(g.p, 1) * wp, c.stream);
+    launch_row_lut(c, g, s.lut.get(), W32.get(), wp, out.get());
+}
+
+// S (n x wp, FP64) = Y_hat Q, Q = p x wp FP32
+void col_contract(Ctx& c, const Geno& g, const SnpStd& s, const float* Q, int wp, DBuf<double>& S) {
+    S.alloc(g.n * wp, c.stream);
+    launch_col_lut(c, g, s.lut.get(), Q, wp, S.get());
+}
+
+// ---------------------------------------------------------------------------
+// Step 0 (src/precompute.rs:30-88) in thin form
+// ---------------------------------------------------------------------------
+struct Step0 {
+    uint64_t n = 0;
+    int d = 0, r = 0;
+    DBuf<double> xs;         // n x d centred covariates
+    DBuf<double> qd;         // n x r left singular vectors of X
+    DBuf<double> qd_omd;     // n x r: Q_d diag(1 - d_j)
+    DBuf<double> qd_omdinv;  // n x r: Q_d diag(1 - 1/d_j)
+    DBuf<double> ridge_inv;  // d x d
+};
+
+void center_covariates_dev(Ctx& c, double* xs, uint64_t n, int d, bool scale) {
+    DBuf<double> means(std::max(d, 1), c.stream);
+    launch_colmeans(c, xs, n, d, d, means.get());
+    launch_center_cols(c, xs, n, d, d, means.get());
+    if (scale) launch_scale_cols_sd(c, xs, n, d, d);
+}
+
+void step0(Ctx& c, const double* x_host, uint64_t n, int d, double lambda, bool scale_cov, Step0& s) {
+    SLFMM_REQUIRE(lambda > 0.0, SLFMM_ERR_BAD_ARG,
+                  "Ridge penalty lambda must be positive, got " + std::to_string(lambda) +
+                      ". lambda=0 makes the D_lambda diagonal singular. Use a small positive value like 1e-10.");
+    SLFMM_REQUIRE(d >= 1 && d <= 64, SLFMM_ERR_BAD_ARG, "number of covariates must be in 1..64");
+    s.n = n;
+    s.d = d;
+    s.xs = upload(c, x_host, n * d);
+    center_covariates_dev(c, s.xs.get(), n, d, scale_cov);
+    DBuf<double> gx(d * d, c.stream), gtmp(d * d, c.stream), V(d * d, c.stream), sig(d, c.stream);
+    launch_atb(c, s.xs.get(), d, s.xs.get(), d, n, d, d, gx.get());
+    SLFMM_CUDA(cudaMemcpyAsync(gtmp.get(), gx.get(), d * d * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+    launch_jacobi_svd(c, gtmp.get(), d, V.get(), sig.get());
+    // ridge: (X^T X + lambda I)^-1 with safe_inv semantics
+    std::vector<double> gxh = fetch(c, gx.get(), (size_t)d * d);
+    for (int j = 0; j < d; ++j) gxh[j * d + j] += lambda;
+    DBuf<double> gl = upload(c, gxh.data(), gxh.size());
+    s.ridge_inv.alloc(d * d, c.stream);
+    DBuf<int> st(1, c.stream);
+    DBuf<double> eps(1, c.stream);
+    launch_inverse(c, gl.get(), d, s.ridge_inv.get(), st.get(), eps.get());
+    std::vector<double> Vh = fetch(c, V.get(), (size_t)d * d);
+    std::vector<double> ev = fetch(c, sig.get(), (size_t)d);
+    const int status = fetch(c, st.get(), 1)[0];
+    if (status == 2) throw Error(SLFMM_ERR_SINGULAR, "X^T X + lambda I (ridge) inversion failed even with regularization");
+    if (status == 1)
+        fprintf(stderr, "Warning: X^T X + lambda I (ridge) is singular, adding epsilon=%.2e diagonal regularization\n",
+                fetch(c, eps.get(), 1)[0]);
+    // kept directions: sigma_j^2 = eigenvalue of X^T X
+    std::vector<int> keep;
+    const double emax = ev.empty() ? 0.0 : ev[0];
+    for (int j = 0; j < d; ++j)
+        if (ev[j] > 0.0 && ev[j] > emax * 1e-24) keep.push_back(j);
+    s.r = (int)keep.size();
+    std::vector<double> Vs(d * std::max(s.r, 1)), Vo(Vs.size()), Vi(Vs.size());
+    for (int k = 0; k < s.r; ++k) {
+        const int j = keep[k];
+        const double sigma = std::sqrt(ev[j]);
+        const double dl = std::sqrt(lambda / (lambda + ev[j]));  // src/precompute.rs:55-59
+        for (int i = 0; i < d; ++i) {
+            const double v = Vh[i * d + j] / sigma;
+            Vs[i * s.r + k] = v;
+            Vo[i * s.r + k] = v * (1.0 - dl);
+            Vi[i * s.r + k] = v * (1.0 - 1.0 / dl);
+        }
+    }
+    s.qd.alloc(n * std::max(s.r, 1), c.stream);
+    s.qd_omd.alloc(n * std::max(s.r, 1), c.stream);
+    s.qd_omdinv.alloc(n * std::max(s.r, 1), c.stream);
+    if (s.r) {
+        DBuf<double> a = upload(c, Vs.data(), Vs.size()), b = upload(c, Vo.data(), Vo.size()),
+                     e = upload(c, Vi.data(), Vi.size());
+        launch_gemm_small(c, s.xs.get(), d, n, d, a.get(), s.r, s.r, 1.0, 0.0, s.qd.get(), s.r);
+        launch_gemm_small(c, s.xs.get(), d, n, d, b.get(), s.r, s.r, 1.0, 0.0, s.qd_omd.get(), s.r);
+        launch_gemm_small(c, s.xs.get(), d, n, d, e.get(), s.r, s.r, 1.0, 0.0, s.qd_omdinv.get(), s.r);
+        sync(c);
+    }
+}
+
+// A (n x b, lda) <- P A  or P^-1 A, P = I - Q_d (1 - D_d) Q_d^T
+void apply_p(Ctx& c, const Step0& s, double* A, int b, int lda, bool inverse) {
+    if (s.r == 0 || b == 0) return;
+    DBuf<double> T(s.r * b, c.stream);
+    launch_atb(c, s.qd.get(), s.r, A, lda, s.n, s.r, b, T.get());
+    launch_gemm_small(c, inverse ? s.qd_omdinv.get() : s.qd_omd.get(), s.r, s.n, s.r, T.get(), b, b, -1.0,
+                      1.0, A, lda);
+}
+
+void center_columns(Ctx& c, double* A, uint64_t m, int b, int lda) {
+    DBuf<double> means(std::max(b, 1), c.stream);
+    launch_colmeans(c, A, m, b, lda, means.get());
+    launch_center_cols(c, A, m, b, lda, means.get());
+}
+
+// ---------------------------------------------------------------------------
+// orthonormalisation (Cholesky-QR2, FP64 Gram + Cholesky)
+// ---------------------------------------------------------------------------
+void cholqr2_f32(Ctx& c, float* Z, uint64_t m, int a, int ld) {
+    DBuf<double> G(a * a, c.stream), Linv(a * a, c.stream);
+    DBuf<int> st(1, c.stream);
+    for (int round = 0; round < 2; ++round) {
+        launch_gram_f32(c, Z, ld, m, a, G.get());
+        launch_cholesky(c, G.get(), a, st.get());
+        launch_tri_inv_lower(c, G.get(), a, Linv.get());
+        launch_trmul_f32(c, Z, ld, m, a, Linv.get());
+    }
+}
+
+void cholqr2_f64(Ctx& c, double* A, uint64_t m, int a, int ld) {
+    DBuf<double> G(a * a, c.stream), Linv(a * a, c.stream), LinvT(a * a, c.stream), tmp(m * a, c.stream);
+    DBuf<int> st(1, c.stream);
+    for (int round = 0; round < 2; ++round) {
+        launch_atb(c, A, ld, A, ld, m, a, a, G.get());
+        launch_cholesky(c, G.get(), a, st.get());
+        launch_tri_inv_lower(c, G.get(), a, Linv.get());
+        launch_transpose(c, Linv.get(), a, a, LinvT.get());
+        launch_gemm_small(c, A, ld, m, a, LinvT.get(), a, a, 1.0, 0.0, tmp.get(), a);
+        SLFMM_CUDA(cudaMemcpy2DAsync(A, ld * sizeof(double), tmp.get(), a * sizeof(double), a * sizeof(double), m,
+                                     cudaMemcpyDeviceToDevice, c.stream));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// randomized SVD (src/rsvd.rs:26-177), thin form: sketch P Omega, forward
+// passes P (Y Q_z), U_hat = P^-1 U(P Y Q_z)[:, :K]
+// ---------------------------------------------------------------------------
+void rsvd(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, int K, int l, int q,
+          uint64_t seed, const double* omega_host, DBuf<double>& u_hat) {
+    const uint64_t n = g.n;
+    SLFMM_REQUIRE(l <= 64, SLFMM_ERR_BAD_ARG, "K + oversampling must be <= 64");
+    SLFMM_REQUIRE(g.p >= (uint64_t)l, SLFMM_ERR_BAD_ARG, "fewer estimation SNPs than K + oversampling");
+    SLFMM_REQUIRE(n >= (uint64_t)l, SLFMM_ERR_BAD_ARG, "fewer samples than K + oversampling");
+    DBuf<double> W(n * l, c.stream);
+    if (omega_host) h2d(c, W.get(), omega_host, n * l);
+    else launch_normal(c, seed, n, l, W.get());
+    apply_p(c, s0, W.get(), l, l, false);                    // M^T Omega analogue (:51)
+    center_columns(c, W.get(), n, l, l);
+    DBuf<float> Z;
+    int wp = 0;
+    row_contract(c, g, st, W.get(), l, l, Z, wp);           // sketch (:56-72)
+    cholqr2_f32(c, Z.get(), g.p, l, wp);                     // QR (:75)
+    for (int it = 0; it < q; ++it) {
+        DBuf<double> S;
+        col_contract(c, g, st, Z.get(), wp, S);              // fwd (:88-97)
+        apply_p(c, s0, S.get(), l, wp, false);
+        cholqr2_f64(c, S.get(), n, l, wp);                   // QR(a_qz) (:104-105)
+        apply_p(c, s0, S.get(), l, wp, false);               // M^T Q (:106)
+        center_columns(c, S.get(), n, l, wp);
+        row_contract(c, g, st, S.get(), l, wp, Z, wp);       // bwd (:111-128)
+        cholqr2_f32(c, Z.get(), g.p, l, wp);                 // QR (:131)
+    }
+    DBuf<double> B;
+    col_contract(c, g, st, Z.get(), wp, B);                  // projection (:138-157)
+    apply_p(c, s0, B.get(), l, wp, false);
+    // small SVD (:160-173): eigen-decomposition of the l x l Gram (FP64)
+    DBuf<double> G(l * l, c.stream), V(l * l, c.stream), sig(l, c.stream);
+    launch_atb(c, B.get(), wp, B.get(), wp, n, l, l, G.get());
+    launch_jacobi_svd(c, G.get(), l, V.get(), sig.get());
+    std::vector<double> Vh = fetch(c, V.get(), (size_t)l * l);
+    std::vector<double> ev = fetch(c, sig.get(), (size_t)l);
+    std::vector<double> Vk((size_t)l * K);
+    for (int k = 0; k < K; ++k) {
+        const double sg = std::sqrt(std::max(ev[k], 0.0));
+        for (int i = 0; i < l; ++i) Vk[i * K + k] = sg > 0 ? Vh[i * l + k] / sg : 0.0;
+    }
+    DBuf<double> Vkd = upload(c, Vk.data(), Vk.size());
+    u_hat.alloc(n * K, c.stream);
+    launch_gemm_small(c, B.get(), wp, n, l, Vkd.get(), K, K, 1.0, 0.0, u_hat.get(), K);
+    apply_p(c, s0, u_hat.get(), K, K, true);                 // U_hat = Q D^-1 U_small
+    sync(c);
+}
+
+// ---------------------------------------------------------------------------
+// association pass (src/testing.rs:252-528)
+// ---------------------------------------------------------------------------
+struct AssocOut {
+    double* beta;
+    double* tstat;
+    double* pvalue;
+    double* r2;
+    double* gif_per_trait;
+    double gif;
+};
+
+void assoc(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, const double* u_hat_dev, int K,
+           AssocOut& out) {
+    const uint64_t n = g.n, p = g.p;
+    const int d = s0.d, w = 1 + d + K;
+    if (n <= (uint64_t)(1 + d + K))
+        throw Error(SLFMM_ERR_DF_NONPOSITIVE,
+                    "Insufficient degrees of freedom: n=" + std::to_string(n) + " samples but 1+d+K=1+" +
+                        std::to_string(d) + "+" + std::to_string(K) + "=" + std::to_string(1 + d + K) +
+                        ". Need n > 1 + d + K for valid t-tests. Reduce K or add more samples.");
+    SLFMM_REQUIRE(w <= kMaxSmall, SLFMM_ERR_BAD_ARG, "1 + d + K must be <= 128");
+    const double df = (double)(n - 1 - d - K);
+    // design C = [1 | X | U_hat], unit-norm columns
+    DBuf<double> C(n * w, c.stream), G(w * w, c.stream);
+    launch_build_design(c, s0.xs.get(), d, u_hat_dev, K, n, C.get());
+    launch_atb(c, C.get(), w, C.get(), w, n, w, w, G.get());
+    std::vector<double> Gh = fetch(c, G.get(), (size_t)w * w);
+    std::vector<double> f(w);
+    for (int k = 0; k < w; ++k) f[k] = Gh[k * w + k] > 0 ? 1.0 / std::sqrt(Gh[k * w + k]) : 0.0;
+    DBuf<double> fd = upload(c, f.data(), w);
+    launch_scale_cols(c, C.get(), n, w, w, fd.get());
+    for (int i = 0; i < w; ++i)
+        for (int j = 0; j < w; ++j) Gh[i * w + j] *= f[i] * f[j];
+    for (int k = 0; k < w; ++k)
+        if (f[k] == 0.0) Gh[k * w + k] = 0.0;
+    DBuf<double> L = upload(c, Gh.data(), Gh.size());
+    DBuf<int> st1(1, c.stream), dropped(w, c.stream);
+    launch_cholesky(c, L.get(), w, st1.get(), 1e-10, dropped.get());
+    DBuf<double> Linv(w * w, c.stream);
+    launch_tri_inv_lower(c, L.get(), w, Linv.get());
+    std::vector<double> Li = fetch(c, Linv.get(), (size_t)w * w);
+    std::vector<int> dr = fetch(c, dropped.get(), (size_t)w);
+    for (int k = 0; k < w; ++k)
+        if (dr[k])
+            for (int m = 0; m < w; ++m) Li[k * w + m] = 0.0;
+    // Q_C = C Linv^T (dropped columns zero)
+    std::vector<double> LiT((size_t)w * w);
+    for (int i = 0; i < w; ++i)
+        for (int j = 0; j < w; ++j) LiT[j * w + i] = Li[i * w + j];
+    DBuf<double> LiTd = upload(c, LiT.data(), LiT.size());
+    DBuf<double> QC(n * w, c.stream);
+    launch_gemm_small(c, C.get(), w, n, w, LiTd.get(), w, w, 1.0, 0.0, QC.get(), w);
+    // theta rows and c_jj (coefficients of the X columns, src/testing.rs:1036-1048)
+    const int wu = w - 1;
+    std::vector<float> th((size_t)d * wu, 0.f), bt((size_t)d * wu, 0.f);
+    std::vector<double> cjj(d, 0.0);
+    std::vector<uint8_t> drop_x(d, 0);
+    for (int jj = 0; jj < d; ++jj) {
+        const int col = 1 + jj;
+        drop_x[jj] = (uint8_t)(dr[col] != 0);
+        double s = 0.0;
+        for (int k = col; k < w; ++k) {
+            th[jj * wu + (k - 1)] = (float)Li[k * w + col];
+            s += Li[k * w + col] * Li[k * w + col];
+        }
+        cjj[jj] = s;
+    }
+    // beta rows: R ((I - P_U) X)^T Q_C  (src/testing.rs:285-296, 360-362)
+    {
+        DBuf<double> UtU(K * K, c.stream), UtUi(K * K, c.stream), M1(K * d, c.stream), M2(K * d, c.stream),
+            F(n * d, c.stream), FtQ(d * w, c.stream), Bpp(d * w, c.stream);
+        DBuf<int> sti(1, c.stream);
+        DBuf<double> epsd(1, c.stream);
+        launch_atb(c, u_hat_dev, K, u_hat_dev, K, n, K, K, UtU.get());
+        launch_inverse(c, UtU.get(), K, UtUi.get(), sti.get(), epsd.get());
+        launch_atb(c, u_hat_dev, K, s0.xs.get(), d, n, K, d, M1.get());
+        launch_gemm_small(c, UtUi.get(), K, K, K, M1.get(), d, d, 1.0, 0.0, M2.get(), d);
+        SLFMM_CUDA(cudaMemcpyAsync(F.get(), s0.xs.get(), n * d * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+        launch_gemm_small(c, u_hat_dev, K, n, K, M2.get(), d, d, -1.0, 1.0, F.get(), d);
+        launch_atb(c, F.get(), d, QC.get(), w, n, d, w, FtQ.get());
+        launch_gemm_small(c, s0.ridge_inv.get(), d, d, d, FtQ.get(), w, w, 1.0, 0.0, Bpp.get(), w);
+        const int sst = fetch(c, sti.get(), 1)[0];
+        if (sst == 2) throw Error(SLFMM_ERR_SINGULAR, "U_hat^T U_hat inversion failed even with regularization");
+        if (sst == 1)
+            fprintf(stderr, "Warning: U_hat^T U_hat is singular, adding epsilon=%.2e diagonal regularization\n",
+                    fetch(c, epsd.get(), 1)[0]);
+        std::vector<double> Bh = fetch(c, Bpp.get(), (size_t)d * w);
+        for (int jj = 0; jj < d; ++jj)
+            for (int k = 1; k < w; ++k) bt[jj * wu + (k - 1)] = (float)Bh[jj * w + k];
+    }
+    // u = Q_C[:, 1:]^T y for every SNP
+    DBuf<float> U;
+    int wp = 0;
+    row_contract(c, g, st, QC.get() + 1, wu, w, U, wp);
+    DBuf<float> thd = upload(c, th.data(), th.size()), btd = upload(c, bt.data(), bt.size());
+    DBuf<double> cjjd = upload(c, cjj.data(), cjj.size());
+    DBuf<uint8_t> dxd = upload(c, drop_x.data(), drop_x.size());
+    AssocConsts k{d, wu, df, thd.get(), btd.get(), cjjd.get(), dxd.get(), st.zero_var.get()};
+    const uint64_t pp = std::max<uint64_t>(p, 1);
+    DBuf<double> beta(pp * d, c.stream), r2(pp * 3, c.stream), t64(pp * d, c.stream), pv(pp * d, c.stream);
+    DBuf<float> t32(pp * d, c.stream);
+    DBuf<uint32_t> hist((size_t)d * kHistBins, c.stream);
+    hist.zero();
+    launch_assoc_epilogue(c, p, U.get(), wp, st.tss.get(), k, beta.get(), t32.get(), r2.get(), hist.get());
+    DBuf<double> graw(d, c.stream);
+    launch_gif(c, hist.get(), d, graw.get());
+    std::vector<double> gr = fetch(c, graw.get(), (size_t)d);
+    std::vector<double> gpt(d);
+    double gsum = 0.0;
+    for (int jj = 0; jj < d; ++jj) {
+        gpt[jj] = std::max(gr[jj], 1.0);
+        gsum += gr[jj];
+    }
+    out.gif = gsum / d;
+    if (out.gif_per_trait) std::copy(gpt.begin(), gpt.end(), out.gif_per_trait);
+    DBuf<double> gptd = upload(c, gpt.data(), gpt.size());
+    launch_calibrate(c, p, d, t32.get(), gptd.get(), t64.get(), pv.get());
+    if (out.beta) d2h(c, out.beta, beta.get(), p * d);
+    if (out.tstat) d2h(c, out.tstat, t64.get(), p * d);
+    if (out.pvalue) d2h(c, out.pvalue, pv.get(), p * d);
+    if (out.r2) d2h(c, out.r2, r2.get(), p * 3);
+    sync(c);
+}
+
+void check_cfg(const slfmm_config* cfg) {
+    SLFMM_REQUIRE(cfg != nullptr, SLFMM_ERR_BAD_ARG, "null config");
+    SLFMM_REQUIRE(cfg->k >= 1, SLFMM_ERR_BAD_ARG, "K must be >= 1");
+    SLFMM_REQUIRE(cfg->norm == SLFMM_NORM_CENTER_ONLY || cfg->norm == SLFMM_NORM_EIGENSTRAT, SLFMM_ERR_BAD_ARG,
+                  "unknown normalisation");
+    SLFMM_REQUIRE(cfg->impute == SLFMM_IMPUTE_MEAN || cfg->impute == SLFMM_IMPUTE_NMF, SLFMM_ERR_BAD_ARG,
+                  "unknown imputation strategy");
+}
+
+void fit_impl(Ctx& c, const Geno& ge, const Geno& gf, const double* x, int d, const slfmm_config* cfg,
+              const double* omega, slfmm_results* res) {
+    check_cfg(cfg);
+    SLFMM_REQUIRE(ge.n == gf.n, SLFMM_ERR_BAD_ARG, "estimation and testing genotypes have different sample counts");
+    SLFMM_REQUIRE(cfg->impute == SLFMM_IMPUTE_MEAN, SLFMM_ERR_BAD_ARG, "NMF imputation not available in this build");
+    Step0 s0;
+    step0(c, x, gf.n, d, cfg->lambda, cfg->scale_cov != 0, s0);
+    SnpStd se, sf;
+    std_mean(c, ge, cfg->norm, se);
+    const SnpStd* sfp = &se;
+    if (&ge != &gf) {
+        std_mean(c, gf, cfg->norm, sf);
+        sfp = &sf;
+    }
+    DBuf<double> u_hat;
+    const int K = (int)cfg->k, l = K + (int)cfg->oversampling;
+    rsvd(c, ge, se, s0, K, l, (int)cfg->n_power_iter, cfg->seed, omega, u_hat);
+    if (res && res->u_hat) d2h(c, res->u_hat, u_hat.get(), gf.n * K);
+    AssocOut out{res ? res->beta : nullptr, res ? res->tstat : nullptr, res ? res->pvalue : nullptr,
+                 res ? res->r2 : nullptr, res ? res->gif_per_trait : nullptr, 0.0};
+    assoc(c, gf, *sfp, s0, u_hat.get(), K, out);
+    if (res) res->gif = out.gif;
+}
+
+// ---------------------------------------------------------------------------
+// Rust "{:.6e}" formatting (src/testing.rs:780-797)
+// ---------------------------------------------------------------------------
+int format_exp6(double v, char* buf, size_t len) {
+    if (std::isnan(v)) return snprintf(buf, len, "NaN");
+    if (std::isinf(v)) return snprintf(buf, len, v > 0 ? "inf" : "-inf");
+    char tmp[48];
+    snprintf(tmp, sizeof tmp, "%.6e", v);
+    char* e = std::strchr(tmp, 'e');
+    if (!e) return snprintf(buf, len, "%s", tmp);
+    *e = '\0';
+    const int ex = std::atoi(e + 1);
+    return snprintf(buf, len, "%se%d", tmp, ex);
+}
+
+}  // namespace
+}  // namespace slfmm
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+using namespace slfmm;
+
+#define API_TRY try {
+#define API_CATCH(ctxp)                                                        \
+    }                                                                          \
+    catch (const slfmm::Error& e) {                                            \
+        if (ctxp) (ctxp)->last_error = e.what();                               \
+        return e.code;                                                         \
+    }                                                                          \
+    catch (const std::bad_alloc&) {                                            \
+        if (ctxp) (ctxp)->last_error = "host allocation failed";               \
+        return SLFMM_ERR_NOMEM;                                                \
+    }                                                                          \
+    catch (const std::exception& e) {                                          \
+        if (ctxp) (ctxp)->last_error = e.what();                               \
+        return SLFMM_ERR_CUDA;                                                 \
+    }                                                                          \
+    return SLFMM_OK;
+
+extern "C" {
+
+int slfmm_create(int device, const slfmm_opts* opts, slfmm_ctx** out) {
+    if (!out) return SLFMM_ERR_BAD_ARG;
+    *out = nullptr;
+    slfmm_ctx* c = new (std::nothrow) slfmm_ctx();
+    if (!c) return SLFMM_ERR_NOMEM;
+    try {
+        int ndev = 0;
+        SLFMM_CUDA(cudaGetDeviceCount(&ndev));
+        SLFMM_REQUIRE(device >= 0 && device < ndev, SLFMM_ERR_CUDA, "no such CUDA device");
+        SLFMM_CUDA(cudaSetDevice(device));
+        cudaDeviceProp prop{};
+        SLFMM_CUDA(cudaGetDeviceProperties(&prop, device));
+        SLFMM_REQUIRE(prop.major == 10 && prop.minor == 3, SLFMM_ERR_CUDA,
+                      std::string("schnelgpu is built for sm_103a (GB300); device is ") + prop.name);
+        c->device = device;
+        c->sm_count = prop.multiProcessorCount;
+        if (opts) {
+            c->precision = opts->precision;
+            c->verbose = opts->verbose;
+        }
+        if (opts && opts->stream) {
+            c->stream = (cudaStream_t)opts->stream;
+        } else {
+            SLFMM_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+            c->own_stream = true;
+        }
+        SLFMM_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        cudaMemPool_t pool;
+        SLFMM_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+        uint64_t thr = UINT64_MAX;
+        SLFMM_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+        c->dev_flags.alloc(4, c->stream);
+        c->dev_flags.zero();
+        SLFMM_CUDA(cudaStreamSynchronize(c->stream));
+    } catch (const slfmm::Error& e) {
+        fprintf(stderr, "schnelgpu: %s\n", e.what());
+        const int code = e.code;
+        delete c;
+        return code;
+    }
+    *out = c;
+    return SLFMM_OK;
+}
+
+void slfmm_destroy(slfmm_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    c->dev_flags.release();
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char* slfmm_last_error(const slfmm_ctx* c) { return c ? c->last_error.c_str() : "null context"; }
+uint64_t slfmm_launch_count(const slfmm_ctx* c) { return c ? c->launches : 0; }
+void* slfmm_stream(const slfmm_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int slfmm_bed_validate(const char* bed_path, uint64_t n_samples, uint64_t n_snps, uint8_t* payload_out,
+                       char* err, size_t err_len) {
+    auto fail = [&](int code, const std::string& m) {
+        if (err && err_len) snprintf(err, err_len, "%s", m.c_str());
+        return code;
+    };
+    if (!bed_path) return fail(SLFMM_ERR_BAD_ARG, "null path");
+    std::ifstream f(bed_path, std::ios::binary | std::ios::ate);
+    if (!f) return fail(SLFMM_ERR_IO, std::string("Failed to open ") + bed_path);
+    const uint64_t size = (uint64_t)f.tellg();
+    f.seekg(0);
+    unsigned char magic[3] = {0, 0, 0};
+    if (size >= 3) f.read((char*)magic, 3);
+    if (size < 3 || magic[0] != 0x6C || magic[1] != 0x1B || magic[2] != 0x01)
+        return fail(SLFMM_ERR_BAD_BED, std::string("Invalid .bed file (bad magic bytes): ") + bed_path);
+    const uint64_t bps = (n_samples + 3) / 4;
+    const uint64_t expected = 3 + bps * n_snps;
+    if (size != expected)
+        return fail(SLFMM_ERR_BAD_BED, "BED file size mismatch: expected " + std::to_string(expected) + " bytes (" +
+                                           std::to_string(n_samples) + " samples x " + std::to_string(n_snps) +
+                                           " SNPs), got " + std::to_string(size));
+    if (payload_out) {
+        f.read((char*)payload_out, (std::streamsize)(bps * n_snps));
+        if (!f) return fail(SLFMM_ERR_IO, std::string("short read from ") + bed_path);
+    }
+    return SLFMM_OK;
+}
+
+int slfmm_geno_upload(slfmm_ctx* c, const uint8_t* packed, uint64_t n_physical, uint64_t n_snps,
+                      const uint64_t* sample_keep, uint64_t n_keep, const slfmm_subset* snps, slfmm_geno** out) {
+    if (!c || !out) return SLFMM_ERR_BAD_ARG;
+    *out = nullptr;
+    API_TRY
+    SLFMM_CUDA(cudaSetDevice(c->device));
+    std::unique_ptr<slfmm_geno> g(new slfmm_geno());
+    std::vector<uint64_t> idx = subset_indices(snps, n_snps);
+    upload_geno(*c, *g, packed, n_physical, n_snps, sample_keep, n_keep, idx);
+    *out = g.release();
+    API_CATCH(c)
+}
+
+int slfmm_geno_free(slfmm_ctx* c, slfmm_geno* g) {
+    if (!g) return SLFMM_OK;
+    if (c) cudaSetDevice(c->device);
+    delete g;
+    return SLFMM_OK;
+}
+
+uint64_t slfmm_geno_n_samples(const slfmm_geno* g) { return g ? g->n : 0; }
+uint64_t slfmm_geno_n_snps(const slfmm_geno* g) { return g ? g->p : 0; }
+
+int slfmm_decode_stats(slfmm_ctx* c, const slfmm_geno* g, int norm, int32_t* counts4, double* mean,
+                       double* scale, double* tss) {
+    if (!c || !g) return SLFMM_ERR_BAD_ARG;
+    API_TRY
+    SLFMM_CUDA(cudaSetDevice(c->device));
+    SLFMM_REQUIRE(norm == SLFMM_NORM_CENTER_ONLY || norm == SLFMM_NORM_EIGENSTRAT, SLFMM_ERR_BAD_ARG,
+                  "unknown normalisation");
+    SnpStd s;
+    std_mean(*c, *g, norm, s);
+    if (counts4) d2h(*c, counts4, g->counts.get(), g->p * 4);
+    if (mean) d2h(*c, mean, s.mean.get(), g->p);
+    if (scale) d2h(*c, scale, s.scale.get(), g->p);
+    if (tss) d2h(*c, tss, s.tss.get(), g->p);
+    sync(*c);
+    API_CATCH(c)
+}
+
+int slfmm_decode_chunk(slfmm_ctx* c, const slfmm_geno* g, uint64_t snp0, uint64_t ncols, int norm, double* out) {
+    if (!c || !g || !out) return SLFMM_ERR_BAD_ARG;
+    API_TRY
+    SLFMM_CUDA(cudaSetDevice(c->device));
+    SLFMM_REQUIRE(snp0 + ncols <= g->p, SLFMM_ERR_BAD_ARG, "SNP range out of bounds");
+    SnpStd s;
+    std_mean(*c, *g, norm, s);
+    DBuf<double> o(std::max<uint64_t>(g->n * ncols, 1), c->stream);
+    launch_decode_chunk(*c, *g, snp0, ncols, s.mean.get(), s.scale.get(), o.get());
+    d2h(*c, out, o.get(), g->n * ncols);
+    sync(*c);
+    API_CATCH(c)
+}
+
+int slfmm_center_covariates(slfmm_ctx* c, const double* x, uint64_t n, uint32_t d, int scale, double* out) {
+    if (!c || !x || !out) return SLFMM_ERR_BAD_ARG;
+    API_TRY
+    SLFMM_CUDA(cudaSetDevice(c->device));
+    DBuf<double> xs = upload(*c, x, n * d);
+    center_covariates_dev(*c, xs.get(), n, (int)d, scale != 0);
+    d2h(*c, out, xs.get(), n * d);
+    sync(*c);
+    API_CATCH(c)
+}
+
+int slfmm_generate_omega(slfmm_ctx* c, uint64_t seed, uint64_t n, uint32_t l, double* out) {
+    if (!c || !out) return SLFMM_ERR_BAD_ARG;
+    API_TRY
+    SLFMM_CUDA(cudaSetDevice(c->device));
+    DBuf<double> o(std::max<uint64_t>(n * l, 1), c->stream);
+    launch_normal(*c, seed, n, (int)l, o.get());
+    d2h(*c, out, o.get(), n * l);
+    sync(*c);
+    API_CATCH(c)
+}
+
+int slfmm_estimate_factors(slfmm_ctx* c, const slfmm_geno* y_est, const double* x, uint32_t d,
+                           const slfmm_config* cfg, const double* omega, double* u_hat) {
+    if (!c || !y_est || !x || !u_hat) return SLFMM_ERR_BAD_ARG;
+    API_TRY
+    SLFMM_CUDA(cudaSetDevice(c->device));
+    check_cfg(cfg);
+    SLFMM_REQUIRE(cfg->impute == SLFMM_IMPUTE_MEAN, SLFMM_ERR_BAD_ARG, "estimate_factors uses mean imputation");
+    Step0 s0;
+    step0(*c, x, y_est->n, (int)d, cfg->lambda, cfg->scale_cov != 0, s0);
+    SnpStd st;
+    std_mean(*c, *y_est, cfg->norm, st);
+    DBuf<double> u;
+    const int K = (int)cfg->k;
+    rsvd(*c, *y_est, st, s0, K, K + (int)cfg->oversampling, (int)cfg->n_power_iter, cfg->seed, omega, u);
+    d2h(*c, u_hat, u.get(), y_est->n * K);
+    sync(*c);
+    API_CATCH(c)
+}
+
+int slfmm_test_associations(slfmm_ctx* c, const slfmm_geno* y_full, const double* x, uint32_t d,
+                            const double* u_hat, const slfmm_config* cfg, slfmm_results* res) {
+    if (!c || !y_full || !x || !u_hat || !res) return SLFMM_ERR_BAD_ARG;
+    API_TRY
+    SLFMM_CUDA(cudaSetDevice(c->device));
+    check_cfg(cfg);
+    SLFMM_REQUIRE(cfg->impute == SLFMM_IMPUTE_MEAN, SLFMM_ERR_BAD_ARG, "test_associations uses mean imputation");
+    Step0 s0;
+    step0(*c, x, y_full->n, (int)d, cfg->lambda, cfg->scale_cov != 0, s0);
+    SnpStd st;
+    std_mean(*c, *y_full, cfg->norm, st);
+    const int K = (int)cfg->k;
+    DBuf<double> u = upload(*c, u_hat, y_full->n * K);
+    AssocOut out{res->beta, res->tstat, res->pvalue, res->r2, res->gif_per_trait, 0.0};
+    assoc(*c, *y_full, st, s0, u.get(), K, out);
+    res->gif = out.gif;
+    if (res->u_hat && res->u_hat != u_hat) std::memcpy(res->u_hat, u_hat, y_full->n * K * sizeof(double));
+    API_CATCH(c)
+}
+
+int slfmm_fit(slfmm_ctx* c, const slfmm_geno* y_est, const slfmm_geno* y_full, const double* x, uint32_t d,
+              const slfmm_config* cfg, const double* omega, slfmm_results* res) {
+    if (!c || !y_full || !x) return SLFMM_ERR_BAD_ARG;
+    API_TRY
+    SLFMM_CUDA(cudaSetDevice(c->device));
+    fit_impl(*c, y_est ? *y_est : *y_full, *y_full, x, (int)d, cfg, omega, res);
+    API_CATCH(c)
+}
+
+int slfmm_fit_host(slfmm_ctx* c, const uint8_t* packed, uint64_t n_physical, uint64_t n_snps,
+                   const uint64_t* sample_keep, uint64_t n_keep, const slfmm_subset* est, const double* x,
+                   uint32_t d, const slfmm_config* cfg, const double* omega, slfmm_results* res) {
+    if (!c || !packed || !x) return SLFMM_ERR_BAD_ARG;
+    API_TRY
+    SLFMM_CUDA(cudaSetDevice(c->device));
+    Geno full, sub;
+    upload_geno(*c, full, packed, n_physical, n_snps, sample_keep, n_keep, subset_indices(nullptr, n_snps));
+    const Geno* ge = &full;
+    if (est && est->kind != SLFMM_SUBSET_ALL) {
+        upload_geno(*c, sub, packed, n_physical, n_snps, sample_keep, n_keep, subset_indices(est, n_snps));
+        ge = &sub;
+    }
+    fit_impl(*c, *ge, full, x, (int)d, cfg, omega, res);
+    API_CATCH(c)
+}
+
+int slfmm_format_exp6(double v, char* buf, size_t len) { return format_exp6(v, buf, len); }
+
+int slfmm_write_tsv(const char* path, uint64_t p, uint32_t d, const char* const* chrom, const uint64_t* pos,
+                    const char* const* snp_id, const char* const* cov_names, const slfmm_results* res,
+                    int n_threads) {
+    if (!path || !res || !chrom || !pos || !snp_id || !cov_names) return SLFMM_ERR_BAD_ARG;
+    if (!res->pvalue || !res->beta || !res->tstat || !res->r2) return SLFMM_ERR_BAD_ARG;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return SLFMM_ERR_IO;
+    std::string head = "chr\tpos\tsnp_id";
+    for (uint32_t j = 0; j < d; ++j) {
+        const std::string nm = cov_names[j];
+        head += "\tp_" + nm + "\tbeta_" + nm + "\tt_" + nm;
+    }
+    head += "\tr2_cov\tr2_latent\tr2_resid\n";
+    std::fwrite(head.data(), 1, head.size(), f);
+    int nt = n_threads > 0 ? n_threads : (int)std::max(1u, std::thread::hardware_concurrency());
+    const uint64_t block = 65536;
+    bool ok = true;
+    for (uint64_t b0 = 0; b0 < p && ok; b0 += block * nt) {
+        std::vector<std::string> parts(nt);
+        std::vector<std::thread> th;
+        for (int t = 0; t < nt; ++t) {
+            th.emplace_back([&, t]() {
+                const uint64_t r0 = b0 + t * block, r1 = std::min(p, r0 + block);
+                std::string& s = parts[t];
+                char buf[64];
+                for (uint64_t i = r0; i < r1; ++i) {
+                    s += chrom[i];
+                    s += '\t';
+                    s += std::to_string(pos[i]);
+                    s += '\t';
+                    s += snp_id[i];
+                    for (uint32_t j = 0; j < d; ++j) {
+                        const double vals[3] = {res->pvalue[i * d + j], res->beta[i * d + j], res->tstat[i * d + j]};
+                        for (double v : vals) {
+                            s += '\t';
+                            s.append(buf, (size_t)format_exp6(v, buf, sizeof buf));
+                        }
+                    }
+                    for (int k = 0; k < 3; ++k) {
+                        s += '\t';
+                        s.append(buf, (size_t)format_exp6(res->r2[i * 3 + k], buf, sizeof buf));
+                    }
+                    s += '\n';
+                }
+            });
+        }
+        for (auto& x : th) x.join();
+        for (auto& s : parts)
+            if (!s.empty() && std::fwrite(s.data(), 1, s.size(), f) != s.size()) ok = false;
+    }
+    if (std::fclose(f) != 0) ok = false;
+    return ok ? SLFMM_OK : SLFMM_ERR_IO;
+}
+
+}  // extern "C"

@@ -1,0 +1,206 @@
+// Stage (c): per-SNP association statistics, t^2 histogram, genomic
+// inflation factor and calibrated p-values.
+//
+// Reference: test_associations_fused (src/testing.rs:252-528), t_test
+// (:1036-1048), TsqHistogram (:114-225), calibrate_batch (:685-728).
+//
+// The contraction produces, per SNP j, u = Q_C^T y_j where Q_C is an
+// orthonormal basis of [1 | X | U_hat] built by Cholesky-Gram-Schmidt in
+// that column order (the intercept coordinate is identically zero because
+// every standardised column sums to zero).  From u and the exact TSS:
+//   RSS     = TSS - ||u||^2                     (= ||y - C theta||^2)
+//   SS_cov  = sum_{k<d} u_k^2                   (= ||H_X y||^2)
+//   theta_j = (L^-T u)_{1+j},  c_jj = [(C^T C)^-1]_{1+j,1+j}
+//   beta    = R ((I - P_U) X)^T Q_C u          (ridge effect, Step 3)
+// which is the reference's O(n^2)-per-SNP algebra in O(n (1+d+K)).
+#include "slfmm_internal.h"
+
+namespace slfmm {
+namespace {
+
+constexpr int kEpiSnps = 32;  // SNPs per CTA, 8 threads each
+
+__global__ void __launch_bounds__(256) k_assoc_epilogue(
+    uint64_t p, const float* __restrict__ u, int ldu, const double* __restrict__ tss,
+    const uint8_t* __restrict__ zero_var, int d, int w, double df,
+    const float* __restrict__ theta_rows, const float* __restrict__ beta_rows,
+    const double* __restrict__ cjj, const uint8_t* __restrict__ dropped,
+    double* __restrict__ beta, float* __restrict__ t32, double* __restrict__ r2,
+    uint32_t* __restrict__ hist) {
+    extern __shared__ float sm[];
+    float* th = sm;                    // d x w
+    float* bt = th + d * w;            // d x w
+    float* us = bt + d * w;            // kEpiSnps x w
+    const int tid = threadIdx.x;
+    for (int e = tid; e < d * w; e += blockDim.x) {
+        th[e] = theta_rows[e];
+        bt[e] = beta_rows[e];
+    }
+    const int s = tid >> 3, l8 = tid & 7;
+    const uint64_t j0 = (uint64_t)blockIdx.x * kEpiSnps;
+    const uint64_t j = j0 + s;
+    const bool live = j < p;
+    for (int e = tid; e < kEpiSnps * w; e += blockDim.x) {
+        const int r = e / w, k = e - r * w;
+        const uint64_t jj = j0 + r;
+        us[e] = jj < p ? u[jj * ldu + k] : 0.f;
+    }
+    __syncthreads();
+    const float* ur = us + s * w;
+    float ss = 0.f, sc = 0.f;
+    for (int k = l8; k < w; k += 8) {
+        const float v = ur[k];
+        ss = fmaf(v, v, ss);
+        if (k < d) sc = fmaf(v, v, sc);
+    }
+#pragma unroll
+    for (int o = 4; o > 0; o >>= 1) {
+        ss += __shfl_xor_sync(0xffffffffu, ss, o);
+        sc += __shfl_xor_sync(0xffffffffu, sc, o);
+    }
+    if (!live) return;
+    const bool zv = zero_var && zero_var[j];
+    const double T = tss[j];
+    double rss = T - (double)ss;
+    if (rss < 0.0 || zv) rss = 0.0;
+    const double sigma2 = rss / df;
+    if (l8 == 0) {
+        double a = 0.0, b = 0.0, c = 0.0;
+        if (T > 1e-300 && !zv) {                            // src/testing.rs:394-404
+            const double ssc = (double)sc;
+            a = ssc / T;
+            b = fmax(T - rss - ssc, 0.0) / T;
+            c = rss / T;
+        }
+        r2[j * 3 + 0] = a;
+        r2[j * 3 + 1] = b;
+        r2[j * 3 + 2] = c;
+    }
+    const float s2f = (float)sigma2;
+    for (int jj = l8; jj < d; jj += 8) {
+        float theta = 0.f, bb = 0.f;
+        const float* trow = th + jj * w;
+        const float* brow = bt + jj * w;
+        for (int k = 0; k < w; ++k) {
+            theta = fmaf(trow[k], ur[k], theta);
+            bb = fmaf(brow[k], ur[k], bb);
+        }
+        float t = 0.f;
+        const float var = s2f * (float)cjj[jj];
+        if (!zv && !dropped[jj] && var > 0.f && isfinite(var)) {  // t_test guards
+            t = theta * rsqrtf(var);
+            if (!isfinite(t)) t = 0.f;
+        }
+        if (zv) bb = 0.f;
+        beta[j * d + jj] = (double)bb;
+        t32[j * d + jj] = t;
+        const float t2 = t * t;
+        if (isfinite(t2)) {
+            unsigned bin = (unsigned)fminf(t2 * 1000.0f, (float)(kHistBins - 1));
+            if (bin > (unsigned)(kHistBins - 1)) bin = kHistBins - 1;
+            atomicAdd(&hist[(uint64_t)jj * kHistBins + bin], 1u);
+        }
+    }
+}
+
+// Median of the t^2 histogram of one trait (src/testing.rs:179-224) and the
+// raw GIF (median < 1e-10 -> 1, else median / 0.4549).
+__global__ void __launch_bounds__(1024) k_gif(const uint32_t* __restrict__ hist,
+                                              double* __restrict__ gif_raw) {
+    constexpr int kT = 1024;
+    constexpr int kSeg = (kHistBins + kT - 1) / kT;
+    __shared__ unsigned long long seg[kT];
+    __shared__ unsigned long long excl[kT];
+    __shared__ long long b1, b2;
+    __shared__ unsigned long long total;
+    const uint32_t* h = hist + (uint64_t)blockIdx.x * kHistBins;
+    const int t = threadIdx.x;
+    const int lo = t * kSeg, hi = min(kHistBins, lo + kSeg);
+    unsigned long long s = 0;
+    for (int b = lo; b < hi; ++b) s += h[b];
+    seg[t] = s;
+    if (t == 0) { b1 = -1; b2 = -1; }
+    __syncthreads();
+    if (t == 0) {
+        unsigned long long acc = 0;
+        for (int i = 0; i < kT; ++i) { excl[i] = acc; acc += seg[i]; }
+        total = acc;
+    }
+    __syncthreads();
+    const unsigned long long n = total;
+    if (n == 0) {
+        if (t == 0) gif_raw[blockIdx.x] = 1.0;  // median 0 -> GIF 1
+        return;
+    }
+    const bool even = (n % 2) == 0;
+    const unsigned long long target = even ? n / 2 - 1 : n / 2;
+    // first bin whose cumulative count exceeds `target` (and target+1)
+    for (int which = 0; which < (even ? 2 : 1); ++which) {
+        const unsigned long long tg = target + which;
+        if (tg >= excl[t] && tg < excl[t] + seg[t]) {
+            unsigned long long cum = excl[t];
+            for (int b = lo; b < hi; ++b) {
+                cum += h[b];
+                if (cum > tg) {
+                    if (which == 0) b1 = b; else b2 = b;
+                    break;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    if (t == 0) {
+        double med;
+        if (!even) med = ((double)b1 + 0.5) * kHistWidth;
+        else med = (((double)b1 + 0.5) * kHistWidth + ((double)b2 + 0.5) * kHistWidth) / 2.0;
+        gif_raw[blockIdx.x] = med < 1e-10 ? 1.0 : med / kGifDivisor;
+    }
+}
+
+// p = 2 * Phi(-|t| / sqrt(GIF_j)) = erfc(|z| / sqrt 2)  (src/testing.rs:691-712)
+__global__ void k_calibrate(uint64_t p, int d, const float* __restrict__ t32,
+                            const double* __restrict__ gif, double* __restrict__ t64,
+                            double* __restrict__ pval) {
+    const uint64_t total = p * (uint64_t)d;
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < total;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        const int jj = (int)(e % d);
+        const double t = (double)t32[e];
+        if (t64) t64[e] = t;
+        if (pval) {
+            const double z = t / sqrt(gif[jj]);
+            pval[e] = 2.0 * (0.5 * erfc(fabs(z) / 1.4142135623730951));
+        }
+    }
+}
+
+}  // namespace
+
+void launch_assoc_epilogue(Ctx& c, uint64_t p, const float* u, int ldu, const double* tss,
+                           const AssocConsts& k, double* beta, float* t32, double* r2,
+                           uint32_t* hist) {
+    if (p == 0) return;
+    const size_t smem = (size_t)(2 * k.d * k.w + kEpiSnps * k.w) * sizeof(float);
+    if (smem > 48 * 1024)
+        SLFMM_CUDA(cudaFuncSetAttribute(k_assoc_epilogue, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smem));
+    k_assoc_epilogue<<<(unsigned)ceil_div(p, kEpiSnps), 256, smem, c.stream>>>(
+        p, u, ldu, tss, k.zero_var, k.d, k.w, k.df, k.theta_rows, k.beta_rows, k.cjj, k.dropped,
+        beta, t32, r2, hist);
+    SLFMM_LAUNCHED(c, "k_assoc_epilogue");
+}
+
+void launch_gif(Ctx& c, const uint32_t* hist, int d, double* gif_raw) {
+    if (d == 0) return;
+    k_gif<<<d, 1024, 0, c.stream>>>(hist, gif_raw);
+    SLFMM_LAUNCHED(c, "k_gif");
+}
+
+void launch_calibrate(Ctx& c, uint64_t p, int d, const float* t32, const double* gif, double* t64,
+                      double* pval) {
+    if (p == 0 || d == 0) return;
+    k_calibrate<<<grid_for(c, p * d, 256), 256, 0, c.stream>>>(p, d, t32, gif, t64, pval);
+    SLFMM_LAUNCHED(c, "k_calibrate");
+}
+
+}  // namespace slfmm

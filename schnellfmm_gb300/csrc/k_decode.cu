@@ -1,0 +1,327 @@
+// Stage (a): PLINK 2-bit ingest, allele counting, missing-call lists,
+// per-SNP mean / scale / TSS and standardised decode.
+//
+// Reference behaviour: src/bed.rs:262-395 (decode_raw_single_snp,
+// decode_single_snp, compute_scale), src/parallel.rs:53-71 and :129-146.
+#include <cub/cub.cuh>
+
+#include "slfmm_internal.h"
+
+namespace slfmm {
+
+namespace {
+
+constexpr uint32_t kLo = 0x55555555u;
+
+__device__ __forceinline__ uint32_t code_at(const uint8_t* row, uint64_t s) {
+    return (row[s >> 2] >> ((s & 3) * 2)) & 3u;
+}
+
+// Re-pack `rows` physical SNP rows (in_bps bytes each, contiguous) into the
+// device layout: `stride` bytes per row, samples in sample_keep order (or
+// physical order), codes of samples >= n_out forced to 00.
+__global__ void k_repack(const uint8_t* __restrict__ in, uint64_t rows, uint64_t in_bps,
+                         const uint32_t* __restrict__ keep, uint64_t n_out,
+                         uint8_t* __restrict__ out, uint64_t stride) {
+    const uint64_t words_per_row = stride / 4;
+    const uint64_t total = rows * words_per_row;
+    const uint64_t out_bps = (n_out + 3) / 4;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t r = t / words_per_row;
+        const uint64_t w = t - r * words_per_row;
+        const uint8_t* src = in + r * in_bps;
+        uint32_t word = 0;
+        if (keep == nullptr) {
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const uint64_t byte = w * 4 + b;
+                if (byte < out_bps) {
+                    uint32_t v = src[byte];
+                    if (byte == out_bps - 1 && (n_out & 3)) v &= (1u << (2 * (n_out & 3))) - 1u;
+                    word |= v << (8 * b);
+                }
+            }
+        } else {
+            const uint64_t s0 = w * 16;
+#pragma unroll 4
+            for (int k = 0; k < 16; ++k) {
+                const uint64_t s = s0 + k;
+                if (s < n_out) word |= code_at(src, keep[s]) << (2 * k);
+            }
+        }
+        reinterpret_cast<uint32_t*>(out + r * stride)[w] = word;
+    }
+}
+
+// One warp per SNP: popcount the 2-bit codes.  Padding codes are 00, so c0
+// is derived as n - c1 - c2 - cmiss.
+__global__ void k_snp_counts(const uint8_t* __restrict__ packed, uint64_t p, uint64_t stride,
+                             uint64_t n, int32_t* __restrict__ counts,
+                             uint64_t* __restrict__ miss_count) {
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x & 31;
+    if (warp >= p) return;
+    const uint32_t* row = reinterpret_cast<const uint32_t*>(packed + warp * stride);
+    const uint64_t nwords = (n + 15) / 16;
+    uint32_t c1 = 0, c2 = 0, cm = 0;
+    for (uint64_t w = lane; w < nwords; w += 32) {
+        const uint32_t v = row[w];
+        const uint32_t lo = v & kLo, hi = (v >> 1) & kLo;
+        c1 += __popc(hi & ~lo);
+        c2 += __popc(hi & lo);
+        cm += __popc(~hi & lo);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        c1 += __shfl_xor_sync(0xffffffffu, c1, o);
+        c2 += __shfl_xor_sync(0xffffffffu, c2, o);
+        cm += __shfl_xor_sync(0xffffffffu, cm, o);
+    }
+    if (lane == 0) {
+        counts[warp * 4 + 0] = (int32_t)(n - c1 - c2 - cm);
+        counts[warp * 4 + 1] = (int32_t)c1;
+        counts[warp * 4 + 2] = (int32_t)c2;
+        counts[warp * 4 + 3] = (int32_t)cm;
+        if (miss_count) miss_count[warp] = cm;
+    }
+}
+
+// One warp per SNP: write the ascending sample indices of missing calls.
+__global__ void k_miss_fill(const uint8_t* __restrict__ packed, uint64_t p, uint64_t stride,
+                            uint64_t n, const uint64_t* __restrict__ ptr,
+                            uint32_t* __restrict__ idx, uint32_t* __restrict__ rowid) {
+    const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x & 31;
+    if (warp >= p) return;
+    const uint32_t* row = reinterpret_cast<const uint32_t*>(packed + warp * stride);
+    const uint64_t nwords = (n + 15) / 16;
+    uint64_t base = ptr[warp];
+    for (uint64_t w0 = 0; w0 < nwords; w0 += 32) {
+        const uint64_t w = w0 + lane;
+        uint32_t m = 0;
+        if (w < nwords) {
+            const uint32_t v = row[w];
+            m = ~(v >> 1) & v & kLo;
+        }
+        const uint32_t cnt = __popc(m);
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        uint64_t pos = base + incl - cnt;
+        while (m) {
+            const int b = __ffs(m) - 1;
+            m &= m - 1;
+            idx[pos] = (uint32_t)(w * 16 + (b >> 1));
+            if (rowid) rowid[pos] = (uint32_t)warp;
+            ++pos;
+        }
+        base += total;
+    }
+}
+
+__global__ void k_count_keys(const uint32_t* __restrict__ keys, uint64_t nnz,
+                             uint32_t* __restrict__ cnt) {
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < nnz;
+         t += (uint64_t)gridDim.x * blockDim.x)
+        atomicAdd(&cnt[keys[t]], 1u);
+}
+
+__global__ void k_u32_to_u64(const uint32_t* __restrict__ a, uint64_t m, uint64_t* __restrict__ b) {
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < m;
+         t += (uint64_t)gridDim.x * blockDim.x)
+        b[t] = a[t];
+}
+
+// Per-SNP mean over observed calls, scale and TSS, with the reference's
+// operation order (src/bed.rs:349-361, :382-395) in round-to-nearest FP64
+// intrinsics so that no FMA contraction changes the bits.
+__device__ __forceinline__ double scale_from_mean(double mean, int norm) {
+    const double pp = __ddiv_rn(mean, 2.0);
+    const double twopq = __dmul_rn(__dmul_rn(2.0, pp), __dsub_rn(1.0, pp));
+    if (norm == SLFMM_NORM_CENTER_ONLY) return twopq < 1e-20 ? 0.0 : 1.0;
+    const double denom = __dsqrt_rn(twopq);
+    return denom > 1e-10 ? __ddiv_rn(1.0, denom) : 0.0;
+}
+
+__global__ void k_stats_mean(const int32_t* __restrict__ counts, uint64_t p, int norm,
+                             double* __restrict__ mean, double* __restrict__ scale,
+                             double* __restrict__ tss, uint8_t* __restrict__ zero_var) {
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < p;
+         j += (uint64_t)gridDim.x * blockDim.x) {
+        const int64_t c0 = counts[j * 4 + 0], c1 = counts[j * 4 + 1], c2 = counts[j * 4 + 2];
+        const int64_t nobs = c0 + c1 + c2;
+        const int64_t s1 = c1 + 2 * c2, s2 = c1 + 4 * c2;
+        const double mu = nobs > 0 ? __ddiv_rn((double)s1, (double)nobs) : 0.0;
+        const double sc = scale_from_mean(mu, norm);
+        const int64_t num = nobs * s2 - s1 * s1;  // exact: n_obs * centred sum of squares
+        if (mean) mean[j] = mu;
+        if (scale) scale[j] = sc;
+        if (tss) tss[j] = nobs > 0 ? __dmul_rn(__dmul_rn(sc, sc), __ddiv_rn((double)num, (double)nobs)) : 0.0;
+        if (zero_var) zero_var[j] = (num == 0 || sc == 0.0) ? 1 : 0;
+    }
+}
+
+__global__ void k_decode_chunk(const uint8_t* __restrict__ packed, uint64_t stride, uint64_t n,
+                               uint64_t snp0, uint64_t ncols, const double* __restrict__ mean,
+                               const double* __restrict__ scale, double* __restrict__ out) {
+    const uint64_t total = n * ncols;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = t / ncols, c = t - i * ncols;
+        const uint64_t j = snp0 + c;
+        const uint32_t code = code_at(packed + j * stride, i);
+        double v = 0.0;
+        if (code != 1u) {
+            const double g = code == 0 ? 0.0 : (double)(code - 1);
+            v = __dmul_rn(__dsub_rn(g, mean[j]), scale[j]);
+        }
+        out[t] = v;
+    }
+}
+
+__global__ void k_lut_std(uint64_t p, const double* __restrict__ mean,
+                          const double* __restrict__ scale, float* __restrict__ lut) {
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < p;
+         j += (uint64_t)gridDim.x * blockDim.x) {
+        const double mu = mean[j], sc = scale[j];
+        float4 v;
+        v.x = (float)((0.0 - mu) * sc);
+        v.y = 0.0f;
+        v.z = (float)((1.0 - mu) * sc);
+        v.w = (float)((2.0 - mu) * sc);
+        reinterpret_cast<float4*>(lut)[j] = v;
+    }
+}
+
+__global__ void k_lut_raw(uint64_t p, const double* __restrict__ fill, float* __restrict__ lut) {
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < p;
+         j += (uint64_t)gridDim.x * blockDim.x) {
+        float4 v;
+        v.x = 0.0f;
+        v.y = fill ? (float)fill[j] : 0.0f;
+        v.z = 1.0f;
+        v.w = 2.0f;
+        reinterpret_cast<float4*>(lut)[j] = v;
+    }
+}
+
+}  // namespace
+
+void launch_repack(Ctx& c, const uint8_t* in, uint64_t rows, uint64_t in_bps, uint64_t /*n_phys*/,
+                   const uint32_t* keep, uint64_t n_out, uint8_t* out, uint64_t stride) {
+    if (rows == 0) return;
+    const uint64_t work = rows * (stride / 4);
+    k_repack<<<grid_for(c, work, 256), 256, 0, c.stream>>>(in, rows, in_bps, keep, n_out, out, stride);
+    SLFMM_LAUNCHED(c, "k_repack");
+}
+
+void launch_snp_counts(Ctx& c, const Geno& g, uint64_t* miss_count_out) {
+    if (g.p == 0) return;
+    const int block = 256;
+    const uint64_t grid = ceil_div(g.p * 32, block);
+    k_snp_counts<<<(unsigned)grid, block, 0, c.stream>>>(g.packed.get(), g.p, g.stride, g.n,
+                                                         g.counts.get(), miss_count_out);
+    SLFMM_LAUNCHED(c, "k_snp_counts");
+}
+
+void build_missing_lists(Ctx& c, const Geno& g) {
+    if (g.have_csr) return;
+    DBuf<uint64_t> mc(g.p + 1, c.stream);
+    SLFMM_CUDA(cudaMemsetAsync(mc.get() + g.p, 0, sizeof(uint64_t), c.stream));
+    launch_snp_counts(c, g, mc.get());
+    g.miss_ptr.alloc(g.p + 1, c.stream);
+    size_t tmp_bytes = 0;
+    SLFMM_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, mc.get(), g.miss_ptr.get(),
+                                             (int64_t)(g.p + 1), c.stream));
+    DBuf<uint8_t> tmp(tmp_bytes, c.stream);
+    SLFMM_CUDA(cub::DeviceScan::ExclusiveSum(tmp.get(), tmp_bytes, mc.get(), g.miss_ptr.get(),
+                                             (int64_t)(g.p + 1), c.stream));
+    uint64_t nnz = 0;
+    SLFMM_CUDA(cudaMemcpyAsync(&nnz, g.miss_ptr.get() + g.p, sizeof(uint64_t),
+                               cudaMemcpyDeviceToHost, c.stream));
+    SLFMM_CUDA(cudaStreamSynchronize(c.stream));
+    g.nnz = nnz;
+    g.miss_idx.alloc(std::max<uint64_t>(nnz, 1), c.stream);
+    if (nnz && g.p) {
+        const int block = 256;
+        k_miss_fill<<<(unsigned)ceil_div(g.p * 32, block), block, 0, c.stream>>>(
+            g.packed.get(), g.p, g.stride, g.n, g.miss_ptr.get(), g.miss_idx.get(), nullptr);
+        SLFMM_LAUNCHED(c, "k_miss_fill");
+    }
+    g.have_csr = true;
+}
+
+void build_missing_csc(Ctx& c, const Geno& g) {
+    if (g.have_csc) return;
+    build_missing_lists(c, g);
+    g.missT_ptr.alloc(g.n + 1, c.stream);
+    g.missT_ptr.zero();
+    g.missT_idx.alloc(std::max<uint64_t>(g.nnz, 1), c.stream);
+    if (g.nnz == 0) { g.have_csc = true; return; }
+    SLFMM_REQUIRE(g.nnz < (1ull << 31), SLFMM_ERR_BAD_ARG, "too many missing calls for the sort");
+    DBuf<uint32_t> rowid(g.nnz, c.stream), keys_out(g.nnz, c.stream);
+    const int block = 256;
+    k_miss_fill<<<(unsigned)ceil_div(g.p * 32, block), block, 0, c.stream>>>(
+        g.packed.get(), g.p, g.stride, g.n, g.miss_ptr.get(), keys_out.get(), rowid.get());
+    SLFMM_LAUNCHED(c, "k_miss_fill");
+    int end_bit = 1;
+    while ((1ull << end_bit) < g.n) ++end_bit;
+    size_t tmp_bytes = 0;
+    DBuf<uint32_t> keys_sorted(g.nnz, c.stream);
+    SLFMM_CUDA(cub::DeviceRadixSort::SortPairs(nullptr, tmp_bytes, keys_out.get(), keys_sorted.get(),
+                                               rowid.get(), g.missT_idx.get(), (int64_t)g.nnz, 0,
+                                               end_bit, c.stream));
+    DBuf<uint8_t> tmp(tmp_bytes, c.stream);
+    SLFMM_CUDA(cub::DeviceRadixSort::SortPairs(tmp.get(), tmp_bytes, keys_out.get(), keys_sorted.get(),
+                                               rowid.get(), g.missT_idx.get(), (int64_t)g.nnz, 0,
+                                               end_bit, c.stream));
+    DBuf<uint32_t> cnt(g.n + 1, c.stream);
+    cnt.zero();
+    k_count_keys<<<grid_for(c, g.nnz, 256), 256, 0, c.stream>>>(keys_sorted.get(), g.nnz, cnt.get());
+    SLFMM_LAUNCHED(c, "k_count_keys");
+    DBuf<uint64_t> cnt64(g.n + 1, c.stream);
+    k_u32_to_u64<<<grid_for(c, g.n + 1, 256), 256, 0, c.stream>>>(cnt.get(), g.n + 1, cnt64.get());
+    SLFMM_LAUNCHED(c, "k_u32_to_u64");
+    size_t tb2 = 0;
+    SLFMM_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tb2, cnt64.get(), g.missT_ptr.get(),
+                                             (int64_t)(g.n + 1), c.stream));
+    DBuf<uint8_t> tmp2(tb2, c.stream);
+    SLFMM_CUDA(cub::DeviceScan::ExclusiveSum(tmp2.get(), tb2, cnt64.get(), g.missT_ptr.get(),
+                                             (int64_t)(g.n + 1), c.stream));
+    g.have_csc = true;
+}
+
+void launch_stats_mean(Ctx& c, const Geno& g, int norm, double* mean, double* scale, double* tss,
+                       uint8_t* zero_var) {
+    if (g.p == 0) return;
+    k_stats_mean<<<grid_for(c, g.p, 256), 256, 0, c.stream>>>(g.counts.get(), g.p, norm, mean,
+                                                              scale, tss, zero_var);
+    SLFMM_LAUNCHED(c, "k_stats_mean");
+}
+
+void launch_decode_chunk(Ctx& c, const Geno& g, uint64_t snp0, uint64_t ncols, const double* mean,
+                         const double* scale, double* out) {
+    if (ncols == 0 || g.n == 0) return;
+    k_decode_chunk<<<grid_for(c, g.n * ncols, 256), 256, 0, c.stream>>>(
+        g.packed.get(), g.stride, g.n, snp0, ncols, mean, scale, out);
+    SLFMM_LAUNCHED(c, "k_decode_chunk");
+}
+
+void launch_lut_std(Ctx& c, uint64_t p, const double* mean, const double* scale, float* lut) {
+    if (p == 0) return;
+    k_lut_std<<<grid_for(c, p, 256), 256, 0, c.stream>>>(p, mean, scale, lut);
+    SLFMM_LAUNCHED(c, "k_lut_std");
+}
+
+void launch_lut_raw(Ctx& c, uint64_t p, const double* fill, float* lut) {
+    if (p == 0) return;
+    k_lut_raw<<<grid_for(c, p, 256), 256, 0, c.stream>>>(p, fill, lut);
+    SLFMM_LAUNCHED(c, "k_lut_raw");
+}
+
+}  // namespace slfmm

@@ -1,0 +1,705 @@
+// FP64 dense helpers for the small / tall-skinny linear algebra of the path:
+// covariate centring (src/lib.rs:102-117), Step 0 (src/precompute.rs:30-88),
+// Cholesky-QR2 of the sketches (replacing the LAPACK QR of
+// src/rsvd.rs:75,105,131), the small SVD (src/rsvd.rs:162, src/nmf.rs:321)
+// and safe_inv (src/testing.rs:996-1024).  GB300's FP64 rate is low, so
+// these only ever touch n x w, w x w or p x w objects with tiny w.
+#include "slfmm_internal.h"
+
+namespace slfmm {
+namespace {
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// block-wide sum with a fixed reduction order (deterministic)
+__device__ double block_sum(double v, double* red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    v = warp_sum(v);
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    const int nw = (blockDim.x + 31) >> 5;
+    double t = 0.0;
+    if (wid == 0) {
+        t = lane < nw ? red[lane] : 0.0;
+        t = warp_sum(t);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) red[0] = t;
+    __syncthreads();
+    const double r = red[0];
+    __syncthreads();
+    return r;
+}
+
+__global__ void k_colmeans(const double* __restrict__ A, uint64_t m, int lda, double* __restrict__ out) {
+    __shared__ double red[32];
+    const int col = blockIdx.x;
+    double s = 0.0;
+    for (uint64_t i = threadIdx.x; i < m; i += blockDim.x) s += A[i * lda + col];
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) out[col] = m ? s / (double)m : 0.0;
+}
+
+__global__ void k_center_cols(double* __restrict__ A, uint64_t m, int a, int lda,
+                              const double* __restrict__ means) {
+    const uint64_t total = m * a;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = t / a;
+        const int c = (int)(t - i * a);
+        A[i * lda + c] -= means[c];
+    }
+}
+
+// divide a column by its sample sd (n-1 denominator) unless sd <= 1e-14
+__global__ void k_scale_cols_sd(double* __restrict__ A, uint64_t m, int lda) {
+    __shared__ double red[32];
+    const int col = blockIdx.x;
+    double s = 0.0;
+    for (uint64_t i = threadIdx.x; i < m; i += blockDim.x) {
+        const double v = A[i * lda + col];
+        s += v * v;
+    }
+    s = block_sum(s, red);
+    const double sd = sqrt(s / ((double)m - 1.0));
+    if (sd > 1e-14)
+        for (uint64_t i = threadIdx.x; i < m; i += blockDim.x) A[i * lda + col] /= sd;
+}
+
+// Tiled A^T B over a row range: 32x32 output tile per CTA, 16x16 threads,
+// FP64 accumulation; partial[split] written, reduced by k_sum_partials.
+template <typename T>
+__global__ void __launch_bounds__(256) k_atb(const T* __restrict__ A, int lda, const T* __restrict__ B,
+                                             int ldb, uint64_t m, int a, int b, uint64_t rows_per_split,
+                                             double* __restrict__ part) {
+    __shared__ double As[32][33];
+    __shared__ double Bs[32][33];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+    const uint64_t i0 = (uint64_t)blockIdx.z * rows_per_split;
+    const uint64_t i1 = min(m, i0 + rows_per_split);
+    double acc[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
+    for (uint64_t ib = i0; ib < i1; ib += 32) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < 32 * 32; e += 256) {
+            const int ii = e >> 5, cc = e & 31;
+            const uint64_t i = ib + ii;
+            As[ii][cc] = (i < i1 && r0 + cc < a) ? (double)A[i * lda + r0 + cc] : 0.0;
+            Bs[ii][cc] = (i < i1 && c0 + cc < b) ? (double)B[i * ldb + c0 + cc] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int ii = 0; ii < 32; ++ii) {
+            const double a0 = As[ii][ty], a1 = As[ii][ty + 16];
+            const double b0 = Bs[ii][tx], b1 = Bs[ii][tx + 16];
+            acc[0][0] = fma(a0, b0, acc[0][0]);
+            acc[0][1] = fma(a0, b1, acc[0][1]);
+            acc[1][0] = fma(a1, b0, acc[1][0]);
+            acc[1][1] = fma(a1, b1, acc[1][1]);
+        }
+    }
+    double* dst = part + (uint64_t)blockIdx.z * a * b;
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+#pragma unroll
+        for (int v = 0; v < 2; ++v) {
+            const int r = r0 + ty + 16 * u, cc = c0 + tx + 16 * v;
+            if (r < a && cc < b) dst[r * b + cc] = acc[u][v];
+        }
+}
+
+// FP32 Gram with FP32 products summed over 32-row tiles and FP64 across
+// tiles (used for the p x l sketches, whose FP64 Gram would dominate).
+__global__ void __launch_bounds__(256) k_gram_f32(const float* __restrict__ A, int lda, uint64_t m, int a,
+                                                  uint64_t rows_per_split, double* __restrict__ part) {
+    __shared__ float As[32][33];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int r0 = blockIdx.x * 32, c0 = blockIdx.y * 32;
+    const uint64_t i0 = (uint64_t)blockIdx.z * rows_per_split;
+    const uint64_t i1 = min(m, i0 + rows_per_split);
+    __shared__ float Bs[32][33];
+    double acc[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
+    for (uint64_t ib = i0; ib < i1; ib += 32) {
+        __syncthreads();
+        for (int e = threadIdx.x; e < 32 * 32; e += 256) {
+            const int ii = e >> 5, cc = e & 31;
+            const uint64_t i = ib + ii;
+            As[ii][cc] = (i < i1 && r0 + cc < a) ? A[i * lda + r0 + cc] : 0.f;
+            Bs[ii][cc] = (i < i1 && c0 + cc < a) ? A[i * lda + c0 + cc] : 0.f;
+        }
+        __syncthreads();
+        float t[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll 8
+        for (int ii = 0; ii < 32; ++ii) {
+            const float a0 = As[ii][ty], a1 = As[ii][ty + 16];
+            const float b0 = Bs[ii][tx], b1 = Bs[ii][tx + 16];
+            t[0][0] = fmaf(a0, b0, t[0][0]);
+            t[0][1] = fmaf(a0, b1, t[0][1]);
+            t[1][0] = fmaf(a1, b0, t[1][0]);
+            t[1][1] = fmaf(a1, b1, t[1][1]);
+        }
+#pragma unroll
+        for (int u = 0; u < 2; ++u)
+#pragma unroll
+            for (int v = 0; v < 2; ++v) acc[u][v] += (double)t[u][v];
+    }
+    double* dst = part + (uint64_t)blockIdx.z * a * a;
+#pragma unroll
+    for (int u = 0; u < 2; ++u)
+#pragma unroll
+        for (int v = 0; v < 2; ++v) {
+            const int r = r0 + ty + 16 * u, cc = c0 + tx + 16 * v;
+            if (r < a && cc < a) dst[r * a + cc] = acc[u][v];
+        }
+}
+
+__global__ void k_sum_partials(const double* __restrict__ part, int splits, uint64_t count,
+                               double* __restrict__ out) {
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < count;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        double s = 0.0;
+        for (int k = 0; k < splits; ++k) s += part[(uint64_t)k * count + t];
+        out[t] = s;
+    }
+}
+
+// C = alpha * A B + beta * C with A (m x a), B (a x b) small; one thread per output.
+template <typename TO>
+__global__ void k_gemm_small(const double* __restrict__ A, int lda, uint64_t m, int a,
+                             const double* __restrict__ B, int ldb, int b, double alpha, double beta,
+                             TO* __restrict__ C, int ldc) {
+    extern __shared__ double Bsm[];  // a x b
+    for (int e = threadIdx.x; e < a * b; e += blockDim.x) Bsm[e] = B[(e / b) * ldb + (e % b)];
+    __syncthreads();
+    const uint64_t total = m * b;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = t / b;
+        const int cc = (int)(t - i * b);
+        double s = 0.0;
+        const double* ar = A + i * lda;
+        for (int k = 0; k < a; ++k) s = fma(ar[k], Bsm[k * b + cc], s);
+        const double prev = beta != 0.0 ? (double)C[i * ldc + cc] : 0.0;
+        C[i * ldc + cc] = (TO)(alpha * s + beta * prev);
+    }
+}
+
+// A (m x a, FP32) <- A * Linv^T with Linv lower-triangular (a x a, FP64),
+// i.e. A <- A R^-1 for the Cholesky factor R = L^T of A^T A.
+__global__ void k_trmul_f32(float* __restrict__ A, int lda, uint64_t m, int a,
+                            const double* __restrict__ Linv) {
+    __shared__ float R[64 * 64];  // R[k][c] = Linv[c][k]
+    for (int e = threadIdx.x; e < a * a; e += blockDim.x) R[(e % a) * a + e / a] = (float)Linv[e];
+    __syncthreads();
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        float row[64];
+        float* ar = A + i * lda;
+        for (int k = 0; k < a; ++k) row[k] = ar[k];
+        for (int cc = a - 1; cc >= 0; --cc) {
+            float s = 0.f;
+            for (int k = 0; k <= cc; ++k) s = fmaf(row[k], R[k * a + cc], s);
+            ar[cc] = s;
+        }
+    }
+}
+
+// In-place Cholesky (lower) of an a x a SPD matrix in one CTA.  status[0] =
+// number of pivots that were not positive (replaced by a tiny positive value).
+// With drop_tol >= 0 a column whose residual pivot is <= drop_tol times its
+// original diagonal is dropped instead: L_kk = 1, L_ik = 0, dropped[k] = 1
+// (rank-deficient design columns).  status[0] counts replaced/dropped pivots.
+__global__ void k_cholesky(double* __restrict__ G, int a, int* __restrict__ status,
+                           double drop_tol, int* __restrict__ dropped) {
+    extern __shared__ double S[];
+    __shared__ double piv;
+    __shared__ int bad;
+    __shared__ int drop_k;
+    for (int e = threadIdx.x; e < a * a; e += blockDim.x) S[e] = G[e];
+    if (threadIdx.x == 0) bad = 0;
+    __syncthreads();
+    double dmax = 0.0;
+    for (int k = 0; k < a; ++k) dmax = fmax(dmax, fabs(S[k * a + k]));
+    for (int k = 0; k < a; ++k) {
+        if (threadIdx.x == 0) {
+            double v = S[k * a + k];
+            drop_k = 0;
+            if (drop_tol >= 0.0) {
+                if (!(v > drop_tol * fabs(G[k * a + k])) || !(v > 1e-300)) { drop_k = 1; ++bad; v = 1.0; }
+            } else if (!(v > 1e-300 + 1e-28 * dmax)) {
+                v = 1e-28 * dmax + 1e-300;
+                ++bad;
+            }
+            if (dropped) dropped[k] = drop_k;
+            piv = sqrt(v);
+            S[k * a + k] = piv;
+        }
+        __syncthreads();
+        for (int i = k + 1 + threadIdx.x; i < a; i += blockDim.x) S[i * a + k] = drop_k ? 0.0 : S[i * a + k] / piv;
+        __syncthreads();
+        const int rem = a - k - 1;
+        for (int e = threadIdx.x; e < rem * rem; e += blockDim.x) {
+            const int i = k + 1 + e / rem, j = k + 1 + e % rem;
+            if (j <= i) S[i * a + j] -= S[i * a + k] * S[j * a + k];
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < a * a; e += blockDim.x) {
+        const int i = e / a, j = e % a;
+        G[e] = j <= i ? S[e] : 0.0;
+    }
+    if (threadIdx.x == 0 && status) status[0] = bad;
+}
+
+// Inverse of a lower-triangular matrix: one thread per column.
+__global__ void k_tri_inv_lower(const double* __restrict__ L, int a, double* __restrict__ X) {
+    extern __shared__ double S[];
+    for (int e = threadIdx.x; e < a * a; e += blockDim.x) S[e] = L[e];
+    __syncthreads();
+    for (int cc = threadIdx.x; cc < a; cc += blockDim.x) {
+        for (int i = 0; i < cc; ++i) X[i * a + cc] = 0.0;
+        for (int i = cc; i < a; ++i) {
+            double s = (i == cc) ? 1.0 : 0.0;
+            for (int k = cc; k < i; ++k) s -= S[i * a + k] * X[k * a + cc];
+            X[i * a + cc] = s / S[i * a + i];
+        }
+    }
+}
+
+// LU with partial pivoting in smem; returns 0 if an exactly zero pivot was met.
+__device__ bool lu_smem(double* S, int* piv, int a) {
+    __shared__ int p_sh;
+    __shared__ int ok;
+    if (threadIdx.x == 0) ok = 1;
+    __syncthreads();
+    for (int k = 0; k < a; ++k) {
+        if (threadIdx.x == 0) {
+            int p = k;
+            double best = fabs(S[k * a + k]);
+            for (int i = k + 1; i < a; ++i) {
+                const double v = fabs(S[i * a + k]);
+                if (v > best) { best = v; p = i; }
+            }
+            p_sh = p;
+            piv[k] = p;
+            if (best == 0.0) ok = 0;
+        }
+        __syncthreads();
+        if (!ok) return false;
+        const int p = p_sh;
+        if (p != k)
+            for (int j = threadIdx.x; j < a; j += blockDim.x) {
+                const double t = S[k * a + j];
+                S[k * a + j] = S[p * a + j];
+                S[p * a + j] = t;
+            }
+        __syncthreads();
+        const double d = S[k * a + k];
+        for (int i = k + 1 + threadIdx.x; i < a; i += blockDim.x) S[i * a + k] /= d;
+        __syncthreads();
+        const int rem = a - k - 1;
+        for (int e = threadIdx.x; e < rem * rem; e += blockDim.x) {
+            const int i = k + 1 + e / rem, j = k + 1 + e % rem;
+            S[i * a + j] -= S[i * a + k] * S[k * a + j];
+        }
+        __syncthreads();
+    }
+    return true;
+}
+
+// safe_inv (src/testing.rs:996-1024): invert; on an exactly zero pivot add
+// eps = 1e-8 * max(max|diag|, 1e-300) to the diagonal and retry.
+// status: 0 ok, 1 regularised, 2 failed.  eps_used[0] = eps (0 if none).
+__global__ void k_inverse(const double* __restrict__ A, int a, double* __restrict__ X,
+                          int* __restrict__ status, double* __restrict__ eps_used) {
+    extern __shared__ double S[];
+    __shared__ int piv[kMaxSmall];
+    __shared__ double eps;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        if (threadIdx.x == 0) {
+            double dmax = 0.0;
+            for (int k = 0; k < a; ++k) dmax = fmax(dmax, fabs(A[k * a + k]));
+            dmax = fmax(dmax, 1e-300);
+            eps = attempt == 0 ? 0.0 : 1e-8 * dmax;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < a * a; e += blockDim.x)
+            S[e] = A[e] + ((e / a == e % a) ? eps : 0.0);
+        __syncthreads();
+        if (lu_smem(S, piv, a)) {
+            // solve for each unit vector: one thread per column
+            for (int cc = threadIdx.x; cc < a; cc += blockDim.x) {
+                double* x = X;  // column cc written strided
+                // b = P e_cc
+                for (int i = 0; i < a; ++i) x[i * a + cc] = (i == cc) ? 1.0 : 0.0;
+                for (int k = 0; k < a; ++k) {
+                    const int p = piv[k];
+                    if (p != k) {
+                        const double t = x[k * a + cc];
+                        x[k * a + cc] = x[p * a + cc];
+                        x[p * a + cc] = t;
+                    }
+                }
+                for (int i = 0; i < a; ++i) {
+                    double s = x[i * a + cc];
+                    for (int k = 0; k < i; ++k) s -= S[i * a + k] * x[k * a + cc];
+                    x[i * a + cc] = s;
+                }
+                for (int i = a - 1; i >= 0; --i) {
+                    double s = x[i * a + cc];
+                    for (int k = i + 1; k < a; ++k) s -= S[i * a + k] * x[k * a + cc];
+                    x[i * a + cc] = s / S[i * a + i];
+                }
+            }
+            if (threadIdx.x == 0) {
+                if (status) status[0] = attempt;
+                if (eps_used) eps_used[0] = eps;
+            }
+            return;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        if (status) status[0] = 2;
+        if (eps_used) eps_used[0] = eps;
+    }
+}
+
+// One-sided (Hestenes) Jacobi SVD of a square a x a matrix (a <= 64) in one
+// CTA: A V = U diag(sig).  Outputs V (a x a), sig (descending) and U = A V
+// / sig in place of A.  Pairs are rotated in parallel with a round-robin
+// ordering, one warp per pair.
+__global__ void __launch_bounds__(1024) k_jacobi_svd(double* __restrict__ A, int a,
+                                                     double* __restrict__ V, double* __restrict__ sig) {
+    extern __shared__ double sm[];
+    const int ap = a + (a & 1);     // even number of columns (padded column is zero)
+    double* M = sm;                 // column-major ap x ap (rows a used)
+    double* Vs = sm + ap * ap;      // column-major
+    __shared__ int pairs[64];
+    __shared__ int rotated;
+    __shared__ double sg[64];
+    __shared__ int order[64];
+    for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) {
+        const int col = e / ap, row = e % ap;
+        M[e] = (row < a && col < a) ? A[row * a + col] : 0.0;
+        Vs[e] = (row == col) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    const int npairs = ap / 2;
+    for (int sweep = 0; sweep < 60; ++sweep) {
+        if (threadIdx.x == 0) rotated = 0;
+        __syncthreads();
+        for (int round = 0; round < ap - 1; ++round) {
+            if (threadIdx.x < npairs) {
+                // round-robin tournament: player 0 fixed, others rotate
+                const int k = threadIdx.x;
+                auto pos = [&](int idx) { return idx == 0 ? 0 : 1 + ((idx - 1 + round) % (ap - 1)); };
+                pairs[2 * k] = pos(k);
+                pairs[2 * k + 1] = pos(ap - 1 - k);
+            }
+            __syncthreads();
+            for (int pr = warp; pr < npairs; pr += nwarps) {
+                int pcol = pairs[2 * pr], qcol = pairs[2 * pr + 1];
+                if (pcol > qcol) { const int t = pcol; pcol = qcol; qcol = t; }
+                double* mp = M + pcol * ap;
+                double* mq = M + qcol * ap;
+                double al = 0.0, be = 0.0, ga = 0.0;
+                for (int r = lane; r < a; r += 32) {
+                    al += mp[r] * mp[r];
+                    be += mq[r] * mq[r];
+                    ga += mp[r] * mq[r];
+                }
+                al = warp_sum(al);
+                be = warp_sum(be);
+                ga = warp_sum(ga);
+                if (fabs(ga) > 1e-15 * sqrt(al * be) && fabs(ga) > 1e-300) {
+                    const double zeta = (be - al) / (2.0 * ga);
+                    const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                    const double cs = 1.0 / sqrt(1.0 + t * t), sn = cs * t;
+                    for (int r = lane; r < ap; r += 32) {
+                        const double x = mp[r], y = mq[r];
+                        mp[r] = cs * x - sn * y;
+                        mq[r] = sn * x + cs * y;
+                        double* vp = Vs + pcol * ap;
+                        double* vq = Vs + qcol * ap;
+                        const double vx = vp[r], vy = vq[r];
+                        vp[r] = cs * vx - sn * vy;
+                        vq[r] = sn * vx + cs * vy;
+                    }
+                    if (lane == 0) rotated = 1;
+                }
+            }
+            __syncthreads();
+        }
+        if (!rotated) break;
+        __syncthreads();
+    }
+    // singular values and descending order
+    for (int cc = warp; cc < a; cc += nwarps) {
+        double s = 0.0;
+        for (int r = lane; r < a; r += 32) s += M[cc * ap + r] * M[cc * ap + r];
+        s = warp_sum(s);
+        if (lane == 0) sg[cc] = sqrt(s);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int i = 0; i < a; ++i) order[i] = i;
+        for (int i = 0; i < a; ++i) {
+            int best = i;
+            for (int j = i + 1; j < a; ++j)
+                if (sg[order[j]] > sg[order[best]]) best = j;
+            const int t = order[i]; order[i] = order[best]; order[best] = t;
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < a * a; e += blockDim.x) {
+        const int row = e / a, cc = e % a;
+        const int src = order[cc];
+        V[row * a + cc] = Vs[src * ap + row];
+        const double s = sg[src];
+        A[row * a + cc] = s > 0.0 ? M[src * ap + row] / s : 0.0;
+    }
+    for (int cc = threadIdx.x; cc < a; cc += blockDim.x) sig[cc] = sg[order[cc]];
+}
+
+// SplitMix64 counter RNG + Box-Muller (identical stream definition in the
+// CPU oracle): element (i, c) of a rows x cols matrix is draw i*cols+c.
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+__global__ void k_normal(uint64_t seed, uint64_t total, double* __restrict__ out) {
+    const uint64_t key = mix64(seed + 0x9E3779B97F4A7C15ull);
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t a = mix64(key + (2 * t + 1) * 0x9E3779B97F4A7C15ull);
+        const uint64_t b = mix64(key + (2 * t + 2) * 0x9E3779B97F4A7C15ull);
+        const double u1 = ((double)(a >> 11) + 1.0) * 0x1.0p-53;
+        const double u2 = (double)(b >> 11) * 0x1.0p-53;
+        out[t] = sqrt(-2.0 * log(u1)) * cospi(2.0 * u2);
+    }
+}
+
+__global__ void k_f64_to_f32_pad(const double* __restrict__ A, uint64_t m, int a, int lda,
+                                 float* __restrict__ out, uint64_t m_pad, int ldo) {
+    const uint64_t total = m_pad * ldo;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = t / ldo;
+        const int cc = (int)(t - i * ldo);
+        out[t] = (i < m && cc < a) ? (float)A[i * lda + cc] : 0.f;
+    }
+}
+
+__global__ void k_f32_to_f64(const float* __restrict__ A, uint64_t m, int a, int lda,
+                             double* __restrict__ out, int ldo) {
+    const uint64_t total = m * a;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = t / a;
+        const int cc = (int)(t - i * a);
+        out[i * ldo + cc] = (double)A[i * lda + cc];
+    }
+}
+
+__global__ void k_transpose(const double* __restrict__ A, int rows, int cols, double* __restrict__ At) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < rows * cols; e += gridDim.x * blockDim.x) {
+        const int i = e / cols, j = e % cols;
+        At[j * rows + i] = A[e];
+    }
+}
+
+__global__ void k_scale_cols(double* __restrict__ A, uint64_t m, int a, int lda,
+                             const double* __restrict__ f) {
+    const uint64_t total = m * a;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = t / a;
+        const int cc = (int)(t - i * a);
+        A[i * lda + cc] *= f[cc];
+    }
+}
+
+// C = [1 | X | U] (n x (1+d+K))
+__global__ void k_build_design(const double* __restrict__ X, int d, const double* __restrict__ U, int K,
+                               uint64_t n, double* __restrict__ C) {
+    const int w = 1 + d + K;
+    const uint64_t total = n * w;
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t i = t / w;
+        const int cc = (int)(t - i * w);
+        C[t] = cc == 0 ? 1.0 : (cc <= d ? X[i * d + cc - 1] : U[i * K + cc - 1 - d]);
+    }
+}
+
+size_t smem_sq(int a) { return (size_t)a * a * sizeof(double); }
+
+void set_smem(const void* fn, size_t bytes) {
+    if (bytes > 48 * 1024)
+        SLFMM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+}
+
+}  // namespace
+
+void launch_colmeans(Ctx& c, const double* A, uint64_t m, int a, int lda, double* out) {
+    if (a == 0) return;
+    k_colmeans<<<a, 256, 0, c.stream>>>(A, m, lda, out);
+    SLFMM_LAUNCHED(c, "k_colmeans");
+}
+
+void launch_center_cols(Ctx& c, double* A, uint64_t m, int a, int lda, const double* means) {
+    if (a == 0 || m == 0) return;
+    k_center_cols<<<grid_for(c, m * a, 256), 256, 0, c.stream>>>(A, m, a, lda, means);
+    SLFMM_LAUNCHED(c, "k_center_cols");
+}
+
+void launch_scale_cols_sd(Ctx& c, double* A, uint64_t m, int a, int lda) {
+    if (a == 0) return;
+    k_scale_cols_sd<<<a, 256, 0, c.stream>>>(A, m, lda);
+    SLFMM_LAUNCHED(c, "k_scale_cols_sd");
+}
+
+template <typename T>
+static void atb_impl(Ctx& c, const T* A, int lda, const T* B, int ldb, uint64_t m, int a, int b,
+                     double* out) {
+    const int ta = (int)ceil_div(a, 32), tb = (int)ceil_div(b, 32);
+    uint64_t splits = std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(m, 2048),
+                                          ceil_div((uint64_t)c.sm_count * 4, (uint64_t)ta * tb)));
+    splits = std::min<uint64_t>(splits, 65535);
+    const uint64_t per = round_up(ceil_div(std::max<uint64_t>(m, 1), splits), 32);
+    splits = std::max<uint64_t>(1, ceil_div(m, per));
+    DBuf<double> part(splits * a * b, c.stream);
+    dim3 grid(ta, tb, (unsigned)splits);
+    k_atb<T><<<grid, 256, 0, c.stream>>>(A, lda, B, ldb, m, a, b, per, part.get());
+    SLFMM_LAUNCHED(c, "k_atb");
+    k_sum_partials<<<grid_for(c, (uint64_t)a * b, 256), 256, 0, c.stream>>>(part.get(), (int)splits,
+                                                                            (uint64_t)a * b, out);
+    SLFMM_LAUNCHED(c, "k_sum_partials");
+}
+
+void launch_atb(Ctx& c, const double* A, int lda, const double* B, int ldb, uint64_t m, int a, int b,
+                double* out) {
+    atb_impl<double>(c, A, lda, B, ldb, m, a, b, out);
+}
+
+void launch_gram_f32(Ctx& c, const float* A, int lda, uint64_t m, int a, double* out) {
+    const int ta = (int)ceil_div(a, 32);
+    uint64_t splits = std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(m, 4096),
+                                          ceil_div((uint64_t)c.sm_count * 4, (uint64_t)ta * ta)));
+    splits = std::min<uint64_t>(splits, 65535);
+    const uint64_t per = round_up(ceil_div(std::max<uint64_t>(m, 1), splits), 32);
+    splits = std::max<uint64_t>(1, ceil_div(m, per));
+    DBuf<double> part(splits * a * a, c.stream);
+    dim3 grid(ta, ta, (unsigned)splits);
+    k_gram_f32<<<grid, 256, 0, c.stream>>>(A, lda, m, a, per, part.get());
+    SLFMM_LAUNCHED(c, "k_gram_f32");
+    k_sum_partials<<<grid_for(c, (uint64_t)a * a, 256), 256, 0, c.stream>>>(part.get(), (int)splits,
+                                                                            (uint64_t)a * a, out);
+    SLFMM_LAUNCHED(c, "k_sum_partials");
+}
+
+void launch_gemm_small(Ctx& c, const double* A, int lda, uint64_t m, int a, const double* B, int ldb,
+                       int b, double alpha, double beta, double* C, int ldc) {
+    if (m == 0 || b == 0) return;
+    const size_t sm = (size_t)a * b * sizeof(double);
+    set_smem((const void*)k_gemm_small<double>, sm);
+    k_gemm_small<double><<<grid_for(c, m * b, 256), 256, sm, c.stream>>>(A, lda, m, a, B, ldb, b, alpha,
+                                                                         beta, C, ldc);
+    SLFMM_LAUNCHED(c, "k_gemm_small");
+}
+
+void launch_gemm_small_f32out(Ctx& c, const double* A, int lda, uint64_t m, int a, const double* B,
+                              int ldb, int b, float* C, int ldc) {
+    if (m == 0 || b == 0) return;
+    const size_t sm = (size_t)a * b * sizeof(double);
+    set_smem((const void*)k_gemm_small<float>, sm);
+    k_gemm_small<float><<<grid_for(c, m * b, 256), 256, sm, c.stream>>>(A, lda, m, a, B, ldb, b, 1.0,
+                                                                        0.0, C, ldc);
+    SLFMM_LAUNCHED(c, "k_gemm_small");
+}
+
+void launch_trmul_f32(Ctx& c, float* A, int lda, uint64_t m, int a, const double* Rinv) {
+    SLFMM_REQUIRE(a <= 64, SLFMM_ERR_BAD_ARG, "sketch width must be <= 64");
+    if (m == 0) return;
+    k_trmul_f32<<<grid_for(c, m, 128), 128, 0, c.stream>>>(A, lda, m, a, Rinv);
+    SLFMM_LAUNCHED(c, "k_trmul_f32");
+}
+
+void launch_cholesky(Ctx& c, double* A, int a, int* status, double drop_tol, int* dropped) {
+    SLFMM_REQUIRE(a <= kMaxSmall, SLFMM_ERR_BAD_ARG, "matrix too large for the small Cholesky");
+    set_smem((const void*)k_cholesky, smem_sq(a));
+    k_cholesky<<<1, 512, smem_sq(a), c.stream>>>(A, a, status, drop_tol, dropped);
+    SLFMM_LAUNCHED(c, "k_cholesky");
+}
+
+void launch_tri_inv_lower(Ctx& c, const double* L, int a, double* Linv) {
+    SLFMM_REQUIRE(a <= kMaxSmall, SLFMM_ERR_BAD_ARG, "matrix too large for the triangular inverse");
+    set_smem((const void*)k_tri_inv_lower, smem_sq(a));
+    k_tri_inv_lower<<<1, 128, smem_sq(a), c.stream>>>(L, a, Linv);
+    SLFMM_LAUNCHED(c, "k_tri_inv_lower");
+}
+
+void launch_inverse(Ctx& c, const double* A, int a, double* Ainv, int* status, double* eps_used) {
+    SLFMM_REQUIRE(a <= kMaxSmall, SLFMM_ERR_BAD_ARG, "matrix too large for the small inverse");
+    set_smem((const void*)k_inverse, smem_sq(a));
+    k_inverse<<<1, 256, smem_sq(a), c.stream>>>(A, a, Ainv, status, eps_used);
+    SLFMM_LAUNCHED(c, "k_inverse");
+}
+
+void launch_jacobi_svd(Ctx& c, const double* A, int a, double* V, double* sig) {
+    SLFMM_REQUIRE(a <= 64, SLFMM_ERR_BAD_ARG, "Jacobi SVD limited to 64 x 64");
+    const int ap = a + (a & 1);
+    const size_t sm = 2 * (size_t)ap * ap * sizeof(double);
+    set_smem((const void*)k_jacobi_svd, sm);
+    k_jacobi_svd<<<1, 1024, sm, c.stream>>>(const_cast<double*>(A), a, V, sig);
+    SLFMM_LAUNCHED(c, "k_jacobi_svd");
+}
+
+void launch_transpose(Ctx& c, const double* A, int rows, int cols, double* At) {
+    if (!rows || !cols) return;
+    k_transpose<<<grid_for(c, (uint64_t)rows * cols, 256), 256, 0, c.stream>>>(A, rows, cols, At);
+    SLFMM_LAUNCHED(c, "k_transpose");
+}
+
+void launch_scale_cols(Ctx& c, double* A, uint64_t m, int a, int lda, const double* f) {
+    if (!m || !a) return;
+    k_scale_cols<<<grid_for(c, m * a, 256), 256, 0, c.stream>>>(A, m, a, lda, f);
+    SLFMM_LAUNCHED(c, "k_scale_cols");
+}
+
+void launch_build_design(Ctx& c, const double* X, int d, const double* U, int K, uint64_t n, double* C) {
+    if (!n) return;
+    k_build_design<<<grid_for(c, n * (1 + d + K), 256), 256, 0, c.stream>>>(X, d, U, K, n, C);
+    SLFMM_LAUNCHED(c, "k_build_design");
+}
+
+void launch_normal(Ctx& c, uint64_t seed, uint64_t rows, int cols, double* out) {
+    const uint64_t total = rows * cols;
+    if (!total) return;
+    k_normal<<<grid_for(c, total, 256), 256, 0, c.stream>>>(seed, total, out);
+    SLFMM_LAUNCHED(c, "k_normal");
+}
+
+void launch_f64_to_f32_pad(Ctx& c, const double* A, uint64_t m, int a, int lda, float* out,
+                           uint64_t m_pad, int ldo) {
+    if (!m_pad || !ldo) return;
+    k_f64_to_f32_pad<<<grid_for(c, m_pad * ldo, 256), 256, 0, c.stream>>>(A, m, a, lda, out, m_pad, ldo);
+    SLFMM_LAUNCHED(c, "k_f64_to_f32_pad");
+}
+
+void launch_f32_to_f64(Ctx& c, const float* A, uint64_t m, int a, int lda, double* out, int ldo) {
+    if (!m || !a) return;
+    k_f32_to_f64<<<grid_for(c, m * a, 256), 256, 0, c.stream>>>(A, m, a, lda, out, ldo);
+    SLFMM_LAUNCHED(c, "k_f32_to_f64");
+}
+
+}  // namespace slfmm

@@ -1,0 +1,218 @@
+// Internal declarations of the schnelgpu runtime (host C++ + sm_103a kernels).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/schnelgpu.h"
+
+namespace slfmm {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+struct Error : std::runtime_error {
+    int code;
+    Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define SLFMM_CUDA(call)                                                          \
+    do {                                                                          \
+        cudaError_t e_ = (call);                                                  \
+        if (e_ != cudaSuccess)                                                    \
+            throw ::slfmm::Error(SLFMM_ERR_CUDA, std::string(#call) + ": " +     \
+                                 cudaGetErrorString(e_));                        \
+    } while (0)
+
+#define SLFMM_REQUIRE(cond, code, msg)                                            \
+    do {                                                                          \
+        if (!(cond)) throw ::slfmm::Error((code), (msg));                         \
+    } while (0)
+
+// ---------------------------------------------------------------------------
+// constants shared by host and device
+// ---------------------------------------------------------------------------
+constexpr int kHistBins = 100000;      // src/testing.rs:124
+constexpr double kHistWidth = 0.001;   // src/testing.rs:125
+constexpr double kGifDivisor = 0.4549; // src/testing.rs:169
+constexpr int kMaxW = 128;             // widest GEMM operand (columns)
+constexpr int kMaxSmall = 128;         // largest small dense matrix (w x w)
+
+inline uint64_t round_up(uint64_t x, uint64_t m) { return (x + m - 1) / m * m; }
+inline uint64_t ceil_div(uint64_t x, uint64_t m) { return (x + m - 1) / m; }
+
+// ---------------------------------------------------------------------------
+// device buffers (stream-ordered pool allocator)
+// ---------------------------------------------------------------------------
+struct Ctx;
+
+template <typename T>
+struct DBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaStream_t s = nullptr;
+    DBuf() = default;
+    DBuf(size_t count, cudaStream_t st) { alloc(count, st); }
+    DBuf(const DBuf&) = delete;
+    DBuf& operator=(const DBuf&) = delete;
+    DBuf(DBuf&& o) noexcept : p(o.p), n(o.n), s(o.s) { o.p = nullptr; o.n = 0; }
+    DBuf& operator=(DBuf&& o) noexcept {
+        if (this != &o) { release(); p = o.p; n = o.n; s = o.s; o.p = nullptr; o.n = 0; }
+        return *this;
+    }
+    void alloc(size_t count, cudaStream_t st) {
+        release();
+        s = st;
+        n = count;
+        if (count == 0) return;
+        cudaError_t e = cudaMallocAsync((void**)&p, count * sizeof(T), st);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            throw Error(e == cudaErrorMemoryAllocation ? SLFMM_ERR_NOMEM : SLFMM_ERR_CUDA,
+                        std::string("device allocation of ") + std::to_string(count * sizeof(T)) +
+                            " bytes failed: " + cudaGetErrorString(e));
+        }
+    }
+    void zero() {
+        if (n) SLFMM_CUDA(cudaMemsetAsync(p, 0, n * sizeof(T), s));
+    }
+    void release() {
+        if (p) cudaFreeAsync(p, s);
+        p = nullptr;
+        n = 0;
+    }
+    ~DBuf() { release(); }
+    T* get() const { return p; }
+    size_t bytes() const { return n * sizeof(T); }
+};
+
+// ---------------------------------------------------------------------------
+// resident genotype matrix
+// ---------------------------------------------------------------------------
+struct Geno {
+    uint64_t n = 0;        // samples (after sample_keep)
+    uint64_t p = 0;        // SNPs (after SNP subset)
+    uint64_t stride = 0;   // bytes per SNP row on device (multiple of 128)
+    DBuf<uint8_t> packed;  // p x stride, codes of samples >= n are 00
+    DBuf<int32_t> counts;  // p x 4: c0, c1(het), c2(hom alt), cmiss
+    // missing-call lists, built on first use (caches of the packed matrix)
+    mutable bool have_csr = false;
+    mutable uint64_t nnz = 0;
+    mutable DBuf<uint64_t> miss_ptr;   // p+1, CSR by SNP
+    mutable DBuf<uint32_t> miss_idx;   // nnz sample indices (ascending)
+    mutable bool have_csc = false;
+    mutable DBuf<uint64_t> missT_ptr;  // n+1, CSC by sample
+    mutable DBuf<uint32_t> missT_idx;  // nnz SNP indices (ascending)
+};
+
+// ---------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------
+struct Ctx {
+    int device = 0;
+    int precision = SLFMM_PREC_SPLIT_BF16;
+    int verbose = 0;
+    bool own_stream = false;
+    cudaStream_t stream = nullptr;
+    cudaStream_t copy_stream = nullptr;
+    std::string last_error;
+    uint64_t launches = 0;
+    int sm_count = 0;
+    DBuf<int> dev_flags;   // [0] device timeout flag, [1] error info
+};
+
+// grid size for a grid-stride loop over `work` items
+inline int grid_for(const Ctx& c, uint64_t work, int block) {
+    const uint64_t want = ceil_div(work, (uint64_t)block);
+    const uint64_t cap = (uint64_t)(c.sm_count > 0 ? c.sm_count : 1) * 32;
+    const uint64_t g = want < cap ? want : cap;
+    return (int)(g > 0 ? g : 1);
+}
+
+// count + check a kernel launch
+void after_launch(Ctx& c, const char* name);
+#define SLFMM_LAUNCHED(ctx, name) ::slfmm::after_launch((ctx), (name))
+
+// ---------------------------------------------------------------------------
+// kernel entry points (host wrappers, defined in the .cu files)
+// ---------------------------------------------------------------------------
+// k_decode.cu
+void launch_repack(Ctx& c, const uint8_t* in, uint64_t rows, uint64_t in_bps, uint64_t n_phys,
+                   const uint32_t* keep, uint64_t n_out, uint8_t* out, uint64_t stride);
+void launch_snp_counts(Ctx& c, const Geno& g, uint64_t* miss_count_out);
+void build_missing_lists(Ctx& c, const Geno& g);
+void build_missing_csc(Ctx& c, const Geno& g);
+void launch_stats_mean(Ctx& c, const Geno& g, int norm, double* mean, double* scale,
+                       double* tss, uint8_t* zero_var);
+void launch_decode_chunk(Ctx& c, const Geno& g, uint64_t snp0, uint64_t ncols,
+                         const double* mean, const double* scale, double* out);
+// per-SNP 4-entry lookup tables (value of code 0,1,2,3)
+void launch_lut_std(Ctx& c, uint64_t p, const double* mean, const double* scale, float* lut);
+void launch_lut_raw(Ctx& c, uint64_t p, const double* fill_missing, float* lut);
+
+// k_simt.cu : plain FP32 contractions over the packed matrix
+// out[j, c] = sum_i lut_j[code_ij] * W[i, c]      (j in [0,p), ldw = wp)
+void launch_row_lut(Ctx& c, const Geno& g, const float* lut, const float* W, int wp, float* out);
+// S[i, c] = sum_j lut_j[code_ij] * Q[j, c]        (FP64 result, n x wp)
+void launch_col_lut(Ctx& c, const Geno& g, const float* lut, const float* Q, int wp, double* S);
+
+// k_tc.cu : tcgen05 split-BF16 contractions
+bool tc_available(Ctx& c);
+// out[j, c] = sum_i g_ij * W[i, c] with exact genotypes (missing -> 0)
+void launch_row_tc(Ctx& c, const Geno& g, const float* W, int w, float* out, int ldo);
+// S[i, c] = sum_j g_ij * Q[j, c]  (missing -> 0), FP64 n x ldS
+void launch_col_tc(Ctx& c, const Geno& g, const float* Q, int w, double* S, int ldS);
+
+// k_small.cu : FP64 dense helpers (row-major)
+void launch_colmeans(Ctx& c, const double* A, uint64_t m, int a, int lda, double* out);
+void launch_center_cols(Ctx& c, double* A, uint64_t m, int a, int lda, const double* means);
+void launch_scale_cols_sd(Ctx& c, double* A, uint64_t m, int a, int lda);
+void launch_atb(Ctx& c, const double* A, int lda, const double* B, int ldb, uint64_t m, int a,
+                int b, double* out);  // out (a x b) = A^T B
+void launch_gram_f32(Ctx& c, const float* A, int lda, uint64_t m, int a, double* out);
+void launch_gemm_small(Ctx& c, const double* A, int lda, uint64_t m, int a, const double* B,
+                       int ldb, int b, double alpha, double beta, double* C, int ldc);
+void launch_gemm_small_f32out(Ctx& c, const double* A, int lda, uint64_t m, int a,
+                              const double* B, int ldb, int b, float* C, int ldc);
+// A <- A * Linv^T (Linv lower-triangular a x a, a <= 64)
+void launch_trmul_f32(Ctx& c, float* A, int lda, uint64_t m, int a, const double* Linv);
+// in place lower Cholesky; drop_tol < 0: replace non-positive pivots by a
+// tiny value; drop_tol >= 0: drop (L_kk = 1, column zero) dependent columns
+void launch_cholesky(Ctx& c, double* A, int a, int* status, double drop_tol = -1.0,
+                     int* dropped = nullptr);
+void launch_transpose(Ctx& c, const double* A, int rows, int cols, double* At);
+void launch_scale_cols(Ctx& c, double* A, uint64_t m, int a, int lda, const double* f);
+void launch_build_design(Ctx& c, const double* X, int d, const double* U, int K, uint64_t n,
+                         double* C);
+void launch_tri_inv_lower(Ctx& c, const double* L, int a, double* Linv);
+void launch_inverse(Ctx& c, const double* A, int a, double* Ainv, int* status, double* eps_used);
+// one-sided Jacobi SVD (a <= 64): A is overwritten with U, V and sig
+// (descending) written
+void launch_jacobi_svd(Ctx& c, const double* A, int a, double* V, double* sig);
+void launch_normal(Ctx& c, uint64_t seed, uint64_t rows, int cols, double* out);
+void launch_f64_to_f32_pad(Ctx& c, const double* A, uint64_t m, int a, int lda, float* out,
+                           uint64_t m_pad, int ldo);
+void launch_f32_to_f64(Ctx& c, const float* A, uint64_t m, int a, int lda, double* out, int ldo);
+
+// k_assoc.cu
+struct AssocConsts {
+    int d, w;           // covariates, latent-augmented width (cols of u = w)
+    double df;
+    const float* theta_rows;  // d x w (rows of L^-T restricted to X coefficients)
+    const float* beta_rows;   // d x w
+    const double* cjj;        // d
+    const uint8_t* dropped;   // d
+    const uint8_t* zero_var;  // p (may be null): SNP with no variance
+};
+void launch_assoc_epilogue(Ctx& c, uint64_t p, const float* u, int ldu, const double* tss,
+                           const AssocConsts& k, double* beta, float* t32, double* r2,
+                           uint32_t* hist);
+void launch_gif(Ctx& c, const uint32_t* hist, int d, double* gif_raw);
+void launch_calibrate(Ctx& c, uint64_t p, int d, const float* t32, const double* gif_per_trait,
+                      double* t64, double* pval);
+
+}  // namespace slfmm
