@@ -1,0 +1,386 @@
+#!/usr/bin/env python
+"""Benchmark of the streaming LFMM2 fit on GB300: SNPs/s of one whole
+fit_lfmm2 job (Step 0, the 2q+2 randomized-SVD passes, the association
+pass with GIF calibration) on a synthetic cohort.
+
+Default workload ("biobank"): n = 20,000 samples, p = 2,000,000 SNPs,
+10 admixed populations (Dirichlet(0.3)), Fst 0.05, allele frequencies
+U(0.01, 0.5), 0.5 % MCAR missing calls, 50 Gaussian traits jointly as
+covariates (each with U(0, 30 %) of its values masked and mean-imputed the
+way the reference CLI does), K = 20, oversampling 10, 2 power iterations.
+
+Reported:
+* ``value``  SNPs/s with the packed genotypes already resident in HBM;
+* ``e2e``    SNPs/s through the C-ABI host entry point slfmm_fit_host:
+             pinned host payload -> H2D -> fit -> results D2H, every step;
+* ``roofline`` of the dominant contraction kernel (CUDA events, live);
+* ``cpu_baseline`` the faithful n x n CPU restatement of the reference
+             timed on a bounded SNP sample and extrapolated to p.
+
+``--impl reference`` times only that CPU restatement (the reference crate
+itself is Rust and cannot be built here).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "SNPs/s end-to-end, split-FP8 vs FP32 GPU at max|Δt|≤1e-3; HBM/TC % of peak"
+
+WORKLOADS = {
+    # the configuration the headline metric is quoted on
+    "biobank": dict(n=20_000, p=2_000_000, k=20, d=50, oversampling=10, power_iter=2, n_pop=10, alpha=0.3,
+                    fst=0.05, f_lo=0.01, f_hi=0.5, miss=0.005, inbreeding=0.0, lam=1e-5, mask_max=0.3,
+                    est_rate=None),
+    # inbred-plant shape (parity/scale case)
+    "plant": dict(n=1_135, p=1_800_000, k=12, d=1, oversampling=10, power_iter=2, n_pop=8, alpha=0.5,
+                  fst=0.1, f_lo=0.01, f_hi=0.5, miss=0.02, inbreeding=0.9, lam=1e-5, mask_max=0.0,
+                  est_rate=0.01),
+    # the reference's CPU-runnable case
+    "small": dict(n=200, p=10_000, k=3, d=1, oversampling=10, power_iter=2, n_pop=2, alpha=1.0,
+                  fst=0.1, f_lo=0.05, f_hi=0.5, miss=0.01, inbreeding=0.0, lam=1e-5, mask_max=0.0,
+                  est_rate=None),
+}
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), float(d["bf16_tflops"]), float(d.get("bf16_tflops_sustained", d["bf16_tflops"])), "measured"
+    return 6800.0, 1900.0, 1700.0, "fallback"
+
+
+def traffic_from_profiles(kernel: str, workload: str):
+    """dram bytes per launch from a committed ncu summary, if any."""
+    f = ROOT / "profiles" / f"{kernel}_{workload}.md"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].strip().split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.rows = []
+        self.proc = None
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for k, nm in enumerate(names):
+                if len(r) > 5 + k and r[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def make_covariates(n: int, d: int, q: np.ndarray, mask_max: float, seed: int) -> np.ndarray:
+    """Gaussian traits with a population term; each trait has U(0, mask_max)
+    of its values masked and imputed to the observed column mean, the way the
+    reference CLI treats NA covariates (src/main.rs:543-568)."""
+    rng = np.random.default_rng(seed)
+    pop = q @ rng.normal(size=(q.shape[1], d))
+    pop /= pop.std(axis=0) + 1e-12
+    x = 0.4 * pop + rng.normal(size=(n, d))
+    for t in range(d):
+        frac = rng.uniform(0.0, mask_max) if mask_max > 0 else 0.0
+        m = rng.random(n) < frac
+        if m.any() and (~m).any():
+            x[m, t] = x[~m, t].mean()
+    return np.ascontiguousarray(x)
+
+
+def pinned_empty(shape, dtype):
+    import schnellfmm_gb300 as sg
+    pa = sg.PinnedArray(shape, dtype)
+    return pa.array, pa
+
+
+def run_reference(args, w):
+    """Time the CPU restatement of the reference on a bounded SNP sample."""
+    from oracle import cpu_baseline, lfmm_oracle as O
+    n, p = w["n"], w["p"]
+    rng = np.random.default_rng(123)
+    q = rng.dirichlet(np.full(w["n_pop"], w["alpha"]), size=n)
+    x = make_covariates(n, w["d"], q, w["mask_max"], 7)
+    sample = args.cpu_sample
+    f_anc = rng.uniform(w["f_lo"], w["f_hi"], size=sample)
+    sd = np.sqrt(w["fst"] * f_anc * (1 - f_anc))
+    f_pop = np.clip(f_anc[None, :] + sd[None, :] * rng.normal(size=(w["n_pop"], sample)), 1e-3, 1 - 1e-3)
+    g = rng.binomial(2, q @ f_pop).astype(np.int16)
+    g[rng.random(g.shape) < w["miss"]] = 255
+    packed = O.pack_codes(O.genotypes_to_codes(g.T))
+    per_step = []
+    info = None
+    for it in range(args.warmup + args.steps):
+        info = cpu_baseline.time_reference_cpu(packed, n, x, k=w["k"], oversampling=w["oversampling"],
+                                               power_iter=w["power_iter"], lam=w["lam"], norm=O.NORM_EIGENSTRAT,
+                                               p_total=p)
+        if it >= args.warmup:
+            per_step.append(info["snps_per_s"])
+    return float(np.median(per_step)), info
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=sorted(WORKLOADS), default="biobank")
+    ap.add_argument("--precision", choices=["split_bf16", "fp32"], default="split_bf16")
+    ap.add_argument("--cpu-sample", type=int, default=1000, help="SNPs in the CPU baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp32-path", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--out", default=None, help="also write the JSON line to this file")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    w = WORKLOADS[args.workload]
+    config = {"workload": f"{args.workload}: n={w['n']} p={w['p']} K={w['k']} d={w['d']} "
+                          f"l={w['k'] + w['oversampling']} q={w['power_iter']}",
+              "n_samples": w["n"], "n_snps": w["p"], "K": w["k"], "d": w["d"], "oversampling": w["oversampling"],
+              "power_iter": w["power_iter"], "est_rate": w["est_rate"], "precision": args.precision,
+              "l2": "inputs larger than L2 (packed genotypes %.1f GB vs 129 MB L2)" % (w["p"] * ((w["n"] + 3) // 4) / 1e9)}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        val, info = run_reference(args, w)
+        line = {"metric": METRIC, "impl": "reference", "value": val, "unit": "SNPs/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": config,
+                "cpu_baseline": {"value": val, "unit": "SNPs/s", "cores": info["cores"], "kind": "port",
+                                 "sample": f"{info['sample_snps']} SNPs x {w['n']} samples through every pass of "
+                                           f"the n x n CPU restatement, extrapolated to p={w['p']}"},
+                "e2e": {"value": val, "unit": "SNPs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "detail": info}
+        print(json.dumps(line))
+        return
+
+    import torch
+    import schnellfmm_gb300 as sg
+
+    dist = None
+    if world > 1:
+        import torch.distributed as td
+        torch.cuda.set_device(local_rank)
+        td.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+        dist = td
+    else:
+        torch.cuda.set_device(0)
+    dev = local_rank if world > 1 else 0
+    torch_stream = torch.cuda.current_stream()
+    prec = sg.Precision.SPLIT_BF16 if args.precision == "split_bf16" else sg.Precision.FP32
+    eng = sg.Engine(dev, prec, stream=torch_stream.cuda_stream)
+    n, p, d, k = w["n"], w["p"], w["d"], w["k"]
+    rng = np.random.default_rng(100 + rank)
+    q = rng.dirichlet(np.full(w["n_pop"], w["alpha"]), size=n).astype(np.float32)
+    x = make_covariates(n, d, q.astype(np.float64), w["mask_max"], 7 + rank)
+    geno = eng.simulate(q, p, fst=w["fst"], f_lo=w["f_lo"], f_hi=w["f_hi"], miss=w["miss"],
+                        inbreeding=w["inbreeding"], seed=42 + rank)
+    cfg = sg.Lfmm2Config(k=k, lambda_=w["lam"], oversampling=w["oversampling"], n_power_iter=w["power_iter"],
+                         norm=sg.SnpNorm.EIGENSTRAT)
+    est = sg.SubsetSpec.from_rate(w["est_rate"]) if w["est_rate"] else sg.SubsetSpec.all()
+    bps = (n + 3) // 4
+    host_packed, _keep_alive = pinned_empty((p, bps), np.uint8)
+    geno.download(host_packed)
+    geno_est = geno
+    if w["est_rate"]:
+        geno_est = eng.upload(host_packed, n, snps=est)
+
+    def barrier():
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def maxover(v):
+        if not dist:
+            return v
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def _fit_device_only(e):
+        # slfmm_fit on the resident matrices with NULL host outputs: the whole
+        # fit runs, results stay in device memory (no D2H)
+        r = sg._Results(None, None, None, None, None, None, 0.0, None, 0.0, 0.0, 0.0, 0)
+        c = cfg._c()
+        e.check(e.lib.slfmm_fit(e.h, geno_est.h, geno.h, sg._ptr(x), d, ctypes.byref(c), None, ctypes.byref(r)))
+        return r.gif
+
+    # ---- resident (device) throughput ----
+    for _ in range(args.warmup):
+        _fit_device_only(eng)
+    barrier()
+    eng.profile(True)
+    launches0 = eng.launches
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev) as clk:
+        barrier()
+        ev0.record(torch_stream)
+        for _ in range(args.steps):
+            _fit_device_only(eng)
+        ev1.record(torch_stream)
+        barrier()
+    ms_total = maxover(ev0.elapsed_time(ev1))
+    launches = eng.launches - launches0
+    prof = {kname: eng.profile_read(kname) for kname in ("row_contract", "col_contract", "assoc_epilogue")}
+    eng.profile(False)
+    ms_step = ms_total / args.steps
+    value = world * p / (ms_step / 1e3)
+
+    # ---- end-to-end through the host entry point ----
+    e2e = None
+    if not args.no_e2e:
+        out = {}
+        keep = []
+        for name, shape in (("u_hat", (n, k)), ("beta", (p, d)), ("tstat", (p, d)), ("pvalue", (p, d)),
+                            ("r2", (p, 3)), ("gif_per_trait", (d,))):
+            a, t = pinned_empty(shape, np.float64)
+            out[name] = a
+            keep.append(t)
+        for _ in range(args.warmup):
+            sg.fit_lfmm2_host(host_packed, n, x, cfg, est_subset=est, engine=eng, out=out)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(torch_stream)
+        for _ in range(args.steps):
+            sg.fit_lfmm2_host(host_packed, n, x, cfg, est_subset=est, engine=eng, out=out)
+        e1.record(torch_stream)
+        barrier()
+        wall = (time.perf_counter() - t0) * 1e3 / args.steps
+        e2e_ms = maxover(max(e0.elapsed_time(e1) / args.steps, wall))
+        h2d = p * bps + (int(p * (w["est_rate"] or 0) + 1) * bps if w["est_rate"] else 0) + x.nbytes
+        d2h = sum(a.nbytes for a in out.values())
+        e2e = {"value": world * p / (e2e_ms / 1e3), "unit": "SNPs/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms}
+
+    # ---- plain FP32 GPU path, same resident inputs ----
+    fp32 = None
+    if not args.no_fp32_path and prec != sg.Precision.FP32:
+        eng32 = sg.Engine(dev, sg.Precision.FP32, stream=torch_stream.cuda_stream)
+        _fit_device_only(eng32)
+        barrier()
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        reps = max(1, min(3, args.steps))
+        f0.record(torch_stream)
+        for _ in range(reps):
+            _fit_device_only(eng32)
+        f1.record(torch_stream)
+        barrier()
+        ms32 = maxover(f0.elapsed_time(f1) / reps)
+        fp32 = {"value": world * p / (ms32 / 1e3), "unit": "SNPs/s", "ms_per_step": ms32,
+                "speedup_of_headline": (world * p / (ms_step / 1e3)) / (world * p / (ms32 / 1e3))}
+        eng32.close()
+
+    # ---- roofline of the dominant kernel class ----
+    hbm, bf16, bf16s, src = peaks()
+    dom = max(("row_contract", "col_contract"), key=lambda kk: prof[kk]["ms"])
+    pr = prof[dom]
+    avg_ms = pr["ms"] / max(pr["launches"], 1)
+    bytes_per = pr["bytes"] / max(pr["launches"], 1)
+    flops_per = pr["flops"] / max(pr["launches"], 1)
+    achieved_gbs = bytes_per / (avg_ms / 1e3) / 1e9
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved_gbs, "peak": hbm, "unit": "GB/s",
+            "frac": achieved_gbs / hbm, "peak_source": src,
+            "traffic": traffic_from_profiles(dom, args.workload),
+            "avg_launch_ms": avg_ms, "launches": pr["launches"], "algorithmic_bytes_per_launch": bytes_per,
+            "algorithmic_tflops": flops_per / (avg_ms / 1e3) / 1e12, "tensor_peak_tflops": bf16,
+            "share_of_step": {kk: prof[kk]["ms"] / ms_total for kk in prof}}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        from oracle import cpu_baseline, lfmm_oracle as O  # noqa: F401
+        s = min(args.cpu_sample, p)
+        info = cpu_baseline.time_reference_cpu(np.asarray(host_packed[:s]), n, x, k=k, oversampling=w["oversampling"],
+                                               power_iter=w["power_iter"], lam=w["lam"], norm=1, p_total=p)
+        cpu = {"value": info["snps_per_s"], "unit": "SNPs/s", "cores": info["cores"], "kind": "port",
+               "sample": f"first {s} SNPs x {n} samples of this workload through every pass of the n x n CPU "
+                         f"restatement of the reference (numpy FP64), extrapolated to p={p}",
+               "extrapolated_total_s": info["extrapolated_total_s"]}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "SNPs/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_step,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "bf16x2 split (exact bf16 genotypes, fp32 accumulate)" if prec == sg.Precision.SPLIT_BF16
+                else "fp32",
+                "data": "synthetic (seeded structured cohort drawn on the device)",
+                "config": config, "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
+                "cpu_baseline": cpu, "fp32_gpu_path": fp32, "clocks": clk.summary()}
+        s = json.dumps(line)
+        print(s)
+        if args.out:
+            Path(args.out).write_text(s + "\n")
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

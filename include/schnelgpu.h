@@ -174,6 +174,32 @@ int slfmm_fit_host(slfmm_ctx* ctx, const uint8_t* packed, uint64_t n_physical,
                    const slfmm_subset* est, const double* x, uint32_t d,
                    const slfmm_config* cfg, const double* omega, slfmm_results* res);
 
+/* ---- synthetic cohorts (plays the role of src/simulate.rs:49-142) ------- */
+/* Draw a structured cohort directly into a device-resident matrix: n
+ * samples with admixture proportions admix (n x n_pop, host, rows sum to 1),
+ * p SNPs with ancestral frequency U(f_lo, f_hi), population drift Fst,
+ * inbreeding (probability a genotype is homozygous by descent) and MCAR
+ * missing rate. */
+int slfmm_simulate(slfmm_ctx* ctx, uint64_t n, uint64_t p, uint32_t n_pop, const float* admix,
+                   double fst, double f_lo, double f_hi, double miss_rate, double inbreeding,
+                   uint64_t seed, slfmm_geno** out);
+/* Copy a resident matrix back as a PLINK payload (p x ceil(n/4) bytes). */
+int slfmm_geno_download(slfmm_ctx* ctx, const slfmm_geno* g, uint8_t* packed_out);
+
+/* Page-locked host buffers (cudaMallocHost) for payloads and results, so
+ * that slfmm_fit_host copies by DMA without a staging memcpy. */
+int slfmm_host_alloc(size_t bytes, void** out);
+int slfmm_host_free(void* p);
+
+/* ---- instrumentation ----------------------------------------------------- */
+/* Record CUDA events around the streaming contraction kernels (resets the
+ * counters).  slfmm_profile_read returns, for a kernel class
+ * ("row_contract", "col_contract", "assoc_epilogue"), the summed device time,
+ * the number of launches and the algorithmic bytes / flops they moved. */
+int slfmm_profile_enable(slfmm_ctx* ctx, int on);
+int slfmm_profile_read(slfmm_ctx* ctx, const char* kernel, double* total_ms, uint64_t* launches,
+                       double* algo_bytes, double* algo_flops);
+
 /* ---- output (src/testing.rs:740-801) ------------------------------------ */
 /* Write <out>.tsv: header chr pos snp_id {p_,beta_,t_}xcov r2_cov r2_latent
  * r2_resid, numbers in Rust "{:.6e}" form.  chrom/snp_id are arrays of p

@@ -103,7 +103,8 @@ EXPORTED_SYMBOLS = (
     "slfmm_bed_validate", "slfmm_geno_upload", "slfmm_geno_free", "slfmm_geno_n_samples",
     "slfmm_geno_n_snps", "slfmm_decode_stats", "slfmm_decode_chunk", "slfmm_center_covariates",
     "slfmm_generate_omega", "slfmm_estimate_factors", "slfmm_test_associations", "slfmm_fit",
-    "slfmm_fit_host", "slfmm_write_tsv", "slfmm_format_exp6",
+    "slfmm_fit_host", "slfmm_write_tsv", "slfmm_format_exp6", "slfmm_simulate", "slfmm_geno_download",
+    "slfmm_profile_enable", "slfmm_profile_read", "slfmm_host_alloc", "slfmm_host_free",
 )
 
 _lib_handle = None
@@ -142,6 +143,13 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
         "slfmm_write_tsv": (i32, [C.c_char_p, u64, u32, C.POINTER(C.c_char_p), C.POINTER(u64),
                                   C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.POINTER(_Results), i32]),
         "slfmm_format_exp6": (i32, [C.c_double, C.c_char_p, C.c_size_t]),
+        "slfmm_simulate": (i32, [vp, u64, u64, u32, vp, C.c_double, C.c_double, C.c_double, C.c_double,
+                                 C.c_double, u64, C.POINTER(vp)]),
+        "slfmm_geno_download": (i32, [vp, vp, vp]),
+        "slfmm_profile_enable": (i32, [vp, i32]),
+        "slfmm_profile_read": (i32, [vp, C.c_char_p, _dp, C.POINTER(u64), _dp, _dp]),
+        "slfmm_host_alloc": (i32, [C.c_size_t, C.POINTER(vp)]),
+        "slfmm_host_free": (i32, [vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -150,6 +158,33 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
     if path is None:
         _lib_handle = lib
     return lib
+
+
+class PinnedArray:
+    """Page-locked host array (cudaMallocHost) exposed as a numpy array."""
+
+    def __init__(self, shape, dtype):
+        self.lib = load_library()
+        dt = np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * dt.itemsize
+        self.ptr = C.c_void_p()
+        rc = self.lib.slfmm_host_alloc(nbytes, C.byref(self.ptr))
+        if rc != OK:
+            raise SchnelGpuError(rc, f"pinned allocation of {nbytes} bytes failed")
+        buf = (C.c_uint8 * max(nbytes, 1)).from_address(self.ptr.value) if nbytes else bytearray(1)
+        self.array = np.frombuffer(buf, dtype=dt, count=int(np.prod(shape))).reshape(shape)
+
+    def free(self):
+        if self.ptr:
+            self.array = None
+            self.lib.slfmm_host_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
 
 
 def _ptr(a: Optional[np.ndarray]):
@@ -318,6 +353,25 @@ class Engine:
             0 if keep is None else len(keep), C.byref(sub), C.byref(h)))
         return Genotypes(self, h)
 
+    def simulate(self, admix: np.ndarray, p: int, *, fst: float, f_lo: float, f_hi: float, miss: float,
+                 inbreeding: float = 0.0, seed: int = 42) -> "Genotypes":
+        """Structured synthetic cohort drawn on the device (benchmark inputs)."""
+        q = np.ascontiguousarray(admix, dtype=np.float32)
+        h = C.c_void_p()
+        self.check(self.lib.slfmm_simulate(self.h, q.shape[0], p, q.shape[1], _ptr(q), fst, f_lo, f_hi, miss,
+                                           inbreeding, seed & 0xFFFFFFFFFFFFFFFF, C.byref(h)))
+        return Genotypes(self, h)
+
+    def profile(self, on: bool) -> None:
+        self.check(self.lib.slfmm_profile_enable(self.h, int(on)))
+
+    def profile_read(self, kernel: str) -> dict:
+        ms, b, f = C.c_double(), C.c_double(), C.c_double()
+        n = C.c_uint64()
+        self.check(self.lib.slfmm_profile_read(self.h, kernel.encode(), C.byref(ms), C.byref(n), C.byref(b),
+                                               C.byref(f)))
+        return {"ms": ms.value, "launches": n.value, "bytes": b.value, "flops": f.value}
+
     def generate_omega(self, seed: int, n: int, l: int) -> np.ndarray:
         out = np.empty((n, l))
         self.check(self.lib.slfmm_generate_omega(self.h, seed & 0xFFFFFFFFFFFFFFFF, n, l, _ptr(out)))
@@ -363,6 +417,14 @@ class Genotypes:
         self.eng.check(self.eng.lib.slfmm_decode_stats(self.eng.h, self.h, int(norm), _ptr(counts), _ptr(mean),
                                                        _ptr(scale), _ptr(tss)))
         return counts, mean, scale, tss
+
+    def download(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        """PLINK payload (p x ceil(n/4) bytes) of the resident matrix."""
+        bps = (self.n_samples + 3) // 4
+        if out is None:
+            out = np.empty((self.n_snps, bps), dtype=np.uint8)
+        self.eng.check(self.eng.lib.slfmm_geno_download(self.eng.h, self.h, _ptr(out)))
+        return out
 
     def decode_chunk(self, snp0: int, ncols: int, norm: SnpNorm) -> np.ndarray:
         out = np.empty((self.n_samples, ncols))
@@ -597,6 +659,35 @@ def fit_lfmm2(y_est, est_subset: SubsetSpec, y_full, x: np.ndarray, config: Lfmm
     if output is not None:
         write_tsv(output.path, output.bim, output.cov_names, res)
     return res
+
+
+def fit_lfmm2_host(packed: np.ndarray, n_physical: int, x: np.ndarray, config: Lfmm2Config,
+                   est_subset: Optional[SubsetSpec] = None, sample_keep: Optional[Sequence[int]] = None,
+                   omega: Optional[np.ndarray] = None, engine: Optional[Engine] = None,
+                   out: Optional[dict] = None) -> TestResults:
+    """fit_lfmm2 from a HOST payload (upload, fit, copy back) in one C-ABI call.
+    ``out`` may hold preallocated (e.g. pinned) result arrays."""
+    eng = engine or default_engine()
+    bps = (n_physical + 3) // 4
+    n_snps = packed.size // bps
+    n = n_physical if sample_keep is None else len(sample_keep)
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    d = x.shape[1]
+    if out is None:
+        r, arr = _alloc_results(n, n_snps, d, config.k, config.nmf.n_iter if config.nmf else 0)
+    else:
+        arr = out
+        r = _Results(_dptr(arr["u_hat"]), _dptr(arr["beta"]), _dptr(arr["tstat"]), _dptr(arr["pvalue"]),
+                     _dptr(arr["r2"]), _dptr(arr["gif_per_trait"]), 0.0, _dptr(arr.get("nmf_cv")), 0.0, 0.0, 0.0, 0)
+    keep = None if sample_keep is None else np.ascontiguousarray(sample_keep, dtype=np.uint64)
+    sub = (est_subset or SubsetSpec.all())._c()
+    om = None if omega is None else np.ascontiguousarray(omega, dtype=np.float64)
+    cfg = config._c()
+    eng.check(eng.lib.slfmm_fit_host(eng.h, _ptr(packed), n_physical, n_snps,
+                                     None if keep is None else keep.ctypes.data_as(C.POINTER(C.c_uint64)),
+                                     0 if keep is None else len(keep), C.byref(sub), _ptr(x), d, C.byref(cfg),
+                                     _ptr(om), C.byref(r)))
+    return _to_results(r, arr, config)
 
 
 def format_exp6(v: float) -> str:

@@ -23,6 +23,19 @@ struct slfmm_geno : slfmm::Geno {};
 
 namespace slfmm {
 
+void profile_collect(Ctx& c) {
+    for (auto& kv : c.prof) {
+        for (auto& ev : kv.second.pending) {
+            float ms = 0.f;
+            if (cudaEventSynchronize(ev.second) == cudaSuccess && cudaEventElapsedTime(&ms, ev.first, ev.second) == cudaSuccess)
+                kv.second.ms += ms;
+            cudaEventDestroy(ev.first);
+            cudaEventDestroy(ev.second);
+        }
+        kv.second.pending.clear();
+    }
+}
+
 void after_launch(Ctx& c, const char* name) {
     ++c.launches;
     cudaError_t e = cudaGetLastError();
@@ -222,12 +235,16 @@ void row_contract(Ctx& c, const Geno& g, const SnpStd& s, const double* W, int w
     DBuf<float> W32(n_pad * wp, c.stream);
     launch_f64_to_f32_pad(c, W, g.n, w, ldw, W32.get(), n_pad, wp);
     out.alloc(std::max<uint64_t>(g.p, 1) * wp, c.stream);
+    ProfScope ps(c, "row_contract", (double)g.p * ceil_div(g.n, 4) + (double)g.p * w * 4 + (double)g.n * w * 4,
+                 2.0 * g.n * g.p * w);
     launch_row_lut(c, g, s.lut.get(), W32.get(), wp, out.get());
 }
 
-// S (n x wp, FP64) = Y_hat Q, Q = p x wp FP32
-void col_contract(Ctx& c, const Geno& g, const SnpStd& s, const float* Q, int wp, DBuf<double>& S) {
+// S (n x wp, FP64) = Y_hat Q, Q = p x wp FP32 (w real columns)
+void col_contract(Ctx& c, const Geno& g, const SnpStd& s, const float* Q, int w, int wp, DBuf<double>& S) {
     S.alloc(g.n * wp, c.stream);
+    ProfScope ps(c, "col_contract", (double)g.p * ceil_div(g.n, 4) + (double)g.p * w * 4 + (double)g.n * w * 8,
+                 2.0 * g.n * g.p * w);
     launch_col_lut(c, g, s.lut.get(), Q, wp, S.get());
 }
 
@@ -374,7 +391,7 @@ void rsvd(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, int K, int l
     cholqr2_f32(c, Z.get(), g.p, l, wp);                     // QR (:75)
     for (int it = 0; it < q; ++it) {
         DBuf<double> S;
-        col_contract(c, g, st, Z.get(), wp, S);              // fwd (:88-97)
+        col_contract(c, g, st, Z.get(), l, wp, S);              // fwd (:88-97)
         apply_p(c, s0, S.get(), l, wp, false);
         cholqr2_f64(c, S.get(), n, l, wp);                   // QR(a_qz) (:104-105)
         apply_p(c, s0, S.get(), l, wp, false);               // M^T Q (:106)
@@ -383,7 +400,7 @@ void rsvd(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, int K, int l
         cholqr2_f32(c, Z.get(), g.p, l, wp);                 // QR (:131)
     }
     DBuf<double> B;
-    col_contract(c, g, st, Z.get(), wp, B);                  // projection (:138-157)
+    col_contract(c, g, st, Z.get(), l, wp, B);                  // projection (:138-157)
     apply_p(c, s0, B.get(), l, wp, false);
     // small SVD (:160-173): eigen-decomposition of the l x l Gram (FP64)
     DBuf<double> G(l * l, c.stream), V(l * l, c.stream), sig(l, c.stream);
@@ -507,7 +524,10 @@ void assoc(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, const doubl
     DBuf<float> t32(pp * d, c.stream);
     DBuf<uint32_t> hist((size_t)d * kHistBins, c.stream);
     hist.zero();
-    launch_assoc_epilogue(c, p, U.get(), wp, st.tss.get(), k, beta.get(), t32.get(), r2.get(), hist.get());
+    {
+        ProfScope ps(c, "assoc_epilogue", (double)p * (wu * 4 + 8 + d * 12 + 24), 4.0 * p * d * wu);
+        launch_assoc_epilogue(c, p, U.get(), wp, st.tss.get(), k, beta.get(), t32.get(), r2.get(), hist.get());
+    }
     DBuf<double> graw(d, c.stream);
     launch_gif(c, hist.get(), d, graw.get());
     std::vector<double> gr = fetch(c, graw.get(), (size_t)d);
@@ -827,6 +847,81 @@ int slfmm_fit_host(slfmm_ctx* c, const uint8_t* packed, uint64_t n_physical, uin
         ge = &sub;
     }
     fit_impl(*c, *ge, full, x, (int)d, cfg, omega, res);
+    API_CATCH(c)
+}
+
+int slfmm_simulate(slfmm_ctx* c, uint64_t n, uint64_t p, uint32_t n_pop, const float* admix, double fst,
+                   double f_lo, double f_hi, double miss_rate, double inbreeding, uint64_t seed, slfmm_geno** out) {
+    if (!c || !admix || !out) return SLFMM_ERR_BAD_ARG;
+    *out = nullptr;
+    API_TRY
+    SLFMM_CUDA(cudaSetDevice(c->device));
+    SLFMM_REQUIRE(n > 0 && p > 0 && n < (1ull << 31), SLFMM_ERR_BAD_ARG, "bad cohort shape");
+    std::unique_ptr<slfmm_geno> g(new slfmm_geno());
+    g->n = n;
+    g->p = p;
+    g->stride = round_up(ceil_div(n, 4), 128);
+    g->packed.alloc(p * g->stride, c->stream);
+    g->counts.alloc(p * 4, c->stream);
+    DBuf<float> q = upload(*c, admix, n * n_pop);
+    launch_simulate(*c, n, p, (int)n_pop, q.get(), fst, f_lo, f_hi, miss_rate, inbreeding, seed, g->packed.get(),
+                    g->stride);
+    launch_snp_counts(*c, *g, nullptr);
+    sync(*c);
+    *out = g.release();
+    API_CATCH(c)
+}
+
+int slfmm_geno_download(slfmm_ctx* c, const slfmm_geno* g, uint8_t* packed_out) {
+    if (!c || !g || !packed_out) return SLFMM_ERR_BAD_ARG;
+    API_TRY
+    SLFMM_CUDA(cudaSetDevice(c->device));
+    const uint64_t bps = ceil_div(g->n, 4);
+    if (g->p)
+        SLFMM_CUDA(cudaMemcpy2DAsync(packed_out, bps, g->packed.get(), g->stride, bps, g->p, cudaMemcpyDeviceToHost,
+                                     c->stream));
+    sync(*c);
+    API_CATCH(c)
+}
+
+int slfmm_host_alloc(size_t bytes, void** out) {
+    if (!out) return SLFMM_ERR_BAD_ARG;
+    *out = nullptr;
+    if (bytes == 0) return SLFMM_OK;
+    cudaError_t e = cudaMallocHost(out, bytes);
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        return e == cudaErrorMemoryAllocation ? SLFMM_ERR_NOMEM : SLFMM_ERR_CUDA;
+    }
+    return SLFMM_OK;
+}
+
+int slfmm_host_free(void* p) {
+    if (p && cudaFreeHost(p) != cudaSuccess) return SLFMM_ERR_CUDA;
+    return SLFMM_OK;
+}
+
+int slfmm_profile_enable(slfmm_ctx* c, int on) {
+    if (!c) return SLFMM_ERR_BAD_ARG;
+    API_TRY
+    profile_collect(*c);
+    c->prof.clear();
+    c->profiling = on != 0;
+    API_CATCH(c)
+}
+
+int slfmm_profile_read(slfmm_ctx* c, const char* kernel, double* total_ms, uint64_t* launches, double* bytes,
+                       double* flops) {
+    if (!c || !kernel) return SLFMM_ERR_BAD_ARG;
+    API_TRY
+    profile_collect(*c);
+    auto it = c->prof.find(kernel);
+    const ProfRec empty;
+    const ProfRec& r = it == c->prof.end() ? empty : it->second;
+    if (total_ms) *total_ms = r.ms;
+    if (launches) *launches = r.launches;
+    if (bytes) *bytes = r.bytes;
+    if (flops) *flops = r.flops;
     API_CATCH(c)
 }
 

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
+#include <map>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -112,6 +113,13 @@ struct Geno {
 // ---------------------------------------------------------------------------
 // context
 // ---------------------------------------------------------------------------
+// CUDA-event timing of named kernels (enabled by slfmm_profile_enable)
+struct ProfRec {
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> pending;
+    uint64_t launches = 0;
+    double ms = 0.0, bytes = 0.0, flops = 0.0;
+};
+
 struct Ctx {
     int device = 0;
     int precision = SLFMM_PREC_SPLIT_BF16;
@@ -123,7 +131,35 @@ struct Ctx {
     uint64_t launches = 0;
     int sm_count = 0;
     DBuf<int> dev_flags;   // [0] device timeout flag, [1] error info
+    bool profiling = false;
+    std::map<std::string, ProfRec> prof;
 };
+
+// bracket a launch with CUDA events when profiling is on
+struct ProfScope {
+    Ctx& c;
+    const char* name;
+    double bytes, flops;
+    cudaEvent_t a = nullptr, b = nullptr;
+    ProfScope(Ctx& ctx, const char* nm, double by, double fl) : c(ctx), name(nm), bytes(by), flops(fl) {
+        if (c.profiling) {
+            cudaEventCreate(&a);
+            cudaEventCreate(&b);
+            cudaEventRecord(a, c.stream);
+        }
+    }
+    ~ProfScope() {
+        if (a) {
+            cudaEventRecord(b, c.stream);
+            ProfRec& r = c.prof[name];
+            r.pending.emplace_back(a, b);
+            r.launches += 1;
+            r.bytes += bytes;
+            r.flops += flops;
+        }
+    }
+};
+void profile_collect(Ctx& c);
 
 // grid size for a grid-stride loop over `work` items
 inline int grid_for(const Ctx& c, uint64_t work, int block) {
@@ -153,6 +189,11 @@ void launch_decode_chunk(Ctx& c, const Geno& g, uint64_t snp0, uint64_t ncols,
 // per-SNP 4-entry lookup tables (value of code 0,1,2,3)
 void launch_lut_std(Ctx& c, uint64_t p, const double* mean, const double* scale, float* lut);
 void launch_lut_raw(Ctx& c, uint64_t p, const double* fill_missing, float* lut);
+
+// k_sim.cu : synthetic structured cohort written into a device packed matrix
+void launch_simulate(Ctx& c, uint64_t n, uint64_t p, int n_pop, const float* admix_dev, double fst,
+                     double f_lo, double f_hi, double miss, double inbreeding, uint64_t seed, uint8_t* out,
+                     uint64_t stride);
 
 // k_simt.cu : plain FP32 contractions over the packed matrix
 // out[j, c] = sum_i lut_j[code_ij] * W[i, c]      (j in [0,p), ldw = wp)
