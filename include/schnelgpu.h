@@ -147,6 +147,13 @@ int slfmm_decode_stats(slfmm_ctx* ctx, const slfmm_geno* g, int norm,
 int slfmm_decode_chunk(slfmm_ctx* ctx, const slfmm_geno* g, uint64_t snp0,
                        uint64_t ncols, int norm, double* out);
 
+/* Raw tensor-core contraction of the exact genotypes (missing calls = 0)
+ * with the hi + lo BF16 split of W: transposed = 0 gives out (p x w) =
+ * G~^T W for W n x w; transposed = 1 gives out (n x w) = G~ W for W p x w.
+ * Parity hook for the per-chunk dgemms of src/rsvd.rs:61-153. */
+int slfmm_contract_raw(slfmm_ctx* ctx, const slfmm_geno* g, int transposed, const double* w,
+                       uint32_t w_cols, float* out);
+
 /* ---- library API (src/lib.rs) ------------------------------------------- */
 /* center_covariates (src/lib.rs:102-117). x, out: n x d row-major. */
 int slfmm_center_covariates(slfmm_ctx* ctx, const double* x, uint64_t n, uint32_t d,

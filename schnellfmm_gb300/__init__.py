@@ -104,7 +104,7 @@ EXPORTED_SYMBOLS = (
     "slfmm_geno_n_snps", "slfmm_decode_stats", "slfmm_decode_chunk", "slfmm_center_covariates",
     "slfmm_generate_omega", "slfmm_estimate_factors", "slfmm_test_associations", "slfmm_fit",
     "slfmm_fit_host", "slfmm_write_tsv", "slfmm_format_exp6", "slfmm_simulate", "slfmm_geno_download",
-    "slfmm_profile_enable", "slfmm_profile_read", "slfmm_host_alloc", "slfmm_host_free",
+    "slfmm_profile_enable", "slfmm_profile_read", "slfmm_host_alloc", "slfmm_host_free", "slfmm_contract_raw",
 )
 
 _lib_handle = None
@@ -150,6 +150,7 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
         "slfmm_profile_read": (i32, [vp, C.c_char_p, _dp, C.POINTER(u64), _dp, _dp]),
         "slfmm_host_alloc": (i32, [C.c_size_t, C.POINTER(vp)]),
         "slfmm_host_free": (i32, [vp]),
+        "slfmm_contract_raw": (i32, [vp, vp, i32, vp, u32, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -424,6 +425,16 @@ class Genotypes:
         if out is None:
             out = np.empty((self.n_snps, bps), dtype=np.uint8)
         self.eng.check(self.eng.lib.slfmm_geno_download(self.eng.h, self.h, _ptr(out)))
+        return out
+
+    def contract_raw(self, w: np.ndarray, transposed: bool = False) -> np.ndarray:
+        """Tensor-core product of the exact genotypes (missing = 0) with the
+        BF16 hi+lo split of ``w``: G~^T w (w is n x c) or G~ w (w is p x c)."""
+        w = np.ascontiguousarray(w, dtype=np.float64)
+        rows = self.n_samples if transposed else self.n_snps
+        out = np.empty((rows, w.shape[1]), dtype=np.float32)
+        self.eng.check(self.eng.lib.slfmm_contract_raw(self.eng.h, self.h, int(transposed), _ptr(w), w.shape[1],
+                                                       _ptr(out)))
         return out
 
     def decode_chunk(self, snp0: int, ncols: int, norm: SnpNorm) -> np.ndarray:

@@ -235,16 +235,56 @@ void row_contract(Ctx& c, const Geno& g, const SnpStd& s, const double* W, int w
     DBuf<float> W32(n_pad * wp, c.stream);
     launch_f64_to_f32_pad(c, W, g.n, w, ldw, W32.get(), n_pad, wp);
     out.alloc(std::max<uint64_t>(g.p, 1) * wp, c.stream);
-    ProfScope ps(c, "row_contract", (double)g.p * ceil_div(g.n, 4) + (double)g.p * w * 4 + (double)g.n * w * 4,
-                 2.0 * g.n * g.p * w);
+    const double bytes = (double)g.p * ceil_div(g.n, 4) + (double)g.p * w * 4 + (double)g.n * w * 4;
+    if (tc_available(c)) {
+        // exact genotypes x (hi + lo) BF16 split of W on the tensor cores, then
+        // out = s_j (P - mu_j (colsum(W) - sum_{missing} W))
+        DBuf<__nv_bfloat16> bs(2 * (uint64_t)wp * n_pad, c.stream);
+        launch_split_bf16_f64(c, W, ldw, g.n, w, wp, n_pad, nullptr, bs.get());
+        build_missing_lists(c, g);
+        DBuf<double> cs(wp, c.stream);
+        cs.zero();
+        launch_colsums(c, W, g.n, w, ldw, cs.get());
+        {
+            ProfScope ps(c, "row_contract", bytes, 2.0 * g.n * g.p * w);
+            launch_tc_rows(c, g.packed.get(), g.stride, g.p, g.n, bs.get(), n_pad, wp, out.get(), wp, 1, 0);
+        }
+        launch_rowfix_mean(c, out.get(), wp, g.p, w, g.miss_ptr.get(), g.miss_idx.get(), W32.get(), wp, cs.get(),
+                           s.mean.get(), s.scale.get());
+        return;
+    }
+    ProfScope ps(c, "row_contract", bytes, 2.0 * g.n * g.p * w);
     launch_row_lut(c, g, s.lut.get(), W32.get(), wp, out.get());
 }
 
 // S (n x wp, FP64) = Y_hat Q, Q = p x wp FP32 (w real columns)
 void col_contract(Ctx& c, const Geno& g, const SnpStd& s, const float* Q, int w, int wp, DBuf<double>& S) {
     S.alloc(g.n * wp, c.stream);
-    ProfScope ps(c, "col_contract", (double)g.p * ceil_div(g.n, 4) + (double)g.p * w * 4 + (double)g.n * w * 8,
-                 2.0 * g.n * g.p * w);
+    const double bytes = (double)g.p * ceil_div(g.n, 4) + (double)g.p * w * 4 + (double)g.n * w * 8;
+    if (tc_available(c)) {
+        // forward pass on the transposed matrix (rows = samples, K = SNPs):
+        // S = G~ (diag(s) Q) - 1 (mu s)^T Q + missing-call corrections
+        build_transposed(c, g);
+        build_missing_csc(c, g);
+        const uint64_t p_pad = round_up(g.p, 128);
+        DBuf<__nv_bfloat16> bs(2 * (uint64_t)wp * p_pad, c.stream);
+        launch_split_bf16_f32(c, Q, wp, g.p, w, wp, p_pad, s.scale.get(), bs.get());
+        const int splits = tc_split_count(c, g.n, g.p);
+        DBuf<float> part((uint64_t)splits * g.n * wp, c.stream);
+        {
+            ProfScope ps(c, "col_contract", bytes, 2.0 * g.n * g.p * w);
+            launch_tc_rows(c, g.packedT.get(), g.strideT, g.n, g.p, bs.get(), p_pad, wp, part.get(), wp, splits,
+                           g.n * wp);
+        }
+        launch_reduce_splits(c, part.get(), splits, g.n, wp, g.n, S.get());
+        DBuf<double> coef(std::max<uint64_t>(g.p, 1), c.stream), colterm(wp, c.stream);
+        launch_scale_product(c, s.mean.get(), s.scale.get(), g.p, coef.get());
+        launch_weighted_colsum(c, Q, wp, g.p, w, coef.get(), colterm.get());
+        launch_colfix_mean(c, S.get(), wp, g.n, w, g.missT_ptr.get(), g.missT_idx.get(), Q, wp, coef.get(),
+                           colterm.get());
+        return;
+    }
+    ProfScope ps(c, "col_contract", bytes, 2.0 * g.n * g.p * w);
     launch_col_lut(c, g, s.lut.get(), Q, wp, S.get());
 }
 
@@ -922,6 +962,31 @@ int slfmm_profile_read(slfmm_ctx* c, const char* kernel, double* total_ms, uint6
     if (launches) *launches = r.launches;
     if (bytes) *bytes = r.bytes;
     if (flops) *flops = r.flops;
+    API_CATCH(c)
+}
+
+int slfmm_contract_raw(slfmm_ctx* c, const slfmm_geno* g, int transposed, const double* w_host, uint32_t w,
+                       float* out) {
+    if (!c || !g || !w_host || !out) return SLFMM_ERR_BAD_ARG;
+    API_TRY
+    SLFMM_CUDA(cudaSetDevice(c->device));
+    const int wp = pad16((int)w);
+    SLFMM_REQUIRE(wp <= kMaxW, SLFMM_ERR_BAD_ARG, "operand wider than 128 columns");
+    const uint64_t K = transposed ? g->p : g->n, rows = transposed ? g->n : g->p;
+    const uint64_t K_pad = round_up(K, 128);
+    DBuf<double> Wd = upload(*c, w_host, K * w);
+    DBuf<__nv_bfloat16> bs(2 * (uint64_t)wp * K_pad, c->stream);
+    launch_split_bf16_f64(*c, Wd.get(), (int)w, K, (int)w, wp, K_pad, nullptr, bs.get());
+    DBuf<float> o(std::max<uint64_t>(rows, 1) * wp, c->stream);
+    if (transposed) {
+        build_transposed(*c, *g);
+        launch_tc_rows(*c, g->packedT.get(), g->strideT, rows, K, bs.get(), K_pad, wp, o.get(), wp, 1, 0);
+    } else {
+        launch_tc_rows(*c, g->packed.get(), g->stride, rows, K, bs.get(), K_pad, wp, o.get(), wp, 1, 0);
+    }
+    SLFMM_CUDA(cudaMemcpy2DAsync(out, w * sizeof(float), o.get(), wp * sizeof(float), w * sizeof(float), rows,
+                                 cudaMemcpyDeviceToHost, c->stream));
+    sync(*c);
     API_CATCH(c)
 }
 

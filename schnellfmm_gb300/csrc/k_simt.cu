@@ -203,6 +203,12 @@ void col_lut_impl(Ctx& c, const Geno& g, const float* lut, const float* Q, doubl
 
 }  // namespace
 
+void launch_reduce_splits(Ctx& c, const float* part, int splits, uint64_t n, int wp, uint64_t n_pad, double* S) {
+    if (!n) return;
+    k_reduce_splits<<<grid_for(c, n * wp, 256), 256, 0, c.stream>>>(part, splits, n, wp, n_pad, S);
+    SLFMM_LAUNCHED(c, "k_reduce_splits");
+}
+
 void launch_row_lut(Ctx& c, const Geno& g, const float* lut, const float* W, int wp, float* out) {
     if (g.p == 0) return;
     switch (wp) {

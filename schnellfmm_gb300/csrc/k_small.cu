@@ -36,13 +36,14 @@ __device__ double block_sum(double v, double* red) {
     return r;
 }
 
-__global__ void k_colmeans(const double* __restrict__ A, uint64_t m, int lda, double* __restrict__ out) {
+__global__ void k_colmeans(const double* __restrict__ A, uint64_t m, int lda, double* __restrict__ out,
+                           int divide) {
     __shared__ double red[32];
     const int col = blockIdx.x;
     double s = 0.0;
     for (uint64_t i = threadIdx.x; i < m; i += blockDim.x) s += A[i * lda + col];
     s = block_sum(s, red);
-    if (threadIdx.x == 0) out[col] = m ? s / (double)m : 0.0;
+    if (threadIdx.x == 0) out[col] = divide ? (m ? s / (double)m : 0.0) : s;
 }
 
 __global__ void k_center_cols(double* __restrict__ A, uint64_t m, int a, int lda,
@@ -552,8 +553,20 @@ void set_smem(const void* fn, size_t bytes) {
 
 void launch_colmeans(Ctx& c, const double* A, uint64_t m, int a, int lda, double* out) {
     if (a == 0) return;
-    k_colmeans<<<a, 256, 0, c.stream>>>(A, m, lda, out);
+    k_colmeans<<<a, 256, 0, c.stream>>>(A, m, lda, out, 1);
     SLFMM_LAUNCHED(c, "k_colmeans");
+}
+
+void launch_colsums(Ctx& c, const double* A, uint64_t m, int a, int lda, double* out) {
+    if (a == 0) return;
+    k_colmeans<<<a, 256, 0, c.stream>>>(A, m, lda, out, 0);
+    SLFMM_LAUNCHED(c, "k_colsums");
+}
+
+void launch_sum_partials(Ctx& c, const double* part, int splits, uint64_t count, double* out) {
+    if (!count) return;
+    k_sum_partials<<<grid_for(c, count, 256), 256, 0, c.stream>>>(part, splits, count, out);
+    SLFMM_LAUNCHED(c, "k_sum_partials");
 }
 
 void launch_center_cols(Ctx& c, double* A, uint64_t m, int a, int lda, const double* means) {

@@ -1,0 +1,614 @@
+// tcgen05 tensor-core contraction of the packed genotype matrix.
+//
+//   P[r, c] = sum_k g(r, k) * W[k, c]        r = tile row, k = K index
+//
+// g is read straight from the resident 2-bit matrix (rows = SNPs for the
+// sketch / backward / association passes, rows = samples on the transposed
+// copy for the forward passes) and expanded to exact BF16 {0, 1, 2} (missing
+// calls contribute 0; the host applies the mean / scale / missing-call
+// corrections afterwards).  W is split hi + lo into two BF16 matrices so the
+// product is accurate to ~2^-16 relative with FP32 accumulation; this replaces
+// the reference's per-chunk FP64 dgemms (src/rsvd.rs:61-69, :88-97, :117-125,
+// :144-153 and src/testing.rs:355-374).
+//
+// Per CTA: one 128-row tile, a K range of 128-element stages.
+//   warp 0      TMA producer: packed codes (128 rows x 32 B) and the two
+//               128B-swizzled halves of the W tile (N rows x 64 BF16 each)
+//   warp 1      TMEM allocator + single-thread tcgen05.mma issuer
+//   warps 2-5   expand codes -> BF16 pairs -> tcgen05.st into TMEM (the A
+//               operand lives in TMEM, so shared memory only carries W),
+//               then the epilogue: tcgen05.ld, hi + lo, store FP32
+// Every mbarrier wait is bounded by the global timer; on expiry the CTA
+// records an error code, drains its own TMA loads, frees TMEM and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include "slfmm_internal.h"
+
+namespace slfmm {
+namespace {
+
+constexpr int kM = 128;                      // tile rows = TMEM lanes
+constexpr int kKB = 128;                     // K elements per stage
+constexpr int kPackedStage = kM * kKB / 4;   // 4096 B of 2-bit codes
+constexpr int kThreads = 192;
+constexpr uint64_t kWaitNs = 4000000000ull;  // 4 s per wait
+
+struct TcArgs {
+    uint32_t rows;          // valid tile rows in the matrix
+    uint32_t kb_total;      // K stages in the matrix
+    uint32_t kb_per_split;  // K stages per grid.y split
+    uint32_t wpad;          // output columns; MMA N = 2 * wpad
+    uint32_t stages;        // pipeline depth
+    uint32_t tmem_cols;     // TMEM columns allocated
+    uint32_t a_col0;        // first TMEM column of the A stages
+    uint32_t b_stage_bytes; // 2 * N * 128
+    float* out;
+    uint32_t ldo;
+    uint64_t split_stride;  // elements between split outputs
+    int* err;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ uint64_t globaltimer() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+// Wait for completion of the phase with the given parity; bounded.
+__device__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+    const uint32_t addr = smem_u32(bar);
+    uint64_t t0 = 0;
+    for (uint32_t it = 0;; ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}"
+            : "=r"(done)
+            : "r"(addr), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if ((it & 255) == 0) {
+            const uint64_t now = globaltimer();
+            if (it == 0) t0 = now;
+            if (*(volatile int*)err != 0 || now - t0 > kWaitNs) {
+                atomicCAS(err, 0, code);
+                return false;
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ void tma_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+            "r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// K-major operand in 128B-swizzled smem: SBO = 1024 B between 8-row groups.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+    uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+    d |= (uint64_t)1 << 16;             // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
+    d |= (uint64_t)1 << 46;             // descriptor version
+    d |= (uint64_t)2 << 61;             // 128-byte swizzle
+    return d;
+}
+
+// kind::f16 instruction descriptor: BF16 x BF16 -> F32, K-major A and B.
+__device__ __forceinline__ uint32_t instr_desc(uint32_t n) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((uint32_t)(kM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc, uint32_t idesc,
+                                       uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
+        "r"(a_tmem), "l"(b_desc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tmem_st_x64(uint32_t taddr, const uint32_t (&v)[64]) {
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x64.b32 [%0], {"
+        "%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, "
+        "%17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32, "
+        "%33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47, %48, "
+        "%49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63, %64};" ::"r"(taddr),
+        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]),
+        "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15]), "r"(v[16]),
+        "r"(v[17]), "r"(v[18]), "r"(v[19]), "r"(v[20]), "r"(v[21]), "r"(v[22]), "r"(v[23]), "r"(v[24]),
+        "r"(v[25]), "r"(v[26]), "r"(v[27]), "r"(v[28]), "r"(v[29]), "r"(v[30]), "r"(v[31]), "r"(v[32]),
+        "r"(v[33]), "r"(v[34]), "r"(v[35]), "r"(v[36]), "r"(v[37]), "r"(v[38]), "r"(v[39]), "r"(v[40]),
+        "r"(v[41]), "r"(v[42]), "r"(v[43]), "r"(v[44]), "r"(v[45]), "r"(v[46]), "r"(v[47]), "r"(v[48]),
+        "r"(v[49]), "r"(v[50]), "r"(v[51]), "r"(v[52]), "r"(v[53]), "r"(v[54]), "r"(v[55]), "r"(v[56]),
+        "r"(v[57]), "r"(v[58]), "r"(v[59]), "r"(v[60]), "r"(v[61]), "r"(v[62]), "r"(v[63])
+        : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld_x16(uint32_t taddr, float (&v)[16]) {
+    uint32_t r[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+        "%14, %15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ uint32_t bf16_of_code(uint32_t c) {
+    return c == 2u ? 0x3F80u : (c == 3u ? 0x4000u : 0u);  // 00 -> 0, 01 (missing) -> 0
+}
+
+__global__ void __launch_bounds__(kThreads, 1)
+    k_tc_rows(const __grid_constant__ CUtensorMap tm_packed, const __grid_constant__ CUtensorMap tm_b, TcArgs a) {
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const uint32_t S = a.stages, N = 2 * a.wpad;
+    uint8_t* bsm = smem;
+    uint8_t* psm = bsm + S * a.b_stage_bytes;
+    uint2* lut = reinterpret_cast<uint2*>(psm + S * kPackedStage);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<uint8_t*>(lut) + 256 * sizeof(uint2));
+    uint64_t* full_tma = bars;
+    uint64_t* full_a = bars + S;
+    uint64_t* empty = bars + 2 * S;
+    uint64_t* tmem_full = bars + 3 * S;
+    uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 3 * S + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const uint32_t row0 = blockIdx.x * kM;
+    const uint32_t kb0 = blockIdx.y * a.kb_per_split;
+    const uint32_t kb1 = min(a.kb_total, kb0 + a.kb_per_split);
+    const uint32_t nkb = kb1 > kb0 ? kb1 - kb0 : 0;
+
+    if (threadIdx.x == 0) {
+        for (uint32_t s = 0; s < S; ++s) {
+            mbar_init(full_tma + s, 1);
+            mbar_init(full_a + s, 128);
+            mbar_init(empty + s, 1);
+        }
+        mbar_init(tmem_full, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_holder)),
+                     "r"(a.tmem_cols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    for (int e = threadIdx.x; e < 256; e += blockDim.x) {
+        uint2 v;
+        v.x = bf16_of_code(e & 3) | (bf16_of_code((e >> 2) & 3) << 16);
+        v.y = bf16_of_code((e >> 4) & 3) | (bf16_of_code((e >> 6) & 3) << 16);
+        lut[e] = v;
+    }
+    fence_before();
+    __syncthreads();
+    fence_after();
+    const uint32_t tmem = *tmem_holder;
+
+    if (warp == 0) {
+        if (lane == 0) {
+            uint32_t issued = 0;
+            for (uint32_t i = 0; i < nkb; ++i) {
+                const uint32_t s = i % S, r = i / S;
+                if (r > 0 && !mbar_wait(empty + s, (r - 1) & 1, a.err, 1)) break;
+                mbar_arrive_tx(full_tma + s, kPackedStage + a.b_stage_bytes);
+                const int kb = (int)(kb0 + i);
+                tma_2d(psm + s * kPackedStage, &tm_packed, kb * (kKB / 4), (int)row0, full_tma + s);
+                tma_2d(bsm + s * a.b_stage_bytes, &tm_b, kb * kKB, 0, full_tma + s);
+                tma_2d(bsm + s * a.b_stage_bytes + N * 128, &tm_b, kb * kKB + 64, 0, full_tma + s);
+                issued = i + 1;
+            }
+            // never leave with loads in flight into this CTA's shared memory
+            for (uint32_t i = issued > S ? issued - S : 0; i < issued; ++i)
+                mbar_wait(full_tma + i % S, (i / S) & 1, a.err, 2);
+        }
+    } else if (warp == 1) {
+        if (lane == 0) {
+            const uint32_t idesc = instr_desc(N);
+            for (uint32_t i = 0; i < nkb; ++i) {
+                const uint32_t s = i % S, r = i / S;
+                if (!mbar_wait(full_tma + s, r & 1, a.err, 3)) break;
+                if (!mbar_wait(full_a + s, r & 1, a.err, 4)) break;
+                fence_after();
+                const uint32_t b_base = smem_u32(bsm + s * a.b_stage_bytes);
+                const uint32_t a_base = tmem + a.a_col0 + s * (kKB / 2);
+#pragma unroll
+                for (int kk = 0; kk < kKB / 16; ++kk) {
+                    const uint64_t bd = smem_desc(b_base + (kk >> 2) * (N * 128) + (kk & 3) * 32);
+                    mma_ts(tmem, a_base + kk * 8, bd, idesc, (i > 0 || kk > 0) ? 1u : 0u);
+                }
+                mma_commit(empty + s);
+            }
+            mma_commit(tmem_full);
+        }
+    } else {
+        const uint32_t q = (uint32_t)warp & 3u;          // TMEM sub-partition of this warp
+        const uint32_t row = q * 32 + lane;              // tile row == TMEM lane
+        const uint32_t lane_base = tmem + ((q * 32) << 16);
+        for (uint32_t i = 0; i < nkb; ++i) {
+            const uint32_t s = i % S, r = i / S;
+            // warp-uniform decisions: the tcgen05.st below is .sync.aligned
+            if (!__all_sync(0xffffffffu, r == 0 || mbar_wait(empty + s, (r - 1) & 1, a.err, 5))) break;
+            if (!__all_sync(0xffffffffu, mbar_wait(full_tma + s, r & 1, a.err, 6))) break;
+            const uint4* src = reinterpret_cast<const uint4*>(psm + s * kPackedStage + row * (kKB / 4));
+            const uint4 p0 = src[0], p1 = src[1];
+            const uint32_t w8[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
+            uint32_t v[64];
+#pragma unroll
+            for (int b = 0; b < 32; ++b) {
+                const uint2 e = lut[(w8[b >> 2] >> (8 * (b & 3))) & 0xffu];
+                v[2 * b] = e.x;
+                v[2 * b + 1] = e.y;
+            }
+            tmem_st_x64(lane_base + a.a_col0 + s * (kKB / 2), v);
+            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+            fence_before();
+            mbar_arrive(full_a + s);
+        }
+        // epilogue: D[row, c] + D[row, wpad + c]
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(tmem_full, 0, a.err, 7));
+        fence_after();
+        const uint32_t grow = row0 + row;
+        float* dst = a.out + (uint64_t)blockIdx.y * a.split_stride + (uint64_t)grow * a.ldo;
+        for (uint32_t c0 = 0; c0 < a.wpad; c0 += 16) {
+            float hi[16], lo[16];
+            tmem_ld_x16(lane_base + c0, hi);
+            tmem_ld_x16(lane_base + a.wpad + c0, lo);
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (ok && grow < a.rows) {
+                float4* d4 = reinterpret_cast<float4*>(dst + c0);
+#pragma unroll
+                for (int t = 0; t < 4; ++t)
+                    d4[t] = make_float4(hi[4 * t] + lo[4 * t], hi[4 * t + 1] + lo[4 * t + 1],
+                                        hi[4 * t + 2] + lo[4 * t + 2], hi[4 * t + 3] + lo[4 * t + 3]);
+            }
+        }
+    }
+    fence_before();
+    __syncthreads();
+    if (warp == 1) {
+        fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tmem_cols)
+                     : "memory");
+    }
+}
+
+// W (K x w, row-major, FP32 or FP64, optional per-row scale) -> two BF16
+// matrices hi, lo stored as [2 * wpad][K_pad] (K contiguous), zero padded.
+template <typename T>
+__global__ void k_split_bf16(const T* __restrict__ src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
+                             const double* __restrict__ kscale, __nv_bfloat16* __restrict__ dst) {
+    __shared__ float tile[64][33];
+    const uint64_t k0 = (uint64_t)blockIdx.x * 64;
+    const int c0 = blockIdx.y * 32;
+    for (int e = threadIdx.x; e < 64 * 32; e += blockDim.x) {
+        const int kk = e / 32, cc = e % 32;
+        const uint64_t k = k0 + kk;
+        const int c = c0 + cc;
+        float v = 0.f;
+        if (k < K && c < w) {
+            double x = (double)src[k * ld + c];
+            if (kscale) x *= kscale[k];
+            v = (float)x;
+        }
+        tile[kk][cc] = v;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 64 * 32; e += blockDim.x) {
+        const int cc = e / 64, kk = e % 64;
+        const int c = c0 + cc;
+        if (c >= wpad) continue;
+        const uint64_t k = k0 + kk;
+        if (k >= K_pad) continue;
+        const float v = tile[kk][cc];
+        const __nv_bfloat16 hi = __float2bfloat16_rn(v);
+        const __nv_bfloat16 lo = __float2bfloat16_rn(v - __bfloat162float(hi));
+        dst[(uint64_t)c * K_pad + k] = hi;
+        dst[(uint64_t)(wpad + c) * K_pad + k] = lo;
+    }
+}
+
+// Transposed 2-bit matrix: row i (sample) holds the codes of every SNP.
+__global__ void k_transpose_packed(const uint8_t* __restrict__ in, uint64_t p, uint64_t stride, uint64_t n,
+                                   uint8_t* __restrict__ out, uint64_t strideT) {
+    __shared__ uint8_t tile[128][33];
+    const uint64_t j0 = (uint64_t)blockIdx.x * 128;  // SNPs
+    const uint64_t i0 = (uint64_t)blockIdx.y * 128;  // samples
+    for (int e = threadIdx.x; e < 128 * 32; e += blockDim.x) {
+        const int r = e / 32, b = e % 32;
+        const uint64_t j = j0 + r;
+        tile[r][b] = j < p ? in[j * stride + i0 / 4 + b] : 0;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < 128 * 32; e += blockDim.x) {
+        const int il = e / 32, bj = e % 32;
+        const uint64_t i = i0 + il;
+        if (i >= n) continue;
+        uint32_t byte = 0;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const uint32_t code = (tile[bj * 4 + t][il >> 2] >> (2 * (il & 3))) & 3u;
+            byte |= code << (2 * t);
+        }
+        out[i * strideT + j0 / 4 + bj] = (uint8_t)byte;
+    }
+}
+
+// per-row fix of a row pass (mean imputation):
+//   out[j, c] = s_j * (P[j, c] - mu_j * (cs_c - sum_{i in miss_j} W[i, c]))
+__global__ void k_rowfix_mean(float* __restrict__ P, int ldp, uint64_t rows, int w,
+                              const uint64_t* __restrict__ ptr, const uint32_t* __restrict__ idx,
+                              const float* __restrict__ W, int ldw, const double* __restrict__ cs,
+                              const double* __restrict__ mean, const double* __restrict__ scale) {
+    const uint64_t j = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x & 31;
+    if (j >= rows) return;
+    const uint64_t e0 = ptr[j], e1 = ptr[j + 1];
+    const double mu = mean[j], sc = scale[j];
+    for (int c = lane; c < w; c += 32) {
+        float acc = 0.f;
+        for (uint64_t e = e0; e < e1; ++e) acc += W[(uint64_t)idx[e] * ldw + c];
+        const double v = (double)P[j * ldp + c] - mu * (cs[c] - (double)acc);
+        P[j * ldp + c] = (float)(sc * v);
+    }
+}
+
+// per-sample fix of a forward pass on the transposed matrix (mean imputation):
+//   S[i, c] += sum_{j in missT_i} coef_j Q[j, c] - colterm_c,  coef_j = mu_j s_j
+__global__ void k_colfix_mean(double* __restrict__ S, int lds, uint64_t n, int w,
+                              const uint64_t* __restrict__ ptr, const uint32_t* __restrict__ idx,
+                              const float* __restrict__ Q, int ldq, const double* __restrict__ coef,
+                              const double* __restrict__ colterm) {
+    const uint64_t i = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x & 31;
+    if (i >= n) return;
+    const uint64_t e0 = ptr[i], e1 = ptr[i + 1];
+    for (int c = lane; c < w; c += 32) {
+        double acc = 0.0;
+        for (uint64_t e = e0; e < e1; ++e) {
+            const uint32_t j = idx[e];
+            acc += coef[j] * (double)Q[(uint64_t)j * ldq + c];
+        }
+        S[i * lds + c] += acc - colterm[c];
+    }
+}
+
+// colterm[c] = sum_j coef_j Q[j, c]  (block partials, fixed order)
+__global__ void k_weighted_colsum(const float* __restrict__ Q, int ldq, uint64_t p, int w,
+                                  const double* __restrict__ coef, uint64_t per, double* __restrict__ part) {
+    const int c = threadIdx.x;
+    if (c >= w) return;
+    const uint64_t j0 = (uint64_t)blockIdx.x * per, j1 = min(p, j0 + per);
+    double acc = 0.0;
+    for (uint64_t j = j0; j < j1; ++j) acc += coef[j] * (double)Q[j * ldq + c];
+    part[(uint64_t)blockIdx.x * w + c] = acc;
+}
+
+__global__ void k_scale_product(const double* __restrict__ a, const double* __restrict__ b, uint64_t n,
+                                double* __restrict__ out) {
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x)
+        out[t] = a[t] * b[t];
+}
+
+// -------------------------------------------------------------------------
+// host side
+// -------------------------------------------------------------------------
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        SLFMM_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
+        SLFMM_REQUIRE(q == cudaDriverEntryPointSuccess && p, SLFMM_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
+CUtensorMap map_packed(const uint8_t* base, uint64_t stride, uint64_t rows) {
+    CUtensorMap m;
+    cuuint64_t dims[2] = {stride, rows};
+    cuuint64_t strides[1] = {stride};
+    cuuint32_t box[2] = {kKB / 4, kM};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<uint8_t*>(base), dims, strides, box, es,
+                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    SLFMM_REQUIRE(r == CUDA_SUCCESS, SLFMM_ERR_CUDA, "tensor map (packed) encode failed: " + std::to_string((int)r));
+    return m;
+}
+
+CUtensorMap map_bsplit(const __nv_bfloat16* base, uint64_t k_pad, uint32_t n_rows) {
+    CUtensorMap m;
+    cuuint64_t dims[2] = {k_pad, n_rows};
+    cuuint64_t strides[1] = {k_pad * 2};
+    cuuint32_t box[2] = {64, n_rows};
+    cuuint32_t es[2] = {1, 1};
+    CUresult r = encode_fn()(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<__nv_bfloat16*>(base), dims, strides,
+                             box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    SLFMM_REQUIRE(r == CUDA_SUCCESS, SLFMM_ERR_CUDA, "tensor map (W) encode failed: " + std::to_string((int)r));
+    return m;
+}
+
+struct TcPlan {
+    uint32_t stages, tmem_cols, a_col0, b_stage_bytes;
+    size_t smem;
+};
+
+TcPlan plan(uint32_t wpad) {
+    const uint32_t N = 2 * wpad;
+    TcPlan p;
+    p.b_stage_bytes = 2 * N * 128;
+    const uint32_t dcols = (uint32_t)round_up(N, 64);
+    const size_t fixed = 1024 + 256 * 8 + 64 * 8 + 64;
+    const size_t per_stage = p.b_stage_bytes + kPackedStage;
+    // two CTAs per SM when the stages fit half of TMEM and shared memory
+    uint32_t st2 = std::min<uint32_t>((256 - dcols) / (kKB / 2), (uint32_t)((110 * 1024 - fixed) / per_stage));
+    if (dcols < 256 && st2 >= 2) {
+        p.stages = std::min<uint32_t>(st2, 4);
+        p.tmem_cols = 256;
+    } else {
+        p.stages = std::min<uint32_t>((512 - dcols) / (kKB / 2), (uint32_t)((220 * 1024 - fixed) / per_stage));
+        p.stages = std::min<uint32_t>(p.stages, 6);
+        p.tmem_cols = 512;
+    }
+    p.a_col0 = dcols;
+    p.smem = fixed + p.stages * per_stage;
+    return p;
+}
+
+void check_err(Ctx& c, DBuf<int>& err) {
+    int h = 0;
+    SLFMM_CUDA(cudaMemcpyAsync(&h, err.get(), sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    SLFMM_CUDA(cudaStreamSynchronize(c.stream));
+    if (h != 0)
+        throw Error(SLFMM_ERR_DEVICE_TIMEOUT,
+                    "tensor-core contraction: a bounded device wait expired (site " + std::to_string(h) + ")");
+}
+
+}  // namespace
+
+bool tc_available(Ctx& c) { return c.precision == SLFMM_PREC_SPLIT_BF16; }
+
+void launch_split_bf16_f64(Ctx& c, const double* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
+                           const double* kscale, __nv_bfloat16* dst) {
+    dim3 grid((unsigned)ceil_div(K_pad, 64), (unsigned)ceil_div(wpad, 32));
+    k_split_bf16<double><<<grid, 256, 0, c.stream>>>(src, ld, K, w, wpad, K_pad, kscale, dst);
+    SLFMM_LAUNCHED(c, "k_split_bf16");
+}
+
+void launch_split_bf16_f32(Ctx& c, const float* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
+                           const double* kscale, __nv_bfloat16* dst) {
+    dim3 grid((unsigned)ceil_div(K_pad, 64), (unsigned)ceil_div(wpad, 32));
+    k_split_bf16<float><<<grid, 256, 0, c.stream>>>(src, ld, K, w, wpad, K_pad, kscale, dst);
+    SLFMM_LAUNCHED(c, "k_split_bf16");
+}
+
+void build_transposed(Ctx& c, const Geno& g) {
+    if (g.have_T) return;
+    g.strideT = round_up(ceil_div(g.p, 4), 128);
+    g.packedT.alloc(g.n * g.strideT, c.stream);
+    SLFMM_CUDA(cudaMemsetAsync(g.packedT.get(), 0, g.n * g.strideT, c.stream));
+    dim3 grid((unsigned)ceil_div(g.p, 128), (unsigned)ceil_div(g.n, 128));
+    k_transpose_packed<<<grid, 256, 0, c.stream>>>(g.packed.get(), g.p, g.stride, g.n, g.packedT.get(), g.strideT);
+    SLFMM_LAUNCHED(c, "k_transpose_packed");
+    g.have_T = true;
+}
+
+// out (rows x ldo, or splits x rows x ldo) = G^T-style product of the packed
+// rows with the split W (B operand [2 wpad][K_pad]).
+void launch_tc_rows(Ctx& c, const uint8_t* packed, uint64_t stride, uint64_t rows, uint64_t K,
+                    const __nv_bfloat16* bsplit, uint64_t K_pad, int wpad, float* out, int ldo, int splits,
+                    uint64_t split_stride) {
+    SLFMM_REQUIRE(wpad % 16 == 0 && wpad >= 16 && 2 * wpad <= 256, SLFMM_ERR_BAD_ARG,
+                  "tensor-core operand width must be a multiple of 16 in [16, 128]");
+    SLFMM_REQUIRE(K_pad % kKB == 0 && K_pad >= ceil_div(K, kKB) * kKB, SLFMM_ERR_BAD_ARG, "bad K padding");
+    SLFMM_REQUIRE(stride % 16 == 0 && stride * 4 >= ceil_div(K, kKB) * kKB, SLFMM_ERR_BAD_ARG, "bad packed stride");
+    SLFMM_REQUIRE(rows < (1ull << 31), SLFMM_ERR_BAD_ARG, "too many rows");
+    const TcPlan pl = plan((uint32_t)wpad);
+    static thread_local size_t configured = 0;
+    if (configured < pl.smem) {
+        SLFMM_CUDA(cudaFuncSetAttribute(k_tc_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
+        configured = pl.smem;
+    }
+    const CUtensorMap tp = map_packed(packed, stride, rows);
+    const CUtensorMap tb = map_bsplit(bsplit, K_pad, 2 * wpad);
+    DBuf<int> err(1, c.stream);
+    err.zero();
+    TcArgs a;
+    a.rows = (uint32_t)rows;
+    a.kb_total = (uint32_t)ceil_div(K, kKB);
+    a.kb_per_split = (uint32_t)ceil_div(a.kb_total, (uint64_t)std::max(splits, 1));
+    a.wpad = (uint32_t)wpad;
+    a.stages = pl.stages;
+    a.tmem_cols = pl.tmem_cols;
+    a.a_col0 = pl.a_col0;
+    a.b_stage_bytes = pl.b_stage_bytes;
+    a.out = out;
+    a.ldo = (uint32_t)ldo;
+    a.split_stride = split_stride;
+    a.err = err.get();
+    const unsigned gy = (unsigned)ceil_div(a.kb_total, a.kb_per_split);
+    dim3 grid((unsigned)ceil_div(rows, kM), gy);
+    k_tc_rows<<<grid, kThreads, pl.smem, c.stream>>>(tp, tb, a);
+    SLFMM_LAUNCHED(c, "k_tc_rows");
+    check_err(c, err);
+}
+
+int tc_split_count(Ctx& c, uint64_t rows, uint64_t K) {
+    const uint64_t tiles = ceil_div(rows, kM);
+    const uint64_t kb = ceil_div(K, kKB);
+    uint64_t want = ceil_div((uint64_t)c.sm_count * 2, tiles);
+    want = std::max<uint64_t>(1, std::min<uint64_t>(want, kb));
+    return (int)want;
+}
+
+void launch_rowfix_mean(Ctx& c, float* P, int ldp, uint64_t rows, int w, const uint64_t* ptr, const uint32_t* idx,
+                        const float* W, int ldw, const double* cs, const double* mean, const double* scale) {
+    if (!rows) return;
+    k_rowfix_mean<<<(unsigned)ceil_div(rows * 32, 256), 256, 0, c.stream>>>(P, ldp, rows, w, ptr, idx, W, ldw, cs,
+                                                                           mean, scale);
+    SLFMM_LAUNCHED(c, "k_rowfix_mean");
+}
+
+void launch_colfix_mean(Ctx& c, double* S, int lds, uint64_t n, int w, const uint64_t* ptr, const uint32_t* idx,
+                        const float* Q, int ldq, const double* coef, const double* colterm) {
+    if (!n) return;
+    k_colfix_mean<<<(unsigned)ceil_div(n * 32, 256), 256, 0, c.stream>>>(S, lds, n, w, ptr, idx, Q, ldq, coef,
+                                                                        colterm);
+    SLFMM_LAUNCHED(c, "k_colfix_mean");
+}
+
+void launch_weighted_colsum(Ctx& c, const float* Q, int ldq, uint64_t p, int w, const double* coef, double* out) {
+    SLFMM_REQUIRE(w <= 128, SLFMM_ERR_BAD_ARG, "width");
+    const uint64_t blocks = std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(p, 4096), 1024));
+    const uint64_t per = ceil_div(std::max<uint64_t>(p, 1), blocks);
+    DBuf<double> part(blocks * w, c.stream);
+    k_weighted_colsum<<<(unsigned)blocks, 128, 0, c.stream>>>(Q, ldq, p, w, coef, per, part.get());
+    SLFMM_LAUNCHED(c, "k_weighted_colsum");
+    launch_sum_partials(c, part.get(), (int)blocks, (uint64_t)w, out);
+}
+
+void launch_scale_product(Ctx& c, const double* a, const double* b, uint64_t n, double* out) {
+    if (!n) return;
+    k_scale_product<<<grid_for(c, n, 256), 256, 0, c.stream>>>(a, b, n, out);
+    SLFMM_LAUNCHED(c, "k_scale_product");
+}
+
+}  // namespace slfmm

@@ -1,6 +1,7 @@
 // Internal declarations of the schnelgpu runtime (host C++ + sm_103a kernels).
 #pragma once
 
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <cstdio>
@@ -108,6 +109,10 @@ struct Geno {
     mutable bool have_csc = false;
     mutable DBuf<uint64_t> missT_ptr;  // n+1, CSC by sample
     mutable DBuf<uint32_t> missT_idx;  // nnz SNP indices (ascending)
+    // transposed copy (rows = samples, codes of every SNP), built on first use
+    mutable bool have_T = false;
+    mutable uint64_t strideT = 0;
+    mutable DBuf<uint8_t> packedT;     // n x strideT
 };
 
 // ---------------------------------------------------------------------------
@@ -201,15 +206,34 @@ void launch_row_lut(Ctx& c, const Geno& g, const float* lut, const float* W, int
 // S[i, c] = sum_j lut_j[code_ij] * Q[j, c]        (FP64 result, n x wp)
 void launch_col_lut(Ctx& c, const Geno& g, const float* lut, const float* Q, int wp, double* S);
 
+void launch_reduce_splits(Ctx& c, const float* part, int splits, uint64_t n, int wp, uint64_t n_pad,
+                          double* S);
+
 // k_tc.cu : tcgen05 split-BF16 contractions
 bool tc_available(Ctx& c);
-// out[j, c] = sum_i g_ij * W[i, c] with exact genotypes (missing -> 0)
-void launch_row_tc(Ctx& c, const Geno& g, const float* W, int w, float* out, int ldo);
-// S[i, c] = sum_j g_ij * Q[j, c]  (missing -> 0), FP64 n x ldS
-void launch_col_tc(Ctx& c, const Geno& g, const float* Q, int w, double* S, int ldS);
+// W (K x w, ld) -> [2 wpad][K_pad] BF16 hi/lo (optional per-K-row scale)
+void launch_split_bf16_f64(Ctx& c, const double* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
+                           const double* kscale, __nv_bfloat16* dst);
+void launch_split_bf16_f32(Ctx& c, const float* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
+                           const double* kscale, __nv_bfloat16* dst);
+void build_transposed(Ctx& c, const Geno& g);
+// out[r, c] = sum_k g(r, k) * (hi + lo)[c, k] over packed rows; split-K over
+// grid.y writes splits x rows x ldo partials (split_stride apart)
+void launch_tc_rows(Ctx& c, const uint8_t* packed, uint64_t stride, uint64_t rows, uint64_t K,
+                    const __nv_bfloat16* bsplit, uint64_t K_pad, int wpad, float* out, int ldo, int splits,
+                    uint64_t split_stride);
+int tc_split_count(Ctx& c, uint64_t rows, uint64_t K);
+void launch_rowfix_mean(Ctx& c, float* P, int ldp, uint64_t rows, int w, const uint64_t* ptr, const uint32_t* idx,
+                        const float* W, int ldw, const double* cs, const double* mean, const double* scale);
+void launch_colfix_mean(Ctx& c, double* S, int lds, uint64_t n, int w, const uint64_t* ptr, const uint32_t* idx,
+                        const float* Q, int ldq, const double* coef, const double* colterm);
+void launch_weighted_colsum(Ctx& c, const float* Q, int ldq, uint64_t p, int w, const double* coef, double* out);
+void launch_scale_product(Ctx& c, const double* a, const double* b, uint64_t n, double* out);
 
 // k_small.cu : FP64 dense helpers (row-major)
 void launch_colmeans(Ctx& c, const double* A, uint64_t m, int a, int lda, double* out);
+void launch_colsums(Ctx& c, const double* A, uint64_t m, int a, int lda, double* out);
+void launch_sum_partials(Ctx& c, const double* part, int splits, uint64_t count, double* out);
 void launch_center_cols(Ctx& c, double* A, uint64_t m, int a, int lda, const double* means);
 void launch_scale_cols_sd(Ctx& c, double* A, uint64_t m, int a, int lda);
 void launch_atb(Ctx& c, const double* A, int lda, const double* B, int ldb, uint64_t m, int a,
