@@ -46,6 +46,10 @@ WORKLOADS = {
     "biobank": dict(n=20_000, p=2_000_000, k=20, d=50, oversampling=10, power_iter=2, n_pop=10, alpha=0.3,
                     fst=0.05, f_lo=0.01, f_hi=0.5, miss=0.005, inbreeding=0.0, lam=1e-5, mask_max=0.3,
                     est_rate=None),
+    # same per-SNP shape on 100k SNPs (profiling slice, ~0.5 GB packed)
+    "biobank-slice": dict(n=20_000, p=100_000, k=20, d=50, oversampling=10, power_iter=2, n_pop=10, alpha=0.3,
+                          fst=0.05, f_lo=0.01, f_hi=0.5, miss=0.005, inbreeding=0.0, lam=1e-5, mask_max=0.3,
+                          est_rate=None),
     # inbred-plant shape (parity/scale case)
     "plant": dict(n=1_135, p=1_800_000, k=12, d=1, oversampling=10, power_iter=2, n_pop=8, alpha=0.5,
                   fst=0.1, f_lo=0.01, f_hi=0.5, miss=0.02, inbreeding=0.9, lam=1e-5, mask_max=0.0,
@@ -186,7 +190,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="biobank")
-    ap.add_argument("--precision", choices=["split_bf16", "fp32"], default="split_bf16")
+    ap.add_argument("--precision", choices=["split_fp8", "split_bf16", "fp32"], default="split_fp8")
     ap.add_argument("--cpu-sample", type=int, default=1000, help="SNPs in the CPU baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp32-path", action="store_true")
@@ -235,7 +239,8 @@ def main():
         torch.cuda.set_device(0)
     dev = local_rank if world > 1 else 0
     torch_stream = torch.cuda.current_stream()
-    prec = sg.Precision.SPLIT_BF16 if args.precision == "split_bf16" else sg.Precision.FP32
+    prec = {"split_fp8": sg.Precision.SPLIT_FP8, "split_bf16": sg.Precision.SPLIT_BF16,
+            "fp32": sg.Precision.FP32}[args.precision]
     eng = sg.Engine(dev, prec, stream=torch_stream.cuda_stream)
     n, p, d, k = w["n"], w["p"], w["d"], w["k"]
     rng = np.random.default_rng(100 + rank)
@@ -369,8 +374,9 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": "SNPs/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "bf16x2 split (exact bf16 genotypes, fp32 accumulate)" if prec == sg.Precision.SPLIT_BF16
-                else "fp32",
+                "dtype": {sg.Precision.SPLIT_FP8: "e4m3x4 split (exact e4m3 genotypes, fp32 accumulate)",
+                          sg.Precision.SPLIT_BF16: "bf16x2 split (exact bf16 genotypes, fp32 accumulate)",
+                          sg.Precision.FP32: "fp32"}[prec],
                 "data": "synthetic (seeded structured cohort drawn on the device)",
                 "config": config, "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
                 "cpu_baseline": cpu, "fp32_gpu_path": fp32, "clocks": clk.summary()}

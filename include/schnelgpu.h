@@ -46,6 +46,9 @@ extern "C" {
 #define SLFMM_PREC_FP32        0      /* plain FP32 SIMT contractions            */
 #define SLFMM_PREC_SPLIT_BF16  1      /* tcgen05 tensor cores, exact BF16
                                          genotypes x hi+lo BF16 operand          */
+#define SLFMM_PREC_SPLIT_FP8   2      /* tcgen05 kind::f8f6f4, exact E4M3
+                                         genotypes x 4 scaled E4M3 terms, exact
+                                         missing-call operand (default)          */
 
 #define SLFMM_IMPUTE_MEAN      0      /* ImputeStrategy::Mean (src/lib.rs:39-44) */
 #define SLFMM_IMPUTE_NMF       1      /* ImputeStrategy::Nmf                     */
@@ -148,10 +151,12 @@ int slfmm_decode_chunk(slfmm_ctx* ctx, const slfmm_geno* g, uint64_t snp0,
                        uint64_t ncols, int norm, double* out);
 
 /* Raw tensor-core contraction of the exact genotypes (missing calls = 0)
- * with the hi + lo BF16 split of W: transposed = 0 gives out (p x w) =
- * G~^T W for W n x w; transposed = 1 gives out (n x w) = G~ W for W p x w.
- * Parity hook for the per-chunk dgemms of src/rsvd.rs:61-153. */
-int slfmm_contract_raw(slfmm_ctx* ctx, const slfmm_geno* g, int transposed, const double* w,
+ * with the split operand of the context's precision.  flags bit 0: 0 gives
+ * out (p x w) = G~^T W for W n x w, 1 gives out (n x w) = G~ W for W p x w
+ * (transposed copy); bit 1 (split-FP8 only): add the missing-call indicator
+ * product, i.e. missing calls count as 1.  Parity hook for the per-chunk
+ * dgemms of src/rsvd.rs:61-153. */
+int slfmm_contract_raw(slfmm_ctx* ctx, const slfmm_geno* g, int flags, const double* w,
                        uint32_t w_cols, float* out);
 
 /* ---- library API (src/lib.rs) ------------------------------------------- */

@@ -26,6 +26,7 @@ from __future__ import annotations
 
 import ctypes as C
 import enum
+import weakref
 import math
 import os
 from dataclasses import dataclass, field
@@ -67,6 +68,7 @@ class ImputeStrategy(enum.IntEnum):
 class Precision(enum.IntEnum):
     FP32 = 0
     SPLIT_BF16 = 1
+    SPLIT_FP8 = 2
 
 
 # ---------------------------------------------------------------------------
@@ -297,7 +299,7 @@ class TestResults:
 class Engine:
     """One CUDA context + stream on one device (replaces the worker pool)."""
 
-    def __init__(self, device: int = 0, precision: Precision = Precision.SPLIT_BF16, stream: Optional[int] = None,
+    def __init__(self, device: int = 0, precision: Precision = Precision.SPLIT_FP8, stream: Optional[int] = None,
                  verbose: bool = False):
         self.lib = load_library()
         opts = _Opts(int(precision), int(verbose), C.c_void_p(stream) if stream else None)
@@ -307,9 +309,12 @@ class Engine:
             raise SchnelGpuError(rc, f"slfmm_create failed ({rc})")
         self.h = h
         self.precision = Precision(precision)
+        self._genos = weakref.WeakSet()
 
     def close(self):
         if getattr(self, "h", None):
+            for g in list(self._genos):     # device buffers go first, on a live stream
+                g.free()
             self.lib.slfmm_destroy(self.h)
             self.h = None
 
@@ -391,6 +396,7 @@ class Genotypes:
     def __init__(self, eng: Engine, h: C.c_void_p):
         self.eng = eng
         self.h = h
+        eng._genos.add(self)
 
     @property
     def n_samples(self) -> int:
@@ -402,7 +408,7 @@ class Genotypes:
 
     def free(self):
         if self.h:
-            self.eng.lib.slfmm_geno_free(self.eng.h, self.h)
+            self.eng.lib.slfmm_geno_free(self.eng.h, self.h)   # eng.h may be None: default stream
             self.h = None
 
     def __del__(self):
@@ -427,14 +433,15 @@ class Genotypes:
         self.eng.check(self.eng.lib.slfmm_geno_download(self.eng.h, self.h, _ptr(out)))
         return out
 
-    def contract_raw(self, w: np.ndarray, transposed: bool = False) -> np.ndarray:
-        """Tensor-core product of the exact genotypes (missing = 0) with the
-        BF16 hi+lo split of ``w``: G~^T w (w is n x c) or G~ w (w is p x c)."""
+    def contract_raw(self, w: np.ndarray, transposed: bool = False, missing_as_one: bool = False) -> np.ndarray:
+        """Tensor-core product of the exact genotypes (missing = 0, or 1 with
+        ``missing_as_one``) with the engine's split of ``w``: G~^T w (w is
+        n x c) or G~ w (w is p x c)."""
         w = np.ascontiguousarray(w, dtype=np.float64)
         rows = self.n_samples if transposed else self.n_snps
         out = np.empty((rows, w.shape[1]), dtype=np.float32)
-        self.eng.check(self.eng.lib.slfmm_contract_raw(self.eng.h, self.h, int(transposed), _ptr(w), w.shape[1],
-                                                       _ptr(out)))
+        flags = int(transposed) | (2 if missing_as_one else 0)
+        self.eng.check(self.eng.lib.slfmm_contract_raw(self.eng.h, self.h, flags, _ptr(w), w.shape[1], _ptr(out)))
         return out
 
     def decode_chunk(self, snp0: int, ncols: int, norm: SnpNorm) -> np.ndarray:

@@ -236,6 +236,38 @@ void row_contract(Ctx& c, const Geno& g, const SnpStd& s, const double* W, int w
     launch_f64_to_f32_pad(c, W, g.n, w, ldw, W32.get(), n_pad, wp);
     out.alloc(std::max<uint64_t>(g.p, 1) * wp, c.stream);
     const double bytes = (double)g.p * ceil_div(g.n, 4) + (double)g.p * w * 4 + (double)g.n * w * 4;
+    if (c.precision == SLFMM_PREC_SPLIT_FP8) {
+        // exact E4M3 genotypes x 4 scaled E4M3 terms of W; with the missing-call
+        // indicator operand the epilogue applies out = s_j (P - mu_j (cs - M)).
+        // Operands too wide for TMEM run as column blocks of 64.
+        const uint64_t tiles = ceil_div(g.p, 128);
+        Fp8Plan pl = fp8_plan(wp, true, tiles);
+        const bool ind = pl.ok;
+        if (!ind) pl = fp8_plan(wp, false, tiles);
+        const int cb = pl.ok ? wp : 64;
+        DBuf<double> cs(wp, c.stream);
+        cs.zero();
+        launch_colsums(c, W, g.n, w, ldw, cs.get());
+        for (int c0 = 0; c0 < w; c0 += cb) {
+            // the epilogue writes pb.wpad columns: the last block is padded only to 16
+            const int wb = std::min(cb, w - c0), bp = std::min(cb, pad16(wb));
+            const Fp8Plan pb = bp == wp ? pl : fp8_plan(bp, false, tiles);
+            DBuf<uint8_t> B((uint64_t)pb.n_total * n_pad, c.stream);
+            DBuf<float> isc(pb.n_total, c.stream);
+            launch_fp8_terms_f64(c, W + c0, ldw, g.n, wb, bp, n_pad, nullptr, 4, 0, B.get(), isc.get());
+            if (ind) launch_fp8_terms_f64(c, W + c0, ldw, g.n, wb, bp, n_pad, nullptr, 3, (int)pb.n_main, B.get(),
+                                          isc.get());
+            ProfScope ps(c, "row_contract", bytes * wb / w, 2.0 * g.n * g.p * wb);
+            launch_tc8_rows(c, pb, g.packed.get(), g.stride, g.p, g.n, B.get(), isc.get(), n_pad, ind ? 1 : 0,
+                            s.mean.get(), s.scale.get(), cs.get(), out.get() + c0, wp, 1, 0);
+        }
+        if (!ind) {
+            build_missing_lists(c, g);
+            launch_rowfix_mean(c, out.get(), wp, g.p, w, g.miss_ptr.get(), g.miss_idx.get(), W32.get(), wp,
+                               cs.get(), s.mean.get(), s.scale.get());
+        }
+        return;
+    }
     if (tc_available(c)) {
         // exact genotypes x (hi + lo) BF16 split of W on the tensor cores, then
         // out = s_j (P - mu_j (colsum(W) - sum_{missing} W))
@@ -261,6 +293,41 @@ void row_contract(Ctx& c, const Geno& g, const SnpStd& s, const double* W, int w
 void col_contract(Ctx& c, const Geno& g, const SnpStd& s, const float* Q, int w, int wp, DBuf<double>& S) {
     S.alloc(g.n * wp, c.stream);
     const double bytes = (double)g.p * ceil_div(g.n, 4) + (double)g.p * w * 4 + (double)g.n * w * 8;
+    if (c.precision == SLFMM_PREC_SPLIT_FP8) {
+        // forward pass on the transposed matrix: terms of diag(s) Q against the
+        // genotypes plus terms of diag(mu s) Q against the missing-call
+        // indicator, then S -= (mu s)^T Q
+        build_transposed(c, g);
+        const uint64_t p_pad = round_up(g.p, 128);
+        const uint64_t tiles = ceil_div(g.n, 128);
+        Fp8Plan pl = fp8_plan(wp, true, tiles);
+        const bool ind = pl.ok;
+        if (!ind) pl = fp8_plan(wp, false, tiles);
+        DBuf<uint8_t> B((uint64_t)pl.n_total * p_pad, c.stream);
+        DBuf<float> isc(pl.n_total, c.stream);
+        DBuf<double> coef(std::max<uint64_t>(g.p, 1), c.stream), colterm(wp, c.stream);
+        launch_scale_product(c, s.mean.get(), s.scale.get(), g.p, coef.get());
+        launch_fp8_terms_f32(c, Q, wp, g.p, w, wp, p_pad, s.scale.get(), 4, 0, B.get(), isc.get());
+        if (ind) launch_fp8_terms_f32(c, Q, wp, g.p, w, wp, p_pad, coef.get(), 3, (int)pl.n_main, B.get(), isc.get());
+        const int splits = tc_split_count(c, g.n, g.p);
+        DBuf<float> part((uint64_t)splits * g.n * wp, c.stream);
+        int used = 0;
+        {
+            ProfScope ps(c, "col_contract", bytes, 2.0 * g.n * g.p * w);
+            used = launch_tc8_rows(c, pl, g.packedT.get(), g.strideT, g.n, g.p, B.get(), isc.get(), p_pad, 0, nullptr,
+                                   nullptr, nullptr, part.get(), wp, splits, g.n * wp);
+        }
+        launch_reduce_splits(c, part.get(), used, g.n, wp, g.n, S.get());
+        launch_weighted_colsum(c, Q, wp, g.p, w, coef.get(), colterm.get());
+        if (ind) {
+            launch_sub_colterm(c, S.get(), wp, g.n, w, colterm.get());
+        } else {
+            build_missing_csc(c, g);
+            launch_colfix_mean(c, S.get(), wp, g.n, w, g.missT_ptr.get(), g.missT_idx.get(), Q, wp, coef.get(),
+                               colterm.get());
+        }
+        return;
+    }
     if (tc_available(c)) {
         // forward pass on the transposed matrix (rows = samples, K = SNPs):
         // S = G~ (diag(s) Q) - 1 (mu s)^T Q + missing-call corrections
@@ -271,12 +338,13 @@ void col_contract(Ctx& c, const Geno& g, const SnpStd& s, const float* Q, int w,
         launch_split_bf16_f32(c, Q, wp, g.p, w, wp, p_pad, s.scale.get(), bs.get());
         const int splits = tc_split_count(c, g.n, g.p);
         DBuf<float> part((uint64_t)splits * g.n * wp, c.stream);
+        int used = 0;
         {
             ProfScope ps(c, "col_contract", bytes, 2.0 * g.n * g.p * w);
-            launch_tc_rows(c, g.packedT.get(), g.strideT, g.n, g.p, bs.get(), p_pad, wp, part.get(), wp, splits,
-                           g.n * wp);
+            used = launch_tc_rows(c, g.packedT.get(), g.strideT, g.n, g.p, bs.get(), p_pad, wp, part.get(), wp, splits,
+                                  g.n * wp);
         }
-        launch_reduce_splits(c, part.get(), splits, g.n, wp, g.n, S.get());
+        launch_reduce_splits(c, part.get(), used, g.n, wp, g.n, S.get());
         DBuf<double> coef(std::max<uint64_t>(g.p, 1), c.stream), colterm(wp, c.stream);
         launch_scale_product(c, s.mean.get(), s.scale.get(), g.p, coef.get());
         launch_weighted_colsum(c, Q, wp, g.p, w, coef.get(), colterm.get());
@@ -765,7 +833,11 @@ int slfmm_geno_upload(slfmm_ctx* c, const uint8_t* packed, uint64_t n_physical, 
 int slfmm_geno_free(slfmm_ctx* c, slfmm_geno* g) {
     if (!g) return SLFMM_OK;
     if (c) cudaSetDevice(c->device);
+    // the context that allocated the buffers may already be destroyed: free on
+    // the given context's stream, or on the legacy default stream
+    g->rebind(c ? c->stream : (cudaStream_t)0);
     delete g;
+    if (!c) cudaDeviceSynchronize();
     return SLFMM_OK;
 }
 
@@ -965,24 +1037,43 @@ int slfmm_profile_read(slfmm_ctx* c, const char* kernel, double* total_ms, uint6
     API_CATCH(c)
 }
 
-int slfmm_contract_raw(slfmm_ctx* c, const slfmm_geno* g, int transposed, const double* w_host, uint32_t w,
+int slfmm_contract_raw(slfmm_ctx* c, const slfmm_geno* g, int flags, const double* w_host, uint32_t w,
                        float* out) {
     if (!c || !g || !w_host || !out) return SLFMM_ERR_BAD_ARG;
     API_TRY
     SLFMM_CUDA(cudaSetDevice(c->device));
+    const bool transposed = (flags & 1) != 0, with_ind = (flags & 2) != 0;
     const int wp = pad16((int)w);
     SLFMM_REQUIRE(wp <= kMaxW, SLFMM_ERR_BAD_ARG, "operand wider than 128 columns");
     const uint64_t K = transposed ? g->p : g->n, rows = transposed ? g->n : g->p;
     const uint64_t K_pad = round_up(K, 128);
     DBuf<double> Wd = upload(*c, w_host, K * w);
-    DBuf<__nv_bfloat16> bs(2 * (uint64_t)wp * K_pad, c->stream);
-    launch_split_bf16_f64(*c, Wd.get(), (int)w, K, (int)w, wp, K_pad, nullptr, bs.get());
     DBuf<float> o(std::max<uint64_t>(rows, 1) * wp, c->stream);
-    if (transposed) {
-        build_transposed(*c, *g);
-        launch_tc_rows(*c, g->packedT.get(), g->strideT, rows, K, bs.get(), K_pad, wp, o.get(), wp, 1, 0);
+    if (transposed) build_transposed(*c, *g);
+    const uint8_t* pk = transposed ? g->packedT.get() : g->packed.get();
+    const uint64_t st = transposed ? g->strideT : g->stride;
+    if (c->precision == SLFMM_PREC_SPLIT_FP8) {
+        const uint64_t tiles = ceil_div(rows, 128);
+        const Fp8Plan pl = fp8_plan(wp, with_ind, tiles);
+        SLFMM_REQUIRE(pl.ok || !with_ind, SLFMM_ERR_BAD_ARG, "indicator operand too wide for one launch");
+        const int cb = pl.ok ? wp : 64;
+        for (int c0 = 0; c0 < (int)w; c0 += cb) {
+            const int wb = std::min(cb, (int)w - c0), bp = std::min(cb, pad16(wb));
+            const Fp8Plan pb = bp == wp ? pl : fp8_plan(bp, false, tiles);
+            DBuf<uint8_t> B((uint64_t)pb.n_total * K_pad, c->stream);
+            DBuf<float> isc(pb.n_total, c->stream);
+            launch_fp8_terms_f64(*c, Wd.get() + c0, (int)w, K, wb, bp, K_pad, nullptr, 4, 0, B.get(), isc.get());
+            if (with_ind)
+                launch_fp8_terms_f64(*c, Wd.get() + c0, (int)w, K, wb, bp, K_pad, nullptr, 3, (int)pb.n_main, B.get(),
+                                     isc.get());
+            launch_tc8_rows(*c, pb, pk, st, rows, K, B.get(), isc.get(), K_pad, 0, nullptr, nullptr, nullptr,
+                            o.get() + c0, wp, 1, 0);
+        }
     } else {
-        launch_tc_rows(*c, g->packed.get(), g->stride, rows, K, bs.get(), K_pad, wp, o.get(), wp, 1, 0);
+        SLFMM_REQUIRE(!with_ind, SLFMM_ERR_BAD_ARG, "indicator operand needs the split-FP8 precision");
+        DBuf<__nv_bfloat16> bs(2 * (uint64_t)wp * K_pad, c->stream);
+        launch_split_bf16_f64(*c, Wd.get(), (int)w, K, (int)w, wp, K_pad, nullptr, bs.get());
+        launch_tc_rows(*c, pk, st, rows, K, bs.get(), K_pad, wp, o.get(), wp, 1, 0);
     }
     SLFMM_CUDA(cudaMemcpy2DAsync(out, w * sizeof(float), o.get(), wp * sizeof(float), w * sizeof(float), rows,
                                  cudaMemcpyDeviceToHost, c->stream));

@@ -157,7 +157,9 @@ __global__ void __launch_bounds__(1024) k_gif(const uint32_t* __restrict__ hist,
     }
 }
 
-// p = 2 * Phi(-|t| / sqrt(GIF_j)) = erfc(|z| / sqrt 2)  (src/testing.rs:691-712)
+// p = 2 * Phi(-|t| / sqrt(GIF_j)) = erfc(|z| / sqrt 2)  (src/testing.rs:691-712).
+// The statistic is FP32, so erfcf carries its precision; the FP64 erfc is
+// only used in the far tail where erfcf would leave the normal FP32 range.
 __global__ void k_calibrate(uint64_t p, int d, const float* __restrict__ t32,
                             const double* __restrict__ gif, double* __restrict__ t64,
                             double* __restrict__ pval) {
@@ -165,11 +167,15 @@ __global__ void k_calibrate(uint64_t p, int d, const float* __restrict__ t32,
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < total;
          e += (uint64_t)gridDim.x * blockDim.x) {
         const int jj = (int)(e % d);
-        const double t = (double)t32[e];
-        if (t64) t64[e] = t;
+        const float tf = t32[e];
+        if (t64) t64[e] = (double)tf;
         if (pval) {
-            const double z = t / sqrt(gif[jj]);
-            pval[e] = 2.0 * (0.5 * erfc(fabs(z) / 1.4142135623730951));
+            const double g = gif[jj];
+            const float zf = fabsf(tf) * (float)(0.7071067811865476 / sqrt(g));
+            double pv;
+            if (zf < 8.0f) pv = (double)erfcf(zf);
+            else pv = 2.0 * (0.5 * erfc(fabs((double)tf / sqrt(g)) / 1.4142135623730951));
+            pval[e] = pv;
         }
     }
 }

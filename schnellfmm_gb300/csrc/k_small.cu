@@ -191,22 +191,33 @@ __global__ void k_gemm_small(const double* __restrict__ A, int lda, uint64_t m, 
 }
 
 // A (m x a, FP32) <- A * Linv^T with Linv lower-triangular (a x a, FP64),
-// i.e. A <- A R^-1 for the Cholesky factor R = L^T of A^T A.
-__global__ void k_trmul_f32(float* __restrict__ A, int lda, uint64_t m, int a,
-                            const double* __restrict__ Linv) {
-    __shared__ float R[64 * 64];  // R[k][c] = Linv[c][k]
-    for (int e = threadIdx.x; e < a * a; e += blockDim.x) R[(e % a) * a + e / a] = (float)Linv[e];
+// i.e. A <- A R^-1 for the Cholesky factor R = L^T of A^T A.  The row lives
+// in registers (fully unrolled up to AMAX columns).
+template <int AMAX>
+__global__ void __launch_bounds__(128) k_trmul_f32(float* __restrict__ A, int lda, uint64_t m, int a,
+                                                   const double* __restrict__ Linv) {
+    __shared__ float R[AMAX * AMAX];  // R[k][c] = Linv[c][k], zero padded
+    for (int e = threadIdx.x; e < AMAX * AMAX; e += blockDim.x) {
+        const int k = e / AMAX, cc = e % AMAX;
+        R[e] = (k < a && cc < a) ? (float)Linv[cc * a + k] : 0.f;
+    }
     __syncthreads();
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < m;
          i += (uint64_t)gridDim.x * blockDim.x) {
-        float row[64];
+        float row[AMAX], out[AMAX];
         float* ar = A + i * lda;
-        for (int k = 0; k < a; ++k) row[k] = ar[k];
-        for (int cc = a - 1; cc >= 0; --cc) {
-            float s = 0.f;
-            for (int k = 0; k <= cc; ++k) s = fmaf(row[k], R[k * a + cc], s);
-            ar[cc] = s;
+#pragma unroll
+        for (int k = 0; k < AMAX; ++k) {
+            row[k] = k < a ? ar[k] : 0.f;
+            out[k] = 0.f;
         }
+#pragma unroll
+        for (int k = 0; k < AMAX; ++k)
+#pragma unroll
+            for (int cc = k; cc < AMAX; ++cc) out[cc] = fmaf(row[k], R[k * AMAX + cc], out[cc]);
+#pragma unroll
+        for (int k = 0; k < AMAX; ++k)
+            if (k < a) ar[k] = out[k];
     }
 }
 
@@ -381,7 +392,6 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(double* __restrict__ A, int
     const int ap = a + (a & 1);     // even number of columns (padded column is zero)
     double* M = sm;                 // column-major ap x ap (rows a used)
     double* Vs = sm + ap * ap;      // column-major
-    __shared__ int pairs[64];
     __shared__ int rotated;
     __shared__ double sg[64];
     __shared__ int order[64];
@@ -393,20 +403,16 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(double* __restrict__ A, int
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
     const int npairs = ap / 2;
-    for (int sweep = 0; sweep < 60; ++sweep) {
+    // convergence: |<a_p, a_q>| <= tol * ||a_p|| ||a_q|| for every pair
+    const double tol = 4.0e-16 * (double)(a > 8 ? a : 8);
+    for (int sweep = 0; sweep < 40; ++sweep) {
         if (threadIdx.x == 0) rotated = 0;
         __syncthreads();
         for (int round = 0; round < ap - 1; ++round) {
-            if (threadIdx.x < npairs) {
-                // round-robin tournament: player 0 fixed, others rotate
-                const int k = threadIdx.x;
-                auto pos = [&](int idx) { return idx == 0 ? 0 : 1 + ((idx - 1 + round) % (ap - 1)); };
-                pairs[2 * k] = pos(k);
-                pairs[2 * k + 1] = pos(ap - 1 - k);
-            }
-            __syncthreads();
             for (int pr = warp; pr < npairs; pr += nwarps) {
-                int pcol = pairs[2 * pr], qcol = pairs[2 * pr + 1];
+                // round-robin tournament: player 0 fixed, the others rotate
+                auto pos = [&](int idx) { return idx == 0 ? 0 : 1 + ((idx - 1 + round) % (ap - 1)); };
+                int pcol = pos(pr), qcol = pos(ap - 1 - pr);
                 if (pcol > qcol) { const int t = pcol; pcol = qcol; qcol = t; }
                 double* mp = M + pcol * ap;
                 double* mq = M + qcol * ap;
@@ -419,7 +425,7 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(double* __restrict__ A, int
                 al = warp_sum(al);
                 be = warp_sum(be);
                 ga = warp_sum(ga);
-                if (fabs(ga) > 1e-15 * sqrt(al * be) && fabs(ga) > 1e-300) {
+                if (fabs(ga) > tol * sqrt(al * be) && fabs(ga) > 1e-300) {
                     const double zeta = (be - al) / (2.0 * ga);
                     const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
                     const double cs = 1.0 / sqrt(1.0 + t * t), sn = cs * t;
@@ -585,8 +591,8 @@ template <typename T>
 static void atb_impl(Ctx& c, const T* A, int lda, const T* B, int ldb, uint64_t m, int a, int b,
                      double* out) {
     const int ta = (int)ceil_div(a, 32), tb = (int)ceil_div(b, 32);
-    uint64_t splits = std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(m, 2048),
-                                          ceil_div((uint64_t)c.sm_count * 4, (uint64_t)ta * tb)));
+    uint64_t splits = std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(m, 256),
+                                          ceil_div((uint64_t)c.sm_count * 8, (uint64_t)ta * tb)));
     splits = std::min<uint64_t>(splits, 65535);
     const uint64_t per = round_up(ceil_div(std::max<uint64_t>(m, 1), splits), 32);
     splits = std::max<uint64_t>(1, ceil_div(m, per));
@@ -606,8 +612,8 @@ void launch_atb(Ctx& c, const double* A, int lda, const double* B, int ldb, uint
 
 void launch_gram_f32(Ctx& c, const float* A, int lda, uint64_t m, int a, double* out) {
     const int ta = (int)ceil_div(a, 32);
-    uint64_t splits = std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(m, 4096),
-                                          ceil_div((uint64_t)c.sm_count * 4, (uint64_t)ta * ta)));
+    uint64_t splits = std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(m, 1024),
+                                          ceil_div((uint64_t)c.sm_count * 8, (uint64_t)ta * ta)));
     splits = std::min<uint64_t>(splits, 65535);
     const uint64_t per = round_up(ceil_div(std::max<uint64_t>(m, 1), splits), 32);
     splits = std::max<uint64_t>(1, ceil_div(m, per));
@@ -640,10 +646,11 @@ void launch_gemm_small_f32out(Ctx& c, const double* A, int lda, uint64_t m, int 
     SLFMM_LAUNCHED(c, "k_gemm_small");
 }
 
-void launch_trmul_f32(Ctx& c, float* A, int lda, uint64_t m, int a, const double* Rinv) {
+void launch_trmul_f32(Ctx& c, float* A, int lda, uint64_t m, int a, const double* Linv) {
     SLFMM_REQUIRE(a <= 64, SLFMM_ERR_BAD_ARG, "sketch width must be <= 64");
     if (m == 0) return;
-    k_trmul_f32<<<grid_for(c, m, 128), 128, 0, c.stream>>>(A, lda, m, a, Rinv);
+    if (a <= 32) k_trmul_f32<32><<<grid_for(c, m, 128), 128, 0, c.stream>>>(A, lda, m, a, Linv);
+    else k_trmul_f32<64><<<grid_for(c, m, 128), 128, 0, c.stream>>>(A, lda, m, a, Linv);
     SLFMM_LAUNCHED(c, "k_trmul_f32");
 }
 

@@ -24,15 +24,16 @@
 #include <cudaTypedefs.h>
 
 #include "slfmm_internal.h"
+#include "tc_common.cuh"
 
 namespace slfmm {
 namespace {
+using namespace tc;
 
 constexpr int kM = 128;                      // tile rows = TMEM lanes
 constexpr int kKB = 128;                     // K elements per stage
 constexpr int kPackedStage = kM * kKB / 4;   // 4096 B of 2-bit codes
 constexpr int kThreads = 192;
-constexpr uint64_t kWaitNs = 4000000000ull;  // 4 s per wait
 
 struct TcArgs {
     uint32_t rows;          // valid tile rows in the matrix
@@ -48,126 +49,6 @@ struct TcArgs {
     uint64_t split_stride;  // elements between split outputs
     int* err;
 };
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ uint64_t globaltimer() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
-    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
-// Wait for completion of the phase with the given parity; bounded.
-__device__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
-    const uint32_t addr = smem_u32(bar);
-    uint64_t t0 = 0;
-    for (uint32_t it = 0;; ++it) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(addr), "r"(parity)
-            : "memory");
-        if (done) return true;
-        if ((it & 255) == 0) {
-            const uint64_t now = globaltimer();
-            if (it == 0) t0 = now;
-            if (*(volatile int*)err != 0 || now - t0 > kWaitNs) {
-                atomicCAS(err, 0, code);
-                return false;
-            }
-        }
-    }
-}
-
-__device__ __forceinline__ void tma_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
-            "r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
-        : "memory");
-}
-
-__device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
-__device__ __forceinline__ void fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
-
-// K-major operand in 128B-swizzled smem: SBO = 1024 B between 8-row groups.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
-    uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
-    d |= (uint64_t)1 << 16;             // leading byte offset (unused for swizzled K-major)
-    d |= (uint64_t)(1024 >> 4) << 32;   // stride byte offset
-    d |= (uint64_t)1 << 46;             // descriptor version
-    d |= (uint64_t)2 << 61;             // 128-byte swizzle
-    return d;
-}
-
-// kind::f16 instruction descriptor: BF16 x BF16 -> F32, K-major A and B.
-__device__ __forceinline__ uint32_t instr_desc(uint32_t n) {
-    return (1u << 4) | (1u << 7) | (1u << 10) | ((n >> 3) << 17) | ((uint32_t)(kM >> 4) << 24);
-}
-
-__device__ __forceinline__ void mma_ts(uint32_t d_tmem, uint32_t a_tmem, uint64_t b_desc, uint32_t idesc,
-                                       uint32_t accumulate) {
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "setp.ne.b32 p, %4, 0;\n\t"
-        "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(d_tmem),
-        "r"(a_tmem), "l"(b_desc), "r"(idesc), "r"(accumulate)
-        : "memory");
-}
-
-__device__ __forceinline__ void mma_commit(uint64_t* bar) {
-    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
-                 : "memory");
-}
-
-__device__ __forceinline__ void tmem_st_x64(uint32_t taddr, const uint32_t (&v)[64]) {
-    asm volatile(
-        "tcgen05.st.sync.aligned.32x32b.x64.b32 [%0], {"
-        "%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, "
-        "%17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32, "
-        "%33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47, %48, "
-        "%49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63, %64};" ::"r"(taddr),
-        "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]), "r"(v[8]),
-        "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15]), "r"(v[16]),
-        "r"(v[17]), "r"(v[18]), "r"(v[19]), "r"(v[20]), "r"(v[21]), "r"(v[22]), "r"(v[23]), "r"(v[24]),
-        "r"(v[25]), "r"(v[26]), "r"(v[27]), "r"(v[28]), "r"(v[29]), "r"(v[30]), "r"(v[31]), "r"(v[32]),
-        "r"(v[33]), "r"(v[34]), "r"(v[35]), "r"(v[36]), "r"(v[37]), "r"(v[38]), "r"(v[39]), "r"(v[40]),
-        "r"(v[41]), "r"(v[42]), "r"(v[43]), "r"(v[44]), "r"(v[45]), "r"(v[46]), "r"(v[47]), "r"(v[48]),
-        "r"(v[49]), "r"(v[50]), "r"(v[51]), "r"(v[52]), "r"(v[53]), "r"(v[54]), "r"(v[55]), "r"(v[56]),
-        "r"(v[57]), "r"(v[58]), "r"(v[59]), "r"(v[60]), "r"(v[61]), "r"(v[62]), "r"(v[63])
-        : "memory");
-}
-
-__device__ __forceinline__ void tmem_ld_x16(uint32_t taddr, float (&v)[16]) {
-    uint32_t r[16];
-    asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-        "%14, %15}, [%16];"
-        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-        : "r"(taddr)
-        : "memory");
-#pragma unroll
-    for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
-}
 
 __device__ __forceinline__ uint32_t bf16_of_code(uint32_t c) {
     return c == 2u ? 0x3F80u : (c == 3u ? 0x4000u : 0u);  // 00 -> 0, 01 (missing) -> 0
@@ -371,6 +252,8 @@ __global__ void k_transpose_packed(const uint8_t* __restrict__ in, uint64_t p, u
 
 // per-row fix of a row pass (mean imputation):
 //   out[j, c] = s_j * (P[j, c] - mu_j * (cs_c - sum_{i in miss_j} W[i, c]))
+// One warp per row: indices are fetched 32 at a time and broadcast so the W
+// row gathers (L2-resident) are independent and overlap.
 __global__ void k_rowfix_mean(float* __restrict__ P, int ldp, uint64_t rows, int w,
                               const uint64_t* __restrict__ ptr, const uint32_t* __restrict__ idx,
                               const float* __restrict__ W, int ldw, const double* __restrict__ cs,
@@ -379,12 +262,27 @@ __global__ void k_rowfix_mean(float* __restrict__ P, int ldp, uint64_t rows, int
     const int lane = threadIdx.x & 31;
     if (j >= rows) return;
     const uint64_t e0 = ptr[j], e1 = ptr[j + 1];
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};   // columns lane, lane+32, lane+64, lane+96
+    for (uint64_t b = e0; b < e1; b += 32) {
+        const uint32_t my = b + lane < e1 ? idx[b + lane] : 0u;
+        const int cnt = (int)(e1 - b < 32 ? e1 - b : 32);
+#pragma unroll 4
+        for (int t = 0; t < cnt; ++t) {
+            const uint64_t i = __shfl_sync(0xffffffffu, my, t);
+            const float* wr = W + i * ldw;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (lane + 32 * q < w) acc[q] += wr[lane + 32 * q];
+        }
+    }
     const double mu = mean[j], sc = scale[j];
-    for (int c = lane; c < w; c += 32) {
-        float acc = 0.f;
-        for (uint64_t e = e0; e < e1; ++e) acc += W[(uint64_t)idx[e] * ldw + c];
-        const double v = (double)P[j * ldp + c] - mu * (cs[c] - (double)acc);
-        P[j * ldp + c] = (float)(sc * v);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int c = lane + 32 * q;
+        if (c < w) {
+            const double v = (double)P[j * ldp + c] - mu * (cs[c] - (double)acc[q]);
+            P[j * ldp + c] = (float)(sc * v);
+        }
     }
 }
 
@@ -398,13 +296,25 @@ __global__ void k_colfix_mean(double* __restrict__ S, int lds, uint64_t n, int w
     const int lane = threadIdx.x & 31;
     if (i >= n) return;
     const uint64_t e0 = ptr[i], e1 = ptr[i + 1];
-    for (int c = lane; c < w; c += 32) {
-        double acc = 0.0;
-        for (uint64_t e = e0; e < e1; ++e) {
-            const uint32_t j = idx[e];
-            acc += coef[j] * (double)Q[(uint64_t)j * ldq + c];
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    for (uint64_t b = e0; b < e1; b += 32) {
+        const uint32_t myj = b + lane < e1 ? idx[b + lane] : 0u;
+        const float myc = b + lane < e1 ? (float)coef[myj] : 0.f;
+        const int cnt = (int)(e1 - b < 32 ? e1 - b : 32);
+#pragma unroll 4
+        for (int t = 0; t < cnt; ++t) {
+            const uint64_t j = __shfl_sync(0xffffffffu, myj, t);
+            const float cj = __shfl_sync(0xffffffffu, myc, t);
+            const float* qr = Q + j * ldq;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (lane + 32 * q < w) acc[q] = fmaf(cj, qr[lane + 32 * q], acc[q]);
         }
-        S[i * lds + c] += acc - colterm[c];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int c = lane + 32 * q;
+        if (c < w) S[i * lds + c] += (double)acc[q] - colterm[c];
     }
 }
 
@@ -533,7 +443,7 @@ void build_transposed(Ctx& c, const Geno& g) {
 
 // out (rows x ldo, or splits x rows x ldo) = G^T-style product of the packed
 // rows with the split W (B operand [2 wpad][K_pad]).
-void launch_tc_rows(Ctx& c, const uint8_t* packed, uint64_t stride, uint64_t rows, uint64_t K,
+int launch_tc_rows(Ctx& c, const uint8_t* packed, uint64_t stride, uint64_t rows, uint64_t K,
                     const __nv_bfloat16* bsplit, uint64_t K_pad, int wpad, float* out, int ldo, int splits,
                     uint64_t split_stride) {
     SLFMM_REQUIRE(wpad % 16 == 0 && wpad >= 16 && 2 * wpad <= 256, SLFMM_ERR_BAD_ARG,
@@ -569,13 +479,15 @@ void launch_tc_rows(Ctx& c, const uint8_t* packed, uint64_t stride, uint64_t row
     k_tc_rows<<<grid, kThreads, pl.smem, c.stream>>>(tp, tb, a);
     SLFMM_LAUNCHED(c, "k_tc_rows");
     check_err(c, err);
+    return (int)gy;
 }
 
 int tc_split_count(Ctx& c, uint64_t rows, uint64_t K) {
+    // about eight waves of CTAs so the last wave is a small tail
     const uint64_t tiles = ceil_div(rows, kM);
     const uint64_t kb = ceil_div(K, kKB);
-    uint64_t want = ceil_div((uint64_t)c.sm_count * 2, tiles);
-    want = std::max<uint64_t>(1, std::min<uint64_t>(want, kb));
+    uint64_t want = ceil_div((uint64_t)c.sm_count * 2 * 8, tiles);
+    want = std::max<uint64_t>(1, std::min<uint64_t>(want, std::max<uint64_t>(1, kb / 8)));
     return (int)want;
 }
 

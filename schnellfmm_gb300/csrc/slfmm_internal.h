@@ -87,6 +87,8 @@ struct DBuf {
         p = nullptr;
         n = 0;
     }
+    // free later on another (live) stream than the one it was allocated on
+    void rebind(cudaStream_t st) { s = st; }
     ~DBuf() { release(); }
     T* get() const { return p; }
     size_t bytes() const { return n * sizeof(T); }
@@ -113,6 +115,11 @@ struct Geno {
     mutable bool have_T = false;
     mutable uint64_t strideT = 0;
     mutable DBuf<uint8_t> packedT;     // n x strideT
+    // make every buffer free on `st` (the owning context may be gone)
+    void rebind(cudaStream_t st) {
+        packed.rebind(st); counts.rebind(st); miss_ptr.rebind(st); miss_idx.rebind(st);
+        missT_ptr.rebind(st); missT_idx.rebind(st); packedT.rebind(st);
+    }
 };
 
 // ---------------------------------------------------------------------------
@@ -127,7 +134,7 @@ struct ProfRec {
 
 struct Ctx {
     int device = 0;
-    int precision = SLFMM_PREC_SPLIT_BF16;
+    int precision = SLFMM_PREC_SPLIT_FP8;
     int verbose = 0;
     bool own_stream = false;
     cudaStream_t stream = nullptr;
@@ -219,7 +226,7 @@ void launch_split_bf16_f32(Ctx& c, const float* src, int ld, uint64_t K, int w, 
 void build_transposed(Ctx& c, const Geno& g);
 // out[r, c] = sum_k g(r, k) * (hi + lo)[c, k] over packed rows; split-K over
 // grid.y writes splits x rows x ldo partials (split_stride apart)
-void launch_tc_rows(Ctx& c, const uint8_t* packed, uint64_t stride, uint64_t rows, uint64_t K,
+int launch_tc_rows(Ctx& c, const uint8_t* packed, uint64_t stride, uint64_t rows, uint64_t K,
                     const __nv_bfloat16* bsplit, uint64_t K_pad, int wpad, float* out, int ldo, int splits,
                     uint64_t split_stride);
 int tc_split_count(Ctx& c, uint64_t rows, uint64_t K);
@@ -229,6 +236,26 @@ void launch_colfix_mean(Ctx& c, double* S, int lds, uint64_t n, int w, const uin
                         const float* Q, int ldq, const double* coef, const double* colterm);
 void launch_weighted_colsum(Ctx& c, const float* Q, int ldq, uint64_t p, int w, const double* coef, double* out);
 void launch_scale_product(Ctx& c, const double* a, const double* b, uint64_t n, double* out);
+
+// k_tc8.cu : split-FP8 tcgen05 contractions with optional missing-call
+// indicator operand and cluster-multicast W tiles
+struct Fp8Plan {
+    uint32_t wpad, n_main, n_ind, n_total, d_cols, a_cols, stages, tmem_cols, b_stage_bytes;
+    uint32_t cluster, box_rows, loads;
+    size_t smem;
+    bool ok;
+};
+Fp8Plan fp8_plan(int wpad, bool ind, uint64_t tiles);
+void launch_fp8_terms_f64(Ctx& c, const double* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
+                          const double* kscale, int terms, int row_off, uint8_t* B, float* inv_scale);
+void launch_fp8_terms_f32(Ctx& c, const float* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
+                          const double* kscale, int terms, int row_off, uint8_t* B, float* inv_scale);
+// mode 0: out = P (+ M); mode 1: out = s_r (P - mu_r (cs_c - M)) (needs the indicator)
+int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const uint8_t* packed, uint64_t stride, uint64_t rows, uint64_t K,
+                     const uint8_t* B, const float* inv_scale, uint64_t K_pad, int mode, const double* row_mean,
+                     const double* row_scale, const double* cs, float* out, int ldo, int splits,
+                     uint64_t split_stride);
+void launch_sub_colterm(Ctx& c, double* S, int lds, uint64_t n, int w, const double* colterm);
 
 // k_small.cu : FP64 dense helpers (row-major)
 void launch_colmeans(Ctx& c, const double* A, uint64_t m, int a, int lda, double* out);

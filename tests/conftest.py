@@ -26,10 +26,24 @@ def _gpu_available() -> bool:
 
 @pytest.fixture(scope="session")
 def engine():
+    """Default engine: split-FP8 tensor-core path."""
+    import schnellfmm_gb300 as sg
+    eng = sg.Engine(precision=sg.Precision.SPLIT_FP8)
+    yield eng
+    eng.close()
+
+
+@pytest.fixture(scope="session")
+def engine_bf16():
     import schnellfmm_gb300 as sg
     eng = sg.Engine(precision=sg.Precision.SPLIT_BF16)
     yield eng
     eng.close()
+
+
+@pytest.fixture(scope="session")
+def engines(engine, engine_bf16, engine_fp32):
+    return {"fp8": engine, "bf16": engine_bf16, "fp32": engine_fp32}
 
 
 @pytest.fixture(scope="session")
