@@ -241,13 +241,15 @@ void row_contract(Ctx& c, const Geno& g, const SnpStd& s, const double* W, int w
         // indicator operand the epilogue applies out = s_j (P - mu_j (cs - M)).
         // Operands too wide for TMEM run as column blocks of 64.
         const uint64_t tiles = ceil_div(g.p, 128);
-        Fp8Plan pl = fp8_plan(wp, true, tiles);
-        const bool ind = pl.ok;
+        const char* ind_env = std::getenv("SLFMM_TC8_ROW_IND");
+        Fp8Plan pl = fp8_plan(wp, !(ind_env && ind_env[0] == '0'), tiles);
+        const bool ind = pl.ok && pl.n_ind != 0;
         if (!ind) pl = fp8_plan(wp, false, tiles);
         const int cb = pl.ok ? wp : 64;
         DBuf<double> cs(wp, c.stream);
         cs.zero();
         launch_colsums(c, W, g.n, w, ldw, cs.get());
+        const TileView tv = build_tiles(c, g, false);
         for (int c0 = 0; c0 < w; c0 += cb) {
             // the epilogue writes pb.wpad columns: the last block is padded only to 16
             const int wb = std::min(cb, w - c0), bp = std::min(cb, pad16(wb));
@@ -258,7 +260,7 @@ void row_contract(Ctx& c, const Geno& g, const SnpStd& s, const double* W, int w
             if (ind) launch_fp8_terms_f64(c, W + c0, ldw, g.n, wb, bp, n_pad, nullptr, 3, (int)pb.n_main, B.get(),
                                           isc.get());
             ProfScope ps(c, "row_contract", bytes * wb / w, 2.0 * g.n * g.p * wb);
-            launch_tc8_rows(c, pb, g.packed.get(), g.stride, g.p, g.n, B.get(), isc.get(), n_pad, ind ? 1 : 0,
+            launch_tc8_rows(c, pb, tv, g.p, g.n, B.get(), isc.get(), n_pad, ind ? 1 : 0,
                             s.mean.get(), s.scale.get(), cs.get(), out.get() + c0, wp, 1, 0);
         }
         if (!ind) {
@@ -297,7 +299,7 @@ void col_contract(Ctx& c, const Geno& g, const SnpStd& s, const float* Q, int w,
         // forward pass on the transposed matrix: terms of diag(s) Q against the
         // genotypes plus terms of diag(mu s) Q against the missing-call
         // indicator, then S -= (mu s)^T Q
-        build_transposed(c, g);
+        const TileView tv = build_tiles(c, g, true);
         const uint64_t p_pad = round_up(g.p, 128);
         const uint64_t tiles = ceil_div(g.n, 128);
         Fp8Plan pl = fp8_plan(wp, true, tiles);
@@ -314,7 +316,7 @@ void col_contract(Ctx& c, const Geno& g, const SnpStd& s, const float* Q, int w,
         int used = 0;
         {
             ProfScope ps(c, "col_contract", bytes, 2.0 * g.n * g.p * w);
-            used = launch_tc8_rows(c, pl, g.packedT.get(), g.strideT, g.n, g.p, B.get(), isc.get(), p_pad, 0, nullptr,
+            used = launch_tc8_rows(c, pl, tv, g.n, g.p, B.get(), isc.get(), p_pad, 0, nullptr,
                                    nullptr, nullptr, part.get(), wp, splits, g.n * wp);
         }
         launch_reduce_splits(c, part.get(), used, g.n, wp, g.n, S.get());
@@ -1049,10 +1051,8 @@ int slfmm_contract_raw(slfmm_ctx* c, const slfmm_geno* g, int flags, const doubl
     const uint64_t K_pad = round_up(K, 128);
     DBuf<double> Wd = upload(*c, w_host, K * w);
     DBuf<float> o(std::max<uint64_t>(rows, 1) * wp, c->stream);
-    if (transposed) build_transposed(*c, *g);
-    const uint8_t* pk = transposed ? g->packedT.get() : g->packed.get();
-    const uint64_t st = transposed ? g->strideT : g->stride;
     if (c->precision == SLFMM_PREC_SPLIT_FP8) {
+        const TileView tv = build_tiles(*c, *g, transposed);
         const uint64_t tiles = ceil_div(rows, 128);
         const Fp8Plan pl = fp8_plan(wp, with_ind, tiles);
         SLFMM_REQUIRE(pl.ok || !with_ind, SLFMM_ERR_BAD_ARG, "indicator operand too wide for one launch");
@@ -1066,11 +1066,14 @@ int slfmm_contract_raw(slfmm_ctx* c, const slfmm_geno* g, int flags, const doubl
             if (with_ind)
                 launch_fp8_terms_f64(*c, Wd.get() + c0, (int)w, K, wb, bp, K_pad, nullptr, 3, (int)pb.n_main, B.get(),
                                      isc.get());
-            launch_tc8_rows(*c, pb, pk, st, rows, K, B.get(), isc.get(), K_pad, 0, nullptr, nullptr, nullptr,
+            launch_tc8_rows(*c, pb, tv, rows, K, B.get(), isc.get(), K_pad, 0, nullptr, nullptr, nullptr,
                             o.get() + c0, wp, 1, 0);
         }
     } else {
         SLFMM_REQUIRE(!with_ind, SLFMM_ERR_BAD_ARG, "indicator operand needs the split-FP8 precision");
+        if (transposed) build_transposed(*c, *g);
+        const uint8_t* pk = transposed ? g->packedT.get() : g->packed.get();
+        const uint64_t st = transposed ? g->strideT : g->stride;
         DBuf<__nv_bfloat16> bs(2 * (uint64_t)wp * K_pad, c->stream);
         launch_split_bf16_f64(*c, Wd.get(), (int)w, K, (int)w, wp, K_pad, nullptr, bs.get());
         launch_tc_rows(*c, pk, st, rows, K, bs.get(), K_pad, wp, o.get(), wp, 1, 0);

@@ -26,6 +26,8 @@
 #include <cuda_fp8.h>
 #include <cudaTypedefs.h>
 
+#include <cstdlib>
+
 #include "slfmm_internal.h"
 #include "tc_common.cuh"
 
@@ -36,7 +38,7 @@ using namespace tc;
 constexpr int kM = 128;
 constexpr int kKB = 128;
 constexpr int kPacked = kM * kKB / 4;  // 4096 B
-constexpr int kThreads = 192;
+constexpr int kThreads = 384;  // code-copy warp, 2 MMA warps, W-copy warp, 2 x 4 unpack warps
 constexpr int kMainTerms = 4;
 constexpr int kIndTerms = 3;
 constexpr uint32_t kTabGeno = 0x40380000u;  // code 00,01 -> 0; 10 -> 1.0; 11 -> 2.0 (E4M3 bytes)
@@ -51,6 +53,11 @@ struct Tc8Args {
     uint32_t d_cols;        // TMEM columns reserved for D
     uint32_t a_cols;        // TMEM columns per A stage (32, or 64 with the indicator)
     uint32_t stages, tmem_cols;
+    uint32_t pstages;       // packed-code prefetch depth
+    uint32_t group;         // K blocks an MMA warp waits for at once (1, 2, 4; divides stages)
+    uint32_t kcopies;       // accumulator copies (2: MMA warps take alternate K groups)
+    uint32_t nsplit;        // 1: MMA warp 0 issues the genotype MMAs, warp 1 the indicator MMAs
+    uint32_t a_base;        // first TMEM column of the A stages
     uint32_t b_stage_bytes; // n_total * 128
     uint32_t cluster;       // CTAs sharing W through multicast
     uint32_t box_rows;      // rows per W TMA box
@@ -63,33 +70,125 @@ struct Tc8Args {
     float* out;
     uint32_t ldo;
     uint64_t split_stride;
+    const uint8_t* tiles;   // tile-major packed codes
+    uint64_t tile_bytes;    // kbt * 4096
     int* err;
 };
 
-// 8 two-bit codes (low 16 bits) -> 8 nibbles, code i in nibble i
-__device__ __forceinline__ uint32_t spread8(uint32_t x) {
-    x &= 0xFFFFu;
-    x = (x | (x << 8)) & 0x00FF00FFu;
-    x = (x | (x << 4)) & 0x0F0F0F0Fu;
-    x = (x | (x << 2)) & 0x33333333u;
-    return x;
+// Ring position: slot index and the parity of its current use.
+struct Ring {
+    uint32_t slot, phase;
+    __device__ __forceinline__ void advance(uint32_t by, uint32_t n) {
+        slot += by;
+        while (slot >= n) {
+            slot -= n;
+            phase ^= 1u;
+        }
+    }
+};
+
+// MMA issue loop of one of the two MMA warps.  Measured properties of the
+// issuing thread shape it: (1) it is latency bound on operand arithmetic
+// between MMAs, so descriptors / TMEM addresses are per-stage bases plus
+// compile-time offsets; (2) an mbarrier wait by the issuing thread returns only
+// after the MMAs it issued before have (nearly) drained from the tensor pipe,
+// so a single issuing warp leaves the pipe idle at every wait.  Two MMA warps
+// whose waits fall at different K blocks keep it busy: without the indicator
+// they take alternate groups of G K blocks into two accumulator copies (summed
+// in the epilogue); with it one issues the genotype MMAs and the other the
+// indicator MMAs of every K block, their group boundaries G/2 apart.
+//
+// This warp's K blocks: [start, start + len0), then groups of G, each
+// followed by `skip` K blocks that belong to the other warp.
+template <int NCH, bool MAIN, bool IND, int G>
+__device__ __forceinline__ void tc8_mma_loop(const Tc8Args& a, uint32_t tmem, uint32_t d_main, uint32_t bsm_addr,
+                                             uint64_t* full_b, uint64_t* full_a, uint64_t* a_empty,
+                                             uint64_t* b_empty, uint32_t nkb, uint16_t mask, uint32_t start,
+                                             uint32_t len0, uint32_t skip) {
+    const uint32_t S = a.stages;
+    const uint32_t chunk = a.n_main / NCH;
+    const uint32_t id_main = instr_desc_e4m3(chunk);
+    const uint32_t id_ind = IND ? instr_desc_e4m3(a.n_ind) : 0u;
+    const uint64_t bdesc0 = smem_desc(bsm_addr);
+    const uint64_t bstep = a.b_stage_bytes >> 4;          // descriptor address units per stage
+    const uint64_t chstep = (uint64_t)chunk * (128 >> 4);  // per main chunk of B rows
+    const uint64_t indoff = (uint64_t)a.n_main * (128 >> 4);
+    const uint32_t d_ind = tmem + a.n_main;
+    const uint32_t a0 = tmem + a.a_base;
+    Ring st{0, 0};
+    st.advance(start, S);
+    uint32_t i = start, len = len0;
+    while (i < nkb) {
+        const uint32_t g = min(len, nkb - i);
+        bool ok = true;
+        Ring w = st;
+        for (uint32_t j = 0; j < g && ok; ++j) {
+            ok = mbar_wait(full_b + w.slot, w.phase, a.err, 25) && mbar_wait(full_a + w.slot, w.phase, a.err, 26);
+            w.advance(1, S);
+        }
+        if (!ok) break;
+        fence_after();
+#pragma unroll
+        for (int j = 0; j < G; ++j) {
+            if ((uint32_t)j < g) {
+                const uint64_t bd = bdesc0 + st.slot * bstep;
+                const uint32_t ad = a0 + st.slot * a.a_cols;
+                const uint32_t acc0 = (i + j) > start ? 1u : 0u;
+#pragma unroll
+                for (int kk = 0; kk < kKB / 32; ++kk) {
+                    const uint32_t acc = kk > 0 ? 1u : acc0;
+                    if (MAIN) {
+#pragma unroll
+                        for (int ch = 0; ch < NCH; ++ch)
+                            mma_ts_f8(d_main + ch * chunk, ad + kk * 8, bd + ch * chstep + kk * 2, id_main, acc);
+                    }
+                    if (IND) mma_ts_f8(d_ind, ad + 32 + kk * 8, bd + indoff + kk * 2, id_ind, acc);
+                }
+                mma_commit(a_empty + st.slot);
+                if (mask != 1) mma_commit_mc(b_empty + st.slot, mask);
+                else mma_commit(b_empty + st.slot);
+                st.advance(1, S);
+            }
+        }
+        i += g + skip;
+        st.advance(skip, S);
+        len = G;
+    }
+}
+
+template <int NCH, bool MAIN, bool IND>
+__device__ __forceinline__ void tc8_mma_dispatch(const Tc8Args& a, uint32_t tmem, uint32_t d_main, uint32_t bsm_addr,
+                                                 uint64_t* full_b, uint64_t* full_a, uint64_t* a_empty,
+                                                 uint64_t* b_empty, uint32_t nkb, uint16_t mask, uint32_t start,
+                                                 uint32_t len0, uint32_t skip) {
+    if (a.group == 4)
+        tc8_mma_loop<NCH, MAIN, IND, 4>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty, nkb, mask, start,
+                                        len0, skip);
+    else if (a.group == 2)
+        tc8_mma_loop<NCH, MAIN, IND, 2>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty, nkb, mask, start,
+                                        len0, skip);
+    else
+        tc8_mma_loop<NCH, MAIN, IND, 1>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty, nkb, mask, start,
+                                        len0, skip);
 }
 
 __global__ void __launch_bounds__(kThreads, 1)
-    k_tc8_rows(const __grid_constant__ CUtensorMap tm_packed, const __grid_constant__ CUtensorMap tm_b, Tc8Args a) {
+    k_tc8_rows(const __grid_constant__ CUtensorMap tm_b, Tc8Args a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    const uint32_t S = a.stages;
+    const uint32_t S = a.stages, P = a.pstages;
     uint8_t* bsm = smem;
     uint8_t* psm = bsm + S * a.b_stage_bytes;
-    float* scl = reinterpret_cast<float*>(psm + S * kPacked);                // up to 512 floats
+    float* scl = reinterpret_cast<float*>(psm + P * kPacked);                 // up to 512 floats
     uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<uint8_t*>(scl) + 2048);
-    uint64_t* full_tma = bars;
-    uint64_t* full_a = bars + S;
-    uint64_t* a_empty = bars + 2 * S;
-    uint64_t* b_empty = bars + 3 * S;
-    uint64_t* tmem_full = bars + 4 * S;
-    uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(bars + 4 * S + 1);
+    uint64_t* full_b = bars;                 // [S] W tile landed (TMA tx)
+    uint64_t* full_a = bars + S;             // [S] A operand written to TMEM (128 arrivals)
+    uint64_t* a_empty = bars + 2 * S;        // [S] own MMAs on the stage done
+    uint64_t* b_empty = bars + 3 * S;        // [S] MMAs of every cluster CTA on the stage done
+    uint64_t* p_full = bars + 4 * S;         // [P] packed codes landed (TMA tx)
+    uint64_t* p_empty = bars + 4 * S + P;    // [P] packed codes consumed (4 warp arrivals)
+    uint64_t* tmem_full = bars + 4 * S + 2 * P;
+    uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(tmem_full + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t C = a.cluster;
@@ -103,12 +202,16 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     if (threadIdx.x == 0) {
         for (uint32_t s = 0; s < S; ++s) {
-            mbar_init(full_tma + s, 1);
+            mbar_init(full_b + s, 1);
             mbar_init(full_a + s, 128);
-            mbar_init(a_empty + s, 1);
-            mbar_init(b_empty + s, C);
+            mbar_init(a_empty + s, a.nsplit ? 2 : 1);   // every MMA warp that reads the stage commits
+            mbar_init(b_empty + s, a.nsplit ? 2 * C : C);
         }
-        mbar_init(tmem_full, 1);
+        for (uint32_t p = 0; p < P; ++p) {
+            mbar_init(p_full + p, 1);
+            mbar_init(p_empty + p, 4);
+        }
+        mbar_init(tmem_full, 2);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
@@ -126,93 +229,148 @@ __global__ void __launch_bounds__(kThreads, 1)
 
     if (warp == 0) {
         if (lane == 0) {
-            const uint32_t y_begin = rank * a.box_rows * a.loads;
+            // packed-code producer: runs up to P stages ahead of the unpackers;
+            // each (tile, K block) operand is one contiguous 4 KiB bulk copy
+            const uint8_t* src = a.tiles + (uint64_t)blockIdx.x * a.tile_bytes + (uint64_t)kb0 * kPacked;
+            Ring pr{0, 0};
             uint32_t issued = 0;
             for (uint32_t i = 0; i < nkb; ++i) {
-                const uint32_t s = i % S, r = i / S;
-                if (r > 0 && !mbar_wait(b_empty + s, (r - 1) & 1, a.err, 11)) break;
-                mbar_arrive_tx(full_tma + s, kPacked + a.b_stage_bytes);
+                if (i >= P && !mbar_wait(p_empty + pr.slot, pr.phase ^ 1u, a.err, 21)) break;
+                mbar_arrive_tx(p_full + pr.slot, kPacked);
+                bulk_g2s(psm + pr.slot * kPacked, src + (uint64_t)i * kPacked, kPacked, p_full + pr.slot);
+                issued = i + 1;
+                pr.advance(1, P);
+            }
+            for (uint32_t i = issued > P ? issued - P : 0; i < issued; ++i)
+                mbar_wait(p_full + i % P, (i / P) & 1, a.err, 22);
+        }
+    } else if (warp == 2) {
+        // each spinning role has a warp of its own: lanes of one warp that
+        // spin in different loops starve each other
+        if (lane == 0) {
+            // W producer: this CTA's share of every W stage, multicast to the cluster
+            const uint32_t y_begin = rank * a.box_rows * a.loads;
+            Ring wr{0, 0};
+            uint32_t issued = 0;
+            for (uint32_t i = 0; i < nkb; ++i) {
+                if (i >= S && !mbar_wait(b_empty + wr.slot, wr.phase ^ 1u, a.err, 23)) break;
+                mbar_arrive_tx(full_b + wr.slot, a.b_stage_bytes);
                 const int kb = (int)(kb0 + i);
-                tma_2d(psm + s * kPacked, &tm_packed, kb * (kKB / 4), (int)row0, full_tma + s);
                 for (uint32_t l = 0; l < a.loads; ++l) {
                     const uint32_t y = y_begin + l * a.box_rows;
-                    uint8_t* dst = bsm + s * a.b_stage_bytes + y * 128;
-                    if (C > 1) tma_2d_mc(dst, &tm_b, kb * kKB, (int)y, full_tma + s, mask);
-                    else tma_2d(dst, &tm_b, kb * kKB, (int)y, full_tma + s);
+                    uint8_t* dst = bsm + wr.slot * a.b_stage_bytes + y * 128;
+                    if (C > 1) tma_2d_mc(dst, &tm_b, kb * kKB, (int)y, full_b + wr.slot, mask);
+                    else tma_2d(dst, &tm_b, kb * kKB, (int)y, full_b + wr.slot);
                 }
                 issued = i + 1;
+                wr.advance(1, S);
             }
             for (uint32_t i = issued > S ? issued - S : 0; i < issued; ++i)
-                mbar_wait(full_tma + i % S, (i / S) & 1, a.err, 12);
+                mbar_wait(full_b + i % S, (i / S) & 1, a.err, 24);
         }
-    } else if (warp == 1) {
+    } else if (warp == 1 || warp == 3) {
         if (lane == 0) {
-            const uint32_t nchunk = (a.n_main + 255) / 256;
-            const uint32_t chunk = a.n_main / nchunk;   // host guarantees divisibility
-            const uint32_t id_main = instr_desc_e4m3(chunk);
-            const uint32_t id_ind = ind ? instr_desc_e4m3(a.n_ind) : 0u;
-            for (uint32_t i = 0; i < nkb; ++i) {
-                const uint32_t s = i % S, r = i / S;
-                if (!mbar_wait(full_tma + s, r & 1, a.err, 13)) break;
-                if (!mbar_wait(full_a + s, r & 1, a.err, 14)) break;
-                fence_after();
-                const uint32_t b_base = smem_u32(bsm + s * a.b_stage_bytes);
-                const uint32_t a_base = tmem + a.d_cols + s * a.a_cols;
-#pragma unroll
-                for (int kk = 0; kk < kKB / 32; ++kk) {
-                    const uint32_t acc = (i > 0 || kk > 0) ? 1u : 0u;
-                    for (uint32_t ch = 0; ch < nchunk; ++ch)
-                        mma_ts_f8(tmem + ch * chunk, a_base + kk * 8, smem_desc(b_base + ch * chunk * 128 + kk * 32),
-                                  id_main, acc);
-                    if (ind)
-                        mma_ts_f8(tmem + a.n_main, a_base + 32 + kk * 8,
-                                  smem_desc(b_base + a.n_main * 128 + kk * 32), id_ind, acc);
+            const uint32_t m = warp == 1 ? 0u : 1u;  // MMA warp index
+            const uint32_t bsm_addr = smem_u32(bsm);
+            const uint32_t G = a.group;
+            const int nch = a.n_main > 256 ? 2 : 1;  // host guarantees an even split into <= 256-wide MMAs
+            if (a.nsplit) {
+                // genotype MMAs on warp 0, indicator MMAs on warp 1, boundaries G/2 apart
+                if (m == 0) {
+                    if (nch == 1)
+                        tc8_mma_dispatch<1, true, false>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty,
+                                                         nkb, mask, 0, G, 0);
+                    else
+                        tc8_mma_dispatch<2, true, false>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty,
+                                                         nkb, mask, 0, G, 0);
+                } else {
+                    tc8_mma_dispatch<1, false, true>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty, nkb,
+                                                     mask, 0, G > 1 ? G / 2 : 1, 0);
                 }
-                mma_commit(a_empty + s);
-                if (C > 1) mma_commit_mc(b_empty + s, mask);
-                else mma_commit(b_empty + s);
+            } else if (a.kcopies == 2) {
+                // alternate groups of G K blocks into accumulator copies m
+                const uint32_t d_main = tmem + m * a.d_cols;
+                if (nch == 1)
+                    tc8_mma_dispatch<1, true, false>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty,
+                                                     nkb, mask, m * G, G, G);
+                else
+                    tc8_mma_dispatch<2, true, false>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty,
+                                                     nkb, mask, m * G, G, G);
+            } else if (m == 0) {
+                // one MMA warp does everything
+                if (nch == 1) {
+                    if (ind)
+                        tc8_mma_dispatch<1, true, true>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty,
+                                                        nkb, mask, 0, G, 0);
+                    else
+                        tc8_mma_dispatch<1, true, false>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty,
+                                                         nkb, mask, 0, G, 0);
+                } else {
+                    if (ind)
+                        tc8_mma_dispatch<2, true, true>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty,
+                                                        nkb, mask, 0, G, 0);
+                    else
+                        tc8_mma_dispatch<2, true, false>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty,
+                                                         nkb, mask, 0, G, 0);
+                }
             }
-            mma_commit(tmem_full);
+            mma_commit(tmem_full);  // both MMA warps arrive (an idle one at once)
         }
     } else {
+        // two sets of four unpack warps take alternate K blocks; warp % 4 is
+        // the TMEM lane quarter a warp may access
+        const uint32_t set = (uint32_t)(warp - 4) >> 2;
         const uint32_t q = (uint32_t)warp & 3u;
         const uint32_t row = q * 32 + lane;
         const uint32_t lane_base = tmem + ((q * 32) << 16);
-        for (uint32_t i = 0; i < nkb; ++i) {
-            const uint32_t s = i % S, r = i / S;
-            if (!__all_sync(0xffffffffu, r == 0 || mbar_wait(a_empty + s, (r - 1) & 1, a.err, 15))) break;
-            if (!__all_sync(0xffffffffu, mbar_wait(full_tma + s, r & 1, a.err, 16))) break;
-            const uint4* src = reinterpret_cast<const uint4*>(psm + s * kPacked + row * (kKB / 4));
+        Ring pr{set, 0}, st{set, 0};  // P, S >= 2
+        for (uint32_t i = set; i < nkb; i += 2) {
+            if (!__all_sync(0xffffffffu, mbar_wait(p_full + pr.slot, pr.phase, a.err, 27))) break;
+            const uint4* src = reinterpret_cast<const uint4*>(psm + pr.slot * kPacked + row * (kKB / 4));
             const uint4 p0 = src[0], p1 = src[1];
+            __syncwarp();
+            if (lane == 0) mbar_arrive(p_empty + pr.slot);   // codes are in registers: release the slot
+            pr.advance(2, P);
+            // a 32-bit word holds 16 two-bit codes; masking the even / odd codes
+            // into nibbles gives PRMT selectors directly (4 codes per PRMT), and
+            // the B operand stores K in the matching even-then-odd order
             const uint32_t w8[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
+            uint32_t ev[8], od[8];
+#pragma unroll
+            for (int t = 0; t < 8; ++t) {
+                ev[t] = w8[t] & 0x33333333u;
+                od[t] = (w8[t] >> 2) & 0x33333333u;
+            }
             uint32_t g[32];
 #pragma unroll
             for (int t = 0; t < 8; ++t) {
-                const uint32_t s0 = spread8(w8[t]), s1 = spread8(w8[t] >> 16);
-                g[4 * t + 0] = __byte_perm(kTabGeno, 0u, s0);
-                g[4 * t + 1] = __byte_perm(kTabGeno, 0u, s0 >> 16);
-                g[4 * t + 2] = __byte_perm(kTabGeno, 0u, s1);
-                g[4 * t + 3] = __byte_perm(kTabGeno, 0u, s1 >> 16);
+                g[4 * t] = __byte_perm(kTabGeno, 0u, ev[t]);
+                g[4 * t + 1] = __byte_perm(kTabGeno, 0u, ev[t] >> 16);
+                g[4 * t + 2] = __byte_perm(kTabGeno, 0u, od[t]);
+                g[4 * t + 3] = __byte_perm(kTabGeno, 0u, od[t] >> 16);
             }
-            const uint32_t a_col = lane_base + a.d_cols + s * a.a_cols;
+            if (!__all_sync(0xffffffffu, i < S || mbar_wait(a_empty + st.slot, st.phase ^ 1u, a.err, 28))) break;
+            const uint32_t a_col = lane_base + a.a_base + st.slot * a.a_cols;
             tmem_st_x32(a_col, g);
             if (ind) {
 #pragma unroll
                 for (int t = 0; t < 8; ++t) {
-                    const uint32_t s0 = spread8(w8[t]), s1 = spread8(w8[t] >> 16);
-                    g[4 * t + 0] = __byte_perm(kTabMiss, 0u, s0);
-                    g[4 * t + 1] = __byte_perm(kTabMiss, 0u, s0 >> 16);
-                    g[4 * t + 2] = __byte_perm(kTabMiss, 0u, s1);
-                    g[4 * t + 3] = __byte_perm(kTabMiss, 0u, s1 >> 16);
+                    g[4 * t] = __byte_perm(kTabMiss, 0u, ev[t]);
+                    g[4 * t + 1] = __byte_perm(kTabMiss, 0u, ev[t] >> 16);
+                    g[4 * t + 2] = __byte_perm(kTabMiss, 0u, od[t]);
+                    g[4 * t + 3] = __byte_perm(kTabMiss, 0u, od[t] >> 16);
                 }
                 tmem_st_x32(a_col + 32, g);
             }
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
             fence_before();
-            mbar_arrive(full_a + s);
+            mbar_arrive(full_a + st.slot);
+            st.advance(2, S);
         }
-        // epilogue
-        const bool ok = __all_sync(0xffffffffu, mbar_wait(tmem_full, 0, a.err, 17));
+        // epilogue: the two sets take alternate 16-column groups
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(tmem_full, 0, a.err, 29));
+        // the second accumulator copy holds data only if its first group exists
+        const bool second_copy = a.kcopies == 2 && nkb > a.group;
         fence_after();
         const uint32_t grow = row0 + row;
         const bool live = ok && grow < a.rows;
@@ -222,7 +380,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             rs = a.row_scale[grow];
         }
         float* dst = a.out + (uint64_t)blockIdx.y * a.split_stride + (uint64_t)grow * a.ldo;
-        for (uint32_t c0 = 0; c0 < a.wpad; c0 += 16) {
+        for (uint32_t c0 = set * 16; c0 < a.wpad; c0 += 32) {
             float pm[16], pi[16], v[16];
 #pragma unroll
             for (int k = 0; k < 16; ++k) pm[k] = pi[k] = 0.f;
@@ -230,6 +388,13 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const uint32_t col = t * a.wpad + c0;
                 tmem_ld_x16(lane_base + col, v);
                 asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (second_copy) {
+                    float v2[16];
+                    tmem_ld_x16(lane_base + a.d_cols + col, v2);
+                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) v[k] += v2[k];
+                }
 #pragma unroll
                 for (int k = 0; k < 16; ++k) pm[k] = fmaf(scl[col + k], v[k], pm[k]);
             }
@@ -325,10 +490,14 @@ __global__ void k_fp8_terms(const T* __restrict__ src, int ld, uint64_t K, int w
             const int t = e / 32, cc = e % 32, c = c0 + cc;
             if (c < wpad) inv_scale[row_off + t * wpad + c] = c < w ? ldexpf(1.f, -(term_e0(colmax[c]) + 4 * t)) : 1.f;
         }
+    // B position kp within each 16-group holds K index kk = perm(kp): the even
+    // K indices of the group, then the odd ones (the order the unpackers emit
+    // the genotypes of a 32-bit code word in)
     for (int e = threadIdx.x; e < terms * 32 * 128; e += blockDim.x) {
-        const int t = e / (32 * 128), rem = e % (32 * 128), cc = rem / 128, kk = rem % 128;
+        const int t = e / (32 * 128), rem = e % (32 * 128), cc = rem / 128, kp = rem % 128;
+        const int kk = (kp & ~15) | ((kp & 7) << 1) | ((kp >> 3) & 1);
         const int c = c0 + cc;
-        const uint64_t k = k0 + kk;
+        const uint64_t k = k0 + kp;
         if (c < wpad && k < K_pad) B[(uint64_t)(row_off + t * wpad + c) * K_pad + k] = tile[t][cc][kk];
     }
 }
@@ -371,6 +540,12 @@ CUtensorMap map2d_u8(const uint8_t* base, uint64_t inner, uint64_t rows, uint32_
 
 }  // namespace
 
+// Tuning overrides (autotuner / experiments): SLFMM_TC8_CLUSTER, _STAGES, _PSTAGES.
+static int env_int(const char* name, int dflt) {
+    const char* v = std::getenv(name);
+    return v && *v ? std::atoi(v) : dflt;
+}
+
 Fp8Plan fp8_plan(int wpad, bool ind, uint64_t tiles) {
     Fp8Plan p{};
     p.wpad = (uint32_t)wpad;
@@ -380,26 +555,38 @@ Fp8Plan fp8_plan(int wpad, bool ind, uint64_t tiles) {
     p.d_cols = (uint32_t)round_up(p.n_total, 32);
     p.a_cols = ind ? 64 : 32;
     p.b_stage_bytes = p.n_total * 128;
-    const size_t fixed = 1024 + 2048 + 64 * 8 + 64;
-    const size_t per_stage = p.b_stage_bytes + kPacked;
-    const uint32_t st2 = p.d_cols < 256 ? std::min<uint32_t>((256 - p.d_cols) / p.a_cols,
-                                                              (uint32_t)((110 * 1024 - fixed) / per_stage))
-                                        : 0;
-    if (st2 >= 3) {
-        p.stages = std::min<uint32_t>(st2, 6);
-        p.tmem_cols = 256;
-    } else {
-        p.stages = p.d_cols < 512 ? std::min<uint32_t>((512 - p.d_cols) / p.a_cols,
-                                                       (uint32_t)((220 * 1024 - fixed) / per_stage))
-                                  : 0;
-        p.stages = std::min<uint32_t>(p.stages, 6);
-        p.tmem_cols = 512;
-    }
-    p.smem = fixed + p.stages * per_stage;
+    // one CTA per SM: all of TMEM, a deep packed-code ring (HBM latency) and a
+    // shallower W / A ring (L2 multicast latency)
+    p.tmem_cols = 512;
+    p.pstages = (uint32_t)std::min(32, std::max(2, env_int("SLFMM_TC8_PSTAGES", 16)));
+    const size_t fixed = 1024 + 2048 + 128 * 8 + 64;
+    const size_t budget = 225 * 1024 - fixed - (size_t)p.pstages * kPacked;
+    // MMA warp roles: with the indicator, genotype and indicator MMAs on
+    // separate warps; without it, two accumulator copies when TMEM holds them
+    // next to at least four A stages
+    p.nsplit = ind ? 1 : 0;
+    p.kcopies = (!ind && 2 * p.d_cols + 4 * p.a_cols <= 512) ? 2 : 1;
+    p.a_base = p.kcopies * p.d_cols;
+    const uint32_t by_tmem = p.a_base < 512 ? (512 - p.a_base) / p.a_cols : 0;
+    const uint32_t by_smem = (uint32_t)(budget / p.b_stage_bytes);
+    p.stages = std::min<uint32_t>(std::min(by_tmem, by_smem), (uint32_t)env_int("SLFMM_TC8_STAGES", 8));
+    // MMA wait groups: up to 16 MMAs per wait and warp, at least two groups in the ring
+    const uint32_t nch = p.n_main > 256 ? 2 : 1;
+    const uint32_t per_stage = 4 * (p.nsplit || p.kcopies == 2 ? nch : nch + (ind ? 1 : 0));
+    p.group = 1;
+    const uint32_t gmax = (uint32_t)env_int("SLFMM_TC8_GROUP", 4);
+    for (uint32_t gsz : {4u, 2u})
+        if (gsz <= gmax && gsz * per_stage <= 16 && p.stages >= 2 * gsz) {
+            p.group = gsz;
+            break;
+        }
+    p.stages -= p.stages % p.group;
+    p.smem = fixed + (size_t)p.pstages * kPacked + (size_t)p.stages * p.b_stage_bytes;
     // cluster multicast of W when there are enough tiles and rows split evenly
     p.cluster = 1;
-    for (uint32_t c : {4u, 2u})
-        if (tiles >= 2 * c && p.n_total % (8 * c) == 0) {
+    const uint32_t cmax = (uint32_t)env_int("SLFMM_TC8_CLUSTER", 4);
+    for (uint32_t c : {8u, 4u, 2u})
+        if (c <= cmax && tiles >= 2 * c && p.n_total % (8 * c) == 0) {
             p.cluster = c;
             break;
         }
@@ -410,6 +597,55 @@ Fp8Plan fp8_plan(int wpad, bool ind, uint64_t tiles) {
     p.ok = p.stages >= 2 && p.n_main % ceil_div(p.n_main, 256) == 0 && (p.n_main / ceil_div(p.n_main, 256)) % 16 == 0 &&
            p.n_ind <= 256;
     return p;
+}
+
+// row-major packed rows (rows x stride) -> tile-major copy; one thread per
+// 16-byte output chunk, so the writes stream and every read is one full
+// 32-byte sector
+__global__ void k_tile_rows(const uint8_t* __restrict__ in, uint64_t rows, uint64_t stride, uint64_t kbt,
+                            uint64_t chunks, uint8_t* __restrict__ out) {
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < chunks;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t h = e & 1u, r = (e >> 1) & 127u, rest = e >> 8;
+        const uint64_t kb = rest % kbt, t = rest / kbt;
+        const uint64_t row = t * kM + r, col = kb * 32 + h * 16;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (row < rows && col < stride) v = *reinterpret_cast<const uint4*>(in + row * stride + col);
+        reinterpret_cast<uint4*>(out)[e] = v;
+    }
+}
+
+static void tile_rows(Ctx& c, const uint8_t* in, uint64_t rows, uint64_t stride, DBuf<uint8_t>& out, uint64_t& kbt,
+                      uint64_t& ntiles) {
+    SLFMM_REQUIRE(stride % 32 == 0, SLFMM_ERR_BAD_ARG, "packed stride must be a multiple of 32 bytes");
+    kbt = stride / 32;
+    ntiles = round_up(std::max<uint64_t>(ceil_div(rows, kM), 1), 8);
+    const uint64_t bytes = ntiles * kbt * kPacked;
+    out.alloc(bytes, c.stream);
+    const uint64_t chunks = bytes / 16;
+    k_tile_rows<<<grid_for(c, chunks, 256), 256, 0, c.stream>>>(in, rows, stride, kbt, chunks, out.get());
+    SLFMM_LAUNCHED(c, "k_tile_rows");
+}
+
+TileView build_tiles(Ctx& c, const Geno& g, bool transposed) {
+    if (!transposed) {
+        if (!g.have_tiles) {
+            tile_rows(c, g.packed.get(), g.p, g.stride, g.tiles, g.kbt, g.ntiles);
+            g.have_tiles = true;
+        }
+        return TileView{g.tiles.get(), g.kbt, g.ntiles};
+    }
+    if (!g.have_tilesT) {
+        const bool had_T = g.have_T;
+        build_transposed(c, g);
+        tile_rows(c, g.packedT.get(), g.n, g.strideT, g.tilesT, g.kbtT, g.ntilesT);
+        g.have_tilesT = true;
+        if (!had_T) {  // the row-major transposed copy was only a staging step
+            g.packedT.release();
+            g.have_T = false;
+        }
+    }
+    return TileView{g.tilesT.get(), g.kbtT, g.ntilesT};
 }
 
 void launch_fp8_terms_f64(Ctx& c, const double* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
@@ -438,20 +674,21 @@ void launch_fp8_terms_f32(Ctx& c, const float* src, int ld, uint64_t K, int w, i
     SLFMM_LAUNCHED(c, "k_fp8_terms");
 }
 
-int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const uint8_t* packed, uint64_t stride, uint64_t rows, uint64_t K,
+int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t rows, uint64_t K,
                      const uint8_t* B, const float* inv_scale, uint64_t K_pad, int mode, const double* row_mean,
                      const double* row_scale, const double* cs, float* out, int ldo, int splits,
                      uint64_t split_stride) {
     SLFMM_REQUIRE(pl.ok, SLFMM_ERR_BAD_ARG, "no feasible split-FP8 tile plan for this width");
     SLFMM_REQUIRE(K_pad % kKB == 0 && K_pad >= ceil_div(K, kKB) * kKB, SLFMM_ERR_BAD_ARG, "bad K padding");
-    SLFMM_REQUIRE(stride % 16 == 0 && stride * 4 >= ceil_div(K, kKB) * kKB, SLFMM_ERR_BAD_ARG, "bad packed stride");
+    SLFMM_REQUIRE(tv.base && tv.kbt >= ceil_div(K, kKB), SLFMM_ERR_BAD_ARG, "tile-major operand too short in K");
+    SLFMM_REQUIRE(tv.ntiles >= round_up(ceil_div(rows, kM), pl.cluster), SLFMM_ERR_BAD_ARG,
+                  "tile-major operand has too few tiles");
     SLFMM_REQUIRE(mode == 0 || pl.n_ind != 0, SLFMM_ERR_BAD_ARG, "row correction needs the indicator operand");
     static thread_local size_t configured = 0;
     if (configured < pl.smem) {
         SLFMM_CUDA(cudaFuncSetAttribute(k_tc8_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
         configured = pl.smem;
     }
-    const CUtensorMap tp = map2d_u8(packed, stride, rows, kKB / 4, kM, false);
     const CUtensorMap tb = map2d_u8(B, K_pad, pl.n_total, 128, pl.box_rows, true);
     DBuf<int> err(1, c.stream);
     err.zero();
@@ -466,6 +703,11 @@ int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const uint8_t* packed, uint64_t s
     a.d_cols = pl.d_cols;
     a.a_cols = pl.a_cols;
     a.stages = pl.stages;
+    a.pstages = pl.pstages;
+    a.group = pl.group;
+    a.kcopies = pl.kcopies;
+    a.nsplit = pl.nsplit;
+    a.a_base = pl.a_base;
     a.tmem_cols = pl.tmem_cols;
     a.b_stage_bytes = pl.b_stage_bytes;
     a.cluster = pl.cluster;
@@ -479,6 +721,8 @@ int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const uint8_t* packed, uint64_t s
     a.out = out;
     a.ldo = (uint32_t)ldo;
     a.split_stride = split_stride;
+    a.tiles = tv.base;
+    a.tile_bytes = tv.kbt * (uint64_t)kPacked;
     a.err = err.get();
     const unsigned gy = (unsigned)ceil_div(a.kb_total, a.kb_per_split);
     const unsigned gx = (unsigned)round_up(ceil_div(rows, kM), pl.cluster);
@@ -494,7 +738,7 @@ int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const uint8_t* packed, uint64_t s
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    SLFMM_CUDA(cudaLaunchKernelEx(&cfg, k_tc8_rows, tp, tb, a));
+    SLFMM_CUDA(cudaLaunchKernelEx(&cfg, k_tc8_rows, tb, a));
     SLFMM_LAUNCHED(c, "k_tc8_rows");
     int h = 0;
     SLFMM_CUDA(cudaMemcpyAsync(&h, err.get(), sizeof(int), cudaMemcpyDeviceToHost, c.stream));

@@ -115,10 +115,19 @@ struct Geno {
     mutable bool have_T = false;
     mutable uint64_t strideT = 0;
     mutable DBuf<uint8_t> packedT;     // n x strideT
+    // tile-major copies for the tensor-core passes, built on first use:
+    // [tile of 128 rows][K block of 128 codes][128 rows][32 B], so every
+    // (tile, K block) operand is one contiguous 4 KiB run of HBM; the tile
+    // count is padded to a multiple of 8 with zero tiles
+    mutable bool have_tiles = false, have_tilesT = false;
+    mutable uint64_t kbt = 0, kbtT = 0;      // K blocks per tile
+    mutable uint64_t ntiles = 0, ntilesT = 0;
+    mutable DBuf<uint8_t> tiles, tilesT;
     // make every buffer free on `st` (the owning context may be gone)
     void rebind(cudaStream_t st) {
         packed.rebind(st); counts.rebind(st); miss_ptr.rebind(st); miss_idx.rebind(st);
         missT_ptr.rebind(st); missT_idx.rebind(st); packedT.rebind(st);
+        tiles.rebind(st); tilesT.rebind(st);
     }
 };
 
@@ -240,18 +249,25 @@ void launch_scale_product(Ctx& c, const double* a, const double* b, uint64_t n, 
 // k_tc8.cu : split-FP8 tcgen05 contractions with optional missing-call
 // indicator operand and cluster-multicast W tiles
 struct Fp8Plan {
-    uint32_t wpad, n_main, n_ind, n_total, d_cols, a_cols, stages, tmem_cols, b_stage_bytes;
+    uint32_t wpad, n_main, n_ind, n_total, d_cols, a_cols, stages, pstages, group, tmem_cols, b_stage_bytes;
+    uint32_t kcopies, nsplit, a_base;
     uint32_t cluster, box_rows, loads;
     size_t smem;
     bool ok;
 };
 Fp8Plan fp8_plan(int wpad, bool ind, uint64_t tiles);
+// tile-major packed operand (rows = SNPs, or samples when transposed)
+struct TileView {
+    const uint8_t* base;
+    uint64_t kbt, ntiles;
+};
+TileView build_tiles(Ctx& c, const Geno& g, bool transposed);
 void launch_fp8_terms_f64(Ctx& c, const double* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
                           const double* kscale, int terms, int row_off, uint8_t* B, float* inv_scale);
 void launch_fp8_terms_f32(Ctx& c, const float* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
                           const double* kscale, int terms, int row_off, uint8_t* B, float* inv_scale);
 // mode 0: out = P (+ M); mode 1: out = s_r (P - mu_r (cs_c - M)) (needs the indicator)
-int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const uint8_t* packed, uint64_t stride, uint64_t rows, uint64_t K,
+int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t rows, uint64_t K,
                      const uint8_t* B, const float* inv_scale, uint64_t K_pad, int mode, const double* row_mean,
                      const double* row_scale, const double* cs, float* out, int ldo, int splits,
                      uint64_t split_stride);

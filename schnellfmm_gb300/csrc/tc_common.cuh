@@ -8,16 +8,8 @@
 namespace slfmm {
 namespace tc {
 
-constexpr uint64_t kWaitNs = 4000000000ull;  // 4 s per wait
-
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ uint64_t globaltimer() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
 }
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
@@ -33,24 +25,33 @@ __device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes) {
                  : "memory");
 }
 
-// Wait for completion of the phase with the given parity; bounded.
+__device__ __forceinline__ bool mbar_try(uint32_t addr, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(addr), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// Wait for completion of the phase with the given parity; bounded by about
+// kWaitCycles SM cycles, after which the shared error flag gets `code`.  The
+// slow checks (SM clock, the global flag another waiter may have set) run
+// only every 1024 polls: a global load on the first miss would put an L2
+// round trip on every wait that is not already complete.
+constexpr long long kWaitCycles = 8000000000ll;  // ~4 s at 2 GHz
+
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
     const uint32_t addr = smem_u32(bar);
-    uint64_t t0 = 0;
-    for (uint32_t it = 0;; ++it) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(addr), "r"(parity)
-            : "memory");
-        if (done) return true;
-        if ((it & 255) == 0) {
-            const uint64_t now = globaltimer();
-            if (it == 0) t0 = now;
-            if (*(volatile int*)err != 0 || now - t0 > kWaitNs) {
+    if (mbar_try(addr, parity)) return true;
+    const long long t0 = clock64();
+    for (uint32_t it = 1;; ++it) {
+        if (mbar_try(addr, parity)) return true;
+        if ((it & 1023u) == 0) {
+            if (*(volatile int*)err != 0 || clock64() - t0 > kWaitCycles) {
                 atomicCAS(err, 0, code);
                 return false;
             }
@@ -64,6 +65,14 @@ __device__ __forceinline__ void tma_2d(void* dst, const CUtensorMap* tm, int x, 
             "r"(smem_u32(dst)),
         "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(smem_u32(bar))
         : "memory");
+}
+
+// contiguous global -> shared bulk copy (16-byte aligned addresses and size)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
 }
 
 __device__ __forceinline__ void fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
