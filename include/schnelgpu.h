@@ -212,6 +212,29 @@ int slfmm_profile_enable(slfmm_ctx* ctx, int on);
 int slfmm_profile_read(slfmm_ctx* ctx, const char* kernel, double* total_ms, uint64_t* launches,
                        double* algo_bytes, double* algo_flops);
 
+/* ---- allocation-free entry point ----------------------------------------- */
+/* Raw genomic inflation factor of each trait from device-resident t
+ * statistics, allocating no device memory.  No counterpart in the reference:
+ * there the GIF is computed inside the test pass (src/testing.rs:179-224).
+ *
+ * t_dev: p x d FP32 t statistics on the context's device (row-major, as the
+ * fit returns them); gif_dev: d doubles on that device receive median(t^2) /
+ * 0.4549 per trait (1 when the median is below 1e-10) -- the fit clamps this
+ * at 1 before calibrating p-values.  The work is queued on the context's
+ * stream; the call does not wait for it.
+ *
+ * For callers that must not allocate device memory while they run: a host
+ * application whose own allocator owns the device memory, or code that calls
+ * in at a point where an allocation would block or fail.  The t^2 histogram
+ * lives in one static device array of 8 x 100000 counters (3.2 MB) per
+ * device, so at most 8 traits per call (more returns SLFMM_ERR_BAD_ARG).
+ * Every call on a device shares that array and zeroes the rows it uses at its
+ * start: calls that overlap in time on one device (other streams, other
+ * threads) race on it and must be serialised by the caller.  The first call
+ * on each device looks up the array's address (cudaGetSymbolAddress) once;
+ * make that first call before any stream capture begins. */
+int slfmm_gif_noalloc(slfmm_ctx* ctx, const float* t_dev, uint64_t p, uint32_t d, double* gif_dev);
+
 /* ---- output (src/testing.rs:740-801) ------------------------------------ */
 /* Write <out>.tsv: header chr pos snp_id {p_,beta_,t_}xcov r2_cov r2_latent
  * r2_resid, numbers in Rust "{:.6e}" form.  chrom/snp_id are arrays of p

@@ -107,6 +107,7 @@ EXPORTED_SYMBOLS = (
     "slfmm_generate_omega", "slfmm_estimate_factors", "slfmm_test_associations", "slfmm_fit",
     "slfmm_fit_host", "slfmm_write_tsv", "slfmm_format_exp6", "slfmm_simulate", "slfmm_geno_download",
     "slfmm_profile_enable", "slfmm_profile_read", "slfmm_host_alloc", "slfmm_host_free", "slfmm_contract_raw",
+    "slfmm_gif_noalloc",
 )
 
 _lib_handle = None
@@ -153,6 +154,7 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
         "slfmm_host_alloc": (i32, [C.c_size_t, C.POINTER(vp)]),
         "slfmm_host_free": (i32, [vp]),
         "slfmm_contract_raw": (i32, [vp, vp, i32, vp, u32, vp]),
+        "slfmm_gif_noalloc": (i32, [vp, vp, u64, u32, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)

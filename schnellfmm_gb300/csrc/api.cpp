@@ -1084,6 +1084,14 @@ int slfmm_contract_raw(slfmm_ctx* c, const slfmm_geno* g, int flags, const doubl
     API_CATCH(c)
 }
 
+int slfmm_gif_noalloc(slfmm_ctx* c, const float* t_dev, uint64_t p, uint32_t d, double* gif_dev) {
+    if (!c) return SLFMM_ERR_BAD_ARG;
+    API_TRY
+    SLFMM_CUDA(cudaSetDevice(c->device));
+    launch_gif_noalloc(*c, t_dev, p, (int)std::min<uint32_t>(d, 1u << 30), gif_dev);
+    API_CATCH(c)
+}
+
 int slfmm_format_exp6(double v, char* buf, size_t len) { return format_exp6(v, buf, len); }
 
 int slfmm_write_tsv(const char* path, uint64_t p, uint32_t d, const char* const* chrom, const uint64_t* pos,

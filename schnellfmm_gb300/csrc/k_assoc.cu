@@ -13,6 +13,9 @@
 //   theta_j = (L^-T u)_{1+j},  c_jj = [(C^T C)^-1]_{1+j,1+j}
 //   beta    = R ((I - P_U) X)^T Q_C u          (ridge effect, Step 3)
 // which is the reference's O(n^2)-per-SNP algebra in O(n (1+d+K)).
+#include <mutex>
+#include <string>
+
 #include "slfmm_internal.h"
 
 namespace slfmm {
@@ -180,7 +183,69 @@ __global__ void k_calibrate(uint64_t p, int d, const float* __restrict__ t32,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Allocation-free GIF (slfmm_gif_noalloc; no counterpart in the reference)
+// ---------------------------------------------------------------------------
+// The t^2 histogram lives in this fixed device array instead of memory
+// allocated per call: kGifNoAllocMaxTraits x kHistBins counters (3.2 MB).
+// Every call on a device shares it; each call zeroes the rows it uses first.
+static __device__ __align__(256) uint32_t g_noalloc_hist[kGifNoAllocMaxTraits * kHistBins];
+
+// Same binning as the association epilogue: bin = min(t^2 * 1000, last) for
+// every finite t^2 of trait j.
+__global__ void k_tsq_hist(const float* __restrict__ t, uint64_t p, int d, uint32_t* __restrict__ hist) {
+    const uint64_t total = p * (uint64_t)d;
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < total;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        const int jj = (int)(e % d);
+        const float tv = t[e];
+        const float t2 = tv * tv;
+        if (isfinite(t2)) {
+            unsigned bin = (unsigned)fminf(t2 * 1000.0f, (float)(kHistBins - 1));
+            if (bin > (unsigned)(kHistBins - 1)) bin = kHistBins - 1;
+            atomicAdd(&hist[(uint64_t)jj * kHistBins + bin], 1u);
+        }
+    }
+}
+
 }  // namespace
+
+// Device address of g_noalloc_hist on the current device.  The first call on
+// a device asks the runtime for it (cudaGetSymbolAddress) and keeps it; later
+// calls only read the cached pointer.
+static uint32_t* noalloc_hist_address(int device) {
+    constexpr int kMaxDevices = 64;
+    static std::mutex mu;
+    static uint32_t* addr[kMaxDevices] = {};
+    SLFMM_REQUIRE(device >= 0 && device < kMaxDevices, SLFMM_ERR_BAD_ARG, "device ordinal out of range");
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[device]) {
+        void* ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_hist);
+        if (e != cudaSuccess || !ptr)
+            throw Error(SLFMM_ERR_CUDA, std::string("cudaGetSymbolAddress of the GIF histogram failed: ") +
+                                            cudaGetErrorString(e));
+        addr[device] = static_cast<uint32_t*>(ptr);
+    }
+    return addr[device];
+}
+
+void launch_gif_noalloc(Ctx& c, const float* t, uint64_t p, int d, double* gif_raw) {
+    SLFMM_REQUIRE(d >= 0 && d <= kGifNoAllocMaxTraits, SLFMM_ERR_BAD_ARG,
+                  "slfmm_gif_noalloc handles at most " + std::to_string(kGifNoAllocMaxTraits) +
+                      " traits (its static histogram holds " + std::to_string(kGifNoAllocMaxTraits) + " x " +
+                      std::to_string(kHistBins) + " counters); got " + std::to_string(d));
+    if (d == 0) return;
+    SLFMM_REQUIRE(gif_raw != nullptr && (p == 0 || t != nullptr), SLFMM_ERR_BAD_ARG, "null device pointer");
+    uint32_t* hist = noalloc_hist_address(c.device);
+    SLFMM_CUDA(cudaMemsetAsync(hist, 0, (size_t)d * kHistBins * sizeof(uint32_t), c.stream));
+    if (p > 0) {
+        k_tsq_hist<<<grid_for(c, p * (uint64_t)d, 256), 256, 0, c.stream>>>(t, p, d, hist);
+        SLFMM_LAUNCHED(c, "k_tsq_hist");
+    }
+    k_gif<<<d, 1024, 0, c.stream>>>(hist, gif_raw);
+    SLFMM_LAUNCHED(c, "k_gif");
+}
 
 void launch_assoc_epilogue(Ctx& c, uint64_t p, const float* u, int ldu, const double* tss,
                            const AssocConsts& k, double* beta, float* t32, double* r2,

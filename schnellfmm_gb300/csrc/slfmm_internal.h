@@ -39,6 +39,7 @@ struct Error : std::runtime_error {
 // constants shared by host and device
 // ---------------------------------------------------------------------------
 constexpr int kHistBins = 100000;      // src/testing.rs:124
+constexpr int kGifNoAllocMaxTraits = 8; // traits the static histogram of slfmm_gif_noalloc holds
 constexpr double kHistWidth = 0.001;   // src/testing.rs:125
 constexpr double kGifDivisor = 0.4549; // src/testing.rs:169
 constexpr int kMaxW = 128;             // widest GEMM operand (columns)
@@ -320,6 +321,9 @@ void launch_assoc_epilogue(Ctx& c, uint64_t p, const float* u, int ldu, const do
                            const AssocConsts& k, double* beta, float* t32, double* r2,
                            uint32_t* hist);
 void launch_gif(Ctx& c, const uint32_t* hist, int d, double* gif_raw);
+// raw GIF per trait from p x d FP32 t statistics using the static per-device
+// histogram (allocates nothing)
+void launch_gif_noalloc(Ctx& c, const float* t, uint64_t p, int d, double* gif_raw);
 void launch_calibrate(Ctx& c, uint64_t p, int d, const float* t32, const double* gif_per_trait,
                       double* t64, double* pval);
 

@@ -1,0 +1,42 @@
+"""slfmm_gif_noalloc (the allocation-free entry point) against the GIF the
+full fit computes from the same FP32 t statistics, on two calls in a row
+(the shared static histogram must be re-zeroed by each call)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import simdata
+
+pytestmark = pytest.mark.gpu
+
+
+def test_gif_noalloc_matches_fit():
+    torch = pytest.importorskip("torch")
+    import schnellfmm_gb300 as sg
+    eng = sg.Engine(precision=sg.Precision.SPLIT_FP8)
+    try:
+        c = simdata.simulate(400, 3000, k_pop=3, fst=0.1, miss=0.02, d=3, n_causal=20, seed=77)
+        geno = eng.upload(c.packed, c.n)
+        cfg = sg.Lfmm2Config(k=3, lambda_=1e-5)
+        res = sg.fit_lfmm2(geno, sg.SubsetSpec.all(), geno, c.x, cfg, engine=eng)
+        p, d = res.tstat.shape
+        # the fit's t statistics are FP32 values widened to double: narrowing is exact
+        t32 = torch.tensor(np.ascontiguousarray(res.tstat.astype(np.float32)), device="cuda")
+        out = torch.empty(d, dtype=torch.float64, device="cuda")
+        for _ in range(2):
+            out.fill_(-1.0)
+            torch.cuda.synchronize()
+            eng.check(eng.lib.slfmm_gif_noalloc(eng.h, C.c_void_p(t32.data_ptr()), p, d,
+                                                C.c_void_p(out.data_ptr())))
+            torch.cuda.synchronize()
+            raw = out.cpu().numpy()
+            np.testing.assert_allclose(np.maximum(raw, 1.0), res.gif_per_trait, rtol=1e-12, atol=0.0)
+            assert abs(raw.mean() - res.gif) <= 1e-12 * max(1.0, abs(res.gif))
+        # beyond the static histogram's 8 traits: a clear error, nothing launched
+        rc = eng.lib.slfmm_gif_noalloc(eng.h, C.c_void_p(t32.data_ptr()), p // 9, 9, C.c_void_p(out.data_ptr()))
+        assert rc == sg.ERR_BAD_ARG
+        assert b"at most 8 traits" in eng.lib.slfmm_last_error(eng.h)
+        geno.free()
+    finally:
+        eng.close()
