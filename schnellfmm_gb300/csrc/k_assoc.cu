@@ -163,9 +163,22 @@ __global__ void __launch_bounds__(1024) k_gif(const uint32_t* __restrict__ hist,
 // p = 2 * Phi(-|t| / sqrt(GIF_j)) = erfc(|z| / sqrt 2)  (src/testing.rs:691-712).
 // The statistic is FP32, so erfcf carries its precision; the FP64 erfc is
 // only used in the far tail where erfcf would leave the normal FP32 range.
+constexpr int kMaxCalibTraits = 1024;
+
+// The per-trait factors 1/sqrt(2 GIF) (FP32) and 1/sqrt(GIF) (FP64) are
+// formed once per block: FP64 square roots and divisions per element would
+// dominate on this part, whose FP64 rate is a small fraction of FP32.
 __global__ void k_calibrate(uint64_t p, int d, const float* __restrict__ t32,
                             const double* __restrict__ gif, double* __restrict__ t64,
                             double* __restrict__ pval) {
+    __shared__ float zs[kMaxCalibTraits];
+    __shared__ double rs[kMaxCalibTraits];
+    for (int j = threadIdx.x; j < d; j += blockDim.x) {
+        const double r = 1.0 / sqrt(gif[j]);
+        rs[j] = r;
+        zs[j] = (float)(0.7071067811865476 * r);
+    }
+    __syncthreads();
     const uint64_t total = p * (uint64_t)d;
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < total;
          e += (uint64_t)gridDim.x * blockDim.x) {
@@ -173,11 +186,10 @@ __global__ void k_calibrate(uint64_t p, int d, const float* __restrict__ t32,
         const float tf = t32[e];
         if (t64) t64[e] = (double)tf;
         if (pval) {
-            const double g = gif[jj];
-            const float zf = fabsf(tf) * (float)(0.7071067811865476 / sqrt(g));
+            const float zf = fabsf(tf) * zs[jj];
             double pv;
             if (zf < 8.0f) pv = (double)erfcf(zf);
-            else pv = 2.0 * (0.5 * erfc(fabs((double)tf / sqrt(g)) / 1.4142135623730951));
+            else pv = erfc(fabs((double)tf) * rs[jj] * 0.7071067811865476);
             pval[e] = pv;
         }
     }
@@ -270,6 +282,7 @@ void launch_gif(Ctx& c, const uint32_t* hist, int d, double* gif_raw) {
 void launch_calibrate(Ctx& c, uint64_t p, int d, const float* t32, const double* gif, double* t64,
                       double* pval) {
     if (p == 0 || d == 0) return;
+    SLFMM_REQUIRE(d <= kMaxCalibTraits, SLFMM_ERR_BAD_ARG, "too many traits for the calibration kernel");
     k_calibrate<<<grid_for(c, p * d, 256), 256, 0, c.stream>>>(p, d, t32, gif, t64, pval);
     SLFMM_LAUNCHED(c, "k_calibrate");
 }

@@ -159,6 +159,73 @@ __global__ void __launch_bounds__(256) k_gram_f32(const float* __restrict__ A, i
         }
 }
 
+// Narrow (a <= 32) FP32 Gram, one warp per run of rows: lane c holds row
+// element c, and for each k the broadcast row[k] (shuffle) times row[c]
+// accumulates G[k][c] in lane c.  FP32 sums over runs of 256 rows, FP64 across
+// runs; the block's warps reduce through shared memory into one partial.
+constexpr int kGramRun = 256;
+constexpr size_t kGramNarrowSmem = 8 * 32 * 33 * sizeof(double);
+__global__ void __launch_bounds__(256, 2) k_gram_narrow(const float* __restrict__ A, int lda, uint64_t m, int a,
+                                                        double* __restrict__ part) {
+    extern __shared__ double gsm[];  // [8 warps][32][33] FP64 sums
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double* mine = gsm + warp * 32 * 33;
+#pragma unroll
+    for (int k = 0; k < 32; ++k) mine[k * 33 + lane] = 0.0;
+    const uint64_t nruns = (m + kGramRun - 1) / kGramRun;
+    for (uint64_t run = (uint64_t)blockIdx.x * 8 + warp; run < nruns; run += (uint64_t)gridDim.x * 8) {
+        float acc[32];
+#pragma unroll
+        for (int k = 0; k < 32; ++k) acc[k] = 0.f;
+        const uint64_t i0 = run * kGramRun, i1 = min(m, i0 + kGramRun);
+        for (uint64_t i = i0; i < i1; i += 8) {
+            float v[8];  // eight rows in flight per warp
+#pragma unroll
+            for (int u = 0; u < 8; ++u) v[u] = (lane < a && i + u < i1) ? A[(i + u) * lda + lane] : 0.f;
+#pragma unroll
+            for (int u = 0; u < 8; ++u)
+#pragma unroll
+                for (int k = 0; k < 32; ++k) acc[k] = fmaf(__shfl_sync(0xffffffffu, v[u], k), v[u], acc[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < 32; ++k) mine[k * 33 + lane] += (double)acc[k];
+    }
+    __syncthreads();
+    // warps summed in a fixed order (deterministic)
+    double* dst = part + (uint64_t)blockIdx.x * a * a;
+    for (int e = threadIdx.x; e < a * a; e += blockDim.x) {
+        const int k = e / a, cc = e % a;
+        double t = 0.0;
+        for (int w = 0; w < 8; ++w) t += gsm[w * 32 * 33 + k * 33 + cc];
+        dst[e] = t;
+    }
+}
+
+// A (m x a, a <= 32) <- A Linv^T in place, one warp per row: lane c holds
+// column c of Linv^T (FP32) and accumulates out[c] = sum_k row[k] Linv[c][k]
+// from the broadcast row elements; loads and stores are whole rows.
+__global__ void __launch_bounds__(256) k_trmul_narrow(float* __restrict__ A, int lda, uint64_t m, int a,
+                                                      const double* __restrict__ Linv) {
+    const int lane = threadIdx.x & 31;
+    float R[32];
+#pragma unroll
+    for (int k = 0; k < 32; ++k) R[k] = (k < a && lane < a) ? (float)Linv[lane * a + k] : 0.f;
+    // each warp takes runs of 4 consecutive rows (four loads in flight)
+    const uint64_t warps = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t i = ((uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 4; i < m; i += warps * 4) {
+        float v[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) v[u] = (lane < a && i + u < m) ? A[(i + u) * lda + lane] : 0.f;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            float out = 0.f;
+#pragma unroll
+            for (int k = 0; k < 32; ++k) out = fmaf(__shfl_sync(0xffffffffu, v[u], k), R[k], out);
+            if (lane < a && i + u < m) A[(i + u) * lda + lane] = out;
+        }
+    }
+}
+
 __global__ void k_sum_partials(const double* __restrict__ part, int splits, uint64_t count,
                                double* __restrict__ out) {
     for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < count;
@@ -386,27 +453,26 @@ __global__ void k_inverse(const double* __restrict__ A, int a, double* __restric
 // CTA: A V = U diag(sig).  Outputs V (a x a), sig (descending) and U = A V
 // / sig in place of A.  Pairs are rotated in parallel with a round-robin
 // ordering, one warp per pair.
-__global__ void __launch_bounds__(1024) k_jacobi_svd(double* __restrict__ A, int a,
-                                                     double* __restrict__ V, double* __restrict__ sig) {
-    extern __shared__ double sm[];
-    const int ap = a + (a & 1);     // even number of columns (padded column is zero)
-    double* M = sm;                 // column-major ap x ap (rows a used)
-    double* Vs = sm + ap * ap;      // column-major
-    __shared__ int rotated;
-    __shared__ double sg[64];
-    __shared__ int order[64];
-    for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) {
-        const int col = e / ap, row = e % ap;
-        M[e] = (row < a && col < a) ? A[row * a + col] : 0.0;
-        Vs[e] = (row == col) ? 1.0 : 0.0;
-    }
-    __syncthreads();
+//
+// GB300 runs FP64 at a small fraction of its FP32 rate, so the sweeps run in
+// FP32 first (to ~1e-6 relative orthogonality); V is then re-orthonormalised
+// in FP64 (classical Gram-Schmidt, twice), M = A V formed in FP64, and FP64
+// sweeps polish to the FP64 tolerance -- typically two, against the ~10 a
+// cold FP64 start needs.
+__device__ __forceinline__ float warp_sumf(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// one Jacobi sweep-set on column-major M (ap x ap, rows a used) with
+// accumulated V; returns after convergence or max_sweeps
+template <typename F>
+__device__ void jacobi_sweeps(F* M, F* Vs, int a, int ap, F tol, int max_sweeps, int* rotated) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
     const int npairs = ap / 2;
-    // convergence: |<a_p, a_q>| <= tol * ||a_p|| ||a_q|| for every pair
-    const double tol = 4.0e-16 * (double)(a > 8 ? a : 8);
-    for (int sweep = 0; sweep < 40; ++sweep) {
-        if (threadIdx.x == 0) rotated = 0;
+    for (int sweep = 0; sweep < max_sweeps; ++sweep) {
+        if (threadIdx.x == 0) *rotated = 0;
         __syncthreads();
         for (int round = 0; round < ap - 1; ++round) {
             for (int pr = warp; pr < npairs; pr += nwarps) {
@@ -414,39 +480,106 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(double* __restrict__ A, int
                 auto pos = [&](int idx) { return idx == 0 ? 0 : 1 + ((idx - 1 + round) % (ap - 1)); };
                 int pcol = pos(pr), qcol = pos(ap - 1 - pr);
                 if (pcol > qcol) { const int t = pcol; pcol = qcol; qcol = t; }
-                double* mp = M + pcol * ap;
-                double* mq = M + qcol * ap;
-                double al = 0.0, be = 0.0, ga = 0.0;
+                F* mp = M + pcol * ap;
+                F* mq = M + qcol * ap;
+                F al = 0, be = 0, ga = 0;
                 for (int r = lane; r < a; r += 32) {
                     al += mp[r] * mp[r];
                     be += mq[r] * mq[r];
                     ga += mp[r] * mq[r];
                 }
-                al = warp_sum(al);
-                be = warp_sum(be);
-                ga = warp_sum(ga);
-                if (fabs(ga) > tol * sqrt(al * be) && fabs(ga) > 1e-300) {
-                    const double zeta = (be - al) / (2.0 * ga);
-                    const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-                    const double cs = 1.0 / sqrt(1.0 + t * t), sn = cs * t;
+                if constexpr (sizeof(F) == 8) {
+                    al = warp_sum(al); be = warp_sum(be); ga = warp_sum(ga);
+                } else {
+                    al = warp_sumf(al); be = warp_sumf(be); ga = warp_sumf(ga);
+                }
+                const F tiny = sizeof(F) == 8 ? (F)1e-300 : (F)1e-37;
+                if (fabs(ga) > tol * sqrt(al * be) && fabs(ga) > tiny) {
+                    const F zeta = (be - al) / (2 * ga);
+                    const F t = (zeta >= 0 ? (F)1 : (F)-1) / (fabs(zeta) + sqrt((F)1 + zeta * zeta));
+                    const F cs = (F)1 / sqrt((F)1 + t * t), sn = cs * t;
                     for (int r = lane; r < ap; r += 32) {
-                        const double x = mp[r], y = mq[r];
+                        const F x = mp[r], y = mq[r];
                         mp[r] = cs * x - sn * y;
                         mq[r] = sn * x + cs * y;
-                        double* vp = Vs + pcol * ap;
-                        double* vq = Vs + qcol * ap;
-                        const double vx = vp[r], vy = vq[r];
+                        F* vp = Vs + pcol * ap;
+                        F* vq = Vs + qcol * ap;
+                        const F vx = vp[r], vy = vq[r];
                         vp[r] = cs * vx - sn * vy;
                         vq[r] = sn * vx + cs * vy;
                     }
-                    if (lane == 0) rotated = 1;
+                    if (lane == 0) *rotated = 1;
                 }
             }
             __syncthreads();
         }
-        if (!rotated) break;
+        if (!*rotated) break;
         __syncthreads();
     }
+}
+
+__global__ void __launch_bounds__(1024) k_jacobi_svd(double* __restrict__ A, int a,
+                                                     double* __restrict__ V, double* __restrict__ sig) {
+    extern __shared__ double sm[];
+    const int ap = a + (a & 1);     // even number of columns (padded column is zero)
+    double* M = sm;                 // column-major ap x ap (rows a used)
+    double* Vs = sm + ap * ap;      // column-major
+    float* M32 = reinterpret_cast<float*>(Vs + ap * ap);
+    float* V32 = M32 + ap * ap;
+    __shared__ int rotated;
+    __shared__ double sg[64];
+    __shared__ double dots[64];
+    __shared__ int order[64];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    // phase 1: FP32 sweeps
+    for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) {
+        const int col = e / ap, row = e % ap;
+        M32[e] = (row < a && col < a) ? (float)A[row * a + col] : 0.f;
+        V32[e] = (row == col) ? 1.f : 0.f;
+    }
+    __syncthreads();
+    jacobi_sweeps<float>(M32, V32, a, ap, 2.0e-6f, 30, &rotated);
+    // phase 2: V <- FP64 Gram-Schmidt (twice) of the FP32 rotations
+    for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) Vs[e] = (double)V32[e];
+    __syncthreads();
+    for (int j = 0; j < ap; ++j) {
+        double* vj = Vs + j * ap;
+        for (int pass = 0; pass < 2; ++pass) {
+            for (int i = warp; i < j; i += nwarps) {
+                const double* vi = Vs + i * ap;
+                double t = 0.0;
+                for (int r = lane; r < ap; r += 32) t += vi[r] * vj[r];
+                t = warp_sum(t);
+                if (lane == 0) dots[i] = t;
+            }
+            __syncthreads();
+            for (int r = threadIdx.x; r < ap; r += blockDim.x) {
+                double t = vj[r];
+                for (int i = 0; i < j; ++i) t -= dots[i] * Vs[i * ap + r];
+                vj[r] = t;
+            }
+            __syncthreads();
+        }
+        if (warp == 0) {
+            double t = 0.0;
+            for (int r = lane; r < ap; r += 32) t += vj[r] * vj[r];
+            t = warp_sum(t);
+            const double inv = t > 0.0 ? 1.0 / sqrt(t) : 0.0;
+            for (int r = lane; r < ap; r += 32) vj[r] *= inv;
+        }
+        __syncthreads();
+    }
+    // phase 3: M = A V in FP64, then FP64 sweeps from there
+    for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) {
+        const int col = e / ap, row = e % ap;
+        double t = 0.0;
+        if (row < a)
+            for (int k = 0; k < a; ++k) t += A[row * a + k] * Vs[col * ap + k];
+        M[e] = t;
+    }
+    __syncthreads();
+    // convergence: |<a_p, a_q>| <= tol * ||a_p|| ||a_q|| for every pair
+    jacobi_sweeps<double>(M, Vs, a, ap, 4.0e-16 * (double)(a > 8 ? a : 8), 40, &rotated);
     // singular values and descending order
     for (int cc = warp; cc < a; cc += nwarps) {
         double s = 0.0;
@@ -611,6 +744,18 @@ void launch_atb(Ctx& c, const double* A, int lda, const double* B, int ldb, uint
 }
 
 void launch_gram_f32(Ctx& c, const float* A, int lda, uint64_t m, int a, double* out) {
+    if (a <= 32) {
+        const uint64_t runs = std::max<uint64_t>(1, ceil_div(m, (uint64_t)kGramRun));
+        const uint64_t blocks = std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(runs, 8), (uint64_t)c.sm_count * 4));
+        DBuf<double> part(blocks * a * a, c.stream);
+        set_smem((const void*)k_gram_narrow, kGramNarrowSmem);
+        k_gram_narrow<<<(unsigned)blocks, 256, kGramNarrowSmem, c.stream>>>(A, lda, m, a, part.get());
+        SLFMM_LAUNCHED(c, "k_gram_narrow");
+        k_sum_partials<<<grid_for(c, (uint64_t)a * a, 256), 256, 0, c.stream>>>(part.get(), (int)blocks,
+                                                                                (uint64_t)a * a, out);
+        SLFMM_LAUNCHED(c, "k_sum_partials");
+        return;
+    }
     const int ta = (int)ceil_div(a, 32);
     uint64_t splits = std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(m, 1024),
                                           ceil_div((uint64_t)c.sm_count * 8, (uint64_t)ta * ta)));
@@ -649,8 +794,12 @@ void launch_gemm_small_f32out(Ctx& c, const double* A, int lda, uint64_t m, int 
 void launch_trmul_f32(Ctx& c, float* A, int lda, uint64_t m, int a, const double* Linv) {
     SLFMM_REQUIRE(a <= 64, SLFMM_ERR_BAD_ARG, "sketch width must be <= 64");
     if (m == 0) return;
-    if (a <= 32) k_trmul_f32<32><<<grid_for(c, m, 128), 128, 0, c.stream>>>(A, lda, m, a, Linv);
-    else k_trmul_f32<64><<<grid_for(c, m, 128), 128, 0, c.stream>>>(A, lda, m, a, Linv);
+    if (a <= 32) {
+        k_trmul_narrow<<<grid_for(c, m, 32), 256, 0, c.stream>>>(A, lda, m, a, Linv);
+        SLFMM_LAUNCHED(c, "k_trmul_narrow");
+        return;
+    }
+    k_trmul_f32<64><<<grid_for(c, m, 128), 128, 0, c.stream>>>(A, lda, m, a, Linv);
     SLFMM_LAUNCHED(c, "k_trmul_f32");
 }
 
@@ -678,7 +827,7 @@ void launch_inverse(Ctx& c, const double* A, int a, double* Ainv, int* status, d
 void launch_jacobi_svd(Ctx& c, const double* A, int a, double* V, double* sig) {
     SLFMM_REQUIRE(a <= 64, SLFMM_ERR_BAD_ARG, "Jacobi SVD limited to 64 x 64");
     const int ap = a + (a & 1);
-    const size_t sm = 2 * (size_t)ap * ap * sizeof(double);
+    const size_t sm = 2 * (size_t)ap * ap * (sizeof(double) + sizeof(float));
     set_smem((const void*)k_jacobi_svd, sm);
     k_jacobi_svd<<<1, 1024, sm, c.stream>>>(const_cast<double*>(A), a, V, sig);
     SLFMM_LAUNCHED(c, "k_jacobi_svd");

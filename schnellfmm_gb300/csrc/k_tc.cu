@@ -319,14 +319,40 @@ __global__ void k_colfix_mean(double* __restrict__ S, int lds, uint64_t n, int w
 }
 
 // colterm[c] = sum_j coef_j Q[j, c]  (block partials, fixed order)
-__global__ void k_weighted_colsum(const float* __restrict__ Q, int ldq, uint64_t p, int w,
-                                  const double* __restrict__ coef, uint64_t per, double* __restrict__ part) {
-    const int c = threadIdx.x;
-    if (c >= w) return;
-    const uint64_t j0 = (uint64_t)blockIdx.x * per, j1 = min(p, j0 + per);
-    double acc = 0.0;
-    for (uint64_t j = j0; j < j1; ++j) acc += coef[j] * (double)Q[j * ldq + c];
-    part[(uint64_t)blockIdx.x * w + c] = acc;
+// out[c] = sum_j coef[j] Q[j, c] (w <= 128): block partials, one warp per run
+// of rows with the row read whole (lane c, c + 32, ...), four rows in flight.
+__global__ void __launch_bounds__(256) k_weighted_colsum(const float* __restrict__ Q, int ldq, uint64_t p, int w,
+                                                         const double* __restrict__ coef, double* __restrict__ part) {
+    __shared__ double red[8][128];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    const uint64_t nw = (uint64_t)gridDim.x * 8;
+    for (uint64_t j = ((uint64_t)blockIdx.x * 8 + warp) * 4; j < p; j += nw * 4) {
+        float q[4][4];
+        double cf[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const bool ok = j + u < p;
+            cf[u] = ok ? coef[j + u] : 0.0;
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const int cc = lane + 32 * t;
+                q[u][t] = (ok && cc < w) ? Q[(j + u) * ldq + cc] : 0.f;
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int t = 0; t < 4; ++t) acc[t] = fma(cf[u], (double)q[u][t], acc[t]);
+    }
+#pragma unroll
+    for (int t = 0; t < 4; ++t) red[warp][lane + 32 * t] = acc[t];
+    __syncthreads();
+    for (int cc = threadIdx.x; cc < w; cc += blockDim.x) {
+        double s = 0.0;
+        for (int ww = 0; ww < 8; ++ww) s += red[ww][cc];
+        part[(uint64_t)blockIdx.x * w + cc] = s;
+    }
 }
 
 __global__ void k_scale_product(const double* __restrict__ a, const double* __restrict__ b, uint64_t n,
@@ -509,10 +535,9 @@ void launch_colfix_mean(Ctx& c, double* S, int lds, uint64_t n, int w, const uin
 
 void launch_weighted_colsum(Ctx& c, const float* Q, int ldq, uint64_t p, int w, const double* coef, double* out) {
     SLFMM_REQUIRE(w <= 128, SLFMM_ERR_BAD_ARG, "width");
-    const uint64_t blocks = std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(p, 4096), 1024));
-    const uint64_t per = ceil_div(std::max<uint64_t>(p, 1), blocks);
+    const uint64_t blocks = std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(p, 256), (uint64_t)c.sm_count * 4));
     DBuf<double> part(blocks * w, c.stream);
-    k_weighted_colsum<<<(unsigned)blocks, 128, 0, c.stream>>>(Q, ldq, p, w, coef, per, part.get());
+    k_weighted_colsum<<<(unsigned)blocks, 256, 0, c.stream>>>(Q, ldq, p, w, coef, part.get());
     SLFMM_LAUNCHED(c, "k_weighted_colsum");
     launch_sum_partials(c, part.get(), (int)blocks, (uint64_t)w, out);
 }

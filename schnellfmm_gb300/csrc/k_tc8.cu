@@ -431,21 +431,32 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
 }
 
-// per-column max |x * kscale| as float bits (non-negative floats order as ints)
+// per-column max |x * kscale| as float bits (non-negative floats order as
+// ints); one warp per row, lanes over columns (w <= 128), the per-row scale
+// converted once per row
 template <typename T>
-__global__ void k_colmax_abs(const T* __restrict__ src, int ld, uint64_t K, int w, const double* __restrict__ kscale,
-                             unsigned* __restrict__ colmax) {
-    const int c = threadIdx.x % w;
-    const int rstep = blockDim.x / w;
-    const int r0 = threadIdx.x / w;
-    if (r0 >= rstep) return;
-    float m = 0.f;
-    for (uint64_t k = (uint64_t)blockIdx.x * rstep + r0; k < K; k += (uint64_t)gridDim.x * rstep) {
-        double x = (double)src[k * ld + c];
-        if (kscale) x *= kscale[k];
-        m = fmaxf(m, fabsf((float)x));
+__global__ void __launch_bounds__(256) k_colmax_abs(const T* __restrict__ src, int ld, uint64_t K, int w,
+                                                    const double* __restrict__ kscale, unsigned* __restrict__ colmax) {
+    const int lane = threadIdx.x & 31;
+    float m[4] = {0.f, 0.f, 0.f, 0.f};
+    const uint64_t nw = (uint64_t)gridDim.x * (blockDim.x >> 5);
+    for (uint64_t k = (uint64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); k < K; k += nw) {
+        float ks = 1.f;
+        if (kscale) {
+            if (lane == 0) ks = (float)kscale[k];
+            ks = __shfl_sync(0xffffffffu, ks, 0);
+        }
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+            const int c = lane + 32 * t;
+            if (c < w) m[t] = fmaxf(m[t], fabsf((float)src[k * ld + c] * ks));
+        }
     }
-    atomicMax(colmax + c, __float_as_uint(m));
+#pragma unroll
+    for (int t = 0; t < 4; ++t) {
+        const int c = lane + 32 * t;
+        if (c < w) atomicMax(colmax + c, __float_as_uint(m[t]));
+    }
 }
 
 __device__ __forceinline__ int term_e0(unsigned bits) {
@@ -456,31 +467,46 @@ __device__ __forceinline__ int term_e0(unsigned bits) {
     return 8 - E;  // cm * 2^e0 in [128, 256)
 }
 
+// exact 2^ex as a float (ldexpf outside the normal exponent range)
+__device__ __forceinline__ float pow2f(int ex) {
+    return (ex >= -126 && ex <= 127) ? __int_as_float((127 + ex) << 23) : ldexpf(1.f, ex);
+}
+
 // W (K x w) -> `terms` E4M3 rows per column at B rows row_off + t * wpad + c,
 // K contiguous, zero padded to K_pad; inv_scale[row] = 2^-(e0 + 4t).
+// Term t is round_e4m3((r - terms_<t) * 2^(e0 + 4t)); the power-of-two scales
+// are exact, so each step's residual is rounded once.
 template <typename T>
-__global__ void k_fp8_terms(const T* __restrict__ src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
-                            const double* __restrict__ kscale, int terms, int row_off,
-                            const unsigned* __restrict__ colmax, uint8_t* __restrict__ B, float* __restrict__ inv_scale) {
-    __shared__ uint8_t tile[kMainTerms][32][129];
+__global__ void __launch_bounds__(256) k_fp8_terms(const T* __restrict__ src, int ld, uint64_t K, int w, int wpad,
+                                                   uint64_t K_pad, const double* __restrict__ kscale, int terms,
+                                                   int row_off, const unsigned* __restrict__ colmax,
+                                                   uint8_t* __restrict__ B, float* __restrict__ inv_scale) {
+    __shared__ __align__(16) uint8_t tile[kMainTerms][32][132];
+    __shared__ float ks[128];
+    __shared__ int e0s[32];
     const uint64_t k0 = (uint64_t)blockIdx.x * 128;
     const int c0 = blockIdx.y * 32;
+    for (int i = threadIdx.x; i < 128; i += blockDim.x) {
+        const uint64_t k = k0 + i;
+        ks[i] = (kscale && k < K) ? (float)kscale[k] : 1.f;
+    }
+    for (int i = threadIdx.x; i < 32; i += blockDim.x) {
+        const int c = c0 + i;
+        e0s[i] = c < w ? term_e0(colmax[c]) : 0;
+    }
+    __syncthreads();
     for (int e = threadIdx.x; e < 128 * 32; e += blockDim.x) {
         const int kk = e / 32, cc = e % 32;
         const uint64_t k = k0 + kk;
         const int c = c0 + cc;
         float r = 0.f;
-        if (k < K && c < w) {
-            double x = (double)src[k * ld + c];
-            if (kscale) x *= kscale[k];
-            r = (float)x;
-        }
-        const int e0 = c < w ? term_e0(colmax[c]) : 0;
+        if (k < K && c < w) r = (float)src[k * ld + c] * ks[kk];
+        const int e0 = e0s[cc];
         for (int t = 0; t < terms; ++t) {
             const int ex = e0 + 4 * t;
-            const __nv_fp8_storage_t qv = __nv_cvt_float_to_fp8(ldexpf(r, ex), __NV_SATFINITE, __NV_E4M3);
+            const __nv_fp8_storage_t qv = __nv_cvt_float_to_fp8(r * pow2f(ex), __NV_SATFINITE, __NV_E4M3);
             const __half_raw hr = __nv_cvt_fp8_to_halfraw(qv, __NV_E4M3);
-            r -= ldexpf(__half2float(__half(hr)), -ex);
+            r = fmaf(-__half2float(__half(hr)), pow2f(-ex), r);
             tile[t][cc][kk] = (uint8_t)qv;
         }
     }
@@ -488,17 +514,23 @@ __global__ void k_fp8_terms(const T* __restrict__ src, int ld, uint64_t K, int w
     if (blockIdx.x == 0)
         for (int e = threadIdx.x; e < terms * 32; e += blockDim.x) {
             const int t = e / 32, cc = e % 32, c = c0 + cc;
-            if (c < wpad) inv_scale[row_off + t * wpad + c] = c < w ? ldexpf(1.f, -(term_e0(colmax[c]) + 4 * t)) : 1.f;
+            if (c < wpad) inv_scale[row_off + t * wpad + c] = c < w ? pow2f(-(e0s[cc] + 4 * t)) : 1.f;
         }
     // B position kp within each 16-group holds K index kk = perm(kp): the even
     // K indices of the group, then the odd ones (the order the unpackers emit
-    // the genotypes of a 32-bit code word in)
-    for (int e = threadIdx.x; e < terms * 32 * 128; e += blockDim.x) {
-        const int t = e / (32 * 128), rem = e % (32 * 128), cc = rem / 128, kp = rem % 128;
-        const int kk = (kp & ~15) | ((kp & 7) << 1) | ((kp >> 3) & 1);
+    // the genotypes of a 32-bit code word in); written as 32-bit words
+    for (int e = threadIdx.x; e < terms * 32 * 32; e += blockDim.x) {
+        const int t = e / (32 * 32), rem = e % (32 * 32), cc = rem / 32, kp0 = (rem % 32) * 4;
         const int c = c0 + cc;
-        const uint64_t k = k0 + kp;
-        if (c < wpad && k < K_pad) B[(uint64_t)(row_off + t * wpad + c) * K_pad + k] = tile[t][cc][kk];
+        if (c >= wpad) continue;
+        uint32_t word = 0;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int kp = kp0 + b;
+            const int kk = (kp & ~15) | ((kp & 7) << 1) | ((kp >> 3) & 1);
+            word |= (uint32_t)tile[t][cc][kk] << (8 * b);
+        }
+        *reinterpret_cast<uint32_t*>(B + (uint64_t)(row_off + t * wpad + c) * K_pad + k0 + kp0) = word;
     }
 }
 
@@ -652,8 +684,8 @@ void launch_fp8_terms_f64(Ctx& c, const double* src, int ld, uint64_t K, int w, 
                           const double* kscale, int terms, int row_off, uint8_t* B, float* inv_scale) {
     DBuf<unsigned> cm(wpad, c.stream);
     cm.zero();
-    const int rstep = 256 / w;
-    k_colmax_abs<double><<<grid_for(c, ceil_div(K, rstep), 1), w * rstep, 0, c.stream>>>(src, ld, K, w, kscale, cm.get());
+    SLFMM_REQUIRE(w >= 1 && w <= 128 && wpad <= 128, SLFMM_ERR_BAD_ARG, "operand wider than 128 columns");
+    k_colmax_abs<double><<<grid_for(c, K, 8), 256, 0, c.stream>>>(src, ld, K, w, kscale, cm.get());
     SLFMM_LAUNCHED(c, "k_colmax_abs");
     dim3 grid((unsigned)ceil_div(K_pad, 128), (unsigned)ceil_div(wpad, 32));
     k_fp8_terms<double><<<grid, 256, 0, c.stream>>>(src, ld, K, w, wpad, K_pad, kscale, terms, row_off, cm.get(), B,
@@ -665,8 +697,8 @@ void launch_fp8_terms_f32(Ctx& c, const float* src, int ld, uint64_t K, int w, i
                           const double* kscale, int terms, int row_off, uint8_t* B, float* inv_scale) {
     DBuf<unsigned> cm(wpad, c.stream);
     cm.zero();
-    const int rstep = 256 / w;
-    k_colmax_abs<float><<<grid_for(c, ceil_div(K, rstep), 1), w * rstep, 0, c.stream>>>(src, ld, K, w, kscale, cm.get());
+    SLFMM_REQUIRE(w >= 1 && w <= 128 && wpad <= 128, SLFMM_ERR_BAD_ARG, "operand wider than 128 columns");
+    k_colmax_abs<float><<<grid_for(c, K, 8), 256, 0, c.stream>>>(src, ld, K, w, kscale, cm.get());
     SLFMM_LAUNCHED(c, "k_colmax_abs");
     dim3 grid((unsigned)ceil_div(K_pad, 128), (unsigned)ceil_div(wpad, 32));
     k_fp8_terms<float><<<grid, 256, 0, c.stream>>>(src, ld, K, w, wpad, K_pad, kscale, terms, row_off, cm.get(), B,
