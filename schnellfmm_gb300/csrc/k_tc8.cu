@@ -647,6 +647,42 @@ __global__ void k_tile_rows(const uint8_t* __restrict__ in, uint64_t rows, uint6
     }
 }
 
+// Tile-major transpose of the 2-bit matrix.  Block (t, kb) of the output --
+// 128 samples of sample tile t x the 128 SNPs of K block kb -- is the 2-bit
+// transpose of block (kb, t) of the SNP-row tiles; both are contiguous 4 KiB
+// runs.  One block per iteration: a coalesced 4 KiB load into shared memory,
+// each thread then assembles 4 output words (16 codes each) of one sample
+// from 16 SNP rows, and the 4 KiB result is stored contiguously.
+__global__ void __launch_bounds__(256) k_transpose_tiles(const uint8_t* __restrict__ src, uint64_t kbt_src,
+                                                         uint64_t ntiles_src, uint8_t* __restrict__ dst,
+                                                         uint64_t kbt_dst, uint64_t ntiles_dst) {
+    __shared__ __align__(16) uint8_t in[128 * 32];
+    const uint64_t nblocks = ntiles_dst * kbt_dst;
+    const int j = threadIdx.x & 127;   // sample within the tile
+    const int h = threadIdx.x >> 7;    // which 64 SNPs
+    for (uint64_t b = blockIdx.x; b < nblocks; b += gridDim.x) {
+        const uint64_t t = b / kbt_dst, kb = b - t * kbt_dst;
+        const bool valid = kb < ntiles_src && t < kbt_src;
+        __syncthreads();
+        const uint4* s4 = reinterpret_cast<const uint4*>(src + (kb * kbt_src + t) * (uint64_t)kPacked);
+        reinterpret_cast<uint4*>(in)[threadIdx.x] = valid ? s4[threadIdx.x] : make_uint4(0, 0, 0, 0);
+        __syncthreads();
+        const int byte = j >> 2, shift = 2 * (j & 3);
+        uint32_t wv[4];
+#pragma unroll
+        for (int w = 0; w < 4; ++w) {
+            uint32_t v = 0;
+#pragma unroll
+            for (int ii = 0; ii < 16; ++ii) {
+                const int i = h * 64 + w * 16 + ii;  // SNP within the K block
+                v |= (uint32_t)((in[i * 32 + byte] >> shift) & 3u) << (2 * ii);
+            }
+            wv[w] = v;
+        }
+        *reinterpret_cast<uint4*>(dst + b * (uint64_t)kPacked + j * 32 + h * 16) = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+    }
+}
+
 static void tile_rows(Ctx& c, const uint8_t* in, uint64_t rows, uint64_t stride, DBuf<uint8_t>& out, uint64_t& kbt,
                       uint64_t& ntiles) {
     SLFMM_REQUIRE(stride % 32 == 0, SLFMM_ERR_BAD_ARG, "packed stride must be a multiple of 32 bytes");
@@ -668,14 +704,16 @@ TileView build_tiles(Ctx& c, const Geno& g, bool transposed) {
         return TileView{g.tiles.get(), g.kbt, g.ntiles};
     }
     if (!g.have_tilesT) {
-        const bool had_T = g.have_T;
-        build_transposed(c, g);
-        tile_rows(c, g.packedT.get(), g.n, g.strideT, g.tilesT, g.kbtT, g.ntilesT);
+        // straight from the SNP-row tiles: sample tiles x K blocks of 128 SNPs
+        build_tiles(c, g, false);
+        g.kbtT = std::max<uint64_t>(ceil_div(g.p, kM), 1);
+        g.ntilesT = round_up(std::max<uint64_t>(ceil_div(g.n, kM), 1), 8);
+        g.tilesT.alloc(g.ntilesT * g.kbtT * kPacked, c.stream);
+        const uint64_t blocks = std::min<uint64_t>(g.ntilesT * g.kbtT, (uint64_t)c.sm_count * 16);
+        k_transpose_tiles<<<(unsigned)blocks, 256, 0, c.stream>>>(g.tiles.get(), g.kbt, g.ntiles, g.tilesT.get(),
+                                                                   g.kbtT, g.ntilesT);
+        SLFMM_LAUNCHED(c, "k_transpose_tiles");
         g.have_tilesT = true;
-        if (!had_T) {  // the row-major transposed copy was only a staging step
-            g.packedT.release();
-            g.have_T = false;
-        }
     }
     return TileView{g.tilesT.get(), g.kbtT, g.ntilesT};
 }
