@@ -231,7 +231,7 @@ void row_contract(Ctx& c, const Geno& g, const SnpStd& s, const double* W, int w
                   DBuf<float>& out, int& wp) {
     wp = pad16(w);
     SLFMM_REQUIRE(wp <= kMaxW, SLFMM_ERR_BAD_ARG, "operand wider than 128 columns");
-    const uint64_t n_pad = round_up(g.n, 128);
+    const uint64_t n_pad = round_up(g.n, 256);  // whole split-FP8 stages (256 codes)
     DBuf<float> W32(n_pad * wp, c.stream);
     launch_f64_to_f32_pad(c, W, g.n, w, ldw, W32.get(), n_pad, wp);
     out.alloc(std::max<uint64_t>(g.p, 1) * wp, c.stream);
@@ -300,7 +300,7 @@ void col_contract(Ctx& c, const Geno& g, const SnpStd& s, const float* Q, int w,
         // genotypes plus terms of diag(mu s) Q against the missing-call
         // indicator, then S -= (mu s)^T Q
         const TileView tv = build_tiles(c, g, true);
-        const uint64_t p_pad = round_up(g.p, 128);
+        const uint64_t p_pad = round_up(g.p, 256);  // whole split-FP8 stages (256 codes)
         const uint64_t tiles = ceil_div(g.n, 128);
         Fp8Plan pl = fp8_plan(wp, true, tiles);
         const bool ind = pl.ok;
@@ -1048,7 +1048,7 @@ int slfmm_contract_raw(slfmm_ctx* c, const slfmm_geno* g, int flags, const doubl
     const int wp = pad16((int)w);
     SLFMM_REQUIRE(wp <= kMaxW, SLFMM_ERR_BAD_ARG, "operand wider than 128 columns");
     const uint64_t K = transposed ? g->p : g->n, rows = transposed ? g->n : g->p;
-    const uint64_t K_pad = round_up(K, 128);
+    const uint64_t K_pad = round_up(K, 256);
     DBuf<double> Wd = upload(*c, w_host, K * w);
     DBuf<float> o(std::max<uint64_t>(rows, 1) * wp, c->stream);
     if (c->precision == SLFMM_PREC_SPLIT_FP8) {

@@ -36,9 +36,13 @@ namespace {
 using namespace tc;
 
 constexpr int kM = 128;
-constexpr int kKB = 128;
-constexpr int kPacked = kM * kKB / 4;  // 4096 B
-constexpr int kThreads = 384;  // code-copy warp, 2 MMA warps, W-copy warp, 2 x 4 unpack warps
+constexpr int kTileK = 128;                        // samples (codes) per tile block
+constexpr int kTileBytes = kM * kTileK / 4;        // 4 KiB: 128 rows x 32 B
+constexpr int kHalves = 2;                         // tile blocks per pipeline stage
+constexpr int kStageK = kTileK * kHalves;          // 256 samples per stage
+constexpr int kStageBytes = kTileBytes * kHalves;  // packed bytes per stage
+constexpr int kUnpackSets = 2;   // sets of four unpack warps taking K blocks round robin
+constexpr int kThreads = 128 + 128 * kUnpackSets;  // code-copy, 2 MMA, W-copy warps + unpack sets
 constexpr int kMainTerms = 4;
 constexpr int kIndTerms = 3;
 constexpr uint32_t kTabGeno = 0x40380000u;  // code 00,01 -> 0; 10 -> 1.0; 11 -> 2.0 (E4M3 bytes)
@@ -58,6 +62,8 @@ struct Tc8Args {
     uint32_t kcopies;       // accumulator copies (2: MMA warps take alternate K groups)
     uint32_t nsplit;        // 1: MMA warp 0 issues the genotype MMAs, warp 1 the indicator MMAs
     uint32_t a_base;        // first TMEM column of the A stages
+    uint32_t usets;         // unpack sets in use: at most `stages`, so that a set never waits on a stage
+                            // two uses ahead (an mbarrier parity wait cannot tell those apart)
     uint32_t b_stage_bytes; // n_total * 128
     uint32_t cluster;       // CTAs sharing W through multicast
     uint32_t box_rows;      // rows per W TMA box
@@ -74,6 +80,27 @@ struct Tc8Args {
     uint64_t tile_bytes;    // kbt * 4096
     int* err;
 };
+
+// Pins 32 values in registers at this point of the program (an empty asm
+// that reads them), so the compiler cannot sink their computation past a
+// following wait.
+__device__ __forceinline__ void keep32(const uint32_t (&v)[32]) {
+    asm volatile("" ::"r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]),
+                 "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]), "r"(v[15]),
+                 "r"(v[16]), "r"(v[17]), "r"(v[18]), "r"(v[19]), "r"(v[20]), "r"(v[21]), "r"(v[22]), "r"(v[23]),
+                 "r"(v[24]), "r"(v[25]), "r"(v[26]), "r"(v[27]), "r"(v[28]), "r"(v[29]), "r"(v[30]), "r"(v[31]));
+}
+
+// Warp-wide bounded wait: lane 0 polls the barrier, the result is broadcast
+// and __syncwarp orders the other lanes after lane 0's observation.  One
+// poller per warp keeps the barrier word's traffic low.
+__device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+    int ok = 1;
+    if ((threadIdx.x & 31) == 0) ok = mbar_wait(bar, parity, err, code) ? 1 : 0;
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    __syncwarp();
+    return ok != 0;
+}
 
 // Ring position: slot index and the parity of its current use.
 struct Ring {
@@ -113,6 +140,7 @@ __device__ __forceinline__ void tc8_mma_loop(const Tc8Args& a, uint32_t tmem, ui
     const uint64_t bstep = a.b_stage_bytes >> 4;          // descriptor address units per stage
     const uint64_t chstep = (uint64_t)chunk * (128 >> 4);  // per main chunk of B rows
     const uint64_t indoff = (uint64_t)a.n_main * (128 >> 4);
+    const uint64_t hstep = (uint64_t)a.n_total * (128 >> 4);  // next 128-sample half of the stage
     const uint32_t d_ind = tmem + a.n_main;
     const uint32_t a0 = tmem + a.a_base;
     Ring st{0, 0};
@@ -135,14 +163,15 @@ __device__ __forceinline__ void tc8_mma_loop(const Tc8Args& a, uint32_t tmem, ui
                 const uint32_t ad = a0 + st.slot * a.a_cols;
                 const uint32_t acc0 = (i + j) > start ? 1u : 0u;
 #pragma unroll
-                for (int kk = 0; kk < kKB / 32; ++kk) {
+                for (int kk = 0; kk < kStageK / 32; ++kk) {
                     const uint32_t acc = kk > 0 ? 1u : acc0;
+                    const uint64_t bk = bd + (kk >> 2) * hstep + (kk & 3) * 2;
                     if (MAIN) {
 #pragma unroll
                         for (int ch = 0; ch < NCH; ++ch)
-                            mma_ts_f8(d_main + ch * chunk, ad + kk * 8, bd + ch * chstep + kk * 2, id_main, acc);
+                            mma_ts_f8(d_main + ch * chunk, ad + kk * 8, bk + ch * chstep, id_main, acc);
                     }
-                    if (IND) mma_ts_f8(d_ind, ad + 32 + kk * 8, bd + indoff + kk * 2, id_ind, acc);
+                    if (IND) mma_ts_f8(d_ind, ad + kStageK / 4 + kk * 8, bk + indoff, id_ind, acc);
                 }
                 mma_commit(a_empty + st.slot);
                 if (mask != 1) mma_commit_mc(b_empty + st.slot, mask);
@@ -179,7 +208,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t S = a.stages, P = a.pstages;
     uint8_t* bsm = smem;
     uint8_t* psm = bsm + S * a.b_stage_bytes;
-    float* scl = reinterpret_cast<float*>(psm + P * kPacked);                 // up to 512 floats
+    float* scl = reinterpret_cast<float*>(psm + P * kStageBytes);             // up to 512 floats
     uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<uint8_t*>(scl) + 2048);
     uint64_t* full_b = bars;                 // [S] W tile landed (TMA tx)
     uint64_t* full_a = bars + S;             // [S] A operand written to TMEM (128 arrivals)
@@ -203,7 +232,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (threadIdx.x == 0) {
         for (uint32_t s = 0; s < S; ++s) {
             mbar_init(full_b + s, 1);
-            mbar_init(full_a + s, 128);
+            mbar_init(full_a + s, 4);     // one arrival per unpack warp
             mbar_init(a_empty + s, a.nsplit ? 2 : 1);   // every MMA warp that reads the stage commits
             mbar_init(b_empty + s, a.nsplit ? 2 * C : C);
         }
@@ -230,14 +259,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (warp == 0) {
         if (lane == 0) {
             // packed-code producer: runs up to P stages ahead of the unpackers;
-            // each (tile, K block) operand is one contiguous 4 KiB bulk copy
-            const uint8_t* src = a.tiles + (uint64_t)blockIdx.x * a.tile_bytes + (uint64_t)kb0 * kPacked;
+            // each (tile, stage) operand is one contiguous bulk copy
+            const uint8_t* src = a.tiles + (uint64_t)blockIdx.x * a.tile_bytes + (uint64_t)kb0 * kStageBytes;
             Ring pr{0, 0};
             uint32_t issued = 0;
             for (uint32_t i = 0; i < nkb; ++i) {
                 if (i >= P && !mbar_wait(p_empty + pr.slot, pr.phase ^ 1u, a.err, 21)) break;
-                mbar_arrive_tx(p_full + pr.slot, kPacked);
-                bulk_g2s(psm + pr.slot * kPacked, src + (uint64_t)i * kPacked, kPacked, p_full + pr.slot);
+                mbar_arrive_tx(p_full + pr.slot, kStageBytes);
+                bulk_g2s(psm + pr.slot * kStageBytes, src + (uint64_t)i * kStageBytes, kStageBytes, p_full + pr.slot);
                 issued = i + 1;
                 pr.advance(1, P);
             }
@@ -256,12 +285,14 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (i >= S && !mbar_wait(b_empty + wr.slot, wr.phase ^ 1u, a.err, 23)) break;
                 mbar_arrive_tx(full_b + wr.slot, a.b_stage_bytes);
                 const int kb = (int)(kb0 + i);
-                for (uint32_t l = 0; l < a.loads; ++l) {
-                    const uint32_t y = y_begin + l * a.box_rows;
-                    uint8_t* dst = bsm + wr.slot * a.b_stage_bytes + y * 128;
-                    if (C > 1) tma_2d_mc(dst, &tm_b, kb * kKB, (int)y, full_b + wr.slot, mask);
-                    else tma_2d(dst, &tm_b, kb * kKB, (int)y, full_b + wr.slot);
-                }
+                for (int h = 0; h < kHalves; ++h)
+                    for (uint32_t l = 0; l < a.loads; ++l) {
+                        const uint32_t y = y_begin + l * a.box_rows;
+                        uint8_t* dst = bsm + wr.slot * a.b_stage_bytes + (h * a.n_total + y) * 128;
+                        const int x = kb * kStageK + h * kTileK;
+                        if (C > 1) tma_2d_mc(dst, &tm_b, x, (int)y, full_b + wr.slot, mask);
+                        else tma_2d(dst, &tm_b, x, (int)y, full_b + wr.slot);
+                    }
                 issued = i + 1;
                 wr.advance(1, S);
             }
@@ -317,41 +348,57 @@ __global__ void __launch_bounds__(kThreads, 1)
             mma_commit(tmem_full);  // both MMA warps arrive (an idle one at once)
         }
     } else {
-        // two sets of four unpack warps take alternate K blocks; warp % 4 is
-        // the TMEM lane quarter a warp may access
+        // kUnpackSets sets of four unpack warps take K blocks round robin;
+        // warp % 4 is the TMEM lane quarter a warp may access
         const uint32_t set = (uint32_t)(warp - 4) >> 2;
         const uint32_t q = (uint32_t)warp & 3u;
         const uint32_t row = q * 32 + lane;
         const uint32_t lane_base = tmem + ((q * 32) << 16);
-        Ring pr{set, 0}, st{set, 0};  // P, S >= 2
-        for (uint32_t i = set; i < nkb; i += 2) {
-            if (!__all_sync(0xffffffffu, mbar_wait(p_full + pr.slot, pr.phase, a.err, 27))) break;
-            const uint4* src = reinterpret_cast<const uint4*>(psm + pr.slot * kPacked + row * (kKB / 4));
-            const uint4 p0 = src[0], p1 = src[1];
+        Ring pr{0, 0}, st{0, 0};
+        pr.advance(set, P);
+        st.advance(set, S);
+        const uint32_t nsets = a.usets;
+        for (uint32_t i = set; i < nkb && set < nsets; i += nsets) {
+            // one lane polls each barrier and the warp follows it (the warp
+            // barrier orders the other lanes after its observation)
+            if (!warp_wait(p_full + pr.slot, pr.phase, a.err, 27)) break;
+            // this row's 256 codes: 32 B in each of the stage's two tile blocks
+            const uint8_t* rp = psm + pr.slot * kStageBytes + row * (kTileK / 4);
+            const uint4 p0 = reinterpret_cast<const uint4*>(rp)[0], p1 = reinterpret_cast<const uint4*>(rp)[1];
+            const uint4 p2 = reinterpret_cast<const uint4*>(rp + kTileBytes)[0];
+            const uint4 p3 = reinterpret_cast<const uint4*>(rp + kTileBytes)[1];
             __syncwarp();
             if (lane == 0) mbar_arrive(p_empty + pr.slot);   // codes are in registers: release the slot
-            pr.advance(2, P);
+            pr.advance(nsets, P);
             // a 32-bit word holds 16 two-bit codes; masking the even / odd codes
             // into nibbles gives PRMT selectors directly (4 codes per PRMT), and
             // the B operand stores K in the matching even-then-odd order
-            const uint32_t w8[8] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w};
-            uint32_t ev[8], od[8];
+            const uint32_t w16[16] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w,
+                                      p2.x, p2.y, p2.z, p2.w, p3.x, p3.y, p3.z, p3.w};
+            uint32_t ev[16], od[16];
 #pragma unroll
-            for (int t = 0; t < 8; ++t) {
-                ev[t] = w8[t] & 0x33333333u;
-                od[t] = (w8[t] >> 2) & 0x33333333u;
+            for (int t = 0; t < 16; ++t) {
+                ev[t] = w16[t] & 0x33333333u;
+                od[t] = (w16[t] >> 2) & 0x33333333u;
             }
-            uint32_t g[32];
+            uint32_t g[32], h[32];
 #pragma unroll
             for (int t = 0; t < 8; ++t) {
                 g[4 * t] = __byte_perm(kTabGeno, 0u, ev[t]);
                 g[4 * t + 1] = __byte_perm(kTabGeno, 0u, ev[t] >> 16);
                 g[4 * t + 2] = __byte_perm(kTabGeno, 0u, od[t]);
                 g[4 * t + 3] = __byte_perm(kTabGeno, 0u, od[t] >> 16);
+                h[4 * t] = __byte_perm(kTabGeno, 0u, ev[8 + t]);
+                h[4 * t + 1] = __byte_perm(kTabGeno, 0u, ev[8 + t] >> 16);
+                h[4 * t + 2] = __byte_perm(kTabGeno, 0u, od[8 + t]);
+                h[4 * t + 3] = __byte_perm(kTabGeno, 0u, od[8 + t] >> 16);
             }
-            if (!__all_sync(0xffffffffu, i < S || mbar_wait(a_empty + st.slot, st.phase ^ 1u, a.err, 28))) break;
+            keep32(g);  // expanded before the stage wait: only the stores follow it
+            keep32(h);
+            if (i >= S && !warp_wait(a_empty + st.slot, st.phase ^ 1u, a.err, 28)) break;
             const uint32_t a_col = lane_base + a.a_base + st.slot * a.a_cols;
             tmem_st_x32(a_col, g);
+            tmem_st_x32(a_col + 32, h);
             if (ind) {
 #pragma unroll
                 for (int t = 0; t < 8; ++t) {
@@ -359,16 +406,22 @@ __global__ void __launch_bounds__(kThreads, 1)
                     g[4 * t + 1] = __byte_perm(kTabMiss, 0u, ev[t] >> 16);
                     g[4 * t + 2] = __byte_perm(kTabMiss, 0u, od[t]);
                     g[4 * t + 3] = __byte_perm(kTabMiss, 0u, od[t] >> 16);
+                    h[4 * t] = __byte_perm(kTabMiss, 0u, ev[8 + t]);
+                    h[4 * t + 1] = __byte_perm(kTabMiss, 0u, ev[8 + t] >> 16);
+                    h[4 * t + 2] = __byte_perm(kTabMiss, 0u, od[8 + t]);
+                    h[4 * t + 3] = __byte_perm(kTabMiss, 0u, od[8 + t] >> 16);
                 }
-                tmem_st_x32(a_col + 32, g);
+                tmem_st_x32(a_col + 64, g);
+                tmem_st_x32(a_col + 96, h);
             }
             asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
             fence_before();
-            mbar_arrive(full_a + st.slot);
-            st.advance(2, S);
+            __syncwarp();
+            if (lane == 0) mbar_arrive(full_a + st.slot);
+            st.advance(nsets, S);
         }
-        // epilogue: the two sets take alternate 16-column groups
-        const bool ok = __all_sync(0xffffffffu, mbar_wait(tmem_full, 0, a.err, 29));
+        // epilogue: the sets take 16-column groups round robin
+        const bool ok = warp_wait(tmem_full, 0, a.err, 29);
         // the second accumulator copy holds data only if its first group exists
         const bool second_copy = a.kcopies == 2 && nkb > a.group;
         fence_after();
@@ -380,7 +433,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             rs = a.row_scale[grow];
         }
         float* dst = a.out + (uint64_t)blockIdx.y * a.split_stride + (uint64_t)grow * a.ldo;
-        for (uint32_t c0 = set * 16; c0 < a.wpad; c0 += 32) {
+        for (uint32_t c0 = set * 16; c0 < a.wpad; c0 += 16 * kUnpackSets) {
             float pm[16], pi[16], v[16];
 #pragma unroll
             for (int k = 0; k < 16; ++k) pm[k] = pi[k] = 0.f;
@@ -585,26 +638,29 @@ Fp8Plan fp8_plan(int wpad, bool ind, uint64_t tiles) {
     p.n_ind = ind ? kIndTerms * wpad : 0;
     p.n_total = p.n_main + p.n_ind;
     p.d_cols = (uint32_t)round_up(p.n_total, 32);
-    p.a_cols = ind ? 64 : 32;
-    p.b_stage_bytes = p.n_total * 128;
-    // one CTA per SM: all of TMEM, a deep packed-code ring (HBM latency) and a
-    // shallower W / A ring (L2 multicast latency)
+    p.a_cols = (ind ? 2 : 1) * (kStageK / 4);  // TMEM columns of one stage's A operand(s)
+    p.b_stage_bytes = p.n_total * 128 * kHalves;
+    // one CTA per SM: all of TMEM; the packed-code ring gives up depth (8, 4,
+    // then 2 stages) until shared memory holds at least two W stages
     p.tmem_cols = 512;
-    p.pstages = (uint32_t)std::min(32, std::max(2, env_int("SLFMM_TC8_PSTAGES", 16)));
     const size_t fixed = 1024 + 2048 + 128 * 8 + 64;
-    const size_t budget = 225 * 1024 - fixed - (size_t)p.pstages * kPacked;
     // MMA warp roles: with the indicator, genotype and indicator MMAs on
     // separate warps; without it, two accumulator copies when TMEM holds them
-    // next to at least four A stages
+    // next to at least three A stages
     p.nsplit = ind ? 1 : 0;
-    p.kcopies = (!ind && 2 * p.d_cols + 4 * p.a_cols <= 512) ? 2 : 1;
+    p.kcopies = (!ind && 2 * p.d_cols + 3 * p.a_cols <= 512) ? 2 : 1;
     p.a_base = p.kcopies * p.d_cols;
     const uint32_t by_tmem = p.a_base < 512 ? (512 - p.a_base) / p.a_cols : 0;
-    const uint32_t by_smem = (uint32_t)(budget / p.b_stage_bytes);
-    p.stages = std::min<uint32_t>(std::min(by_tmem, by_smem), (uint32_t)env_int("SLFMM_TC8_STAGES", 8));
+    const uint32_t pmax = (uint32_t)std::min(16, std::max(2, env_int("SLFMM_TC8_PSTAGES", 8)));
+    for (p.pstages = pmax;; p.pstages /= 2) {
+        const size_t budget = 225 * 1024 - fixed - (size_t)p.pstages * kStageBytes;
+        const uint32_t by_smem = (uint32_t)(budget / p.b_stage_bytes);
+        p.stages = std::min<uint32_t>(std::min(by_tmem, by_smem), (uint32_t)env_int("SLFMM_TC8_STAGES", 8));
+        if (p.stages >= std::min<uint32_t>(by_tmem, 2) || p.pstages <= 2) break;
+    }
     // MMA wait groups: up to 16 MMAs per wait and warp, at least two groups in the ring
     const uint32_t nch = p.n_main > 256 ? 2 : 1;
-    const uint32_t per_stage = 4 * (p.nsplit || p.kcopies == 2 ? nch : nch + (ind ? 1 : 0));
+    const uint32_t per_stage = (kStageK / 32) * (p.nsplit || p.kcopies == 2 ? nch : nch + (ind ? 1 : 0));
     p.group = 1;
     const uint32_t gmax = (uint32_t)env_int("SLFMM_TC8_GROUP", 4);
     for (uint32_t gsz : {4u, 2u})
@@ -613,10 +669,10 @@ Fp8Plan fp8_plan(int wpad, bool ind, uint64_t tiles) {
             break;
         }
     p.stages -= p.stages % p.group;
-    p.smem = fixed + (size_t)p.pstages * kPacked + (size_t)p.stages * p.b_stage_bytes;
+    p.smem = fixed + (size_t)p.pstages * kStageBytes + (size_t)p.stages * p.b_stage_bytes;
     // cluster multicast of W when there are enough tiles and rows split evenly
     p.cluster = 1;
-    const uint32_t cmax = (uint32_t)env_int("SLFMM_TC8_CLUSTER", 4);
+    const uint32_t cmax = (uint32_t)env_int("SLFMM_TC8_CLUSTER", 1);  // co-scheduling a cluster idles SMs: off by default
     for (uint32_t c : {8u, 4u, 2u})
         if (c <= cmax && tiles >= 2 * c && p.n_total % (8 * c) == 0) {
             p.cluster = c;
@@ -664,7 +720,7 @@ __global__ void __launch_bounds__(256) k_transpose_tiles(const uint8_t* __restri
         const uint64_t t = b / kbt_dst, kb = b - t * kbt_dst;
         const bool valid = kb < ntiles_src && t < kbt_src;
         __syncthreads();
-        const uint4* s4 = reinterpret_cast<const uint4*>(src + (kb * kbt_src + t) * (uint64_t)kPacked);
+        const uint4* s4 = reinterpret_cast<const uint4*>(src + (kb * kbt_src + t) * (uint64_t)kTileBytes);
         reinterpret_cast<uint4*>(in)[threadIdx.x] = valid ? s4[threadIdx.x] : make_uint4(0, 0, 0, 0);
         __syncthreads();
         const int byte = j >> 2, shift = 2 * (j & 3);
@@ -679,7 +735,7 @@ __global__ void __launch_bounds__(256) k_transpose_tiles(const uint8_t* __restri
             }
             wv[w] = v;
         }
-        *reinterpret_cast<uint4*>(dst + b * (uint64_t)kPacked + j * 32 + h * 16) = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+        *reinterpret_cast<uint4*>(dst + b * (uint64_t)kTileBytes + j * 32 + h * 16) = make_uint4(wv[0], wv[1], wv[2], wv[3]);
     }
 }
 
@@ -688,7 +744,7 @@ static void tile_rows(Ctx& c, const uint8_t* in, uint64_t rows, uint64_t stride,
     SLFMM_REQUIRE(stride % 32 == 0, SLFMM_ERR_BAD_ARG, "packed stride must be a multiple of 32 bytes");
     kbt = stride / 32;
     ntiles = round_up(std::max<uint64_t>(ceil_div(rows, kM), 1), 8);
-    const uint64_t bytes = ntiles * kbt * kPacked;
+    const uint64_t bytes = ntiles * kbt * kTileBytes;
     out.alloc(bytes, c.stream);
     const uint64_t chunks = bytes / 16;
     k_tile_rows<<<grid_for(c, chunks, 256), 256, 0, c.stream>>>(in, rows, stride, kbt, chunks, out.get());
@@ -706,9 +762,9 @@ TileView build_tiles(Ctx& c, const Geno& g, bool transposed) {
     if (!g.have_tilesT) {
         // straight from the SNP-row tiles: sample tiles x K blocks of 128 SNPs
         build_tiles(c, g, false);
-        g.kbtT = std::max<uint64_t>(ceil_div(g.p, kM), 1);
+        g.kbtT = round_up(std::max<uint64_t>(ceil_div(g.p, kM), 1), kHalves);  // whole stages
         g.ntilesT = round_up(std::max<uint64_t>(ceil_div(g.n, kM), 1), 8);
-        g.tilesT.alloc(g.ntilesT * g.kbtT * kPacked, c.stream);
+        g.tilesT.alloc(g.ntilesT * g.kbtT * kTileBytes, c.stream);
         const uint64_t blocks = std::min<uint64_t>(g.ntilesT * g.kbtT, (uint64_t)c.sm_count * 16);
         k_transpose_tiles<<<(unsigned)blocks, 256, 0, c.stream>>>(g.tiles.get(), g.kbt, g.ntiles, g.tilesT.get(),
                                                                    g.kbtT, g.ntilesT);
@@ -749,8 +805,10 @@ int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t rows
                      const double* row_scale, const double* cs, float* out, int ldo, int splits,
                      uint64_t split_stride) {
     SLFMM_REQUIRE(pl.ok, SLFMM_ERR_BAD_ARG, "no feasible split-FP8 tile plan for this width");
-    SLFMM_REQUIRE(K_pad % kKB == 0 && K_pad >= ceil_div(K, kKB) * kKB, SLFMM_ERR_BAD_ARG, "bad K padding");
-    SLFMM_REQUIRE(tv.base && tv.kbt >= ceil_div(K, kKB), SLFMM_ERR_BAD_ARG, "tile-major operand too short in K");
+    SLFMM_REQUIRE(K_pad % kStageK == 0 && K_pad >= ceil_div(K, kStageK) * kStageK, SLFMM_ERR_BAD_ARG,
+                  "bad K padding");
+    SLFMM_REQUIRE(tv.base && tv.kbt % kHalves == 0 && tv.kbt >= ceil_div(K, kStageK) * kHalves, SLFMM_ERR_BAD_ARG,
+                  "tile-major operand too short in K");
     SLFMM_REQUIRE(tv.ntiles >= round_up(ceil_div(rows, kM), pl.cluster), SLFMM_ERR_BAD_ARG,
                   "tile-major operand has too few tiles");
     SLFMM_REQUIRE(mode == 0 || pl.n_ind != 0, SLFMM_ERR_BAD_ARG, "row correction needs the indicator operand");
@@ -764,7 +822,7 @@ int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t rows
     err.zero();
     Tc8Args a{};
     a.rows = (uint32_t)rows;
-    a.kb_total = (uint32_t)ceil_div(K, kKB);
+    a.kb_total = (uint32_t)ceil_div(K, kStageK);
     a.kb_per_split = (uint32_t)ceil_div(a.kb_total, (uint64_t)std::max(splits, 1));
     a.wpad = pl.wpad;
     a.n_main = pl.n_main;
@@ -778,6 +836,7 @@ int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t rows
     a.kcopies = pl.kcopies;
     a.nsplit = pl.nsplit;
     a.a_base = pl.a_base;
+    a.usets = std::min<uint32_t>(kUnpackSets, std::min(pl.stages, pl.pstages));
     a.tmem_cols = pl.tmem_cols;
     a.b_stage_bytes = pl.b_stage_bytes;
     a.cluster = pl.cluster;
@@ -792,7 +851,7 @@ int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t rows
     a.ldo = (uint32_t)ldo;
     a.split_stride = split_stride;
     a.tiles = tv.base;
-    a.tile_bytes = tv.kbt * (uint64_t)kPacked;
+    a.tile_bytes = tv.kbt * (uint64_t)kTileBytes;
     a.err = err.get();
     const unsigned gy = (unsigned)ceil_div(a.kb_total, a.kb_per_split);
     const unsigned gx = (unsigned)round_up(ceil_div(rows, kM), pl.cluster);
