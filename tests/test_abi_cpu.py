@@ -1,0 +1,100 @@
+"""The C-ABI library on a machine without a GPU: it builds, loads, exports
+every entry point the header declares, its host-only entry points (number
+formatting, TSV writer, .bed validation) match the oracle, and every call that
+needs the device fails loudly instead of falling back to the CPU."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from oracle import lfmm_oracle as O
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "schnelgpu.h"
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from schnellfmm_gb300 import build
+    build.build()
+    import schnellfmm_gb300 as sg
+    return sg.load_library()
+
+
+def _declared():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(slfmm_\w+)\s*\(", text)))
+
+
+def test_header_entry_points_exported(lib):
+    import schnellfmm_gb300 as sg
+    names = _declared()
+    assert len(names) >= 25
+    for name in names:
+        assert hasattr(lib, name), f"{name} declared in schnelgpu.h but not exported"
+    assert sorted(sg.EXPORTED_SYMBOLS) == names
+
+
+@pytest.mark.parametrize("v", [0.0, -0.0, 1.0, 1.23456e-4, -9.87654321e123, 1e-300, 2.5e-320,
+                               123456789.0, 0.1, float("nan"), float("inf"), -float("inf"), 9.9999996e-5])
+def test_format_exp6_matches_rust(lib, v):
+    import schnellfmm_gb300 as sg
+    assert sg.format_exp6(v) == O.rust_lower_exp6(v)
+
+
+def test_write_tsv_matches_oracle(lib, tmp_path):
+    import schnellfmm_gb300 as sg
+    rng = np.random.default_rng(5)
+    p, d = 57, 3
+    res = sg.TestResults(u_hat=np.zeros((4, 2)), gif=1.0, gif_per_trait=np.ones(d),
+                         beta=rng.standard_normal((p, d)), tstat=rng.standard_normal((p, d)) * 3,
+                         pvalue=rng.uniform(1e-12, 1, (p, d)), r2=rng.uniform(0, 1, (p, 3)))
+    res.pvalue[0, 0] = np.nan
+    res.beta[1, 1] = 0.0
+    bim = [sg.BimRecord(str(1 + i // 20), f"rs{i}", 0.0, 1000 + 7 * i, "A", "G") for i in range(p)]
+    names = ["temp", "prec", "alt"]
+    out = tmp_path / "res.tsv"
+    sg.write_tsv(out, bim, names, res, n_threads=3)
+    ref = O.AssocResults(beta=res.beta, tstat=res.tstat, pvalue=res.pvalue, r2=res.r2,
+                         gif=res.gif, gif_per_trait=res.gif_per_trait)
+    rows = O.tsv_rows([b.chrom for b in bim], [b.pos for b in bim], [b.snp_id for b in bim], ref)
+    want = O.tsv_header(names) + "\n" + "".join(r + "\n" for r in rows)
+    assert out.read_text() == want
+
+
+def _write_bed(path, payload, magic=bytes([0x6C, 0x1B, 0x01])):
+    path.write_bytes(magic + payload.tobytes())
+
+
+def test_bed_validate(lib, tmp_path):
+    n, p = 10, 7
+    bps = (n + 3) // 4
+    payload = np.random.default_rng(1).integers(0, 256, size=(p, bps), dtype=np.uint8)
+    good = tmp_path / "good.bed"
+    _write_bed(good, payload)
+    out = np.zeros(p * bps, dtype=np.uint8)
+    err = C.create_string_buffer(256)
+    rc = lib.slfmm_bed_validate(str(good).encode(), n, p, out.ctypes.data_as(C.c_void_p), err, 256)
+    assert rc == 0
+    assert np.array_equal(out.reshape(p, bps), payload)
+    bad_magic = tmp_path / "bad_magic.bed"
+    _write_bed(bad_magic, payload, magic=bytes([0x6C, 0x1B, 0x00]))
+    assert lib.slfmm_bed_validate(str(bad_magic).encode(), n, p, None, err, 256) == -2
+    assert b"magic" in err.value.lower() or b"snp-major" in err.value.lower()
+    short = tmp_path / "short.bed"
+    _write_bed(short, payload[:-1])
+    assert lib.slfmm_bed_validate(str(short).encode(), n, p, None, err, 256) == -2
+    missing = tmp_path / "nope.bed"
+    assert lib.slfmm_bed_validate(str(missing).encode(), n, p, None, err, 256) in (-2, -7)
+
+
+def test_no_gpu_fails_loudly(lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import schnellfmm_gb300 as sg
+    with pytest.raises(sg.SchnelGpuError):
+        sg.Engine()
