@@ -204,10 +204,19 @@ void upload_geno(Ctx& c, Geno& g, const uint8_t* packed, uint64_t n_phys, uint64
 // ---------------------------------------------------------------------------
 // per-SNP standardisation state of one genotype matrix
 // ---------------------------------------------------------------------------
+// NMF values at the missing calls: f_ir = W_i . H_r (W n x k, H one row of k
+// per SNP, FP32); k = 0 means mean imputation
+struct NmfFill {
+    int k = 0;
+    const float* W = nullptr;
+    const float* H = nullptr;
+};
+
 struct SnpStd {
     DBuf<double> mean, scale, tss;
     DBuf<uint8_t> zero_var;
     DBuf<float> lut;  // p x 4
+    NmfFill fill;
 };
 
 void std_mean(Ctx& c, const Geno& g, int norm, SnpStd& s) {
@@ -227,8 +236,8 @@ void std_mean(Ctx& c, const Geno& g, int norm, SnpStd& s) {
 int pad16(int w) { return (int)round_up((uint64_t)w, 16); }
 
 // out (p x wp, FP32) = Y_hat^T W, W = n x w FP64 (leading dim ldw)
-void row_contract(Ctx& c, const Geno& g, const SnpStd& s, const double* W, int w, int ldw,
-                  DBuf<float>& out, int& wp) {
+void row_contract_base(Ctx& c, const Geno& g, const SnpStd& s, const double* W, int w, int ldw,
+                       DBuf<float>& out, int& wp) {
     wp = pad16(w);
     SLFMM_REQUIRE(wp <= kMaxW, SLFMM_ERR_BAD_ARG, "operand wider than 128 columns");
     const uint64_t n_pad = round_up(g.n, 256);  // whole split-FP8 stages (256 codes)
@@ -292,7 +301,7 @@ void row_contract(Ctx& c, const Geno& g, const SnpStd& s, const double* W, int w
 }
 
 // S (n x wp, FP64) = Y_hat Q, Q = p x wp FP32 (w real columns)
-void col_contract(Ctx& c, const Geno& g, const SnpStd& s, const float* Q, int w, int wp, DBuf<double>& S) {
+void col_contract_base(Ctx& c, const Geno& g, const SnpStd& s, const float* Q, int w, int wp, DBuf<double>& S) {
     S.alloc(g.n * wp, c.stream);
     const double bytes = (double)g.p * ceil_div(g.n, 4) + (double)g.p * w * 4 + (double)g.n * w * 8;
     if (c.precision == SLFMM_PREC_SPLIT_FP8) {
@@ -361,6 +370,64 @@ void col_contract(Ctx& c, const Geno& g, const SnpStd& s, const float* Q, int w,
 // ---------------------------------------------------------------------------
 // Step 0 (src/precompute.rs:30-88) in thin form
 // ---------------------------------------------------------------------------
+// The passes with NMF values at the missing calls: the base pass counts a
+// missing call at the SNP mean (standardised 0); the correction adds
+// s_r (f_ir - mu_r) times the operand row.
+void row_contract(Ctx& c, const Geno& g, const SnpStd& s, const double* W, int w, int ldw, DBuf<float>& out,
+                  int& wp) {
+    row_contract_base(c, g, s, W, w, ldw, out, wp);
+    if (s.fill.k) {
+        build_missing_lists(c, g);
+        DBuf<float> W32(std::max<uint64_t>(g.n, 1) * wp, c.stream);
+        launch_f64_to_f32_pad(c, W, g.n, w, ldw, W32.get(), g.n, wp);
+        launch_fill_row_correct(c, g, out.get(), wp, w, W32.get(), wp, s.fill.W, s.fill.H, s.fill.k, s.mean.get(),
+                                s.scale.get());
+    }
+}
+
+void col_contract(Ctx& c, const Geno& g, const SnpStd& s, const float* Q, int w, int wp, DBuf<double>& S) {
+    col_contract_base(c, g, s, Q, w, wp, S);
+    if (s.fill.k) {
+        build_missing_csc(c, g);
+        launch_fill_col_correct(c, g, S.get(), wp, w, Q, wp, s.fill.W, s.fill.H, s.fill.k, s.mean.get(),
+                                s.scale.get());
+    }
+}
+
+// statistics with NMF values at the missing calls
+void std_fill(Ctx& c, const Geno& g, int norm, const NmfFill& f, SnpStd& s) {
+    const uint64_t p = std::max<uint64_t>(g.p, 1);
+    s.mean.alloc(p, c.stream);
+    s.scale.alloc(p, c.stream);
+    s.tss.alloc(p, c.stream);
+    s.zero_var.alloc(p, c.stream);
+    s.lut.alloc(p * 4, c.stream);
+    build_missing_lists(c, g);
+    launch_fill_stats(c, g, norm, f.W, f.H, f.k, s.mean.get(), s.scale.get(), s.tss.get(), s.zero_var.get());
+    launch_lut_std(c, g.p, s.mean.get(), s.scale.get(), s.lut.get());
+    s.fill = f;
+}
+
+// raw products: mean = mean_src (or 0), scale = 1 -- the base passes then
+// give the raw mean-filled product minus mean_r colsum(W) (or, with mean 0,
+// the product with missing calls at 0)
+void std_raw(Ctx& c, const Geno& g, const double* mean_src, SnpStd& s) {
+    const uint64_t p = std::max<uint64_t>(g.p, 1);
+    s.mean.alloc(p, c.stream);
+    s.scale.alloc(p, c.stream);
+    s.tss.alloc(p, c.stream);
+    s.zero_var.alloc(p, c.stream);
+    s.lut.alloc(p * 4, c.stream);
+    if (mean_src) SLFMM_CUDA(cudaMemcpyAsync(s.mean.get(), mean_src, g.p * sizeof(double), cudaMemcpyDeviceToDevice, c.stream));
+    else s.mean.zero();
+    std::vector<double> ones(p, 1.0);
+    h2d(c, s.scale.get(), ones.data(), p);
+    s.tss.zero();
+    s.zero_var.zero();
+    launch_lut_std(c, g.p, s.mean.get(), s.scale.get(), s.lut.get());
+    sync(c);
+}
+
 struct Step0 {
     uint64_t n = 0;
     int d = 0, r = 0;
@@ -658,6 +725,158 @@ void assoc(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, const doubl
     sync(c);
 }
 
+// ---------------------------------------------------------------------------
+// NMF imputation (src/nmf.rs:80-455, src/parallel.rs:219-321,
+// src/testing.rs:423-487)
+// ---------------------------------------------------------------------------
+struct NmfModel {
+    int k = 0;
+    DBuf<double> W;   // n x k
+    DBuf<double> Ht;  // p x k: H transposed, one row per SNP
+    std::vector<double> cv;
+    double cv_mean = 0.0;
+    uint64_t total = 0;
+};
+
+// out (n x k) = W (W^T W)^-1, i.e. (W^+)^T, with safe_inv semantics
+void nmf_pinv_t(Ctx& c, const double* W, uint64_t n, int k, DBuf<double>& out, const char* what) {
+    DBuf<double> wtw(k * k, c.stream), inv(k * k, c.stream), eps(1, c.stream);
+    DBuf<int> st(1, c.stream);
+    launch_atb(c, W, k, W, k, n, k, k, wtw.get());
+    launch_inverse(c, wtw.get(), k, inv.get(), st.get(), eps.get());
+    const int status = fetch(c, st.get(), 1)[0];
+    if (status == 2) throw Error(SLFMM_ERR_SINGULAR, std::string(what) + " inversion failed even with regularization");
+    if (status == 1)
+        fprintf(stderr, "Warning: %s is singular, adding epsilon=%.2e diagonal regularization\n", what,
+                fetch(c, eps.get(), 1)[0]);
+    out.alloc(std::max<uint64_t>(n, 1) * k, c.stream);
+    launch_gemm_small(c, W, k, n, k, inv.get(), k, k, 1.0, 0.0, out.get(), k);
+}
+
+void nmf_normalize(Ctx& c, NmfModel& m, uint64_t n, uint64_t p, double eps) {
+    DBuf<double> cs(m.k, c.stream);
+    cs.zero();
+    launch_colsums(c, m.W.get(), n, m.k, m.k, cs.get());
+    launch_nmf_normalize(c, m.W.get(), n, m.Ht.get(), p, m.k, cs.get(), eps);
+}
+
+// H rows max(0, W^+ y~) for every SNP of g, y~ = raw calls, missing at the
+// SNP's observed mean (the on-the-fly fill, src/parallel.rs:249-282)
+void nmf_h_meanfill(Ctx& c, const Geno& g, const SnpStd& rawm, const double* Wpt, int k, DBuf<double>& Ht) {
+    DBuf<float> U;
+    int up = 0;
+    row_contract(c, g, rawm, Wpt, k, k, U, up);
+    DBuf<double> cs(k, c.stream);
+    cs.zero();
+    launch_colsums(c, Wpt, g.n, k, k, cs.get());
+    launch_add_mean_colsum(c, U.get(), up, g.p, k, rawm.mean.get(), cs.get());
+    Ht.alloc(std::max<uint64_t>(g.p, 1) * k, c.stream);
+    launch_nmf_clamp0_f32(c, U.get(), up, Ht.get(), g.p, k);
+}
+
+void to_f32(Ctx& c, const double* A, uint64_t m, int a, DBuf<float>& out, int ld) {
+    out.alloc(std::max<uint64_t>(m, 1) * ld, c.stream);
+    launch_f64_to_f32_pad(c, A, m, a, a, out.get(), m, ld);
+}
+
+// (sum |g - pred|, sum |g - mean|, count) over a p x 3 partials array
+std::vector<double> sum3(Ctx& c, const DBuf<double>& part, uint64_t p) {
+    DBuf<double> tot(3, c.stream);
+    tot.zero();
+    launch_colsums(c, part.get(), p, 3, 3, tot.get());
+    return fetch(c, tot.get(), 3);
+}
+
+void nmf_estimate(Ctx& c, const Geno& g, const slfmm_config* cfg, NmfModel& m) {
+    const int k = cfg->nmf_k ? (int)cfg->nmf_k : (int)cfg->k;
+    SLFMM_REQUIRE(k >= 1 && k <= kMaxNmfK, SLFMM_ERR_BAD_ARG,
+                  "NMF rank must be in 1.." + std::to_string(kMaxNmfK) + ", got " + std::to_string(k));
+    const double eps = cfg->nmf_eps > 0 ? cfg->nmf_eps : 1e-16;
+    const uint64_t chunk = cfg->chunk_size ? cfg->chunk_size : 10000;
+    const uint64_t n = g.n, p = g.p;
+    const int l = k + 10;
+    SLFMM_REQUIRE(p >= (uint64_t)l && n >= (uint64_t)l, SLFMM_ERR_BAD_ARG, "too few SNPs or samples for the NMF probe");
+    m.k = k;
+    SnpStd sm, raw0, rawm;
+    std_mean(c, g, SLFMM_NORM_EIGENSTRAT, sm);
+    std_raw(c, g, nullptr, raw0);
+    std_raw(c, g, sm.mean.get(), rawm);
+    build_missing_lists(c, g);
+    build_missing_csc(c, g);
+    // init_from_random_probe (src/nmf.rs:279-362): Z = Y_meanraw^T Omega',
+    // W = |Omega' V_k| with V the right singular vectors of Z, H = max(0, W^+ Y)
+    DBuf<double> Om(n * l, c.stream);
+    launch_normal(c, cfg->seed + 1000000ull, n, l, Om.get());
+    DBuf<float> Z;
+    int zp = 0;
+    row_contract(c, g, rawm, Om.get(), l, l, Z, zp);
+    DBuf<double> csO(l, c.stream);
+    csO.zero();
+    launch_colsums(c, Om.get(), n, l, l, csO.get());
+    launch_add_mean_colsum(c, Z.get(), zp, p, l, sm.mean.get(), csO.get());
+    DBuf<double> G(l * l, c.stream), V(l * l, c.stream), sig(l, c.stream), Wr(n * k, c.stream);
+    launch_gram_f32(c, Z.get(), zp, p, l, G.get());
+    launch_jacobi_svd(c, G.get(), l, V.get(), sig.get());
+    launch_gemm_small(c, Om.get(), l, n, l, V.get(), l, k, 1.0, 0.0, Wr.get(), k);
+    m.W.alloc(n * k, c.stream);
+    launch_nmf_abs_f64(c, Wr.get(), k, m.W.get(), n, k);
+    {
+        DBuf<double> Wpt;
+        nmf_pinv_t(c, m.W.get(), n, k, Wpt, "W_init^T W_init");
+        nmf_h_meanfill(c, g, rawm, Wpt.get(), k, m.Ht);
+    }
+    // W, H >= eps, normalise (src/nmf.rs:118-126)
+    DBuf<double> zeros(std::max<uint64_t>(n, p) * k, c.stream);
+    zeros.zero();
+    launch_nmf_update_f64(c, m.W.get(), n, k, m.W.get(), k, zeros.get(), eps);
+    launch_nmf_update_f64(c, m.Ht.get(), p, k, m.Ht.get(), k, zeros.get(), eps);
+    nmf_normalize(c, m, n, p, eps);
+    const int kp = pad16(k);
+    DBuf<double> hh(k * k, c.stream), wtw(k * k, c.stream), denW(n * k, c.stream), denH(p * k, c.stream);
+    DBuf<double> part(std::max<uint64_t>(p, 1) * 3, c.stream);
+    m.cv.clear();
+    m.total = 0;
+    for (int it = 0; it < (int)cfg->nmf_iter; ++it) {
+        // W step: N_W = Y~ H^T, HH = H H^T, W <- W N_W / (W HH)   (src/nmf.rs:140-190)
+        DBuf<float> W32, H32, H32p;
+        to_f32(c, m.W.get(), n, k, W32, k);
+        to_f32(c, m.Ht.get(), p, k, H32, k);
+        to_f32(c, m.Ht.get(), p, k, H32p, kp);
+        DBuf<double> NW;
+        col_contract(c, g, raw0, H32p.get(), k, kp, NW);
+        launch_fill_col_correct(c, g, NW.get(), kp, k, H32p.get(), kp, W32.get(), H32.get(), k, raw0.mean.get(),
+                                raw0.scale.get());
+        launch_atb(c, m.Ht.get(), k, m.Ht.get(), k, p, k, k, hh.get());
+        launch_gemm_small(c, m.W.get(), k, n, k, hh.get(), k, k, 1.0, 0.0, denW.get(), k);
+        launch_nmf_update_f64(c, m.W.get(), n, k, NW.get(), kp, denW.get(), eps);
+        nmf_normalize(c, m, n, p, eps);
+        // H step with the new W: N_H = W^T Y~, H <- H N_H / (W^T W H)   (:192-240)
+        launch_atb(c, m.W.get(), k, m.W.get(), k, n, k, k, wtw.get());
+        to_f32(c, m.W.get(), n, k, W32, k);
+        to_f32(c, m.Ht.get(), p, k, H32, k);
+        DBuf<float> NH;
+        int np_ = 0;
+        row_contract(c, g, raw0, m.W.get(), k, k, NH, np_);
+        launch_fill_row_correct(c, g, NH.get(), np_, k, W32.get(), k, W32.get(), H32.get(), k, raw0.mean.get(),
+                                raw0.scale.get());
+        launch_gemm_small(c, m.Ht.get(), k, p, k, wtw.get(), k, k, 1.0, 0.0, denH.get(), k);
+        launch_nmf_update_f32(c, m.Ht.get(), p, k, NH.get(), np_, denH.get(), eps);
+        nmf_normalize(c, m, n, p, eps);
+        // CV on held-out calls (src/nmf.rs:379-455), mask stream seed + it
+        to_f32(c, m.W.get(), n, k, W32, k);
+        to_f32(c, m.Ht.get(), p, k, H32, k);
+        launch_nmf_cv(c, g, chunk, cfg->seed + (uint64_t)it, cfg->nmf_cv_rate, W32.get(), H32.get(), k, part.get());
+        const std::vector<double> t = sum3(c, part, p);
+        const uint64_t cnt = (uint64_t)(t[2] + 0.5);
+        m.cv.push_back(cnt ? t[0] / (double)cnt : 0.0);
+        m.cv_mean = cnt ? t[1] / (double)cnt : 0.0;
+        m.total += cnt;
+        if (c.verbose)
+            fprintf(stderr, "NMF iteration %d: CV MAE %.6f (mean imputation %.6f, %llu held out)\n", it + 1,
+                    m.cv.back(), m.cv_mean, (unsigned long long)cnt);
+    }
+}
+
 void check_cfg(const slfmm_config* cfg) {
     SLFMM_REQUIRE(cfg != nullptr, SLFMM_ERR_BAD_ARG, "null config");
     SLFMM_REQUIRE(cfg->k >= 1, SLFMM_ERR_BAD_ARG, "K must be >= 1");
@@ -671,15 +890,50 @@ void fit_impl(Ctx& c, const Geno& ge, const Geno& gf, const double* x, int d, co
               const double* omega, slfmm_results* res) {
     check_cfg(cfg);
     SLFMM_REQUIRE(ge.n == gf.n, SLFMM_ERR_BAD_ARG, "estimation and testing genotypes have different sample counts");
-    SLFMM_REQUIRE(cfg->impute == SLFMM_IMPUTE_MEAN, SLFMM_ERR_BAD_ARG, "NMF imputation not available in this build");
     Step0 s0;
     step0(c, x, gf.n, d, cfg->lambda, cfg->scale_cov != 0, s0);
     SnpStd se, sf;
-    std_mean(c, ge, cfg->norm, se);
     const SnpStd* sfp = &se;
-    if (&ge != &gf) {
-        std_mean(c, gf, cfg->norm, sf);
+    // NMF state kept alive for the passes that read its fills
+    NmfModel nmf;
+    DBuf<float> W32, He32, Hf32, Wpt32;
+    if (cfg->impute == SLFMM_IMPUTE_NMF) {
+        // NmfInRam on the estimation SNPs, NmfOnTheFly on the tested SNPs,
+        // then the GWAS-phase CV (src/lib.rs:190-250)
+        nmf_estimate(c, ge, cfg, nmf);
+        const int k = nmf.k;
+        DBuf<double> Wpt, Hf;
+        nmf_pinv_t(c, nmf.W.get(), gf.n, k, Wpt, "W^T W for NMF pinv");
+        to_f32(c, nmf.W.get(), gf.n, k, W32, k);
+        to_f32(c, nmf.Ht.get(), ge.p, k, He32, k);
+        to_f32(c, Wpt.get(), gf.n, k, Wpt32, k);
+        std_fill(c, ge, cfg->norm, NmfFill{k, W32.get(), He32.get()}, se);
+        SnpStd sm, rawm;
+        std_mean(c, gf, SLFMM_NORM_EIGENSTRAT, sm);
+        std_raw(c, gf, sm.mean.get(), rawm);
+        nmf_h_meanfill(c, gf, rawm, Wpt.get(), k, Hf);
+        to_f32(c, Hf.get(), gf.p, k, Hf32, k);
+        std_fill(c, gf, cfg->norm, NmfFill{k, W32.get(), Hf32.get()}, sf);
         sfp = &sf;
+        DBuf<double> part(std::max<uint64_t>(gf.p, 1) * 3, c.stream);
+        launch_nmf_gwas_cv(c, gf, cfg->chunk_size ? cfg->chunk_size : 10000, cfg->seed, cfg->nmf_cv_rate, W32.get(),
+                           Wpt32.get(), k, part.get());
+        const std::vector<double> t = sum3(c, part, gf.p);
+        const uint64_t cnt = (uint64_t)(t[2] + 0.5);
+        if (res) {
+            if (res->nmf_cv)
+                for (size_t i = 0; i < nmf.cv.size(); ++i) res->nmf_cv[i] = nmf.cv[i];
+            res->nmf_cv_mean = nmf.cv_mean;
+            res->nmf_gwas_cv_mae = cnt ? t[0] / (double)cnt : 0.0;
+            res->nmf_gwas_cv_mean_mae = cnt ? t[1] / (double)cnt : 0.0;
+            res->nmf_gwas_cv_count = cnt;
+        }
+    } else {
+        std_mean(c, ge, cfg->norm, se);
+        if (&ge != &gf) {
+            std_mean(c, gf, cfg->norm, sf);
+            sfp = &sf;
+        }
     }
     DBuf<double> u_hat;
     const int K = (int)cfg->k, l = K + (int)cfg->oversampling;

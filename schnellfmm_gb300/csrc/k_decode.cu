@@ -6,6 +6,7 @@
 #include <cub/cub.cuh>
 
 #include "slfmm_internal.h"
+#include "stats_common.cuh"
 
 namespace slfmm {
 
@@ -140,14 +141,6 @@ __global__ void k_u32_to_u64(const uint32_t* __restrict__ a, uint64_t m, uint64_
 // Per-SNP mean over observed calls, scale and TSS, with the reference's
 // operation order (src/bed.rs:349-361, :382-395) in round-to-nearest FP64
 // intrinsics so that no FMA contraction changes the bits.
-__device__ __forceinline__ double scale_from_mean(double mean, int norm) {
-    const double pp = __ddiv_rn(mean, 2.0);
-    const double twopq = __dmul_rn(__dmul_rn(2.0, pp), __dsub_rn(1.0, pp));
-    if (norm == SLFMM_NORM_CENTER_ONLY) return twopq < 1e-20 ? 0.0 : 1.0;
-    const double denom = __dsqrt_rn(twopq);
-    return denom > 1e-10 ? __ddiv_rn(1.0, denom) : 0.0;
-}
-
 __global__ void k_stats_mean(const int32_t* __restrict__ counts, uint64_t p, int norm,
                              double* __restrict__ mean, double* __restrict__ scale,
                              double* __restrict__ tss, uint8_t* __restrict__ zero_var) {

@@ -1,0 +1,477 @@
+// NMF imputation (src/nmf.rs:80-455, src/parallel.rs:219-321,
+// src/testing.rs:423-487) on the resident genotypes.
+//
+// The dense products of the multiplicative updates and of the imputed passes
+// run through the ordinary contractions with missing calls as 0; the values
+// NMF puts at the missing calls, f_ir = W_i . H_r, enter as sparse
+// corrections over the missing-call lists (CSR by SNP, CSC by sample), so no
+// imputed copy of the matrix is ever formed.  W (n x k) and H (p x k, one row
+// per SNP) are FP32 row-major here; k <= kMaxNmfK.
+#include <cstdint>
+
+#include "slfmm_internal.h"
+#include "stats_common.cuh"
+
+namespace slfmm {
+namespace {
+
+constexpr uint64_t kGamma = 0x9E3779B97F4A7C15ull;
+
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// U[0,1) draw `ctr` of the counter stream keyed by mix64(seed + gamma)
+__device__ __forceinline__ double uniform_at(uint64_t key, uint64_t ctr) {
+    return (double)(mix64(key + (ctr + 1) * kGamma) >> 11) * 0x1.0p-53;
+}
+
+__device__ __forceinline__ uint32_t code_at(const uint8_t* row, uint64_t s) {
+    return (row[s >> 2] >> ((s & 3) * 2)) & 3u;
+}
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// f = W_i . h (h in shared memory, k <= kMaxNmfK)
+__device__ __forceinline__ float fill_dot(const float* __restrict__ Wi, const float* h, int k) {
+    float f = 0.f;
+#pragma unroll
+    for (int c = 0; c < kMaxNmfK; ++c)
+        if (c < k) f = fmaf(Wi[c], h[c], f);
+    return f;
+}
+
+// Per-SNP statistics with the NMF values at the missing calls: every call is
+// valid, mu = (S1 + F1) / n, s = scale(mu), TSS = s^2 (S2 + F2 - (S1+F1)^2/n)
+// (decode_single_snp with a fill, src/bed.rs:300-379).  One warp per SNP.
+__global__ void __launch_bounds__(256) k_fill_stats(uint64_t p, uint64_t n, int norm, const int32_t* __restrict__ counts,
+                                                    const uint64_t* __restrict__ ptr, const uint32_t* __restrict__ idx,
+                                                    const float* __restrict__ W, const float* __restrict__ H, int k,
+                                                    double* __restrict__ mean, double* __restrict__ scale,
+                                                    double* __restrict__ tss, uint8_t* __restrict__ zero_var) {
+    __shared__ float hs[8][kMaxNmfK];
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const uint64_t nw = (uint64_t)gridDim.x * 8;
+    for (uint64_t r = (uint64_t)blockIdx.x * 8 + wl; r < p; r += nw) {
+        __syncwarp();
+        if (lane < k) hs[wl][lane] = H[r * k + lane];
+        __syncwarp();
+        double f1 = 0.0, f2 = 0.0;
+        for (uint64_t e = ptr[r] + lane; e < ptr[r + 1]; e += 32) {
+            const float f = fill_dot(W + (uint64_t)idx[e] * k, hs[wl], k);
+            f1 += (double)f;
+            f2 += (double)f * (double)f;
+        }
+        f1 = warp_sum_d(f1);
+        f2 = warp_sum_d(f2);
+        if (lane == 0) {
+            const int64_t c1 = counts[r * 4 + 1], c2 = counts[r * 4 + 2];
+            const double s1 = (double)(c1 + 2 * c2) + f1, s2 = (double)(c1 + 4 * c2) + f2;
+            const double mu = n > 0 ? s1 / (double)n : 0.0;
+            const double sc = scale_from_mean(mu, norm);
+            const double css = n > 0 ? fmax(s2 - s1 * s1 / (double)n, 0.0) : 0.0;
+            mean[r] = mu;
+            scale[r] = sc;
+            tss[r] = sc * sc * css;
+            zero_var[r] = (sc == 0.0 || !(css > 0.0)) ? 1 : 0;
+        }
+    }
+}
+
+// Row pass correction: out[r, c] += s_r * sum_{i in miss(r)} (f_ir - mu_r) Wop[i, c]
+// (the base pass counted the missing calls at the mean).  One warp per SNP;
+// 32 missing indices and their fills are formed per round and broadcast.
+__global__ void __launch_bounds__(256) k_fill_row_correct(float* __restrict__ out, int ldo, uint64_t p, int w,
+                                                          const uint64_t* __restrict__ ptr,
+                                                          const uint32_t* __restrict__ idx, const float* __restrict__ Wop,
+                                                          int ldw, const float* __restrict__ Wn,
+                                                          const float* __restrict__ H, int k,
+                                                          const double* __restrict__ mean,
+                                                          const double* __restrict__ scale) {
+    __shared__ float hs[8][kMaxNmfK];
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const uint64_t nw = (uint64_t)gridDim.x * 8;
+    for (uint64_t r = (uint64_t)blockIdx.x * 8 + wl; r < p; r += nw) {
+        __syncwarp();
+        if (lane < k) hs[wl][lane] = H[r * k + lane];
+        __syncwarp();
+        const uint64_t e0 = ptr[r], e1 = ptr[r + 1];
+        if (e0 == e1) continue;
+        const float mu = (float)mean[r], sc = (float)scale[r];
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        for (uint64_t b = e0; b < e1; b += 32) {
+            uint32_t my = 0;
+            float dm = 0.f;
+            if (b + lane < e1) {
+                my = idx[b + lane];
+                dm = fill_dot(Wn + (uint64_t)my * k, hs[wl], k) - mu;
+            }
+            const int cnt = (int)(e1 - b < 32 ? e1 - b : 32);
+            for (int t = 0; t < cnt; ++t) {
+                const uint64_t i = __shfl_sync(0xffffffffu, my, t);
+                const float d = __shfl_sync(0xffffffffu, dm, t);
+                const float* wr = Wop + i * ldw;
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (lane + 32 * q < w) acc[q] = fmaf(d, wr[lane + 32 * q], acc[q]);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (lane + 32 * q < w) out[r * ldo + lane + 32 * q] += sc * acc[q];
+    }
+}
+
+// Column pass correction: S[i, c] += sum_{r in miss(i)} s_r (f_ir - mu_r) Qop[r, c].
+// One warp per sample over its CSC list.
+__global__ void __launch_bounds__(256) k_fill_col_correct(double* __restrict__ S, int lds, uint64_t n, int w,
+                                                          const uint64_t* __restrict__ cptr,
+                                                          const uint32_t* __restrict__ cidx,
+                                                          const float* __restrict__ Qop, int ldq,
+                                                          const float* __restrict__ Wn, const float* __restrict__ H,
+                                                          int k, const double* __restrict__ mean,
+                                                          const double* __restrict__ scale) {
+    __shared__ float ws[8][kMaxNmfK];
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const uint64_t nw = (uint64_t)gridDim.x * 8;
+    for (uint64_t i = (uint64_t)blockIdx.x * 8 + wl; i < n; i += nw) {
+        __syncwarp();
+        if (lane < k) ws[wl][lane] = Wn[i * k + lane];
+        __syncwarp();
+        const uint64_t e0 = cptr[i], e1 = cptr[i + 1];
+        if (e0 == e1) continue;
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        for (uint64_t b = e0; b < e1; b += 32) {
+            uint32_t my = 0;
+            float dm = 0.f;
+            if (b + lane < e1) {
+                my = cidx[b + lane];
+                const float f = fill_dot(H + (uint64_t)my * k, ws[wl], k);
+                dm = (float)scale[my] * (f - (float)mean[my]);
+            }
+            const int cnt = (int)(e1 - b < 32 ? e1 - b : 32);
+            for (int t = 0; t < cnt; ++t) {
+                const uint64_t r = __shfl_sync(0xffffffffu, my, t);
+                const float d = __shfl_sync(0xffffffffu, dm, t);
+                const float* qr = Qop + r * ldq;
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (lane + 32 * q < w) acc[q] = fmaf(d, qr[lane + 32 * q], acc[q]);
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (lane + 32 * q < w) S[i * lds + lane + 32 * q] += (double)acc[q];
+    }
+}
+
+// out[r, c] += mu_r cs_c: a centred pass (missing at the mean) turned into the
+// raw mean-filled product (MeanRaw, src/parallel.rs:53-71)
+__global__ void k_add_mean_colsum(float* __restrict__ out, int ldo, uint64_t p, int w,
+                                  const double* __restrict__ mean, const double* __restrict__ cs) {
+    const uint64_t total = p * (uint64_t)w;
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < total;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t r = e / w;
+        const int c = (int)(e - r * w);
+        out[r * ldo + c] = (float)((double)out[r * ldo + c] + mean[r] * cs[c]);
+    }
+}
+
+// Multiplicative update (src/nmf.rs:150-230): X <- X num / denom where
+// denom > eps, then X <- max(X, eps).  X, denom: m x k (FP64); num: ld ldn.
+template <typename TN>
+__global__ void k_nmf_update(double* __restrict__ X, uint64_t m, int k, const TN* __restrict__ num, int ldn,
+                             const double* __restrict__ denom, double eps) {
+    const uint64_t total = m * (uint64_t)k;
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < total;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t r = e / k;
+        const int c = (int)(e - r * k);
+        double x = X[e];
+        const double dn = denom[e];
+        if (dn > eps) x = x * ((double)num[r * ldn + c] / dn);
+        X[e] = fmax(x, eps);
+    }
+}
+
+// normalize_w (src/nmf.rs:259-271): W[:, j] /= ||W[:, j]||_1 and
+// H[:, j] *= ||W[:, j]||_1 for columns whose L1 norm (W >= 0) exceeds eps
+__global__ void k_nmf_normalize(double* __restrict__ W, uint64_t n, double* __restrict__ H, uint64_t p, int k,
+                                const double* __restrict__ colsum, double eps) {
+    const uint64_t total = (n + p) * (uint64_t)k;
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < total;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        const int c = (int)(e % k);
+        const double cs = colsum[c];
+        if (!(cs > eps)) continue;
+        if (e < n * (uint64_t)k) W[e] *= 1.0 / cs;
+        else H[e - n * (uint64_t)k] *= cs;
+    }
+}
+
+// X <- |X| (mode 0) or max(X, 0) (mode 1), FP64, with an optional FP32
+// source (ld ldsrc) copied into the m x k destination first
+template <typename TS>
+__global__ void k_nmf_sign(const TS* __restrict__ src, int ldsrc, double* __restrict__ X, uint64_t m, int k,
+                           int mode) {
+    const uint64_t total = m * (uint64_t)k;
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < total;
+         e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t r = e / k;
+        const int c = (int)(e - r * k);
+        const double v = (double)src[r * ldsrc + c];
+        X[e] = mode == 0 ? fabs(v) : fmax(v, 0.0);
+    }
+}
+
+// Estimation-phase CV (compute_cv_error_masked, src/nmf.rs:379-455).  Chunk
+// `seq` of `chunk` SNPs uses the stream of mask_seed + seq; entry (i, r) draws
+// counter (r - chunk start) n + i (column-major, missing calls included) and
+// is held out iff the draw is below `rate` and the call is observed.  Per SNP:
+// sum |g - W_i.H_r|, sum |g - mean_r|, count.
+__global__ void __launch_bounds__(256) k_nmf_cv(const uint8_t* __restrict__ packed, uint64_t stride, uint64_t n,
+                                                uint64_t p, uint64_t chunk, uint64_t mask_seed, double rate,
+                                                const float* __restrict__ W, const float* __restrict__ H, int k,
+                                                const int32_t* __restrict__ counts, double* __restrict__ part) {
+    __shared__ float hs[8][kMaxNmfK];
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const uint64_t nw = (uint64_t)gridDim.x * 8;
+    for (uint64_t r = (uint64_t)blockIdx.x * 8 + wl; r < p; r += nw) {
+        __syncwarp();
+        if (lane < k) hs[wl][lane] = H[r * k + lane];
+        __syncwarp();
+        const uint64_t seq = r / chunk, col = r - seq * chunk;
+        const uint64_t key = mix64(mask_seed + seq + kGamma);
+        const int64_t c0 = counts[r * 4], c1 = counts[r * 4 + 1], c2 = counts[r * 4 + 2];
+        const int64_t nobs = c0 + c1 + c2;
+        const double cm = nobs > 0 ? (double)(c1 + 2 * c2) / (double)nobs : 0.0;
+        const uint8_t* row = packed + r * stride;
+        double e1 = 0.0, e2 = 0.0, cnt = 0.0;
+        for (uint64_t i = lane; i < n; i += 32) {
+            const uint32_t code = code_at(row, i);
+            if (code == 1u) continue;
+            if (uniform_at(key, col * n + i) < rate) {
+                const double g = code == 0 ? 0.0 : (double)(code - 1);
+                e1 += fabs(g - (double)fill_dot(W + i * k, hs[wl], k));
+                e2 += fabs(g - cm);
+                cnt += 1.0;
+            }
+        }
+        e1 = warp_sum_d(e1);
+        e2 = warp_sum_d(e2);
+        cnt = warp_sum_d(cnt);
+        if (lane == 0) {
+            part[r * 3] = e1;
+            part[r * 3 + 1] = e2;
+            part[r * 3 + 2] = cnt;
+        }
+    }
+}
+
+// Observed calls before each SNP within its chunk (the GWAS-phase CV numbers
+// its draws by the rank of the observed call in column-major order)
+__global__ void k_obs_base(const int32_t* __restrict__ counts, uint64_t p, uint64_t chunk, uint64_t* __restrict__ base) {
+    const uint64_t nchunks = (p + chunk - 1) / chunk;
+    for (uint64_t b = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; b < nchunks;
+         b += (uint64_t)gridDim.x * blockDim.x) {
+        uint64_t acc = 0;
+        const uint64_t r1 = min(p, (b + 1) * chunk);
+        for (uint64_t r = b * chunk; r < r1; ++r) {
+            base[r] = acc;
+            acc += (uint64_t)(counts[r * 4] + counts[r * 4 + 1] + counts[r * 4 + 2]);
+        }
+    }
+}
+
+// GWAS-phase CV (src/testing.rs:423-487): per chunk the stream seed + seq,
+// one draw per OBSERVED call (counter = its column-major rank in the chunk),
+// held out iff the draw is below `rate`; the held-out column is refilled with
+// its leave-out mean mu', H = max(0, W+ y~) and the MAE of W_i.H and of mu'
+// over the held-out calls accumulate.  W+ y~ = A + mu' B with A = sum over
+// kept observed calls of W+_i g, B = sum over missing and held-out calls of
+// W+_i.  One warp per SNP, two passes over its codes.
+__global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__ packed, uint64_t stride, uint64_t n,
+                                                     uint64_t p, uint64_t chunk, uint64_t seed, double rate,
+                                                     const float* __restrict__ W, const float* __restrict__ Wpt, int k,
+                                                     const uint64_t* __restrict__ base, double* __restrict__ part) {
+    __shared__ float hh[8][kMaxNmfK];
+    const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    const uint64_t nw = (uint64_t)gridDim.x * 8;
+    for (uint64_t r = (uint64_t)blockIdx.x * 8 + wl; r < p; r += nw) {
+        const uint64_t seq = r / chunk;
+        const uint64_t key = mix64(seed + seq + kGamma);
+        const uint8_t* row = packed + r * stride;
+        float A[kMaxNmfK], B[kMaxNmfK];
+#pragma unroll
+        for (int c = 0; c < kMaxNmfK; ++c) A[c] = B[c] = 0.f;
+        double s1 = 0.0, nk = 0.0;
+        int nmask = 0;
+        uint64_t before = base[r];
+        for (uint64_t i0 = 0; i0 < n; i0 += 32) {
+            const uint64_t i = i0 + lane;
+            const uint32_t code = i < n ? code_at(row, i) : 1u;
+            const bool obs = i < n && code != 1u;
+            const unsigned bal = __ballot_sync(0xffffffffu, obs);
+            bool held = false;
+            if (obs) held = uniform_at(key, before + __popc(bal & lt)) < rate;
+            before += __popc(bal);
+            if (i < n) {
+                const float* wp = Wpt + i * k;
+                if (obs && !held) {
+                    const float g = code == 0 ? 0.f : (float)(code - 1);
+                    s1 += (double)g;
+                    nk += 1.0;
+#pragma unroll
+                    for (int c = 0; c < kMaxNmfK; ++c)
+                        if (c < k) A[c] = fmaf(wp[c], g, A[c]);
+                } else {
+#pragma unroll
+                    for (int c = 0; c < kMaxNmfK; ++c)
+                        if (c < k) B[c] += wp[c];
+                }
+            }
+            nmask += held ? 1 : 0;
+        }
+        nmask = __reduce_add_sync(0xffffffffu, nmask);
+        if (nmask == 0) {
+            if (lane == 0) part[r * 3] = part[r * 3 + 1] = part[r * 3 + 2] = 0.0;
+            continue;
+        }
+        s1 = warp_sum_d(s1);
+        nk = warp_sum_d(nk);
+        const double mu = nk > 0.0 ? s1 / nk : 0.0;
+#pragma unroll
+        for (int c = 0; c < kMaxNmfK; ++c) {
+            if (c < k) {
+                const float a = warp_sum_f(A[c]), b = warp_sum_f(B[c]);
+                if (lane == 0) hh[wl][c] = fmaxf(a + (float)mu * b, 0.f);
+            }
+        }
+        __syncwarp();
+        double e1 = 0.0, e2 = 0.0;
+        before = base[r];
+        for (uint64_t i0 = 0; i0 < n; i0 += 32) {
+            const uint64_t i = i0 + lane;
+            const uint32_t code = i < n ? code_at(row, i) : 1u;
+            const bool obs = i < n && code != 1u;
+            const unsigned bal = __ballot_sync(0xffffffffu, obs);
+            if (obs && uniform_at(key, before + __popc(bal & lt)) < rate) {
+                const double g = code == 0 ? 0.0 : (double)(code - 1);
+                e1 += fabs(g - (double)fill_dot(W + i * k, hh[wl], k));
+                e2 += fabs(g - mu);
+            }
+            before += __popc(bal);
+        }
+        e1 = warp_sum_d(e1);
+        e2 = warp_sum_d(e2);
+        if (lane == 0) {
+            part[r * 3] = e1;
+            part[r * 3 + 1] = e2;
+            part[r * 3 + 2] = (double)nmask;
+        }
+        __syncwarp();
+    }
+}
+
+}  // namespace
+
+void launch_fill_stats(Ctx& c, const Geno& g, int norm, const float* W, const float* H, int k, double* mean,
+                       double* scale, double* tss, uint8_t* zero_var) {
+    if (!g.p) return;
+    SLFMM_REQUIRE(k >= 1 && k <= kMaxNmfK, SLFMM_ERR_BAD_ARG, "NMF rank must be in 1..16");
+    k_fill_stats<<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(g.p, g.n, norm, g.counts.get(), g.miss_ptr.get(),
+                                                             g.miss_idx.get(), W, H, k, mean, scale, tss, zero_var);
+    SLFMM_LAUNCHED(c, "k_fill_stats");
+}
+
+void launch_fill_row_correct(Ctx& c, const Geno& g, float* out, int ldo, int w, const float* Wop, int ldw,
+                             const float* Wn, const float* H, int k, const double* mean, const double* scale) {
+    if (!g.p || !w) return;
+    SLFMM_REQUIRE(w <= 128 && k >= 1 && k <= kMaxNmfK, SLFMM_ERR_BAD_ARG, "NMF correction shape");
+    k_fill_row_correct<<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(out, ldo, g.p, w, g.miss_ptr.get(),
+                                                                   g.miss_idx.get(), Wop, ldw, Wn, H, k, mean, scale);
+    SLFMM_LAUNCHED(c, "k_fill_row_correct");
+}
+
+void launch_fill_col_correct(Ctx& c, const Geno& g, double* S, int lds, int w, const float* Qop, int ldq,
+                             const float* Wn, const float* H, int k, const double* mean, const double* scale) {
+    if (!g.n || !w) return;
+    SLFMM_REQUIRE(w <= 128 && k >= 1 && k <= kMaxNmfK, SLFMM_ERR_BAD_ARG, "NMF correction shape");
+    k_fill_col_correct<<<grid_for(c, g.n, 8), 256, 0, c.stream>>>(S, lds, g.n, w, g.missT_ptr.get(),
+                                                                   g.missT_idx.get(), Qop, ldq, Wn, H, k, mean, scale);
+    SLFMM_LAUNCHED(c, "k_fill_col_correct");
+}
+
+void launch_add_mean_colsum(Ctx& c, float* out, int ldo, uint64_t p, int w, const double* mean, const double* cs) {
+    if (!p || !w) return;
+    k_add_mean_colsum<<<grid_for(c, p * w, 256), 256, 0, c.stream>>>(out, ldo, p, w, mean, cs);
+    SLFMM_LAUNCHED(c, "k_add_mean_colsum");
+}
+
+void launch_nmf_update_f64(Ctx& c, double* X, uint64_t m, int k, const double* num, int ldn, const double* denom,
+                           double eps) {
+    if (!m) return;
+    k_nmf_update<double><<<grid_for(c, m * k, 256), 256, 0, c.stream>>>(X, m, k, num, ldn, denom, eps);
+    SLFMM_LAUNCHED(c, "k_nmf_update");
+}
+
+void launch_nmf_update_f32(Ctx& c, double* X, uint64_t m, int k, const float* num, int ldn, const double* denom,
+                           double eps) {
+    if (!m) return;
+    k_nmf_update<float><<<grid_for(c, m * k, 256), 256, 0, c.stream>>>(X, m, k, num, ldn, denom, eps);
+    SLFMM_LAUNCHED(c, "k_nmf_update");
+}
+
+void launch_nmf_normalize(Ctx& c, double* W, uint64_t n, double* H, uint64_t p, int k, const double* colsum,
+                          double eps) {
+    k_nmf_normalize<<<grid_for(c, (n + p) * k, 256), 256, 0, c.stream>>>(W, n, H, p, k, colsum, eps);
+    SLFMM_LAUNCHED(c, "k_nmf_normalize");
+}
+
+void launch_nmf_abs_f64(Ctx& c, const double* src, int ld, double* X, uint64_t m, int k) {
+    if (!m) return;
+    k_nmf_sign<double><<<grid_for(c, m * k, 256), 256, 0, c.stream>>>(src, ld, X, m, k, 0);
+    SLFMM_LAUNCHED(c, "k_nmf_sign");
+}
+
+void launch_nmf_clamp0_f32(Ctx& c, const float* src, int ld, double* X, uint64_t m, int k) {
+    if (!m) return;
+    k_nmf_sign<float><<<grid_for(c, m * k, 256), 256, 0, c.stream>>>(src, ld, X, m, k, 1);
+    SLFMM_LAUNCHED(c, "k_nmf_sign");
+}
+
+void launch_nmf_cv(Ctx& c, const Geno& g, uint64_t chunk, uint64_t mask_seed, double rate, const float* W,
+                   const float* H, int k, double* part) {
+    if (!g.p) return;
+    k_nmf_cv<<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(g.packed.get(), g.stride, g.n, g.p, chunk, mask_seed, rate, W,
+                                                         H, k, g.counts.get(), part);
+    SLFMM_LAUNCHED(c, "k_nmf_cv");
+}
+
+void launch_nmf_gwas_cv(Ctx& c, const Geno& g, uint64_t chunk, uint64_t seed, double rate, const float* W,
+                        const float* Wpt, int k, double* part) {
+    if (!g.p) return;
+    DBuf<uint64_t> base(g.p, c.stream);
+    const uint64_t nchunks = ceil_div(g.p, chunk);
+    k_obs_base<<<grid_for(c, nchunks, 64), 64, 0, c.stream>>>(g.counts.get(), g.p, chunk, base.get());
+    SLFMM_LAUNCHED(c, "k_obs_base");
+    k_nmf_gwas_cv<<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(g.packed.get(), g.stride, g.n, g.p, chunk, seed, rate, W,
+                                                              Wpt, k, base.get(), part);
+    SLFMM_LAUNCHED(c, "k_nmf_gwas_cv");
+}
+
+}  // namespace slfmm

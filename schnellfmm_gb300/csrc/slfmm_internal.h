@@ -40,6 +40,7 @@ struct Error : std::runtime_error {
 // ---------------------------------------------------------------------------
 constexpr int kHistBins = 100000;      // src/testing.rs:124
 constexpr int kGifNoAllocMaxTraits = 8; // traits the static histogram of slfmm_gif_noalloc holds
+constexpr int kMaxNmfK = 16;            // NMF rank limit of the imputation kernels
 constexpr double kHistWidth = 0.001;   // src/testing.rs:125
 constexpr double kGifDivisor = 0.4549; // src/testing.rs:169
 constexpr int kMaxW = 128;             // widest GEMM operand (columns)
@@ -273,6 +274,28 @@ int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t rows
                      const double* row_scale, const double* cs, float* out, int ldo, int splits,
                      uint64_t split_stride);
 void launch_sub_colterm(Ctx& c, double* S, int lds, uint64_t n, int w, const double* colterm);
+
+// k_nmf.cu : NMF imputation -- fill-aware statistics, sparse corrections of
+// the contractions at the missing calls, multiplicative updates, CV
+void launch_fill_stats(Ctx& c, const Geno& g, int norm, const float* W, const float* H, int k, double* mean,
+                       double* scale, double* tss, uint8_t* zero_var);
+void launch_fill_row_correct(Ctx& c, const Geno& g, float* out, int ldo, int w, const float* Wop, int ldw,
+                             const float* Wn, const float* H, int k, const double* mean, const double* scale);
+void launch_fill_col_correct(Ctx& c, const Geno& g, double* S, int lds, int w, const float* Qop, int ldq,
+                             const float* Wn, const float* H, int k, const double* mean, const double* scale);
+void launch_add_mean_colsum(Ctx& c, float* out, int ldo, uint64_t p, int w, const double* mean, const double* cs);
+void launch_nmf_update_f64(Ctx& c, double* X, uint64_t m, int k, const double* num, int ldn, const double* denom,
+                           double eps);
+void launch_nmf_update_f32(Ctx& c, double* X, uint64_t m, int k, const float* num, int ldn, const double* denom,
+                           double eps);
+void launch_nmf_normalize(Ctx& c, double* W, uint64_t n, double* H, uint64_t p, int k, const double* colsum,
+                          double eps);
+void launch_nmf_abs_f64(Ctx& c, const double* src, int ld, double* X, uint64_t m, int k);
+void launch_nmf_clamp0_f32(Ctx& c, const float* src, int ld, double* X, uint64_t m, int k);
+void launch_nmf_cv(Ctx& c, const Geno& g, uint64_t chunk, uint64_t mask_seed, double rate, const float* W,
+                   const float* H, int k, double* part);
+void launch_nmf_gwas_cv(Ctx& c, const Geno& g, uint64_t chunk, uint64_t seed, double rate, const float* W,
+                        const float* Wpt, int k, double* part);
 
 // k_small.cu : FP64 dense helpers (row-major)
 void launch_colmeans(Ctx& c, const double* A, uint64_t m, int a, int lda, double* out);
