@@ -136,7 +136,11 @@ void upload_geno(Ctx& c, Geno& g, const uint8_t* packed, uint64_t n_phys, uint64
     }
     if (g.p) {
         // staging: ~64 MiB per chunk, two device buffers, two pinned buffers
-        const uint64_t rows_per = std::max<uint64_t>(1, std::min<uint64_t>(g.p, (64ull << 20) / bps));
+        // split-FP8 contexts build the tile-major copies chunk by chunk as the
+        // rows land (chunks then start on 128-row tiles)
+        const bool tiles = c.precision == SLFMM_PREC_SPLIT_FP8;
+        uint64_t rows_per = std::max<uint64_t>(1, std::min<uint64_t>(g.p, (64ull << 20) / bps));
+        if (tiles) rows_per = std::max<uint64_t>(128, rows_per / 128 * 128);
         const bool direct = is_pinned(packed);
         DBuf<uint8_t> dstage[2];
         dstage[0].alloc(rows_per * bps, c.stream);
@@ -193,11 +197,12 @@ void upload_geno(Ctx& c, Geno& g, const uint8_t* packed, uint64_t n_phys, uint64
             launch_repack(c, dstage[b].get(), rows, bps, n_phys, keep_d.get(), g.n,
                           g.packed.get() + r0 * g.stride, g.stride);
             SLFMM_CUDA(cudaEventRecord(consumed[b], c.stream));
+            launch_snp_counts_range(c, g, r0, rows);
+            if (tiles) tile_chunk(c, g, r0, r1, ch + 1 == nchunks);
         }
         SLFMM_CUDA(cudaStreamSynchronize(c.stream));
         SLFMM_CUDA(cudaStreamSynchronize(c.copy_stream));
     }
-    launch_snp_counts(c, g, nullptr);
     sync(c);
 }
 

@@ -222,6 +222,15 @@ void launch_snp_counts(Ctx& c, const Geno& g, uint64_t* miss_count_out) {
     SLFMM_LAUNCHED(c, "k_snp_counts");
 }
 
+void launch_snp_counts_range(Ctx& c, const Geno& g, uint64_t r0, uint64_t rows) {
+    if (rows == 0) return;
+    const int block = 256;
+    const uint64_t grid = ceil_div(rows * 32, block);
+    k_snp_counts<<<(unsigned)grid, block, 0, c.stream>>>(g.packed.get() + r0 * g.stride, rows, g.stride, g.n,
+                                                         g.counts.get() + r0 * 4, nullptr);
+    SLFMM_LAUNCHED(c, "k_snp_counts");
+}
+
 void build_missing_lists(Ctx& c, const Geno& g) {
     if (g.have_csr) return;
     DBuf<uint64_t> mc(g.p + 1, c.stream);

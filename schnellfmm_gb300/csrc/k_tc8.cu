@@ -711,13 +711,16 @@ __global__ void k_tile_rows(const uint8_t* __restrict__ in, uint64_t rows, uint6
 // from 16 SNP rows, and the 4 KiB result is stored contiguously.
 __global__ void __launch_bounds__(256) k_transpose_tiles(const uint8_t* __restrict__ src, uint64_t kbt_src,
                                                          uint64_t ntiles_src, uint8_t* __restrict__ dst,
-                                                         uint64_t kbt_dst, uint64_t ntiles_dst) {
+                                                         uint64_t kbt_dst, uint64_t ntiles_dst, uint64_t kb_lo,
+                                                         uint64_t kb_hi) {
     __shared__ __align__(16) uint8_t in[128 * 32];
-    const uint64_t nblocks = ntiles_dst * kbt_dst;
+    const uint64_t nk = kb_hi - kb_lo;  // output K blocks [kb_lo, kb_hi) of every sample tile
+    const uint64_t nblocks = ntiles_dst * nk;
     const int j = threadIdx.x & 127;   // sample within the tile
     const int h = threadIdx.x >> 7;    // which 64 SNPs
-    for (uint64_t b = blockIdx.x; b < nblocks; b += gridDim.x) {
-        const uint64_t t = b / kbt_dst, kb = b - t * kbt_dst;
+    for (uint64_t bb = blockIdx.x; bb < nblocks; bb += gridDim.x) {
+        const uint64_t t = bb / nk, kb = kb_lo + (bb - t * nk);
+        const uint64_t b = t * kbt_dst + kb;
         const bool valid = kb < ntiles_src && t < kbt_src;
         __syncthreads();
         const uint4* s4 = reinterpret_cast<const uint4*>(src + (kb * kbt_src + t) * (uint64_t)kTileBytes);
@@ -751,6 +754,36 @@ static void tile_rows(Ctx& c, const uint8_t* in, uint64_t rows, uint64_t stride,
     SLFMM_LAUNCHED(c, "k_tile_rows");
 }
 
+// Tile-major copies built chunk by chunk while a matrix is uploaded: rows
+// [r0, r1) of the SNP-major matrix (r0 a multiple of 128) are tiled and
+// transposed as soon as they land.  `last` also writes the padding tiles.
+void tile_chunk(Ctx& c, const Geno& g, uint64_t r0, uint64_t r1, bool last) {
+    SLFMM_REQUIRE(r0 % kM == 0, SLFMM_ERR_BAD_ARG, "upload chunks must start on a 128-row tile");
+    if (r0 == 0) {
+        SLFMM_REQUIRE(g.stride % 32 == 0, SLFMM_ERR_BAD_ARG, "packed stride must be a multiple of 32 bytes");
+        g.kbt = g.stride / 32;
+        g.ntiles = round_up(std::max<uint64_t>(ceil_div(g.p, kM), 1), 8);
+        g.tiles.alloc(g.ntiles * g.kbt * kTileBytes, c.stream);
+        g.kbtT = round_up(std::max<uint64_t>(ceil_div(g.p, kM), 1), kHalves);
+        g.ntilesT = round_up(std::max<uint64_t>(ceil_div(g.n, kM), 1), 8);
+        g.tilesT.alloc(g.ntilesT * g.kbtT * kTileBytes, c.stream);
+    }
+    const uint64_t t0 = r0 / kM, t1 = last ? g.ntiles : ceil_div(r1, kM);
+    const uint64_t chunks = (t1 - t0) * g.kbt * (kTileBytes / 16);
+    k_tile_rows<<<grid_for(c, chunks, 256), 256, 0, c.stream>>>(g.packed.get() + r0 * g.stride, r1 - r0, g.stride,
+                                                                 g.kbt, chunks,
+                                                                 g.tiles.get() + t0 * g.kbt * kTileBytes);
+    SLFMM_LAUNCHED(c, "k_tile_rows");
+    const uint64_t k1 = last ? g.kbtT : std::min(g.kbtT, ceil_div(r1, kM));
+    if (k1 > t0) {
+        const uint64_t blocks = std::min<uint64_t>(g.ntilesT * (k1 - t0), (uint64_t)c.sm_count * 16);
+        k_transpose_tiles<<<(unsigned)blocks, 256, 0, c.stream>>>(g.tiles.get(), g.kbt, g.ntiles, g.tilesT.get(),
+                                                                   g.kbtT, g.ntilesT, t0, k1);
+        SLFMM_LAUNCHED(c, "k_transpose_tiles");
+    }
+    if (last) g.have_tiles = g.have_tilesT = true;
+}
+
 TileView build_tiles(Ctx& c, const Geno& g, bool transposed) {
     if (!transposed) {
         if (!g.have_tiles) {
@@ -767,7 +800,7 @@ TileView build_tiles(Ctx& c, const Geno& g, bool transposed) {
         g.tilesT.alloc(g.ntilesT * g.kbtT * kTileBytes, c.stream);
         const uint64_t blocks = std::min<uint64_t>(g.ntilesT * g.kbtT, (uint64_t)c.sm_count * 16);
         k_transpose_tiles<<<(unsigned)blocks, 256, 0, c.stream>>>(g.tiles.get(), g.kbt, g.ntiles, g.tilesT.get(),
-                                                                   g.kbtT, g.ntilesT);
+                                                                   g.kbtT, g.ntilesT, 0, g.kbtT);
         SLFMM_LAUNCHED(c, "k_transpose_tiles");
         g.have_tilesT = true;
     }

@@ -203,6 +203,8 @@ void after_launch(Ctx& c, const char* name);
 void launch_repack(Ctx& c, const uint8_t* in, uint64_t rows, uint64_t in_bps, uint64_t n_phys,
                    const uint32_t* keep, uint64_t n_out, uint8_t* out, uint64_t stride);
 void launch_snp_counts(Ctx& c, const Geno& g, uint64_t* miss_count_out);
+// counts of rows [r0, r0 + rows) only
+void launch_snp_counts_range(Ctx& c, const Geno& g, uint64_t r0, uint64_t rows);
 void build_missing_lists(Ctx& c, const Geno& g);
 void build_missing_csc(Ctx& c, const Geno& g);
 void launch_stats_mean(Ctx& c, const Geno& g, int norm, double* mean, double* scale,
@@ -264,6 +266,7 @@ struct TileView {
     uint64_t kbt, ntiles;
 };
 TileView build_tiles(Ctx& c, const Geno& g, bool transposed);
+void tile_chunk(Ctx& c, const Geno& g, uint64_t r0, uint64_t r1, bool last);
 void launch_fp8_terms_f64(Ctx& c, const double* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
                           const double* kscale, int terms, int row_off, uint8_t* B, float* inv_scale);
 void launch_fp8_terms_f32(Ctx& c, const float* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
