@@ -54,6 +54,11 @@ WORKLOADS = {
     "plant": dict(n=1_135, p=1_800_000, k=12, d=1, oversampling=10, power_iter=2, n_pop=8, alpha=0.5,
                   fst=0.1, f_lo=0.01, f_hi=0.5, miss=0.02, inbreeding=0.9, lam=1e-5, mask_max=0.0,
                   est_rate=0.01),
+    # NMF-imputation shape: 6 admixed populations, 7 % missing calls (MCAR here;
+    # the 2 % contiguous-block share is drawn as MCAR too), nmf-k 8, 10 updates
+    "nmf": dict(n=5_000, p=500_000, k=8, d=4, oversampling=10, power_iter=2, n_pop=6, alpha=0.4,
+                fst=0.05, f_lo=0.01, f_hi=0.5, miss=0.07, inbreeding=0.0, lam=1e-5, mask_max=0.0,
+                est_rate=None, nmf=dict(k=8, n_iter=10, cv_rate=5e-4)),
     # the reference's CPU-runnable case
     "small": dict(n=200, p=10_000, k=3, d=1, oversampling=10, power_iter=2, n_pop=2, alpha=1.0,
                   fst=0.1, f_lo=0.05, f_hi=0.5, miss=0.01, inbreeding=0.0, lam=1e-5, mask_max=0.0,
@@ -266,6 +271,9 @@ def main():
                         inbreeding=w["inbreeding"], seed=42 + rank)
     cfg = sg.Lfmm2Config(k=k, lambda_=w["lam"], oversampling=w["oversampling"], n_power_iter=w["power_iter"],
                          norm=sg.SnpNorm.EIGENSTRAT)
+    if w.get("nmf"):
+        cfg.impute = sg.ImputeStrategy.NMF
+        cfg.nmf = sg.NmfConfig(k=w["nmf"]["k"], n_iter=w["nmf"]["n_iter"], cv_rate=w["nmf"]["cv_rate"])
     est = sg.SubsetSpec.from_rate(w["est_rate"]) if w["est_rate"] else sg.SubsetSpec.all()
     bps = (n + 3) // 4
     host_packed, _keep_alive = pinned_empty((p, bps), np.uint8)

@@ -609,7 +609,8 @@ def _to_results(r: _Results, arr, config: Lfmm2Config) -> TestResults:
     out = TestResults(arr["u_hat"], r.gif, arr["gif_per_trait"], arr["beta"], arr["tstat"], arr["pvalue"], arr["r2"])
     if config.impute == ImputeStrategy.NMF:
         nmf = config.nmf or NmfConfig(k=config.k)
-        out.nmf_cv = list(arr["nmf_cv"][:nmf.n_iter])
+        cv = arr.get("nmf_cv")
+        out.nmf_cv = [] if cv is None else list(cv[:nmf.n_iter])
         out.nmf_cv_mean = r.nmf_cv_mean
         out.nmf_gwas_cv_mae = r.nmf_gwas_cv_mae
         out.nmf_gwas_cv_mean_mae = r.nmf_gwas_cv_mean_mae

@@ -5,6 +5,8 @@
 // decode_single_snp, compute_scale), src/parallel.rs:53-71 and :129-146.
 #include <cub/cub.cuh>
 
+#include <vector>
+
 #include "slfmm_internal.h"
 #include "stats_common.cuh"
 
@@ -295,6 +297,13 @@ void build_missing_csc(Ctx& c, const Geno& g) {
     DBuf<uint8_t> tmp2(tb2, c.stream);
     SLFMM_CUDA(cub::DeviceScan::ExclusiveSum(tmp2.get(), tb2, cnt64.get(), g.missT_ptr.get(),
                                              (int64_t)(g.n + 1), c.stream));
+    // longest per-sample list (splits the per-sample correction passes)
+    std::vector<uint64_t> hp(g.n + 1);
+    SLFMM_CUDA(cudaMemcpyAsync(hp.data(), g.missT_ptr.get(), (g.n + 1) * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                               c.stream));
+    SLFMM_CUDA(cudaStreamSynchronize(c.stream));
+    g.missT_max = 0;
+    for (uint64_t i = 0; i < g.n; ++i) g.missT_max = std::max<uint64_t>(g.missT_max, hp[i + 1] - hp[i]);
     g.have_csc = true;
 }
 

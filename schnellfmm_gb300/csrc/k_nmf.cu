@@ -7,6 +7,7 @@
 // corrections over the missing-call lists (CSR by SNP, CSC by sample), so no
 // imputed copy of the matrix is ever formed.  W (n x k) and H (p x k, one row
 // per SNP) are FP32 row-major here; k <= kMaxNmfK.
+#include <cmath>
 #include <cstdint>
 
 #include "slfmm_internal.h"
@@ -23,9 +24,11 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
     return z ^ (z >> 31);
 }
 
-// U[0,1) draw `ctr` of the counter stream keyed by mix64(seed + gamma)
-__device__ __forceinline__ double uniform_at(uint64_t key, uint64_t ctr) {
-    return (double)(mix64(key + (ctr + 1) * kGamma) >> 11) * 0x1.0p-53;
+// Draw `ctr` of the counter stream keyed by mix64(seed + gamma) is the
+// uniform (m >> 11) 2^-53; it is below `rate` iff (m >> 11) < ceil(rate 2^53)
+// -- compared as integers, without forming the FP64 uniform
+__device__ __forceinline__ bool draw_below(uint64_t key, uint64_t ctr, uint64_t thresh) {
+    return (mix64(key + (ctr + 1) * kGamma) >> 11) < thresh;
 }
 
 __device__ __forceinline__ uint32_t code_at(const uint8_t* row, uint64_t s) {
@@ -90,9 +93,53 @@ __global__ void __launch_bounds__(256) k_fill_stats(uint64_t p, uint64_t n, int 
     }
 }
 
+// One round of a correction: add d_t * op[row_t, c] over the round's `cnt`
+// (row, d) pairs held by lanes 0..cnt-1.  For operands of width w <= CG
+// (CG = 8, 16, 32) the warp splits into 32/CG groups that take different
+// entries (lane = group * CG + column); CG = 0 is the wide form (one entry per
+// step, columns lane + 32 q, w <= 128).  Steps are unrolled so several
+// gathers are in flight.
+template <int CG>
+__device__ __forceinline__ void round_accum(float (&acc)[4], uint32_t my, float dm, int cnt, const float* __restrict__ op,
+                                            int ldop, int w, int lane) {
+    if constexpr (CG == 0) {
+#pragma unroll 4
+        for (int t = 0; t < 32; ++t) {
+            if (t >= cnt) break;
+            const uint64_t r = __shfl_sync(0xffffffffu, my, t);
+            const float d = __shfl_sync(0xffffffffu, dm, t);
+            const float* row = op + r * ldop;
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (lane + 32 * q < w) acc[q] = fmaf(d, row[lane + 32 * q], acc[q]);
+        }
+    } else {
+        constexpr int EPI = 32 / CG;
+        const int e = lane / CG, c = lane % CG;
+#pragma unroll 4
+        for (int t = 0; t < 32; t += EPI) {
+            if (t >= cnt) break;
+            const int te = t + e;
+            const uint64_t r = __shfl_sync(0xffffffffu, my, te & 31);
+            const float d = __shfl_sync(0xffffffffu, dm, te & 31);
+            if (te < cnt && c < w) acc[0] = fmaf(d, op[r * ldop + c], acc[0]);
+        }
+    }
+}
+
+// after the rounds: column c's total in lane c (narrow form) / lane + 32 q (wide)
+template <int CG>
+__device__ __forceinline__ void round_finish(float (&acc)[4]) {
+    if constexpr (CG != 0) {
+#pragma unroll
+        for (int off = CG; off < 32; off <<= 1) acc[0] += __shfl_xor_sync(0xffffffffu, acc[0], off);
+    }
+}
+
 // Row pass correction: out[r, c] += s_r * sum_{i in miss(r)} (f_ir - mu_r) Wop[i, c]
 // (the base pass counted the missing calls at the mean).  One warp per SNP;
 // 32 missing indices and their fills are formed per round and broadcast.
+template <int CG>
 __global__ void __launch_bounds__(256) k_fill_row_correct(float* __restrict__ out, int ldo, uint64_t p, int w,
                                                           const uint64_t* __restrict__ ptr,
                                                           const uint32_t* __restrict__ idx, const float* __restrict__ Wop,
@@ -118,26 +165,28 @@ __global__ void __launch_bounds__(256) k_fill_row_correct(float* __restrict__ ou
                 my = idx[b + lane];
                 dm = fill_dot(Wn + (uint64_t)my * k, hs[wl], k) - mu;
             }
-            const int cnt = (int)(e1 - b < 32 ? e1 - b : 32);
-            for (int t = 0; t < cnt; ++t) {
-                const uint64_t i = __shfl_sync(0xffffffffu, my, t);
-                const float d = __shfl_sync(0xffffffffu, dm, t);
-                const float* wr = Wop + i * ldw;
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    if (lane + 32 * q < w) acc[q] = fmaf(d, wr[lane + 32 * q], acc[q]);
-            }
+            round_accum<CG>(acc, my, dm, (int)(e1 - b < 32 ? e1 - b : 32), Wop, ldw, w, lane);
         }
+        round_finish<CG>(acc);
+        float* o = out + r * ldo;
+        if constexpr (CG == 0) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
-            if (lane + 32 * q < w) out[r * ldo + lane + 32 * q] += sc * acc[q];
+            for (int q = 0; q < 4; ++q)
+                if (lane + 32 * q < w) o[lane + 32 * q] += sc * acc[q];
+        } else {
+            if (lane < w) o[lane] += sc * acc[0];
+        }
     }
 }
 
 // Column pass correction: S[i, c] += sum_{r in miss(i)} s_r (f_ir - mu_r) Qop[r, c].
-// One warp per sample over its CSC list.
+// Per-sample lists can be long (thousands of calls), so each list is cut into
+// segments of kColSeg calls, one warp per (sample, segment), and the segment
+// sums are added into S with FP64 atomics.
+constexpr uint64_t kColSeg = 1024;
+template <int CG>
 __global__ void __launch_bounds__(256) k_fill_col_correct(double* __restrict__ S, int lds, uint64_t n, int w,
-                                                          const uint64_t* __restrict__ cptr,
+                                                          uint64_t nseg, const uint64_t* __restrict__ cptr,
                                                           const uint32_t* __restrict__ cidx,
                                                           const float* __restrict__ Qop, int ldq,
                                                           const float* __restrict__ Wn, const float* __restrict__ H,
@@ -146,12 +195,13 @@ __global__ void __launch_bounds__(256) k_fill_col_correct(double* __restrict__ S
     __shared__ float ws[8][kMaxNmfK];
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     const uint64_t nw = (uint64_t)gridDim.x * 8;
-    for (uint64_t i = (uint64_t)blockIdx.x * 8 + wl; i < n; i += nw) {
+    for (uint64_t gw = (uint64_t)blockIdx.x * 8 + wl; gw < n * nseg; gw += nw) {
+        const uint64_t i = gw / nseg, sg = gw - i * nseg;
+        const uint64_t e0 = cptr[i] + sg * kColSeg, e1 = min(cptr[i + 1], e0 + kColSeg);
+        if (e0 >= e1) continue;
         __syncwarp();
         if (lane < k) ws[wl][lane] = Wn[i * k + lane];
         __syncwarp();
-        const uint64_t e0 = cptr[i], e1 = cptr[i + 1];
-        if (e0 == e1) continue;
         float acc[4] = {0.f, 0.f, 0.f, 0.f};
         for (uint64_t b = e0; b < e1; b += 32) {
             uint32_t my = 0;
@@ -161,19 +211,17 @@ __global__ void __launch_bounds__(256) k_fill_col_correct(double* __restrict__ S
                 const float f = fill_dot(H + (uint64_t)my * k, ws[wl], k);
                 dm = (float)scale[my] * (f - (float)mean[my]);
             }
-            const int cnt = (int)(e1 - b < 32 ? e1 - b : 32);
-            for (int t = 0; t < cnt; ++t) {
-                const uint64_t r = __shfl_sync(0xffffffffu, my, t);
-                const float d = __shfl_sync(0xffffffffu, dm, t);
-                const float* qr = Qop + r * ldq;
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    if (lane + 32 * q < w) acc[q] = fmaf(d, qr[lane + 32 * q], acc[q]);
-            }
+            round_accum<CG>(acc, my, dm, (int)(e1 - b < 32 ? e1 - b : 32), Qop, ldq, w, lane);
         }
+        round_finish<CG>(acc);
+        double* o = S + i * lds;
+        if constexpr (CG == 0) {
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
-            if (lane + 32 * q < w) S[i * lds + lane + 32 * q] += (double)acc[q];
+            for (int q = 0; q < 4; ++q)
+                if (lane + 32 * q < w) atomicAdd(o + lane + 32 * q, (double)acc[q]);
+        } else {
+            if (lane < w) atomicAdd(o + lane, (double)acc[0]);
+        }
     }
 }
 
@@ -243,7 +291,7 @@ __global__ void k_nmf_sign(const TS* __restrict__ src, int ldsrc, double* __rest
 // is held out iff the draw is below `rate` and the call is observed.  Per SNP:
 // sum |g - W_i.H_r|, sum |g - mean_r|, count.
 __global__ void __launch_bounds__(256) k_nmf_cv(const uint8_t* __restrict__ packed, uint64_t stride, uint64_t n,
-                                                uint64_t p, uint64_t chunk, uint64_t mask_seed, double rate,
+                                                uint64_t p, uint64_t chunk, uint64_t mask_seed, uint64_t thresh,
                                                 const float* __restrict__ W, const float* __restrict__ H, int k,
                                                 const int32_t* __restrict__ counts, double* __restrict__ part) {
     __shared__ float hs[8][kMaxNmfK];
@@ -263,7 +311,7 @@ __global__ void __launch_bounds__(256) k_nmf_cv(const uint8_t* __restrict__ pack
         for (uint64_t i = lane; i < n; i += 32) {
             const uint32_t code = code_at(row, i);
             if (code == 1u) continue;
-            if (uniform_at(key, col * n + i) < rate) {
+            if (draw_below(key, col * n + i, thresh)) {
                 const double g = code == 0 ? 0.0 : (double)(code - 1);
                 e1 += fabs(g - (double)fill_dot(W + i * k, hs[wl], k));
                 e2 += fabs(g - cm);
@@ -304,7 +352,7 @@ __global__ void k_obs_base(const int32_t* __restrict__ counts, uint64_t p, uint6
 // kept observed calls of W+_i g, B = sum over missing and held-out calls of
 // W+_i.  One warp per SNP, two passes over its codes.
 __global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__ packed, uint64_t stride, uint64_t n,
-                                                     uint64_t p, uint64_t chunk, uint64_t seed, double rate,
+                                                     uint64_t p, uint64_t chunk, uint64_t seed, uint64_t thresh,
                                                      const float* __restrict__ W, const float* __restrict__ Wpt, int k,
                                                      const uint64_t* __restrict__ base, double* __restrict__ part) {
     __shared__ float hh[8][kMaxNmfK];
@@ -327,7 +375,7 @@ __global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__
             const bool obs = i < n && code != 1u;
             const unsigned bal = __ballot_sync(0xffffffffu, obs);
             bool held = false;
-            if (obs) held = uniform_at(key, before + __popc(bal & lt)) < rate;
+            if (obs) held = draw_below(key, before + __popc(bal & lt), thresh);
             before += __popc(bal);
             if (i < n) {
                 const float* wp = Wpt + i * k;
@@ -369,7 +417,7 @@ __global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__
             const uint32_t code = i < n ? code_at(row, i) : 1u;
             const bool obs = i < n && code != 1u;
             const unsigned bal = __ballot_sync(0xffffffffu, obs);
-            if (obs && uniform_at(key, before + __popc(bal & lt)) < rate) {
+            if (obs && draw_below(key, before + __popc(bal & lt), thresh)) {
                 const double g = code == 0 ? 0.0 : (double)(code - 1);
                 e1 += fabs(g - (double)fill_dot(W + i * k, hh[wl], k));
                 e2 += fabs(g - mu);
@@ -389,6 +437,13 @@ __global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__
 
 }  // namespace
 
+// ceil(rate 2^53), the integer threshold of draw_below
+static uint64_t rate_threshold(double rate) {
+    if (!(rate > 0.0)) return 0;
+    if (rate >= 1.0) return 1ull << 53;
+    return (uint64_t)std::ceil(std::ldexp(rate, 53));
+}
+
 void launch_fill_stats(Ctx& c, const Geno& g, int norm, const float* W, const float* H, int k, double* mean,
                        double* scale, double* tss, uint8_t* zero_var) {
     if (!g.p) return;
@@ -398,12 +453,31 @@ void launch_fill_stats(Ctx& c, const Geno& g, int norm, const float* W, const fl
     SLFMM_LAUNCHED(c, "k_fill_stats");
 }
 
+// narrow operand group size: the smallest of 8, 16, 32 that holds w, else 0
+static int narrow_group(int w) { return w <= 8 ? 8 : w <= 16 ? 16 : w <= 32 ? 32 : 0; }
+
 void launch_fill_row_correct(Ctx& c, const Geno& g, float* out, int ldo, int w, const float* Wop, int ldw,
                              const float* Wn, const float* H, int k, const double* mean, const double* scale) {
     if (!g.p || !w) return;
     SLFMM_REQUIRE(w <= 128 && k >= 1 && k <= kMaxNmfK, SLFMM_ERR_BAD_ARG, "NMF correction shape");
-    k_fill_row_correct<<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(out, ldo, g.p, w, g.miss_ptr.get(),
-                                                                   g.miss_idx.get(), Wop, ldw, Wn, H, k, mean, scale);
+    const unsigned grid = (unsigned)grid_for(c, g.p, 8);
+    switch (narrow_group(w)) {
+        case 8:
+            k_fill_row_correct<8><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, g.miss_ptr.get(), g.miss_idx.get(),
+                                                              Wop, ldw, Wn, H, k, mean, scale);
+            break;
+        case 16:
+            k_fill_row_correct<16><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, g.miss_ptr.get(), g.miss_idx.get(),
+                                                               Wop, ldw, Wn, H, k, mean, scale);
+            break;
+        case 32:
+            k_fill_row_correct<32><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, g.miss_ptr.get(), g.miss_idx.get(),
+                                                               Wop, ldw, Wn, H, k, mean, scale);
+            break;
+        default:
+            k_fill_row_correct<0><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, g.miss_ptr.get(), g.miss_idx.get(),
+                                                              Wop, ldw, Wn, H, k, mean, scale);
+    }
     SLFMM_LAUNCHED(c, "k_fill_row_correct");
 }
 
@@ -411,8 +485,27 @@ void launch_fill_col_correct(Ctx& c, const Geno& g, double* S, int lds, int w, c
                              const float* Wn, const float* H, int k, const double* mean, const double* scale) {
     if (!g.n || !w) return;
     SLFMM_REQUIRE(w <= 128 && k >= 1 && k <= kMaxNmfK, SLFMM_ERR_BAD_ARG, "NMF correction shape");
-    k_fill_col_correct<<<grid_for(c, g.n, 8), 256, 0, c.stream>>>(S, lds, g.n, w, g.missT_ptr.get(),
-                                                                   g.missT_idx.get(), Qop, ldq, Wn, H, k, mean, scale);
+    const uint64_t nseg = std::max<uint64_t>(1, ceil_div(g.missT_max, kColSeg));
+    const unsigned grid = (unsigned)grid_for(c, g.n * nseg, 8);
+    const uint64_t* cp = g.missT_ptr.get();
+    const uint32_t* ci = g.missT_idx.get();
+    switch (narrow_group(w)) {
+        case 8:
+            k_fill_col_correct<8><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, mean,
+                                                              scale);
+            break;
+        case 16:
+            k_fill_col_correct<16><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, mean,
+                                                               scale);
+            break;
+        case 32:
+            k_fill_col_correct<32><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, mean,
+                                                               scale);
+            break;
+        default:
+            k_fill_col_correct<0><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, mean,
+                                                              scale);
+    }
     SLFMM_LAUNCHED(c, "k_fill_col_correct");
 }
 
@@ -457,8 +550,8 @@ void launch_nmf_clamp0_f32(Ctx& c, const float* src, int ld, double* X, uint64_t
 void launch_nmf_cv(Ctx& c, const Geno& g, uint64_t chunk, uint64_t mask_seed, double rate, const float* W,
                    const float* H, int k, double* part) {
     if (!g.p) return;
-    k_nmf_cv<<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(g.packed.get(), g.stride, g.n, g.p, chunk, mask_seed, rate, W,
-                                                         H, k, g.counts.get(), part);
+    k_nmf_cv<<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(g.packed.get(), g.stride, g.n, g.p, chunk, mask_seed,
+                                                         rate_threshold(rate), W, H, k, g.counts.get(), part);
     SLFMM_LAUNCHED(c, "k_nmf_cv");
 }
 
@@ -469,8 +562,8 @@ void launch_nmf_gwas_cv(Ctx& c, const Geno& g, uint64_t chunk, uint64_t seed, do
     const uint64_t nchunks = ceil_div(g.p, chunk);
     k_obs_base<<<grid_for(c, nchunks, 64), 64, 0, c.stream>>>(g.counts.get(), g.p, chunk, base.get());
     SLFMM_LAUNCHED(c, "k_obs_base");
-    k_nmf_gwas_cv<<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(g.packed.get(), g.stride, g.n, g.p, chunk, seed, rate, W,
-                                                              Wpt, k, base.get(), part);
+    k_nmf_gwas_cv<<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(g.packed.get(), g.stride, g.n, g.p, chunk, seed,
+                                                              rate_threshold(rate), W, Wpt, k, base.get(), part);
     SLFMM_LAUNCHED(c, "k_nmf_gwas_cv");
 }
 

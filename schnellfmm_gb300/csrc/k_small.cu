@@ -696,10 +696,32 @@ void launch_colmeans(Ctx& c, const double* A, uint64_t m, int a, int lda, double
     SLFMM_LAUNCHED(c, "k_colmeans");
 }
 
+// column sums of a tall matrix: row ranges of `per` rows in parallel, then
+// the partials summed in order
+__global__ void k_colsum_split(const double* __restrict__ A, uint64_t m, int a, int lda, uint64_t per,
+                               double* __restrict__ part) {
+    __shared__ double red[32];
+    const int col = blockIdx.x;
+    const uint64_t r0 = (uint64_t)blockIdx.y * per, r1 = min(m, r0 + per);
+    double s = 0.0;
+    for (uint64_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) s += A[i * lda + col];
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) part[(uint64_t)blockIdx.y * a + col] = s;
+}
+
 void launch_colsums(Ctx& c, const double* A, uint64_t m, int a, int lda, double* out) {
     if (a == 0) return;
-    k_colmeans<<<a, 256, 0, c.stream>>>(A, m, lda, out, 0);
-    SLFMM_LAUNCHED(c, "k_colsums");
+    if (m <= 65536) {
+        k_colmeans<<<a, 256, 0, c.stream>>>(A, m, lda, out, 0);
+        SLFMM_LAUNCHED(c, "k_colsums");
+        return;
+    }
+    const uint64_t splits = std::min<uint64_t>(ceil_div(m, 16384), 512);
+    const uint64_t per = ceil_div(m, splits);
+    DBuf<double> part(splits * a, c.stream);
+    k_colsum_split<<<dim3(a, (unsigned)splits), 256, 0, c.stream>>>(A, m, a, lda, per, part.get());
+    SLFMM_LAUNCHED(c, "k_colsum_split");
+    launch_sum_partials(c, part.get(), (int)splits, (uint64_t)a, out);
 }
 
 void launch_sum_partials(Ctx& c, const double* part, int splits, uint64_t count, double* out) {

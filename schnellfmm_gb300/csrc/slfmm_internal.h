@@ -113,6 +113,7 @@ struct Geno {
     mutable bool have_csc = false;
     mutable DBuf<uint64_t> missT_ptr;  // n+1, CSC by sample
     mutable DBuf<uint32_t> missT_idx;  // nnz SNP indices (ascending)
+    mutable uint64_t missT_max = 0;    // longest per-sample list
     // transposed copy (rows = samples, codes of every SNP), built on first use
     mutable bool have_T = false;
     mutable uint64_t strideT = 0;
