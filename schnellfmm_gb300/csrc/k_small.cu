@@ -518,30 +518,9 @@ __device__ void jacobi_sweeps(F* M, F* Vs, int a, int ap, F tol, int max_sweeps,
     }
 }
 
-__global__ void __launch_bounds__(1024) k_jacobi_svd(double* __restrict__ A, int a,
-                                                     double* __restrict__ V, double* __restrict__ sig) {
-    extern __shared__ double sm[];
-    const int ap = a + (a & 1);     // even number of columns (padded column is zero)
-    double* M = sm;                 // column-major ap x ap (rows a used)
-    double* Vs = sm + ap * ap;      // column-major
-    float* M32 = reinterpret_cast<float*>(Vs + ap * ap);
-    float* V32 = M32 + ap * ap;
-    __shared__ int rotated;
-    __shared__ double sg[64];
-    __shared__ double dots[64];
-    __shared__ int order[64];
+// classical Gram-Schmidt, twice, of the ap columns of column-major Vs (FP64)
+__device__ void gs_columns(double* Vs, int ap, double* dots) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-    // phase 1: FP32 sweeps
-    for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) {
-        const int col = e / ap, row = e % ap;
-        M32[e] = (row < a && col < a) ? (float)A[row * a + col] : 0.f;
-        V32[e] = (row == col) ? 1.f : 0.f;
-    }
-    __syncthreads();
-    jacobi_sweeps<float>(M32, V32, a, ap, 2.0e-6f, 30, &rotated);
-    // phase 2: V <- FP64 Gram-Schmidt (twice) of the FP32 rotations
-    for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) Vs[e] = (double)V32[e];
-    __syncthreads();
     for (int j = 0; j < ap; ++j) {
         double* vj = Vs + j * ap;
         for (int pass = 0; pass < 2; ++pass) {
@@ -569,7 +548,49 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(double* __restrict__ A, int
         }
         __syncthreads();
     }
-    // phase 3: M = A V in FP64, then FP64 sweeps from there
+}
+
+// Eigen-decomposition of a symmetric positive semi-definite a x a matrix
+// (a <= 64; the Gram matrices of Step 0, the RSVD and the NMF probe) in one
+// CTA: A V = V diag(sig), sig descending, V orthonormal; A is overwritten by V
+// (its left singular vectors).
+//
+// GB300 runs FP64 at a small fraction of its FP32 rate, so the rotations run
+// as FP32 one-sided Jacobi sweeps (pairs in parallel, round-robin order, one
+// warp per pair) to ~1e-6; V is re-orthonormalised in FP64 (Gram-Schmidt,
+// twice), B = V^T A V formed in FP64, and one first-order step
+// V <- V (I + E), E_ij = B_ij / (B_jj - B_ii), removes the remaining
+// off-diagonal part to second order before a final Gram-Schmidt.  Pairs with
+// (numerically) equal eigenvalues are not mixed: any basis of their span is
+// an eigenbasis.  Eigenvalues are v_j^T A v_j of the final vectors.
+__global__ void __launch_bounds__(1024) k_jacobi_svd(double* __restrict__ A, int a,
+                                                     double* __restrict__ V, double* __restrict__ sig) {
+    extern __shared__ double sm[];
+    const int ap = a + (a & 1);     // even number of columns (padded column is zero)
+    double* M = sm;                 // column-major ap x ap scratch
+    double* Vs = sm + ap * ap;      // column-major eigenvectors
+    float* M32 = reinterpret_cast<float*>(Vs + ap * ap);
+    float* V32 = M32 + ap * ap;
+    double* B = reinterpret_cast<double*>(M32);  // reuses the FP32 area after phase 1
+    __shared__ int rotated;
+    __shared__ double sg[64];
+    __shared__ double dots[64];
+    __shared__ double bmax;
+    __shared__ int order[64];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
+    // phase 1: FP32 sweeps
+    for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) {
+        const int col = e / ap, row = e % ap;
+        M32[e] = (row < a && col < a) ? (float)A[row * a + col] : 0.f;
+        V32[e] = (row == col) ? 1.f : 0.f;
+    }
+    __syncthreads();
+    jacobi_sweeps<float>(M32, V32, a, ap, 2.0e-6f, 30, &rotated);
+    // phase 2: FP64 orthonormal V
+    for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) Vs[e] = (double)V32[e];
+    __syncthreads();
+    gs_columns(Vs, ap, dots);
+    // phase 3: T = A V (in M), B = V^T T (over the FP32 area)
     for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) {
         const int col = e / ap, row = e % ap;
         double t = 0.0;
@@ -578,14 +599,46 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(double* __restrict__ A, int
         M[e] = t;
     }
     __syncthreads();
-    // convergence: |<a_p, a_q>| <= tol * ||a_p|| ||a_q|| for every pair
-    jacobi_sweeps<double>(M, Vs, a, ap, 4.0e-16 * (double)(a > 8 ? a : 8), 40, &rotated);
-    // singular values and descending order
-    for (int cc = warp; cc < a; cc += nwarps) {
+    for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) {
+        const int col = e / ap, row = e % ap;
+        double t = 0.0;
+        for (int k = 0; k < ap; ++k) t += Vs[row * ap + k] * M[col * ap + k];
+        B[e] = t;  // B[col * ap + row] = v_row^T A v_col
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double m = 0.0;
+        for (int j = 0; j < ap; ++j) m = fmax(m, fabs(B[j * ap + j]));
+        bmax = m;
+    }
+    __syncthreads();
+    // phase 4: V <- V (I + E), into M
+    const double gap_tol = 1e-9 * bmax + 1e-300;
+    for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) {
+        const int col = e / ap, row = e % ap;   // new V[row, col]
+        double t = Vs[col * ap + row];
+        const double bjj = B[col * ap + col];
+        for (int i = 0; i < ap; ++i) {
+            if (i == col) continue;
+            const double gap = bjj - B[i * ap + i];
+            if (fabs(gap) > gap_tol) t += Vs[i * ap + row] * (B[col * ap + i] / gap);
+        }
+        M[e] = t;
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) Vs[e] = M[e];
+    __syncthreads();
+    gs_columns(Vs, ap, dots);
+    // phase 5: eigenvalues v_j^T A v_j, descending order
+    for (int cc = warp; cc < ap; cc += nwarps) {
         double s = 0.0;
-        for (int r = lane; r < a; r += 32) s += M[cc * ap + r] * M[cc * ap + r];
+        for (int r = lane; r < a; r += 32) {
+            double t = 0.0;
+            for (int k = 0; k < a; ++k) t += A[r * a + k] * Vs[cc * ap + k];
+            s += Vs[cc * ap + r] * t;
+        }
         s = warp_sum(s);
-        if (lane == 0) sg[cc] = sqrt(s);
+        if (lane == 0) sg[cc] = fabs(s);
     }
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -600,11 +653,10 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(double* __restrict__ A, int
     __syncthreads();
     for (int e = threadIdx.x; e < a * a; e += blockDim.x) {
         const int row = e / a, cc = e % a;
-        const int src = order[cc];
-        V[row * a + cc] = Vs[src * ap + row];
-        const double s = sg[src];
-        A[row * a + cc] = s > 0.0 ? M[src * ap + row] / s : 0.0;
+        V[row * a + cc] = Vs[order[cc] * ap + row];
     }
+    __syncthreads();
+    for (int e = threadIdx.x; e < a * a; e += blockDim.x) A[e] = V[e];
     for (int cc = threadIdx.x; cc < a; cc += blockDim.x) sig[cc] = sg[order[cc]];
 }
 
