@@ -112,8 +112,16 @@ bool is_pinned(const void* p) {
 // ---------------------------------------------------------------------------
 // ingest: host payload -> resident packed matrix
 // ---------------------------------------------------------------------------
+// Work run on each chunk of rows [r0, r1) right after it lands (tiles,
+// counts and missing-call offsets of the chunk are ready).
+struct ChunkHook {
+    virtual void rows(Ctx& c, const Geno& g, uint64_t r0, uint64_t r1) = 0;
+    virtual ~ChunkHook() = default;
+};
+
 void upload_geno(Ctx& c, Geno& g, const uint8_t* packed, uint64_t n_phys, uint64_t n_snps,
-                 const uint64_t* keep, uint64_t n_keep, const std::vector<uint64_t>& snps) {
+                 const uint64_t* keep, uint64_t n_keep, const std::vector<uint64_t>& snps,
+                 ChunkHook* hook = nullptr) {
     SLFMM_REQUIRE(packed != nullptr || n_snps == 0, SLFMM_ERR_BAD_ARG, "null genotype payload");
     SLFMM_REQUIRE(n_phys > 0, SLFMM_ERR_BAD_ARG, "no samples");
     const uint64_t bps = ceil_div(n_phys, 4);
@@ -135,12 +143,19 @@ void upload_geno(Ctx& c, Geno& g, const uint8_t* packed, uint64_t n_phys, uint64
         sync(c);
     }
     if (g.p) {
-        // staging: ~64 MiB per chunk, two device buffers, two pinned buffers
-        // split-FP8 contexts build the tile-major copies chunk by chunk as the
-        // rows land (chunks then start on 128-row tiles)
+        // staging: ~64 MiB (at most 256 Ki rows) per chunk, two device
+        // buffers, two pinned buffers.  Split-FP8 contexts build the
+        // tile-major copies chunk by chunk as the rows land (chunks then start
+        // on 128-row tiles); every context builds the per-SNP missing-call
+        // lists the same way.  The copies are bound by the host link, so this
+        // work hides behind them.
         const bool tiles = c.precision == SLFMM_PREC_SPLIT_FP8;
-        uint64_t rows_per = std::max<uint64_t>(1, std::min<uint64_t>(g.p, (64ull << 20) / bps));
+        uint64_t rows_per = std::max<uint64_t>(1, std::min<uint64_t>({g.p, (64ull << 20) / bps, 1ull << 18}));
         if (tiles) rows_per = std::max<uint64_t>(128, rows_per / 128 * 128);
+        g.miss_ptr.alloc(g.p + 1, c.stream);
+        SLFMM_CUDA(cudaMemsetAsync(g.miss_ptr.get(), 0, sizeof(uint64_t), c.stream));
+        uint64_t cap = 0;  // index capacity, sized from the first chunk's density
+        uint64_t first_end = 0;
         const bool direct = is_pinned(packed);
         DBuf<uint8_t> dstage[2];
         dstage[0].alloc(rows_per * bps, c.stream);
@@ -193,12 +208,39 @@ void upload_geno(Ctx& c, Geno& g, const uint8_t* packed, uint64_t n_phys, uint64
                                            c.copy_stream));
             }
             SLFMM_CUDA(cudaEventRecord(copied[b], c.copy_stream));
+            if (ch == 1) {
+                // the first chunk's list length sizes the index array (the
+                // second chunk's copy is already in flight); 1.5x its density
+                // plus slack, and a chunk that overruns it leaves the lists
+                // to be rebuilt after the upload
+                const uint64_t nnz0 = fetch(c, g.miss_ptr.get() + first_end, 1)[0];
+                const double est = (double)nnz0 * (double)g.p / (double)first_end;
+                cap = (uint64_t)(1.5 * est) + g.p + 4096;
+                g.miss_idx.alloc(cap, c.stream);
+                csr_chunk_fill(c, g, 0, first_end, cap);
+            }
             SLFMM_CUDA(cudaStreamWaitEvent(c.stream, copied[b], 0));
             launch_repack(c, dstage[b].get(), rows, bps, n_phys, keep_d.get(), g.n,
                           g.packed.get() + r0 * g.stride, g.stride);
             SLFMM_CUDA(cudaEventRecord(consumed[b], c.stream));
             launch_snp_counts_range(c, g, r0, rows);
             if (tiles) tile_chunk(c, g, r0, r1, ch + 1 == nchunks);
+            csr_chunk_offsets(c, g, r0, rows);
+            if (ch == 0) first_end = r1;
+            else csr_chunk_fill(c, g, r0, rows, cap);
+            if (hook) hook->rows(c, g, r0, r1);
+        }
+        const uint64_t nnz = fetch(c, g.miss_ptr.get() + g.p, 1)[0];
+        if (nchunks == 1) {
+            cap = std::max<uint64_t>(nnz, 1);
+            g.miss_idx.alloc(cap, c.stream);
+            csr_chunk_fill(c, g, 0, g.p, cap);
+        }
+        if (nnz <= cap) {
+            g.nnz = nnz;
+            g.have_csr = true;
+        } else {
+            g.miss_idx.release();  // rebuilt on first use
         }
         SLFMM_CUDA(cudaStreamSynchronize(c.stream));
         SLFMM_CUDA(cudaStreamSynchronize(c.copy_stream));
@@ -240,25 +282,74 @@ void std_mean(Ctx& c, const Geno& g, int norm, SnpStd& s) {
 // ---------------------------------------------------------------------------
 int pad16(int w) { return (int)round_up((uint64_t)w, 16); }
 
+// Split-FP8 operand of a SNP-row pass with the missing-call indicator: 4 + 3
+// scaled E4M3 terms of W (n x w FP64) and its column sums.  The epilogue then
+// applies out = s_j (P - mu_j (cs - M)) in the same kernel.  ok is false when
+// the width leaves no indicator plan (too wide for TMEM) or it is switched off.
+struct Fp8RowOperand {
+    bool ok = false;
+    Fp8Plan pl{};
+    int wp = 0;
+    uint64_t n_pad = 0;
+    DBuf<uint8_t> B;
+    DBuf<float> isc;
+    DBuf<double> cs;
+};
+
+bool fp8_row_operand(Ctx& c, uint64_t n, uint64_t tiles, const double* W, int w, int ldw, Fp8RowOperand& op) {
+    op.wp = pad16(w);
+    op.n_pad = round_up(n, 256);  // whole split-FP8 stages (256 codes)
+    const char* ind_env = std::getenv("SLFMM_TC8_ROW_IND");
+    if (op.wp > kMaxW || (ind_env && ind_env[0] == '0')) return false;
+    op.pl = fp8_plan(op.wp, true, tiles);
+    if (!op.pl.ok || op.pl.n_ind == 0) return false;
+    op.cs.alloc(op.wp, c.stream);
+    op.cs.zero();
+    launch_colsums(c, W, n, w, ldw, op.cs.get());
+    op.B.alloc((uint64_t)op.pl.n_total * op.n_pad, c.stream);
+    op.isc.alloc(op.pl.n_total, c.stream);
+    launch_fp8_terms_f64(c, W, ldw, n, w, op.wp, op.n_pad, nullptr, 4, 0, op.B.get(), op.isc.get());
+    launch_fp8_terms_f64(c, W, ldw, n, w, op.wp, op.n_pad, nullptr, 3, (int)op.pl.n_main, op.B.get(), op.isc.get());
+    op.ok = true;
+    return true;
+}
+
+// out rows [r0, r0 + rows) of a row pass with an indicator operand; err_dev
+// non-null defers the bounded-wait check to the caller
+void fp8_row_launch(Ctx& c, const Geno& g, const SnpStd& s, const Fp8RowOperand& op, uint64_t r0, uint64_t rows,
+                    float* out, int* err_dev) {
+    const uint64_t t0 = r0 / 128;
+    const TileView tv{g.tiles.get() + t0 * g.kbt * 4096, g.kbt, g.ntiles - t0};
+    launch_tc8_rows(c, op.pl, tv, rows, g.n, op.B.get(), op.isc.get(), op.n_pad, 1, s.mean.get() + r0,
+                    s.scale.get() + r0, op.cs.get(), out + r0 * op.wp, op.wp, 1, 0, err_dev);
+}
+
 // out (p x wp, FP32) = Y_hat^T W, W = n x w FP64 (leading dim ldw)
 void row_contract_base(Ctx& c, const Geno& g, const SnpStd& s, const double* W, int w, int ldw,
                        DBuf<float>& out, int& wp) {
     wp = pad16(w);
     SLFMM_REQUIRE(wp <= kMaxW, SLFMM_ERR_BAD_ARG, "operand wider than 128 columns");
     const uint64_t n_pad = round_up(g.n, 256);  // whole split-FP8 stages (256 codes)
-    DBuf<float> W32(n_pad * wp, c.stream);
-    launch_f64_to_f32_pad(c, W, g.n, w, ldw, W32.get(), n_pad, wp);
     out.alloc(std::max<uint64_t>(g.p, 1) * wp, c.stream);
     const double bytes = (double)g.p * ceil_div(g.n, 4) + (double)g.p * w * 4 + (double)g.n * w * 4;
     if (c.precision == SLFMM_PREC_SPLIT_FP8) {
         // exact E4M3 genotypes x 4 scaled E4M3 terms of W; with the missing-call
         // indicator operand the epilogue applies out = s_j (P - mu_j (cs - M)).
-        // Operands too wide for TMEM run as column blocks of 64.
+        // Operands too wide for TMEM run as column blocks of 64 and a
+        // per-SNP fix over the missing-call lists.
         const uint64_t tiles = ceil_div(g.p, 128);
-        const char* ind_env = std::getenv("SLFMM_TC8_ROW_IND");
-        Fp8Plan pl = fp8_plan(wp, !(ind_env && ind_env[0] == '0'), tiles);
-        const bool ind = pl.ok && pl.n_ind != 0;
-        if (!ind) pl = fp8_plan(wp, false, tiles);
+        {
+            Fp8RowOperand op;
+            if (fp8_row_operand(c, g.n, tiles, W, w, ldw, op)) {
+                build_tiles(c, g, false);
+                ProfScope ps(c, "row_contract", bytes, 2.0 * g.n * g.p * w);
+                fp8_row_launch(c, g, s, op, 0, g.p, out.get(), nullptr);
+                return;
+            }
+        }
+        DBuf<float> W32(n_pad * wp, c.stream);
+        launch_f64_to_f32_pad(c, W, g.n, w, ldw, W32.get(), n_pad, wp);
+        const Fp8Plan pl = fp8_plan(wp, false, tiles);
         const int cb = pl.ok ? wp : 64;
         DBuf<double> cs(wp, c.stream);
         cs.zero();
@@ -271,19 +362,17 @@ void row_contract_base(Ctx& c, const Geno& g, const SnpStd& s, const double* W, 
             DBuf<uint8_t> B((uint64_t)pb.n_total * n_pad, c.stream);
             DBuf<float> isc(pb.n_total, c.stream);
             launch_fp8_terms_f64(c, W + c0, ldw, g.n, wb, bp, n_pad, nullptr, 4, 0, B.get(), isc.get());
-            if (ind) launch_fp8_terms_f64(c, W + c0, ldw, g.n, wb, bp, n_pad, nullptr, 3, (int)pb.n_main, B.get(),
-                                          isc.get());
             ProfScope ps(c, "row_contract", bytes * wb / w, 2.0 * g.n * g.p * wb);
-            launch_tc8_rows(c, pb, tv, g.p, g.n, B.get(), isc.get(), n_pad, ind ? 1 : 0,
-                            s.mean.get(), s.scale.get(), cs.get(), out.get() + c0, wp, 1, 0);
+            launch_tc8_rows(c, pb, tv, g.p, g.n, B.get(), isc.get(), n_pad, 0, s.mean.get(), s.scale.get(),
+                            cs.get(), out.get() + c0, wp, 1, 0);
         }
-        if (!ind) {
-            build_missing_lists(c, g);
-            launch_rowfix_mean(c, out.get(), wp, g.p, w, g.miss_ptr.get(), g.miss_idx.get(), W32.get(), wp,
-                               cs.get(), s.mean.get(), s.scale.get());
-        }
+        build_missing_lists(c, g);
+        launch_rowfix_mean(c, out.get(), wp, g.p, w, g.miss_ptr.get(), g.miss_idx.get(), W32.get(), wp, cs.get(),
+                           s.mean.get(), s.scale.get());
         return;
     }
+    DBuf<float> W32(n_pad * wp, c.stream);
+    launch_f64_to_f32_pad(c, W, g.n, w, ldw, W32.get(), n_pad, wp);
     if (tc_available(c)) {
         // exact genotypes x (hi + lo) BF16 split of W on the tensor cores, then
         // out = s_j (P - mu_j (colsum(W) - sum_{missing} W))
@@ -556,20 +645,37 @@ void cholqr2_f64(Ctx& c, double* A, uint64_t m, int a, int ld) {
 // randomized SVD (src/rsvd.rs:26-177), thin form: sketch P Omega, forward
 // passes P (Y Q_z), U_hat = P^-1 U(P Y Q_z)[:, :K]
 // ---------------------------------------------------------------------------
-void rsvd(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, int K, int l, int q,
-          uint64_t seed, const double* omega_host, DBuf<double>& u_hat) {
-    const uint64_t n = g.n;
-    SLFMM_REQUIRE(l <= 64, SLFMM_ERR_BAD_ARG, "K + oversampling must be <= 64");
-    SLFMM_REQUIRE(g.p >= (uint64_t)l, SLFMM_ERR_BAD_ARG, "fewer estimation SNPs than K + oversampling");
-    SLFMM_REQUIRE(n >= (uint64_t)l, SLFMM_ERR_BAD_ARG, "fewer samples than K + oversampling");
-    DBuf<double> W(n * l, c.stream);
+// the sketch operand P Omega (n x l), centred
+void sketch_operand(Ctx& c, const Step0& s0, uint64_t n, int l, uint64_t seed, const double* omega_host,
+                    DBuf<double>& W) {
+    W.alloc(n * l, c.stream);
     if (omega_host) h2d(c, W.get(), omega_host, n * l);
     else launch_normal(c, seed, n, l, W.get());
     apply_p(c, s0, W.get(), l, l, false);                    // M^T Omega analogue (:51)
     center_columns(c, W.get(), n, l, l);
+}
+
+void rsvd_checks(uint64_t n, uint64_t p, int l) {
+    SLFMM_REQUIRE(l <= 64, SLFMM_ERR_BAD_ARG, "K + oversampling must be <= 64");
+    SLFMM_REQUIRE(p >= (uint64_t)l, SLFMM_ERR_BAD_ARG, "fewer estimation SNPs than K + oversampling");
+    SLFMM_REQUIRE(n >= (uint64_t)l, SLFMM_ERR_BAD_ARG, "fewer samples than K + oversampling");
+}
+
+// Z_pre: the sketch Y_hat^T P Omega already computed (p x pad16(l), FP32)
+void rsvd(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, int K, int l, int q,
+          uint64_t seed, const double* omega_host, DBuf<double>& u_hat, DBuf<float>* Z_pre = nullptr) {
+    const uint64_t n = g.n;
+    rsvd_checks(n, g.p, l);
     DBuf<float> Z;
     int wp = 0;
-    row_contract(c, g, st, W.get(), l, l, Z, wp);           // sketch (:56-72)
+    if (Z_pre) {
+        Z = std::move(*Z_pre);
+        wp = pad16(l);
+    } else {
+        DBuf<double> W;
+        sketch_operand(c, s0, n, l, seed, omega_host, W);
+        row_contract(c, g, st, W.get(), l, l, Z, wp);       // sketch (:56-72)
+    }
     cholqr2_f32(c, Z.get(), g.p, l, wp);                     // QR (:75)
     for (int it = 0; it < q; ++it) {
         DBuf<double> S;
@@ -891,13 +997,56 @@ void check_cfg(const slfmm_config* cfg) {
                   "unknown imputation strategy");
 }
 
+// The sketch pass of the randomized SVD run on each chunk of an upload as it
+// lands: the chunk's SNP statistics, then Y_hat^T (P Omega) for its rows.
+// The operands and kernels are those of the pass after the upload, so the
+// sketch is identical; it only moves under the host-link-bound copies.
+struct Presketch : ChunkHook {
+    Step0 s0;
+    SnpStd se;
+    int norm = 0, l = 0;
+    Fp8RowOperand op;
+    DBuf<float> Z;
+    DBuf<int> err;
+    void rows(Ctx& c, const Geno& g, uint64_t r0, uint64_t r1) override {
+        launch_stats_mean_range(c, g, r0, r1 - r0, norm, se.mean.get(), se.scale.get(), se.tss.get(),
+                                se.zero_var.get());
+        fp8_row_launch(c, g, se, op, r0, r1 - r0, Z.get(), err.get());
+    }
+};
+
+// true when the estimation and testing matrices are the same upload of p SNPs
+// with mean imputation and the sketch width has an indicator plan
+bool presketch_prepare(Ctx& c, uint64_t n, uint64_t p, const double* x, int d, const slfmm_config* cfg,
+                       const double* omega, Presketch& ps) {
+    if (c.precision != SLFMM_PREC_SPLIT_FP8 || cfg->impute != SLFMM_IMPUTE_MEAN || p == 0) return false;
+    check_cfg(cfg);
+    ps.l = (int)cfg->k + (int)cfg->oversampling;
+    if (ps.l > 64 || p < (uint64_t)ps.l || n < (uint64_t)ps.l) return false;  // the fit reports these
+    step0(c, x, n, d, cfg->lambda, cfg->scale_cov != 0, ps.s0);
+    DBuf<double> W;
+    sketch_operand(c, ps.s0, n, ps.l, cfg->seed, omega, W);
+    if (!fp8_row_operand(c, n, ceil_div(p, 128), W.get(), ps.l, ps.l, ps.op)) return false;
+    ps.norm = cfg->norm;
+    ps.se.mean.alloc(p, c.stream);
+    ps.se.scale.alloc(p, c.stream);
+    ps.se.tss.alloc(p, c.stream);
+    ps.se.zero_var.alloc(p, c.stream);
+    ps.Z.alloc(p * ps.op.wp, c.stream);
+    ps.err.alloc(1, c.stream);
+    ps.err.zero();
+    return true;
+}
+
 void fit_impl(Ctx& c, const Geno& ge, const Geno& gf, const double* x, int d, const slfmm_config* cfg,
-              const double* omega, slfmm_results* res) {
+              const double* omega, slfmm_results* res, Presketch* pre = nullptr) {
     check_cfg(cfg);
     SLFMM_REQUIRE(ge.n == gf.n, SLFMM_ERR_BAD_ARG, "estimation and testing genotypes have different sample counts");
-    Step0 s0;
-    step0(c, x, gf.n, d, cfg->lambda, cfg->scale_cov != 0, s0);
-    SnpStd se, sf;
+    Step0 s0_own;
+    Step0& s0 = pre ? pre->s0 : s0_own;
+    if (!pre) step0(c, x, gf.n, d, cfg->lambda, cfg->scale_cov != 0, s0);
+    SnpStd se_own, sf;
+    SnpStd& se = pre ? pre->se : se_own;
     const SnpStd* sfp = &se;
     // NMF state kept alive for the passes that read its fills
     NmfModel nmf;
@@ -934,7 +1083,12 @@ void fit_impl(Ctx& c, const Geno& ge, const Geno& gf, const double* x, int d, co
             res->nmf_gwas_cv_count = cnt;
         }
     } else {
-        std_mean(c, ge, cfg->norm, se);
+        if (pre) {
+            se.lut.alloc(ge.p * 4, c.stream);
+            launch_lut_std(c, ge.p, se.mean.get(), se.scale.get(), se.lut.get());
+        } else {
+            std_mean(c, ge, cfg->norm, se);
+        }
         if (&ge != &gf) {
             std_mean(c, gf, cfg->norm, sf);
             sfp = &sf;
@@ -942,7 +1096,7 @@ void fit_impl(Ctx& c, const Geno& ge, const Geno& gf, const double* x, int d, co
     }
     DBuf<double> u_hat;
     const int K = (int)cfg->k, l = K + (int)cfg->oversampling;
-    rsvd(c, ge, se, s0, K, l, (int)cfg->n_power_iter, cfg->seed, omega, u_hat);
+    rsvd(c, ge, se, s0, K, l, (int)cfg->n_power_iter, cfg->seed, omega, u_hat, pre ? &pre->Z : nullptr);
     if (res && res->u_hat) d2h(c, res->u_hat, u_hat.get(), gf.n * K);
     AssocOut out{res ? res->beta : nullptr, res ? res->tstat : nullptr, res ? res->pvalue : nullptr,
                  res ? res->r2 : nullptr, res ? res->gif_per_trait : nullptr, 0.0};
@@ -1213,13 +1367,23 @@ int slfmm_fit_host(slfmm_ctx* c, const uint8_t* packed, uint64_t n_physical, uin
     API_TRY
     SLFMM_CUDA(cudaSetDevice(c->device));
     Geno full, sub;
-    upload_geno(*c, full, packed, n_physical, n_snps, sample_keep, n_keep, subset_indices(nullptr, n_snps));
+    const bool all = !est || est->kind == SLFMM_SUBSET_ALL;
+    // with every SNP in the estimation, the sketch pass runs under the upload
+    Presketch ps;
+    const bool pre = all && cfg && presketch_prepare(*c, sample_keep ? n_keep : n_physical, n_snps, x, (int)d, cfg,
+                                                     omega, ps);
+    upload_geno(*c, full, packed, n_physical, n_snps, sample_keep, n_keep, subset_indices(nullptr, n_snps),
+                pre ? &ps : nullptr);
+    if (pre) {
+        const int e = fetch(*c, ps.err.get(), 1)[0];
+        if (e) throw_tc8_timeout(e);
+    }
     const Geno* ge = &full;
-    if (est && est->kind != SLFMM_SUBSET_ALL) {
+    if (!all) {
         upload_geno(*c, sub, packed, n_physical, n_snps, sample_keep, n_keep, subset_indices(est, n_snps));
         ge = &sub;
     }
-    fit_impl(*c, *ge, full, x, (int)d, cfg, omega, res);
+    fit_impl(*c, *ge, full, x, (int)d, cfg, omega, res, pre ? &ps : nullptr);
     API_CATCH(c)
 }
 

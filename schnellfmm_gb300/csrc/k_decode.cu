@@ -90,10 +90,11 @@ __global__ void k_snp_counts(const uint8_t* __restrict__ packed, uint64_t p, uin
     }
 }
 
-// One warp per SNP: write the ascending sample indices of missing calls.
+// One warp per SNP: write the ascending sample indices of missing calls
+// (positions at or beyond cap are not written).
 __global__ void k_miss_fill(const uint8_t* __restrict__ packed, uint64_t p, uint64_t stride,
                             uint64_t n, const uint64_t* __restrict__ ptr,
-                            uint32_t* __restrict__ idx, uint32_t* __restrict__ rowid) {
+                            uint32_t* __restrict__ idx, uint32_t* __restrict__ rowid, uint64_t cap) {
     const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
     const int lane = threadIdx.x & 31;
     if (warp >= p) return;
@@ -119,11 +120,60 @@ __global__ void k_miss_fill(const uint8_t* __restrict__ packed, uint64_t p, uint
         while (m) {
             const int b = __ffs(m) - 1;
             m &= m - 1;
-            idx[pos] = (uint32_t)(w * 16 + (b >> 1));
-            if (rowid) rowid[pos] = (uint32_t)warp;
+            if (pos < cap) {
+                idx[pos] = (uint32_t)(w * 16 + (b >> 1));
+                if (rowid) rowid[pos] = (uint32_t)warp;
+            }
             ++pos;
         }
         base += total;
+    }
+}
+
+// List offsets of rows [0, rows) of an upload chunk from their missing-call
+// counts (counts[4 r + 3]): ptr[r + 1] = ptr[0] + sum of the counts of rows
+// 0..r, where ptr[0] holds the previous chunk's end.  One block of 1024
+// threads walks the chunk in tiles of 4096 rows with a running carry.
+__global__ void __launch_bounds__(1024) k_miss_ptr_chunk(const int32_t* __restrict__ counts, uint64_t rows,
+                                                         uint64_t* __restrict__ ptr) {
+    __shared__ uint64_t warp_sum[32];
+    const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+    uint64_t carry = ptr[0];
+    for (uint64_t base = 0; base < rows; base += 4096) {
+        uint64_t v[4], s = 0;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint64_t r = base + (uint64_t)t * 4 + k;
+            v[k] = r < rows ? (uint64_t)counts[r * 4 + 3] : 0ull;
+            s += v[k];
+        }
+        uint64_t incl = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += y;
+        }
+        if (lane == 31) warp_sum[wid] = incl;
+        __syncthreads();
+        if (wid == 0) {
+            uint64_t ws = warp_sum[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint64_t y = __shfl_up_sync(0xffffffffu, ws, o);
+                if (lane >= o) ws += y;
+            }
+            warp_sum[lane] = ws;  // inclusive over warps
+        }
+        __syncthreads();
+        uint64_t run = carry + (wid ? warp_sum[wid - 1] : 0ull) + incl - s;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const uint64_t r = base + (uint64_t)t * 4 + k;
+            run += v[k];
+            if (r < rows) ptr[r + 1] = run;
+        }
+        carry += warp_sum[31];
+        __syncthreads();  // warp_sum is rewritten by the next tile
     }
 }
 
@@ -254,10 +304,24 @@ void build_missing_lists(Ctx& c, const Geno& g) {
     if (nnz && g.p) {
         const int block = 256;
         k_miss_fill<<<(unsigned)ceil_div(g.p * 32, block), block, 0, c.stream>>>(
-            g.packed.get(), g.p, g.stride, g.n, g.miss_ptr.get(), g.miss_idx.get(), nullptr);
+            g.packed.get(), g.p, g.stride, g.n, g.miss_ptr.get(), g.miss_idx.get(), nullptr, ~0ull);
         SLFMM_LAUNCHED(c, "k_miss_fill");
     }
     g.have_csr = true;
+}
+
+void csr_chunk_offsets(Ctx& c, const Geno& g, uint64_t r0, uint64_t rows) {
+    if (rows == 0) return;
+    k_miss_ptr_chunk<<<1, 1024, 0, c.stream>>>(g.counts.get() + r0 * 4, rows, g.miss_ptr.get() + r0);
+    SLFMM_LAUNCHED(c, "k_miss_ptr_chunk");
+}
+
+void csr_chunk_fill(Ctx& c, const Geno& g, uint64_t r0, uint64_t rows, uint64_t cap) {
+    if (rows == 0 || cap == 0) return;
+    const int block = 256;
+    k_miss_fill<<<(unsigned)ceil_div(rows * 32, block), block, 0, c.stream>>>(
+        g.packed.get() + r0 * g.stride, rows, g.stride, g.n, g.miss_ptr.get() + r0, g.miss_idx.get(), nullptr, cap);
+    SLFMM_LAUNCHED(c, "k_miss_fill");
 }
 
 void build_missing_csc(Ctx& c, const Geno& g) {
@@ -271,7 +335,7 @@ void build_missing_csc(Ctx& c, const Geno& g) {
     DBuf<uint32_t> rowid(g.nnz, c.stream), keys_out(g.nnz, c.stream);
     const int block = 256;
     k_miss_fill<<<(unsigned)ceil_div(g.p * 32, block), block, 0, c.stream>>>(
-        g.packed.get(), g.p, g.stride, g.n, g.miss_ptr.get(), keys_out.get(), rowid.get());
+        g.packed.get(), g.p, g.stride, g.n, g.miss_ptr.get(), keys_out.get(), rowid.get(), ~0ull);
     SLFMM_LAUNCHED(c, "k_miss_fill");
     int end_bit = 1;
     while ((1ull << end_bit) < g.n) ++end_bit;
@@ -312,6 +376,14 @@ void launch_stats_mean(Ctx& c, const Geno& g, int norm, double* mean, double* sc
     if (g.p == 0) return;
     k_stats_mean<<<grid_for(c, g.p, 256), 256, 0, c.stream>>>(g.counts.get(), g.p, norm, mean,
                                                               scale, tss, zero_var);
+    SLFMM_LAUNCHED(c, "k_stats_mean");
+}
+
+void launch_stats_mean_range(Ctx& c, const Geno& g, uint64_t r0, uint64_t rows, int norm, double* mean,
+                             double* scale, double* tss, uint8_t* zero_var) {
+    if (rows == 0) return;
+    k_stats_mean<<<grid_for(c, rows, 256), 256, 0, c.stream>>>(g.counts.get() + r0 * 4, rows, norm, mean + r0,
+                                                               scale + r0, tss + r0, zero_var + r0);
     SLFMM_LAUNCHED(c, "k_stats_mean");
 }
 

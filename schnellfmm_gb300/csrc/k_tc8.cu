@@ -833,10 +833,15 @@ void launch_fp8_terms_f32(Ctx& c, const float* src, int ld, uint64_t K, int w, i
     SLFMM_LAUNCHED(c, "k_fp8_terms");
 }
 
+void throw_tc8_timeout(int site) {
+    throw Error(SLFMM_ERR_DEVICE_TIMEOUT,
+                "split-FP8 contraction: a bounded device wait expired (site " + std::to_string(site) + ")");
+}
+
 int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t rows, uint64_t K,
                      const uint8_t* B, const float* inv_scale, uint64_t K_pad, int mode, const double* row_mean,
                      const double* row_scale, const double* cs, float* out, int ldo, int splits,
-                     uint64_t split_stride) {
+                     uint64_t split_stride, int* err_dev) {
     SLFMM_REQUIRE(pl.ok, SLFMM_ERR_BAD_ARG, "no feasible split-FP8 tile plan for this width");
     SLFMM_REQUIRE(K_pad % kStageK == 0 && K_pad >= ceil_div(K, kStageK) * kStageK, SLFMM_ERR_BAD_ARG,
                   "bad K padding");
@@ -851,8 +856,11 @@ int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t rows
         configured = pl.smem;
     }
     const CUtensorMap tb = map2d_u8(B, K_pad, pl.n_total, 128, pl.box_rows, true);
-    DBuf<int> err(1, c.stream);
-    err.zero();
+    DBuf<int> err;
+    if (!err_dev) {
+        err.alloc(1, c.stream);
+        err.zero();
+    }
     Tc8Args a{};
     a.rows = (uint32_t)rows;
     a.kb_total = (uint32_t)ceil_div(K, kStageK);
@@ -885,7 +893,7 @@ int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t rows
     a.split_stride = split_stride;
     a.tiles = tv.base;
     a.tile_bytes = tv.kbt * (uint64_t)kTileBytes;
-    a.err = err.get();
+    a.err = err_dev ? err_dev : err.get();
     const unsigned gy = (unsigned)ceil_div(a.kb_total, a.kb_per_split);
     const unsigned gx = (unsigned)round_up(ceil_div(rows, kM), pl.cluster);
     cudaLaunchConfig_t cfg{};
@@ -902,12 +910,11 @@ int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t rows
     cfg.numAttrs = 1;
     SLFMM_CUDA(cudaLaunchKernelEx(&cfg, k_tc8_rows, tb, a));
     SLFMM_LAUNCHED(c, "k_tc8_rows");
+    if (err_dev) return (int)gy;
     int h = 0;
     SLFMM_CUDA(cudaMemcpyAsync(&h, err.get(), sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     SLFMM_CUDA(cudaStreamSynchronize(c.stream));
-    if (h != 0)
-        throw Error(SLFMM_ERR_DEVICE_TIMEOUT,
-                    "split-FP8 contraction: a bounded device wait expired (site " + std::to_string(h) + ")");
+    if (h != 0) throw_tc8_timeout(h);
     return (int)gy;
 }
 

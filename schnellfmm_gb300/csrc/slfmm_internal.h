@@ -208,6 +208,12 @@ void launch_snp_counts(Ctx& c, const Geno& g, uint64_t* miss_count_out);
 void launch_snp_counts_range(Ctx& c, const Geno& g, uint64_t r0, uint64_t rows);
 void build_missing_lists(Ctx& c, const Geno& g);
 void build_missing_csc(Ctx& c, const Geno& g);
+// missing-call lists of an upload chunk [r0, r0 + rows): offsets continue
+// g.miss_ptr[r0] (needs the chunk's counts); the fill writes below cap only
+void csr_chunk_offsets(Ctx& c, const Geno& g, uint64_t r0, uint64_t rows);
+void csr_chunk_fill(Ctx& c, const Geno& g, uint64_t r0, uint64_t rows, uint64_t cap);
+void launch_stats_mean_range(Ctx& c, const Geno& g, uint64_t r0, uint64_t rows, int norm, double* mean,
+                             double* scale, double* tss, uint8_t* zero_var);
 void launch_stats_mean(Ctx& c, const Geno& g, int norm, double* mean, double* scale,
                        double* tss, uint8_t* zero_var);
 void launch_decode_chunk(Ctx& c, const Geno& g, uint64_t snp0, uint64_t ncols,
@@ -272,11 +278,14 @@ void launch_fp8_terms_f64(Ctx& c, const double* src, int ld, uint64_t K, int w, 
                           const double* kscale, int terms, int row_off, uint8_t* B, float* inv_scale);
 void launch_fp8_terms_f32(Ctx& c, const float* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
                           const double* kscale, int terms, int row_off, uint8_t* B, float* inv_scale);
-// mode 0: out = P (+ M); mode 1: out = s_r (P - mu_r (cs_c - M)) (needs the indicator)
+// mode 0: out = P (+ M); mode 1: out = s_r (P - mu_r (cs_c - M)) (needs the indicator).
+// err_dev null: the launch waits and throws when a bounded device wait expired;
+// non-null: the kernel records the site there and the caller checks it later.
 int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t rows, uint64_t K,
                      const uint8_t* B, const float* inv_scale, uint64_t K_pad, int mode, const double* row_mean,
                      const double* row_scale, const double* cs, float* out, int ldo, int splits,
-                     uint64_t split_stride);
+                     uint64_t split_stride, int* err_dev = nullptr);
+void throw_tc8_timeout(int site);
 void launch_sub_colterm(Ctx& c, double* S, int lds, uint64_t n, int w, const double* colterm);
 
 // k_nmf.cu : NMF imputation -- fill-aware statistics, sparse corrections of
