@@ -7,6 +7,7 @@
 // packed matrix is uploaded once (pinned staging ring, double-buffered) and
 // every pass is a kernel over the resident copy.
 #include <algorithm>
+#include <chrono>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -76,6 +77,21 @@ void log(Ctx& c, const std::string& s) {
     if (c.verbose) fprintf(stderr, "[schnelgpu] %s\n", s.c_str());
 }
 
+// Verbose mode: wall time of each phase of a fit.  The stream is
+// synchronised at every mark, so a phase's time covers its device work.
+void phase(Ctx& c, const char* what, bool start = false) {
+    if (!c.verbose) return;
+    sync(c);
+    const double t = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch())
+                         .count();
+    if (!start) {
+        char buf[160];
+        snprintf(buf, sizeof buf, "%-36s %9.2f ms", what, t - c.phase_t0);
+        log(c, buf);
+    }
+    c.phase_t0 = t;
+}
+
 // ---------------------------------------------------------------------------
 // SNP subset expansion (src/parallel.rs:113-122, src/bed.rs:162-171)
 // ---------------------------------------------------------------------------
@@ -143,15 +159,19 @@ void upload_geno(Ctx& c, Geno& g, const uint8_t* packed, uint64_t n_phys, uint64
         sync(c);
     }
     if (g.p) {
-        // staging: ~64 MiB (at most 256 Ki rows) per chunk, two device
+        // staging: ~96 MiB (at most 256 Ki rows) per chunk, two device
         // buffers, two pinned buffers.  Split-FP8 contexts build the
         // tile-major copies chunk by chunk as the rows land (chunks then start
-        // on 128-row tiles); every context builds the per-SNP missing-call
-        // lists the same way.  The copies are bound by the host link, so this
-        // work hides behind them.
+        // on 128-row tiles, whole waves of one tile per SM where the chunk
+        // holds one); every context builds the per-SNP missing-call lists the
+        // same way.  The copies are bound by the host link, so this work
+        // hides behind them.
         const bool tiles = c.precision == SLFMM_PREC_SPLIT_FP8;
-        uint64_t rows_per = std::max<uint64_t>(1, std::min<uint64_t>({g.p, (64ull << 20) / bps, 1ull << 18}));
-        if (tiles) rows_per = std::max<uint64_t>(128, rows_per / 128 * 128);
+        uint64_t rows_per = std::max<uint64_t>(1, std::min<uint64_t>({g.p, (96ull << 20) / bps, 1ull << 18}));
+        if (tiles) {
+            const uint64_t wave = 128ull * (uint64_t)std::max(c.sm_count, 1);
+            rows_per = rows_per >= wave ? rows_per / wave * wave : std::max<uint64_t>(128, rows_per / 128 * 128);
+        }
         g.miss_ptr.alloc(g.p + 1, c.stream);
         SLFMM_CUDA(cudaMemsetAsync(g.miss_ptr.get(), 0, sizeof(uint64_t), c.stream));
         uint64_t cap = 0;  // index capacity, sized from the first chunk's density
@@ -802,7 +822,9 @@ void assoc(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, const doubl
     // u = Q_C[:, 1:]^T y for every SNP
     DBuf<float> U;
     int wp = 0;
+    phase(c, "association design");
     row_contract(c, g, st, QC.get() + 1, wu, w, U, wp);
+    phase(c, "association row pass");
     DBuf<float> thd = upload(c, th.data(), th.size()), btd = upload(c, bt.data(), bt.size());
     DBuf<double> cjjd = upload(c, cjj.data(), cjj.size());
     DBuf<uint8_t> dxd = upload(c, drop_x.data(), drop_x.size());
@@ -829,11 +851,13 @@ void assoc(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, const doubl
     if (out.gif_per_trait) std::copy(gpt.begin(), gpt.end(), out.gif_per_trait);
     DBuf<double> gptd = upload(c, gpt.data(), gpt.size());
     launch_calibrate(c, p, d, t32.get(), gptd.get(), t64.get(), pv.get());
+    phase(c, "association statistics, GIF");
     if (out.beta) d2h(c, out.beta, beta.get(), p * d);
     if (out.tstat) d2h(c, out.tstat, t64.get(), p * d);
     if (out.pvalue) d2h(c, out.pvalue, pv.get(), p * d);
     if (out.r2) d2h(c, out.r2, r2.get(), p * 3);
     sync(c);
+    phase(c, "results to host");
 }
 
 // ---------------------------------------------------------------------------
@@ -1040,6 +1064,7 @@ bool presketch_prepare(Ctx& c, uint64_t n, uint64_t p, const double* x, int d, c
 
 void fit_impl(Ctx& c, const Geno& ge, const Geno& gf, const double* x, int d, const slfmm_config* cfg,
               const double* omega, slfmm_results* res, Presketch* pre = nullptr) {
+    if (!pre) phase(c, "", true);
     check_cfg(cfg);
     SLFMM_REQUIRE(ge.n == gf.n, SLFMM_ERR_BAD_ARG, "estimation and testing genotypes have different sample counts");
     Step0 s0_own;
@@ -1094,9 +1119,11 @@ void fit_impl(Ctx& c, const Geno& ge, const Geno& gf, const double* x, int d, co
             sfp = &sf;
         }
     }
+    phase(c, "covariates, SNP statistics");
     DBuf<double> u_hat;
     const int K = (int)cfg->k, l = K + (int)cfg->oversampling;
     rsvd(c, ge, se, s0, K, l, (int)cfg->n_power_iter, cfg->seed, omega, u_hat, pre ? &pre->Z : nullptr);
+    phase(c, "randomized SVD");
     if (res && res->u_hat) d2h(c, res->u_hat, u_hat.get(), gf.n * K);
     AssocOut out{res ? res->beta : nullptr, res ? res->tstat : nullptr, res ? res->pvalue : nullptr,
                  res ? res->r2 : nullptr, res ? res->gif_per_trait : nullptr, 0.0};
@@ -1370,14 +1397,17 @@ int slfmm_fit_host(slfmm_ctx* c, const uint8_t* packed, uint64_t n_physical, uin
     const bool all = !est || est->kind == SLFMM_SUBSET_ALL;
     // with every SNP in the estimation, the sketch pass runs under the upload
     Presketch ps;
+    phase(*c, "", true);
     const bool pre = all && cfg && presketch_prepare(*c, sample_keep ? n_keep : n_physical, n_snps, x, (int)d, cfg,
                                                      omega, ps);
+    if (pre) phase(*c, "covariates, sketch operand");
     upload_geno(*c, full, packed, n_physical, n_snps, sample_keep, n_keep, subset_indices(nullptr, n_snps),
                 pre ? &ps : nullptr);
     if (pre) {
         const int e = fetch(*c, ps.err.get(), 1)[0];
         if (e) throw_tc8_timeout(e);
     }
+    phase(*c, pre ? "upload with the sketch pass" : "upload");
     const Geno* ge = &full;
     if (!all) {
         upload_geno(*c, sub, packed, n_physical, n_snps, sample_keep, n_keep, subset_indices(est, n_snps));

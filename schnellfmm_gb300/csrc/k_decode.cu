@@ -57,6 +57,35 @@ __global__ void k_repack(const uint8_t* __restrict__ in, uint64_t rows, uint64_t
     }
 }
 
+// Straight copy without a sample subset when the payload rows are V-aligned:
+// rows of in_bps bytes -> rows of `stride` bytes, the payload's last 32-bit
+// word masked to the codes of n_out samples and the rest of the row zero.
+// One block per row (grid-stride), V-wide loads and stores.
+template <typename V>
+__global__ void k_repack_vec(const uint8_t* __restrict__ in, uint64_t rows, uint64_t in_bps, uint64_t n_out,
+                             uint8_t* __restrict__ out, uint64_t stride) {
+    constexpr int kw = sizeof(V) / 4;
+    const uint64_t in_vecs = in_bps / sizeof(V), out_vecs = stride / sizeof(V);
+    const uint64_t last_word = in_bps / 4 - 1;
+    const uint64_t valid = n_out - 16 * last_word;  // codes in the last word
+    const uint32_t tail = valid >= 16 ? 0xffffffffu : (1u << (2 * valid)) - 1u;
+    for (uint64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+        const V* src = reinterpret_cast<const V*>(in + r * in_bps);
+        V* dst = reinterpret_cast<V*>(out + r * stride);
+        for (uint64_t v = threadIdx.x; v < out_vecs; v += blockDim.x) {
+            V x{};
+            if (v < in_vecs) {
+                x = src[v];
+                uint32_t* xw = reinterpret_cast<uint32_t*>(&x);
+#pragma unroll
+                for (int k = 0; k < kw; ++k)
+                    if (v * kw + k == last_word) xw[k] &= tail;
+            }
+            dst[v] = x;
+        }
+    }
+}
+
 // One warp per SNP: popcount the 2-bit codes.  Padding codes are 00, so c0
 // is derived as n - c1 - c2 - cmiss.
 __global__ void k_snp_counts(const uint8_t* __restrict__ packed, uint64_t p, uint64_t stride,
@@ -65,15 +94,22 @@ __global__ void k_snp_counts(const uint8_t* __restrict__ packed, uint64_t p, uin
     const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
     const int lane = threadIdx.x & 31;
     if (warp >= p) return;
-    const uint32_t* row = reinterpret_cast<const uint32_t*>(packed + warp * stride);
-    const uint64_t nwords = (n + 15) / 16;
+    // rows are 16-byte aligned (the stride is a multiple of 128 bytes)
+    const uint4* row = reinterpret_cast<const uint4*>(packed + warp * stride);
+    const uint64_t nwords = (n + 15) / 16, nvec = (nwords + 3) / 4;
     uint32_t c1 = 0, c2 = 0, cm = 0;
-    for (uint64_t w = lane; w < nwords; w += 32) {
-        const uint32_t v = row[w];
-        const uint32_t lo = v & kLo, hi = (v >> 1) & kLo;
-        c1 += __popc(hi & ~lo);
-        c2 += __popc(hi & lo);
-        cm += __popc(~hi & lo);
+    for (uint64_t v = lane; v < nvec; v += 32) {
+        const uint4 x = row[v];
+        const uint32_t xs[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            if (v * 4 + k < nwords) {
+                const uint32_t lo = xs[k] & kLo, hi = (xs[k] >> 1) & kLo;
+                c1 += __popc(hi & ~lo);
+                c2 += __popc(hi & lo);
+                cm += __popc(~hi & lo);
+            }
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -98,17 +134,21 @@ __global__ void k_miss_fill(const uint8_t* __restrict__ packed, uint64_t p, uint
     const uint64_t warp = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
     const int lane = threadIdx.x & 31;
     if (warp >= p) return;
-    const uint32_t* row = reinterpret_cast<const uint32_t*>(packed + warp * stride);
-    const uint64_t nwords = (n + 15) / 16;
+    // 4 words (64 codes) per lane and step; rows are 16-byte aligned
+    const uint4* row = reinterpret_cast<const uint4*>(packed + warp * stride);
+    const uint64_t nwords = (n + 15) / 16, nvec = (nwords + 3) / 4;
     uint64_t base = ptr[warp];
-    for (uint64_t w0 = 0; w0 < nwords; w0 += 32) {
-        const uint64_t w = w0 + lane;
-        uint32_t m = 0;
-        if (w < nwords) {
-            const uint32_t v = row[w];
-            m = ~(v >> 1) & v & kLo;
+    for (uint64_t v0 = 0; v0 < nvec; v0 += 32) {
+        const uint64_t v = v0 + lane;
+        uint32_t m[4] = {0u, 0u, 0u, 0u};
+        if (v < nvec) {
+            const uint4 x = row[v];
+            const uint32_t xs[4] = {x.x, x.y, x.z, x.w};
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                if (v * 4 + k < nwords) m[k] = ~(xs[k] >> 1) & xs[k] & kLo;
         }
-        const uint32_t cnt = __popc(m);
+        const uint32_t cnt = __popc(m[0]) + __popc(m[1]) + __popc(m[2]) + __popc(m[3]);
         uint32_t incl = cnt;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
@@ -117,14 +157,18 @@ __global__ void k_miss_fill(const uint8_t* __restrict__ packed, uint64_t p, uint
         }
         const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
         uint64_t pos = base + incl - cnt;
-        while (m) {
-            const int b = __ffs(m) - 1;
-            m &= m - 1;
-            if (pos < cap) {
-                idx[pos] = (uint32_t)(w * 16 + (b >> 1));
-                if (rowid) rowid[pos] = (uint32_t)warp;
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            uint32_t mk = m[k];
+            while (mk) {
+                const int b = __ffs(mk) - 1;
+                mk &= mk - 1;
+                if (pos < cap) {
+                    idx[pos] = (uint32_t)((v * 4 + k) * 16 + (b >> 1));
+                    if (rowid) rowid[pos] = (uint32_t)warp;
+                }
+                ++pos;
             }
-            ++pos;
         }
         base += total;
     }
@@ -260,6 +304,18 @@ __global__ void k_lut_raw(uint64_t p, const double* __restrict__ fill, float* __
 void launch_repack(Ctx& c, const uint8_t* in, uint64_t rows, uint64_t in_bps, uint64_t /*n_phys*/,
                    const uint32_t* keep, uint64_t n_out, uint8_t* out, uint64_t stride) {
     if (rows == 0) return;
+    const uintptr_t al = reinterpret_cast<uintptr_t>(in) | reinterpret_cast<uintptr_t>(out) | in_bps | stride;
+    if (keep == nullptr && in_bps == (n_out + 3) / 4 && al % 4 == 0) {
+        const unsigned grid = (unsigned)std::min<uint64_t>(rows, (uint64_t)c.sm_count * 8);
+        if (al % 16 == 0)
+            k_repack_vec<uint4><<<grid, 256, 0, c.stream>>>(in, rows, in_bps, n_out, out, stride);
+        else if (al % 8 == 0)
+            k_repack_vec<uint2><<<grid, 256, 0, c.stream>>>(in, rows, in_bps, n_out, out, stride);
+        else
+            k_repack_vec<uint32_t><<<grid, 256, 0, c.stream>>>(in, rows, in_bps, n_out, out, stride);
+        SLFMM_LAUNCHED(c, "k_repack_vec");
+        return;
+    }
     const uint64_t work = rows * (stride / 4);
     k_repack<<<grid_for(c, work, 256), 256, 0, c.stream>>>(in, rows, in_bps, keep, n_out, out, stride);
     SLFMM_LAUNCHED(c, "k_repack");

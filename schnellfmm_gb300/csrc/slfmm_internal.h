@@ -157,6 +157,7 @@ struct Ctx {
     DBuf<int> dev_flags;   // [0] device timeout flag, [1] error info
     bool profiling = false;
     std::map<std::string, ProfRec> prof;
+    double phase_t0 = 0.0;  // verbose phase log: start of the current phase (ms)
 };
 
 // bracket a launch with CUDA events when profiling is on
