@@ -159,10 +159,24 @@ __global__ void __launch_bounds__(256) k_gram_f32(const float* __restrict__ A, i
         }
 }
 
+// Elements 4 q .. 4 q + 3 of a row (16-byte aligned, 4 q < lda), the ones at
+// or past column a zero (no load when the whole quad is past a).
+__device__ __forceinline__ float4 row_quad(const float* row, int q, int a) {
+    if (4 * q >= a) return make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 b = reinterpret_cast<const float4*>(row)[q];
+    if (4 * q + 4 > a) {
+        b.y = 4 * q + 1 < a ? b.y : 0.f;
+        b.z = 4 * q + 2 < a ? b.z : 0.f;
+        b.w = 4 * q + 3 < a ? b.w : 0.f;
+    }
+    return b;
+}
+
 // Narrow (a <= 32) FP32 Gram, one warp per run of rows: lane c holds row
-// element c, and for each k the broadcast row[k] (shuffle) times row[c]
-// accumulates G[k][c] in lane c.  FP32 sums over runs of 256 rows, FP64 across
-// runs; the block's warps reduce through shared memory into one partial.
+// element c and takes row[k] by shuffle.  FP32 sums over runs of 256 rows,
+// FP64 across runs; the block's warps reduce through shared memory into one
+// partial.  (Rows of any stride; the tiled kernel below covers 16-byte
+// aligned rows of at most 32 floats.)
 constexpr int kGramRun = 256;
 constexpr size_t kGramNarrowSmem = 8 * 32 * 33 * sizeof(double);
 __global__ void __launch_bounds__(256, 2) k_gram_narrow(const float* __restrict__ A, int lda, uint64_t m, int a,
@@ -223,6 +237,181 @@ __global__ void __launch_bounds__(256) k_trmul_narrow(float* __restrict__ A, int
             for (int k = 0; k < 32; ++k) out = fmaf(__shfl_sync(0xffffffffu, v[u], k), R[k], out);
             if (lane < a && i + u < m) A[(i + u) * lda + lane] = out;
         }
+    }
+}
+
+// Tiles of 128 rows of a narrow matrix (a <= lda <= 32, lda % 4 == 0, rows
+// 16-byte aligned) stream through a ring of kPipe shared-memory stages with
+// asynchronous 16-byte copies (cp.async, completion awaited by wait_group):
+// tile i + kPipe - 1 is in flight while tile i is used.  One persistent block
+// of 512 threads per SM takes tiles blockIdx.x, + gridDim.x, ...; each of its
+// 16 warps uses 8 rows of a tile.  Rows past m are neither copied nor used.
+__device__ __forceinline__ uint32_t smem_addr32(const void* p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+constexpr int kNarrowTile = 128;
+constexpr int kPipe = 4;
+constexpr int kPipeThreads = 512;
+constexpr size_t kPipeRing = (size_t)kPipe * kNarrowTile * 32 * sizeof(float);
+
+__device__ __forceinline__ void pipe_issue(const float* A, int lda, uint64_t m, uint64_t t, float* stage) {
+    const int q = lda >> 2, nf4 = kNarrowTile * q;
+    const float4* src = reinterpret_cast<const float4*>(A) + t * kNarrowTile * q;
+    const uint64_t rows = min((uint64_t)kNarrowTile, m - t * kNarrowTile);
+#pragma unroll
+    for (int r = 0; r < 1024 / kPipeThreads; ++r) {
+        const int e = threadIdx.x + kPipeThreads * r;
+        if (e < nf4 && (uint64_t)(e / q) < rows)
+            asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr32(stage + 4 * e)), "l"(src + e)
+                         : "memory");
+    }
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+__device__ __forceinline__ void pipe_commit_empty() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+// wait for tile i (its copy group) and make every thread's copies visible
+__device__ __forceinline__ void pipe_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(kPipe - 2) : "memory");
+    __syncthreads();
+}
+
+// Gram over tiles: lane = 8 ky + cx of each warp owns the block
+// G[8 ky + i][4 cx + j] (i < 8, j < 4) and reads its 12 row elements as three
+// 16-byte shared-memory loads per row.  Elements past column a (padding, or
+// the next row when lda < 32) only reach entries that are never written out.
+// FP32 sums over up to 16 tiles, then into per-warp FP64 sums in shared
+// memory; the warps are added in a fixed order into one partial per block.
+__global__ void __launch_bounds__(kPipeThreads, 1) k_gram_tile(const float* __restrict__ A, int lda, uint64_t m, int a,
+                                                            double* __restrict__ part) {
+    extern __shared__ __align__(16) float ring[];  // [kPipe][128 rows][lda], then [16 warps][32][32] FP64
+    double* dsum = reinterpret_cast<double*>(reinterpret_cast<uint8_t*>(ring) + kPipeRing);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int ky = lane >> 3, cx = lane & 7;
+    double* mine = dsum + warp * 32 * 32;  // [entry][lane]
+#pragma unroll
+    for (int k = 0; k < 32; ++k) mine[k * 32 + lane] = 0.0;
+    const uint64_t ntiles = (m + kNarrowTile - 1) / kNarrowTile;
+    const int tsz = kNarrowTile * lda;
+    float acc[32];
+#pragma unroll
+    for (int k = 0; k < 32; ++k) acc[k] = 0.f;
+    for (int k = 0; k < kPipe - 1; ++k) {
+        const uint64_t t = blockIdx.x + (uint64_t)k * gridDim.x;
+        if (t < ntiles) pipe_issue(A, lda, m, t, ring + k * tsz);
+        else pipe_commit_empty();
+    }
+    int since = 0;
+    for (uint64_t i = 0;; ++i) {
+        const uint64_t t = blockIdx.x + i * gridDim.x;
+        if (t >= ntiles) break;
+        pipe_wait();
+        const uint64_t tn = t + (uint64_t)(kPipe - 1) * gridDim.x;
+        if (tn < ntiles) pipe_issue(A, lda, m, tn, ring + ((i + kPipe - 1) % kPipe) * tsz);
+        else pipe_commit_empty();
+        const int r0 = warp * 8;
+        const uint64_t gr = t * kNarrowTile + r0;
+        const int nrows = gr >= m ? 0 : (m - gr >= 8 ? 8 : (int)(m - gr));
+        const float* base = ring + (i % kPipe) * tsz + r0 * lda;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            if (u < nrows) {
+                const float4* row = reinterpret_cast<const float4*>(base + u * lda);
+                const float4 ka = row[2 * ky], kb = row[2 * ky + 1], cv = row[cx];
+                const float kk[8] = {ka.x, ka.y, ka.z, ka.w, kb.x, kb.y, kb.z, kb.w};
+                const float cc[4] = {cv.x, cv.y, cv.z, cv.w};
+#pragma unroll
+                for (int ii = 0; ii < 8; ++ii)
+#pragma unroll
+                    for (int jj = 0; jj < 4; ++jj) acc[ii * 4 + jj] = fmaf(kk[ii], cc[jj], acc[ii * 4 + jj]);
+            }
+        }
+        if (++since == 32) {
+#pragma unroll
+            for (int k = 0; k < 32; ++k) mine[k * 32 + lane] += (double)acc[k], acc[k] = 0.f;
+            since = 0;
+        }
+    }
+    asm volatile("cp.async.wait_group 0;" ::: "memory");
+#pragma unroll
+    for (int k = 0; k < 32; ++k) mine[k * 32 + lane] += (double)acc[k];
+    __syncthreads();
+    // entry (k, c) of the block partial: lane 8 (k / 8) + c / 4, slot (k % 8) 4 + c % 4
+    for (int e = threadIdx.x; e < a * a; e += kPipeThreads) {
+        const int k = e / a, c = e % a;
+        const int ln = 8 * (k >> 3) + (c >> 2), slot = (k & 7) * 4 + (c & 3);
+        double tsum = 0.0;
+        for (int w = 0; w < kPipeThreads / 32; ++w) tsum += dsum[w * 32 * 32 + slot * 32 + ln];
+        part[(uint64_t)blockIdx.x * a * a + e] = tsum;
+    }
+}
+
+// A (m x a, a <= 32, lda % 4 == 0, rows 16-byte aligned) <- A Linv^T in
+// place for a lower-triangular Linv, one row per thread: the row is read as
+// 16-byte loads (elements past a zero), out[c] = sum_{k <= c} row[k] R[c][k]
+// with R = Linv in FP32 passed as a kernel parameter -- every FMA takes its R
+// operand from the constant bank, the same for the whole warp -- and the row
+// is written back.
+struct Mat32 {
+    float v[32][32];
+};
+__global__ void __launch_bounds__(256) k_trmul_rows(float* __restrict__ A, int lda, uint64_t m, int a,
+                                                    const __grid_constant__ Mat32 R) {
+    for (uint64_t i = (uint64_t)blockIdx.x * 256 + threadIdx.x; i < m; i += (uint64_t)gridDim.x * 256) {
+        float* row = A + i * lda;
+        float x[32];
+#pragma unroll
+        for (int kq = 0; kq < 8; ++kq) {
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (4 * kq < a) {
+                v = reinterpret_cast<const float4*>(row)[kq];
+                if (4 * kq + 4 > a) {
+                    v.y = 4 * kq + 1 < a ? v.y : 0.f;
+                    v.z = 4 * kq + 2 < a ? v.z : 0.f;
+                    v.w = 4 * kq + 3 < a ? v.w : 0.f;
+                }
+            }
+            x[4 * kq] = v.x;
+            x[4 * kq + 1] = v.y;
+            x[4 * kq + 2] = v.z;
+            x[4 * kq + 3] = v.w;
+        }
+        float o[32];
+#pragma unroll
+        for (int c = 0; c < 32; ++c) o[c] = 0.f;
+        // Linv is lower triangular: R[c][k] = 0 for k > c (528 products)
+#pragma unroll
+        for (int k = 0; k < 32; ++k)
+#pragma unroll
+            for (int c = k; c < 32; ++c) o[c] = fmaf(x[k], R.v[c][k], o[c]);
+#pragma unroll
+        for (int cq = 0; cq < 8; ++cq) {
+            if (4 * cq + 4 <= a) {
+                reinterpret_cast<float4*>(row)[cq] = make_float4(o[4 * cq], o[4 * cq + 1], o[4 * cq + 2], o[4 * cq + 3]);
+            } else if (4 * cq < a) {
+#pragma unroll
+                for (int jj = 0; jj < 4; ++jj)
+                    if (4 * cq + jj < a) row[4 * cq + jj] = o[4 * cq + jj];
+            }
+        }
+    }
+}
+
+// one block per entry: thread t sums partials t, t + 128, ... in order, then
+// a fixed-shape tree (warp shuffles, then the four warps in order)
+__global__ void __launch_bounds__(128) k_sum_partials_wide(const double* __restrict__ part, int splits,
+                                                           uint64_t count, double* __restrict__ out) {
+    __shared__ double ws[4];
+    for (uint64_t e = blockIdx.x; e < count; e += gridDim.x) {
+        double s = 0.0;
+        for (int k = threadIdx.x; k < splits; k += 128) s += part[(uint64_t)k * count + e];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x == 0) out[e] = (ws[0] + ws[1]) + (ws[2] + ws[3]);
+        __syncthreads();
     }
 }
 
@@ -735,6 +924,11 @@ __global__ void k_build_design(const double* __restrict__ X, int d, const double
 
 size_t smem_sq(int a) { return (size_t)a * a * sizeof(double); }
 
+// rows of a narrow FP32 matrix the tiled kernels can take
+bool narrow_tiled(const float* A, int lda) {
+    return lda % 4 == 0 && lda <= 32 && reinterpret_cast<uintptr_t>(A) % 16 == 0;
+}
+
 void set_smem(const void* fn, size_t bytes) {
     if (bytes > 48 * 1024)
         SLFMM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
@@ -778,6 +972,12 @@ void launch_colsums(Ctx& c, const double* A, uint64_t m, int a, int lda, double*
 
 void launch_sum_partials(Ctx& c, const double* part, int splits, uint64_t count, double* out) {
     if (!count) return;
+    if (splits >= 32) {
+        k_sum_partials_wide<<<(unsigned)std::min<uint64_t>(count, 65535), 128, 0, c.stream>>>(part, splits, count,
+                                                                                             out);
+        SLFMM_LAUNCHED(c, "k_sum_partials_wide");
+        return;
+    }
     k_sum_partials<<<grid_for(c, count, 256), 256, 0, c.stream>>>(part, splits, count, out);
     SLFMM_LAUNCHED(c, "k_sum_partials");
 }
@@ -807,9 +1007,7 @@ static void atb_impl(Ctx& c, const T* A, int lda, const T* B, int ldb, uint64_t 
     dim3 grid(ta, tb, (unsigned)splits);
     k_atb<T><<<grid, 256, 0, c.stream>>>(A, lda, B, ldb, m, a, b, per, part.get());
     SLFMM_LAUNCHED(c, "k_atb");
-    k_sum_partials<<<grid_for(c, (uint64_t)a * b, 256), 256, 0, c.stream>>>(part.get(), (int)splits,
-                                                                            (uint64_t)a * b, out);
-    SLFMM_LAUNCHED(c, "k_sum_partials");
+    launch_sum_partials(c, part.get(), (int)splits, (uint64_t)a * b, out);
 }
 
 void launch_atb(Ctx& c, const double* A, int lda, const double* B, int ldb, uint64_t m, int a, int b,
@@ -819,15 +1017,24 @@ void launch_atb(Ctx& c, const double* A, int lda, const double* B, int ldb, uint
 
 void launch_gram_f32(Ctx& c, const float* A, int lda, uint64_t m, int a, double* out) {
     if (a <= 32) {
+        if (narrow_tiled(A, lda)) {
+            const uint64_t tb = std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(m, (uint64_t)kNarrowTile),
+                                                                        (uint64_t)c.sm_count));
+            const size_t sm = kPipeRing + (size_t)(kPipeThreads / 32) * 32 * 32 * sizeof(double);
+            DBuf<double> tpart(tb * a * a, c.stream);
+            set_smem((const void*)k_gram_tile, sm);
+            k_gram_tile<<<(unsigned)tb, kPipeThreads, sm, c.stream>>>(A, lda, m, a, tpart.get());
+            SLFMM_LAUNCHED(c, "k_gram_tile");
+            launch_sum_partials(c, tpart.get(), (int)tb, (uint64_t)a * a, out);
+            return;
+        }
         const uint64_t runs = std::max<uint64_t>(1, ceil_div(m, (uint64_t)kGramRun));
         const uint64_t blocks = std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(runs, 8), (uint64_t)c.sm_count * 4));
         DBuf<double> part(blocks * a * a, c.stream);
         set_smem((const void*)k_gram_narrow, kGramNarrowSmem);
         k_gram_narrow<<<(unsigned)blocks, 256, kGramNarrowSmem, c.stream>>>(A, lda, m, a, part.get());
         SLFMM_LAUNCHED(c, "k_gram_narrow");
-        k_sum_partials<<<grid_for(c, (uint64_t)a * a, 256), 256, 0, c.stream>>>(part.get(), (int)blocks,
-                                                                                (uint64_t)a * a, out);
-        SLFMM_LAUNCHED(c, "k_sum_partials");
+        launch_sum_partials(c, part.get(), (int)blocks, (uint64_t)a * a, out);
         return;
     }
     const int ta = (int)ceil_div(a, 32);
@@ -840,9 +1047,7 @@ void launch_gram_f32(Ctx& c, const float* A, int lda, uint64_t m, int a, double*
     dim3 grid(ta, ta, (unsigned)splits);
     k_gram_f32<<<grid, 256, 0, c.stream>>>(A, lda, m, a, per, part.get());
     SLFMM_LAUNCHED(c, "k_gram_f32");
-    k_sum_partials<<<grid_for(c, (uint64_t)a * a, 256), 256, 0, c.stream>>>(part.get(), (int)splits,
-                                                                            (uint64_t)a * a, out);
-    SLFMM_LAUNCHED(c, "k_sum_partials");
+    launch_sum_partials(c, part.get(), (int)splits, (uint64_t)a * a, out);
 }
 
 void launch_gemm_small(Ctx& c, const double* A, int lda, uint64_t m, int a, const double* B, int ldb,
@@ -869,6 +1074,18 @@ void launch_trmul_f32(Ctx& c, float* A, int lda, uint64_t m, int a, const double
     SLFMM_REQUIRE(a <= 64, SLFMM_ERR_BAD_ARG, "sketch width must be <= 64");
     if (m == 0) return;
     if (a <= 32) {
+        if (narrow_tiled(A, lda)) {
+            // the factor travels in the launch (a x a doubles on the device)
+            std::vector<double> L((size_t)a * a);
+            SLFMM_CUDA(cudaMemcpyAsync(L.data(), Linv, L.size() * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+            SLFMM_CUDA(cudaStreamSynchronize(c.stream));
+            Mat32 R{};
+            for (int i = 0; i < a; ++i)
+                for (int k = 0; k <= i; ++k) R.v[i][k] = (float)L[(size_t)i * a + k];
+            k_trmul_rows<<<grid_for(c, m, 256), 256, 0, c.stream>>>(A, lda, m, a, R);
+            SLFMM_LAUNCHED(c, "k_trmul_rows");
+            return;
+        }
         k_trmul_narrow<<<grid_for(c, m, 32), 256, 0, c.stream>>>(A, lda, m, a, Linv);
         SLFMM_LAUNCHED(c, "k_trmul_narrow");
         return;

@@ -318,24 +318,28 @@ __global__ void k_colfix_mean(double* __restrict__ S, int lds, uint64_t n, int w
     }
 }
 
-// colterm[c] = sum_j coef_j Q[j, c]  (block partials, fixed order)
-// out[c] = sum_j coef[j] Q[j, c] (w <= 128): block partials, one warp per run
+// out[c] = sum_j coef[j] Q[j, c] (w <= 32 T): block partials, one warp per run
 // of rows with the row read whole (lane c, c + 32, ...), four rows in flight.
+// T column groups of 32 only: GB300's FP64 rate is low, so no FMA is spent on
+// absent columns.
+template <int T>
 __global__ void __launch_bounds__(256) k_weighted_colsum(const float* __restrict__ Q, int ldq, uint64_t p, int w,
                                                          const double* __restrict__ coef, double* __restrict__ part) {
-    __shared__ double red[8][128];
+    __shared__ double red[8][32 * T];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    double acc[T];
+#pragma unroll
+    for (int t = 0; t < T; ++t) acc[t] = 0.0;
     const uint64_t nw = (uint64_t)gridDim.x * 8;
     for (uint64_t j = ((uint64_t)blockIdx.x * 8 + warp) * 4; j < p; j += nw * 4) {
-        float q[4][4];
+        float q[4][T];
         double cf[4];
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             const bool ok = j + u < p;
             cf[u] = ok ? coef[j + u] : 0.0;
 #pragma unroll
-            for (int t = 0; t < 4; ++t) {
+            for (int t = 0; t < T; ++t) {
                 const int cc = lane + 32 * t;
                 q[u][t] = (ok && cc < w) ? Q[(j + u) * ldq + cc] : 0.f;
             }
@@ -343,10 +347,10 @@ __global__ void __launch_bounds__(256) k_weighted_colsum(const float* __restrict
 #pragma unroll
         for (int u = 0; u < 4; ++u)
 #pragma unroll
-            for (int t = 0; t < 4; ++t) acc[t] = fma(cf[u], (double)q[u][t], acc[t]);
+            for (int t = 0; t < T; ++t) acc[t] = fma(cf[u], (double)q[u][t], acc[t]);
     }
 #pragma unroll
-    for (int t = 0; t < 4; ++t) red[warp][lane + 32 * t] = acc[t];
+    for (int t = 0; t < T; ++t) red[warp][lane + 32 * t] = acc[t];
     __syncthreads();
     for (int cc = threadIdx.x; cc < w; cc += blockDim.x) {
         double s = 0.0;
@@ -537,7 +541,9 @@ void launch_weighted_colsum(Ctx& c, const float* Q, int ldq, uint64_t p, int w, 
     SLFMM_REQUIRE(w <= 128, SLFMM_ERR_BAD_ARG, "width");
     const uint64_t blocks = std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(p, 256), (uint64_t)c.sm_count * 4));
     DBuf<double> part(blocks * w, c.stream);
-    k_weighted_colsum<<<(unsigned)blocks, 256, 0, c.stream>>>(Q, ldq, p, w, coef, part.get());
+    if (w <= 32) k_weighted_colsum<1><<<(unsigned)blocks, 256, 0, c.stream>>>(Q, ldq, p, w, coef, part.get());
+    else if (w <= 64) k_weighted_colsum<2><<<(unsigned)blocks, 256, 0, c.stream>>>(Q, ldq, p, w, coef, part.get());
+    else k_weighted_colsum<4><<<(unsigned)blocks, 256, 0, c.stream>>>(Q, ldq, p, w, coef, part.get());
     SLFMM_LAUNCHED(c, "k_weighted_colsum");
     launch_sum_partials(c, part.get(), (int)blocks, (uint64_t)w, out);
 }
