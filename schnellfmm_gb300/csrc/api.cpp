@@ -432,8 +432,8 @@ void col_contract_base(Ctx& c, const Geno& g, const SnpStd& s, const float* Q, i
         DBuf<float> isc(pl.n_total, c.stream);
         DBuf<double> coef(std::max<uint64_t>(g.p, 1), c.stream), colterm(wp, c.stream);
         launch_scale_product(c, s.mean.get(), s.scale.get(), g.p, coef.get());
-        launch_fp8_terms_f32(c, Q, wp, g.p, w, wp, p_pad, s.scale.get(), 4, 0, B.get(), isc.get());
-        if (ind) launch_fp8_terms_f32(c, Q, wp, g.p, w, wp, p_pad, coef.get(), 3, (int)pl.n_main, B.get(), isc.get());
+        launch_fp8_terms_f32_pair(c, Q, wp, g.p, w, wp, p_pad, s.scale.get(), ind ? coef.get() : nullptr,
+                                  (int)pl.n_main, B.get(), isc.get());
         const int splits = tc_split_count(c, g.n, g.p);
         DBuf<float> part((uint64_t)splits * g.n * wp, c.stream);
         int used = 0;

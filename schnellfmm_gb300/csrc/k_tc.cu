@@ -359,6 +359,66 @@ __global__ void __launch_bounds__(256) k_weighted_colsum(const float* __restrict
     }
 }
 
+// out[c] = sum_j coef[j] Q[j, c] for a narrow operand (w <= ldq <= 32,
+// ldq % 4 == 0, 16-byte aligned rows): a thread keeps one 16-byte column quad
+// and walks rows, four rows in flight; FP32 products and sums over runs of 64
+// of its rows (the precision of the tensor-core sums this term is subtracted
+// from), FP64 across runs, lanes and warps; one partial per block.
+__global__ void __launch_bounds__(256) k_weighted_colsum_quads(const float* __restrict__ Q, int ldq, uint64_t p,
+                                                               int w, const double* __restrict__ coef,
+                                                               double* __restrict__ part) {
+    const int q = ldq >> 2;  // 1, 2, 4 or 8 quads per row
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t step = (uint64_t)gridDim.x * blockDim.x / q;
+    const int qp = (int)(tid % q);
+    const float4* q4 = reinterpret_cast<const float4*>(Q);
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    float f[4] = {0.f, 0.f, 0.f, 0.f};
+    int run = 0;
+    for (uint64_t j0 = tid / q; j0 < p; j0 += 4 * step) {
+        float4 v[4];
+        float cf[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint64_t j = j0 + u * step;
+            const bool ok = j < p;
+            v[u] = ok ? q4[j * q + qp] : make_float4(0.f, 0.f, 0.f, 0.f);
+            cf[u] = ok ? (float)coef[j] : 0.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            f[0] = fmaf(cf[u], v[u].x, f[0]);
+            f[1] = fmaf(cf[u], v[u].y, f[1]);
+            f[2] = fmaf(cf[u], v[u].z, f[2]);
+            f[3] = fmaf(cf[u], v[u].w, f[3]);
+        }
+        if (++run == 16) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i) acc[i] += (double)f[i], f[i] = 0.f;
+            run = 0;
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) acc[i] += (double)f[i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        if (o < q) break;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], o);
+    }
+    __shared__ double red[8][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane < q)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) red[warp][4 * lane + i] = acc[i];
+    __syncthreads();
+    if (threadIdx.x < w) {
+        double t = 0.0;
+        for (int wv = 0; wv < 8; ++wv) t += red[wv][threadIdx.x];
+        part[(uint64_t)blockIdx.x * w + threadIdx.x] = t;
+    }
+}
+
 __global__ void k_scale_product(const double* __restrict__ a, const double* __restrict__ b, uint64_t n,
                                 double* __restrict__ out) {
     for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x)
@@ -539,6 +599,15 @@ void launch_colfix_mean(Ctx& c, double* S, int lds, uint64_t n, int w, const uin
 
 void launch_weighted_colsum(Ctx& c, const float* Q, int ldq, uint64_t p, int w, const double* coef, double* out) {
     SLFMM_REQUIRE(w <= 128, SLFMM_ERR_BAD_ARG, "width");
+    if (ldq % 4 == 0 && ldq <= 32 && w <= ldq && reinterpret_cast<uintptr_t>(Q) % 16 == 0) {
+        const uint64_t qb = std::max<uint64_t>(
+            1, std::min<uint64_t>(ceil_div(p * (uint64_t)(ldq / 4), 1024), (uint64_t)c.sm_count * 4));
+        DBuf<double> qpart(qb * w, c.stream);
+        k_weighted_colsum_quads<<<(unsigned)qb, 256, 0, c.stream>>>(Q, ldq, p, w, coef, qpart.get());
+        SLFMM_LAUNCHED(c, "k_weighted_colsum_quads");
+        launch_sum_partials(c, qpart.get(), (int)qb, (uint64_t)w, out);
+        return;
+    }
     const uint64_t blocks = std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(p, 256), (uint64_t)c.sm_count * 4));
     DBuf<double> part(blocks * w, c.stream);
     if (w <= 32) k_weighted_colsum<1><<<(unsigned)blocks, 256, 0, c.stream>>>(Q, ldq, p, w, coef, part.get());

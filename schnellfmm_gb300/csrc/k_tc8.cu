@@ -587,6 +587,159 @@ __global__ void __launch_bounds__(256) k_fp8_terms(const T* __restrict__ src, in
     }
 }
 
+// The two scalings of one narrow FP32 operand that a transposed pass splits
+// (diag(s) Q for the genotypes, diag(mu s) Q for the missing-call indicator).
+struct TermSet {
+    const double* kscale;    // per-K-row scale (null: 1)
+    int terms;               // E4M3 terms (0: set absent)
+    int row_off;             // first B row of the set
+    const unsigned* colmax;  // per-column max |x * kscale| (float bits)
+};
+
+// Per-column max |x kscale| of both sets in one pass over a narrow operand
+// (w <= ld <= 32, ld % 4 == 0, 16-byte aligned rows): a thread keeps one
+// 16-byte column quad and walks rows, four rows in flight; lanes with the
+// same quad are combined by shuffles before the atomics.
+__global__ void __launch_bounds__(256) k_colmax_pair(const float* __restrict__ src, int ld, uint64_t K, int w,
+                                                     const double* __restrict__ ksa, const double* __restrict__ ksb,
+                                                     unsigned* __restrict__ cma, unsigned* __restrict__ cmb) {
+    const int q = ld >> 2;  // quads per row: 1, 2, 4 or 8 (divides the thread count)
+    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const uint64_t nthreads = (uint64_t)gridDim.x * blockDim.x;
+    const int qp = (int)(tid % q);
+    const uint64_t step = nthreads / q;
+    const float4* s4 = reinterpret_cast<const float4*>(src);
+    float ma[4] = {0.f, 0.f, 0.f, 0.f}, mb[4] = {0.f, 0.f, 0.f, 0.f};
+    for (uint64_t j0 = tid / q; j0 < K; j0 += 4 * step) {
+        float4 v[4];
+        float fa[4], fb[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const uint64_t j = j0 + u * step;
+            const bool ok = j < K;
+            v[u] = ok ? s4[j * q + qp] : make_float4(0.f, 0.f, 0.f, 0.f);
+            fa[u] = ok && ksa ? (float)ksa[j] : 1.f;
+            fb[u] = ok && ksb ? (float)ksb[j] : 1.f;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const float x[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                ma[i] = fmaxf(ma[i], fabsf(x[i] * fa[u]));
+                mb[i] = fmaxf(mb[i], fabsf(x[i] * fb[u]));
+            }
+        }
+    }
+    // lanes l, l + q, l + 2q, ... of a warp hold the same quad
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        if (o < q) break;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            ma[i] = fmaxf(ma[i], __shfl_xor_sync(0xffffffffu, ma[i], o));
+            mb[i] = fmaxf(mb[i], __shfl_xor_sync(0xffffffffu, mb[i], o));
+        }
+    }
+    // then the block's warps through shared memory: one atomic per column
+    // and block (non-negative floats order as their bits)
+    __shared__ unsigned red[8][2][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane < q) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            red[warp][0][4 * lane + i] = __float_as_uint(ma[i]);
+            red[warp][1][4 * lane + i] = __float_as_uint(mb[i]);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x < 64) {
+        const int set = threadIdx.x >> 5, c = threadIdx.x & 31;
+        unsigned* dst = set ? cmb : cma;
+        if (c < w && c < 4 * q && dst) {
+            unsigned m = 0;
+            for (int wv = 0; wv < (int)(blockDim.x >> 5); ++wv) m = max(m, red[wv][set][c]);
+            atomicMax(dst + c, m);
+        }
+    }
+}
+
+// Split-FP8 terms of both sets in one pass (the loads of the operand are
+// shared): as k_fp8_terms, with two K rows per E4M3 conversion (the paired
+// conversion rounds each value as the scalar one does, so the terms are the
+// same) and the power-of-two scales taken from per-column tables.
+__global__ void __launch_bounds__(256) k_fp8_terms_pair(const float* __restrict__ src, int ld, uint64_t K, int w,
+                                                        int wpad, uint64_t K_pad, TermSet sa, TermSet sb,
+                                                        uint8_t* __restrict__ B, float* __restrict__ inv_scale) {
+    constexpr int kT = kMainTerms + kIndTerms;
+    __shared__ __align__(16) uint8_t tile[kT][32][132];
+    __shared__ float ksa[128], ksb[128];
+    __shared__ float up[kT][32], dn[kT][32];
+    const uint64_t k0 = (uint64_t)blockIdx.x * 128;
+    const int c0 = blockIdx.y * 32;
+    const int nt = sa.terms + sb.terms;
+    for (int i = threadIdx.x; i < 128; i += blockDim.x) {
+        const uint64_t k = k0 + i;
+        ksa[i] = (sa.kscale && k < K) ? (float)sa.kscale[k] : 1.f;
+        ksb[i] = (sb.kscale && k < K) ? (float)sb.kscale[k] : 1.f;
+    }
+    for (int e = threadIdx.x; e < nt * 32; e += blockDim.x) {
+        const int t = e / 32, cc = e % 32, c = c0 + cc;
+        const bool first = t < sa.terms;
+        const int tt = first ? t : t - sa.terms;
+        const int e0 = c < w ? term_e0((first ? sa.colmax : sb.colmax)[c]) : 0;
+        up[t][cc] = pow2f(e0 + 4 * tt);
+        dn[t][cc] = pow2f(-(e0 + 4 * tt));
+        if (blockIdx.x == 0 && c < wpad)
+            inv_scale[(first ? sa.row_off : sb.row_off) + tt * wpad + c] = c < w ? pow2f(-(e0 + 4 * tt)) : 1.f;
+    }
+    __syncthreads();
+    for (int pr = threadIdx.x; pr < 64 * 32; pr += blockDim.x) {
+        const int kk = 2 * (pr / 32), cc = pr % 32;
+        const uint64_t k = k0 + kk;
+        const int c = c0 + cc;
+        float x0 = 0.f, x1 = 0.f;
+        if (c < w) {
+            if (k < K) x0 = (float)src[k * ld + c];
+            if (k + 1 < K) x1 = (float)src[(k + 1) * ld + c];
+        }
+#pragma unroll
+        for (int set = 0; set < 2; ++set) {
+            const int terms = set ? sb.terms : sa.terms, base = set ? sa.terms : 0;
+            const float* ks = set ? ksb : ksa;
+            float r0 = x0 * ks[kk], r1 = x1 * ks[kk + 1];
+#pragma unroll
+            for (int t = 0; t < kMainTerms; ++t) {
+                if (t < terms) {
+                    const float u = up[base + t][cc], d = dn[base + t][cc];
+                    const __nv_fp8x2_storage_t q2 =
+                        __nv_cvt_float2_to_fp8x2(make_float2(r0 * u, r1 * u), __NV_SATFINITE, __NV_E4M3);
+                    const float2 f = __half22float2(__half2(__nv_cvt_fp8x2_to_halfraw2(q2, __NV_E4M3)));
+                    r0 = fmaf(-f.x, d, r0);
+                    r1 = fmaf(-f.y, d, r1);
+                    tile[base + t][cc][kk] = (uint8_t)(q2 & 0xffu);
+                    tile[base + t][cc][kk + 1] = (uint8_t)(q2 >> 8);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (int e = threadIdx.x; e < nt * 32 * 32; e += blockDim.x) {
+        const int t = e / (32 * 32), rem = e % (32 * 32), cc = rem / 32, kp0 = (rem % 32) * 4;
+        const int c = c0 + cc;
+        if (c >= wpad) continue;
+        const int row = t < sa.terms ? sa.row_off + t * wpad + c : sb.row_off + (t - sa.terms) * wpad + c;
+        uint32_t word = 0;
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+            const int kp = kp0 + b;
+            const int kk = (kp & ~15) | ((kp & 7) << 1) | ((kp >> 3) & 1);
+            word |= (uint32_t)tile[t][cc][kk] << (8 * b);
+        }
+        *reinterpret_cast<uint32_t*>(B + (uint64_t)row * K_pad + k0 + kp0) = word;
+    }
+}
+
 __global__ void k_sub_colterm(double* __restrict__ S, int lds, uint64_t n, int w, const double* __restrict__ colterm) {
     const uint64_t total = n * w;
     for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total; t += (uint64_t)gridDim.x * blockDim.x) {
@@ -818,6 +971,35 @@ void launch_fp8_terms_f64(Ctx& c, const double* src, int ld, uint64_t K, int w, 
     k_fp8_terms<double><<<grid, 256, 0, c.stream>>>(src, ld, K, w, wpad, K_pad, kscale, terms, row_off, cm.get(), B,
                                                     inv_scale);
     SLFMM_LAUNCHED(c, "k_fp8_terms");
+}
+
+void launch_fp8_terms_f32_pair(Ctx& c, const float* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
+                               const double* ks_main, const double* ks_ind, int ind_row_off, uint8_t* B,
+                               float* inv_scale) {
+    SLFMM_REQUIRE(w >= 1 && w <= 128 && wpad <= 128, SLFMM_ERR_BAD_ARG, "operand wider than 128 columns");
+    DBuf<unsigned> cm(2 * (uint64_t)wpad, c.stream);
+    cm.zero();
+    unsigned* cma = cm.get();
+    unsigned* cmb = ks_ind ? cm.get() + wpad : nullptr;
+    const bool quads = ld % 4 == 0 && ld <= 32 && reinterpret_cast<uintptr_t>(src) % 16 == 0;
+    if (quads) {
+        const unsigned blocks = (unsigned)std::max<uint64_t>(
+            1, std::min<uint64_t>(ceil_div(K * (uint64_t)(ld / 4), 1024), (uint64_t)c.sm_count * 4));
+        k_colmax_pair<<<blocks, 256, 0, c.stream>>>(src, ld, K, w, ks_main, ks_ind, cma, cmb);
+        SLFMM_LAUNCHED(c, "k_colmax_pair");
+    } else {
+        k_colmax_abs<float><<<grid_for(c, K, 8), 256, 0, c.stream>>>(src, ld, K, w, ks_main, cma);
+        SLFMM_LAUNCHED(c, "k_colmax_abs");
+        if (ks_ind) {
+            k_colmax_abs<float><<<grid_for(c, K, 8), 256, 0, c.stream>>>(src, ld, K, w, ks_ind, cmb);
+            SLFMM_LAUNCHED(c, "k_colmax_abs");
+        }
+    }
+    const TermSet sa{ks_main, kMainTerms, 0, cma};
+    const TermSet sb{ks_ind, ks_ind ? kIndTerms : 0, ind_row_off, cmb};
+    dim3 grid((unsigned)ceil_div(K_pad, 128), (unsigned)ceil_div(wpad, 32));
+    k_fp8_terms_pair<<<grid, 256, 0, c.stream>>>(src, ld, K, w, wpad, K_pad, sa, sb, B, inv_scale);
+    SLFMM_LAUNCHED(c, "k_fp8_terms_pair");
 }
 
 void launch_fp8_terms_f32(Ctx& c, const float* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,

@@ -279,6 +279,13 @@ void launch_fp8_terms_f64(Ctx& c, const double* src, int ld, uint64_t K, int w, 
                           const double* kscale, int terms, int row_off, uint8_t* B, float* inv_scale);
 void launch_fp8_terms_f32(Ctx& c, const float* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
                           const double* kscale, int terms, int row_off, uint8_t* B, float* inv_scale);
+// both operands of a transposed pass in one pass over src: 4 terms of
+// diag(ks_main) src at B rows 0.., and (ks_ind non-null) 3 terms of
+// diag(ks_ind) src at B rows ind_row_off..; the same terms as two separate
+// launch_fp8_terms_f32 calls
+void launch_fp8_terms_f32_pair(Ctx& c, const float* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
+                               const double* ks_main, const double* ks_ind, int ind_row_off, uint8_t* B,
+                               float* inv_scale);
 // mode 0: out = P (+ M); mode 1: out = s_r (P - mu_r (cs_c - M)) (needs the indicator).
 // err_dev null: the launch waits and throws when a bounded device wait expired;
 // non-null: the kernel records the site there and the caller checks it later.
