@@ -21,7 +21,13 @@
 namespace slfmm {
 namespace {
 
-constexpr int kEpiSnps = 32;  // SNPs per CTA, 8 threads each
+// Tiles of 64 SNPs; each of 256 threads owns 4 SNPs x 4 traits of theta and
+// beta.  The coefficient rows stay in shared memory (transposed, traits
+// padded to 64) for the whole persistent CTA; the tile's u values are staged
+// k-major, so one k step is three 16-byte loads and 32 FMAs per thread.
+constexpr int kTileSnps = 64;
+constexpr int kTraitPad = 64;
+constexpr int kUsStride = kTileSnps + 4;  // 16-byte rows, staggered banks
 
 __global__ void __launch_bounds__(256) k_assoc_epilogue(
     uint64_t p, const float* __restrict__ u, int ldu, const double* __restrict__ tss,
@@ -30,78 +36,127 @@ __global__ void __launch_bounds__(256) k_assoc_epilogue(
     const double* __restrict__ cjj, const uint8_t* __restrict__ dropped,
     double* __restrict__ beta, float* __restrict__ t32, double* __restrict__ r2,
     uint32_t* __restrict__ hist) {
-    extern __shared__ float sm[];
-    float* th = sm;                    // d x w
-    float* bt = th + d * w;            // d x w
-    float* us = bt + d * w;            // kEpiSnps x w
+    extern __shared__ __align__(16) float sm[];
+    float* thT = sm;                          // [w][64]
+    float* btT = thT + w * kTraitPad;         // [w][64]
+    float* us = btT + w * kTraitPad;          // [w][68]
+    float* s2s = us + w * kUsStride;          // [64] sigma^2 per SNP of the tile
+    int* zvs = reinterpret_cast<int*>(s2s + kTileSnps);
+    __shared__ float cj[kTraitPad];
+    __shared__ int dr[kTraitPad];
     const int tid = threadIdx.x;
-    for (int e = tid; e < d * w; e += blockDim.x) {
-        th[e] = theta_rows[e];
-        bt[e] = beta_rows[e];
+    for (int e = tid; e < w * kTraitPad; e += blockDim.x) {
+        const int k = e / kTraitPad, jj = e % kTraitPad;
+        thT[e] = jj < d ? theta_rows[jj * w + k] : 0.f;
+        btT[e] = jj < d ? beta_rows[jj * w + k] : 0.f;
     }
-    const int s = tid >> 3, l8 = tid & 7;
-    const uint64_t j0 = (uint64_t)blockIdx.x * kEpiSnps;
-    const uint64_t j = j0 + s;
-    const bool live = j < p;
-    for (int e = tid; e < kEpiSnps * w; e += blockDim.x) {
-        const int r = e / w, k = e - r * w;
-        const uint64_t jj = j0 + r;
-        us[e] = jj < p ? u[jj * ldu + k] : 0.f;
+    for (int jj = tid; jj < kTraitPad; jj += blockDim.x) {
+        cj[jj] = jj < d ? (float)cjj[jj] : 0.f;
+        dr[jj] = jj < d ? (int)dropped[jj] : 1;
     }
-    __syncthreads();
-    const float* ur = us + s * w;
-    float ss = 0.f, sc = 0.f;
-    for (int k = l8; k < w; k += 8) {
-        const float v = ur[k];
-        ss = fmaf(v, v, ss);
-        if (k < d) sc = fmaf(v, v, sc);
-    }
+    const int sg = tid >> 4, tg = tid & 15;
+    const uint64_t ntiles = (p + kTileSnps - 1) / kTileSnps;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint64_t j0 = tile * kTileSnps;
+        __syncthreads();  // the previous tile's values are consumed (and the tables are in place)
+        for (int e = tid; e < w * kTileSnps; e += blockDim.x) {
+            const int k = e / kTileSnps, sn = e % kTileSnps;
+            us[k * kUsStride + sn] = j0 + sn < p ? u[(j0 + sn) * ldu + k] : 0.f;
+        }
+        __syncthreads();
+        // per-SNP sums, 8 lanes per SNP with stride-8 partials, two rounds of 32
+        for (int half = 0; half < 2; ++half) {
+            const int sn = half * 32 + (tid >> 3), l8 = tid & 7;
+            float ss = 0.f, sc = 0.f;
+            for (int k = l8; k < w; k += 8) {
+                const float v = us[k * kUsStride + sn];
+                ss = fmaf(v, v, ss);
+                if (k < d) sc = fmaf(v, v, sc);
+            }
 #pragma unroll
-    for (int o = 4; o > 0; o >>= 1) {
-        ss += __shfl_xor_sync(0xffffffffu, ss, o);
-        sc += __shfl_xor_sync(0xffffffffu, sc, o);
-    }
-    if (!live) return;
-    const bool zv = zero_var && zero_var[j];
-    const double T = tss[j];
-    double rss = T - (double)ss;
-    if (rss < 0.0 || zv) rss = 0.0;
-    const double sigma2 = rss / df;
-    if (l8 == 0) {
-        double a = 0.0, b = 0.0, c = 0.0;
-        if (T > 1e-300 && !zv) {                            // src/testing.rs:394-404
-            const double ssc = (double)sc;
-            a = ssc / T;
-            b = fmax(T - rss - ssc, 0.0) / T;
-            c = rss / T;
+            for (int o = 4; o > 0; o >>= 1) {
+                ss += __shfl_xor_sync(0xffffffffu, ss, o);
+                sc += __shfl_xor_sync(0xffffffffu, sc, o);
+            }
+            if (l8 == 0) {
+                const uint64_t j = j0 + sn;
+                float s2f = 0.f;
+                int zv = 1;
+                if (j < p) {
+                    zv = zero_var && zero_var[j];
+                    const double T = tss[j];
+                    double rss = T - (double)ss;
+                    if (rss < 0.0 || zv) rss = 0.0;
+                    s2f = (float)(rss / df);
+                    double a = 0.0, b = 0.0, c = 0.0;
+                    if (T > 1e-300 && !zv) {                        // src/testing.rs:394-404
+                        const double ssc = (double)sc;
+                        a = ssc / T;
+                        b = fmax(T - rss - ssc, 0.0) / T;
+                        c = rss / T;
+                    }
+                    r2[j * 3 + 0] = a;
+                    r2[j * 3 + 1] = b;
+                    r2[j * 3 + 2] = c;
+                }
+                s2s[sn] = s2f;
+                zvs[sn] = zv;
+            }
         }
-        r2[j * 3 + 0] = a;
-        r2[j * 3 + 1] = b;
-        r2[j * 3 + 2] = c;
-    }
-    const float s2f = (float)sigma2;
-    for (int jj = l8; jj < d; jj += 8) {
-        float theta = 0.f, bb = 0.f;
-        const float* trow = th + jj * w;
-        const float* brow = bt + jj * w;
+        __syncthreads();
+        float th[4][4], bb[4][4];
+#pragma unroll
+        for (int a = 0; a < 4; ++a)
+#pragma unroll
+            for (int b = 0; b < 4; ++b) th[a][b] = bb[a][b] = 0.f;
+        // the next k step's loads are issued before this step's FMAs
+        float4 un = *reinterpret_cast<const float4*>(us + 4 * sg);
+        float4 tn = *reinterpret_cast<const float4*>(thT + 4 * tg);
+        float4 bn = *reinterpret_cast<const float4*>(btT + 4 * tg);
         for (int k = 0; k < w; ++k) {
-            theta = fmaf(trow[k], ur[k], theta);
-            bb = fmaf(brow[k], ur[k], bb);
+            const float4 uv = un, tv = tn, bv = bn;
+            if (k + 1 < w) {
+                un = *reinterpret_cast<const float4*>(us + (k + 1) * kUsStride + 4 * sg);
+                tn = *reinterpret_cast<const float4*>(thT + (k + 1) * kTraitPad + 4 * tg);
+                bn = *reinterpret_cast<const float4*>(btT + (k + 1) * kTraitPad + 4 * tg);
+            }
+            const float ua[4] = {uv.x, uv.y, uv.z, uv.w};
+            const float ta[4] = {tv.x, tv.y, tv.z, tv.w};
+            const float ba[4] = {bv.x, bv.y, bv.z, bv.w};
+#pragma unroll
+            for (int a = 0; a < 4; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b) {
+                    th[a][b] = fmaf(ta[b], ua[a], th[a][b]);
+                    bb[a][b] = fmaf(ba[b], ua[a], bb[a][b]);
+                }
         }
-        float t = 0.f;
-        const float var = s2f * (float)cjj[jj];
-        if (!zv && !dropped[jj] && var > 0.f && isfinite(var)) {  // t_test guards
-            t = theta * rsqrtf(var);
-            if (!isfinite(t)) t = 0.f;
-        }
-        if (zv) bb = 0.f;
-        beta[j * d + jj] = (double)bb;
-        t32[j * d + jj] = t;
-        const float t2 = t * t;
-        if (isfinite(t2)) {
-            unsigned bin = (unsigned)fminf(t2 * 1000.0f, (float)(kHistBins - 1));
-            if (bin > (unsigned)(kHistBins - 1)) bin = kHistBins - 1;
-            atomicAdd(&hist[(uint64_t)jj * kHistBins + bin], 1u);
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+            const int sn = 4 * sg + a;
+            const uint64_t j = j0 + sn;
+            if (j >= p) continue;
+            const bool zv = zvs[sn] != 0;
+            const float s2f = s2s[sn];
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const int jj = 4 * tg + b;
+                if (jj >= d) continue;
+                float t = 0.f;
+                const float var = s2f * cj[jj];
+                if (!zv && !dr[jj] && var > 0.f && isfinite(var)) {  // t_test guards
+                    t = th[a][b] * rsqrtf(var);
+                    if (!isfinite(t)) t = 0.f;
+                }
+                beta[j * d + jj] = zv ? 0.0 : (double)bb[a][b];
+                t32[j * d + jj] = t;
+                const float t2 = t * t;
+                if (isfinite(t2)) {
+                    unsigned bin = (unsigned)fminf(t2 * 1000.0f, (float)(kHistBins - 1));
+                    if (bin > (unsigned)(kHistBins - 1)) bin = kHistBins - 1;
+                    atomicAdd(&hist[(uint64_t)jj * kHistBins + bin], 1u);
+                }
+            }
         }
     }
 }
@@ -263,11 +318,14 @@ void launch_assoc_epilogue(Ctx& c, uint64_t p, const float* u, int ldu, const do
                            const AssocConsts& k, double* beta, float* t32, double* r2,
                            uint32_t* hist) {
     if (p == 0) return;
-    const size_t smem = (size_t)(2 * k.d * k.w + kEpiSnps * k.w) * sizeof(float);
+    SLFMM_REQUIRE(k.d <= kTraitPad, SLFMM_ERR_BAD_ARG, "at most 64 traits");
+    const size_t smem = (size_t)(2 * k.w * kTraitPad + k.w * kUsStride + 2 * kTileSnps) * sizeof(float);
     if (smem > 48 * 1024)
         SLFMM_CUDA(cudaFuncSetAttribute(k_assoc_epilogue, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem));
-    k_assoc_epilogue<<<(unsigned)ceil_div(p, kEpiSnps), 256, smem, c.stream>>>(
+    const uint64_t tiles = ceil_div(p, (uint64_t)kTileSnps);
+    const unsigned grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)c.sm_count * 3);
+    k_assoc_epilogue<<<grid, 256, smem, c.stream>>>(
         p, u, ldu, tss, k.zero_var, k.d, k.w, k.df, k.theta_rows, k.beta_rows, k.cjj, k.dropped,
         beta, t32, r2, hist);
     SLFMM_LAUNCHED(c, "k_assoc_epilogue");
