@@ -344,6 +344,77 @@ void fp8_row_launch(Ctx& c, const Geno& g, const SnpStd& s, const Fp8RowOperand&
                     s.scale.get() + r0, op.cs.get(), out + r0 * op.wp, op.wp, 1, 0, err_dev);
 }
 
+// A split-FP8 SNP-row pass prepared once and run over row ranges (r0 a
+// multiple of 128): either the indicator form, or column blocks without the
+// indicator followed by the per-SNP fix over the missing-call lists
+// (operands too wide for TMEM).  The association pass runs it chunk by chunk
+// so that finished rows can be copied out while later ones compute.
+struct Fp8RowPass {
+    int w = 0, wp = 0;
+    uint64_t n_pad = 0;
+    Fp8RowOperand op;  // indicator form when op.ok
+    std::vector<Fp8Plan> plans;
+    std::vector<DBuf<uint8_t>> Bs;
+    std::vector<DBuf<float>> iscs;
+    std::vector<int> c0s;
+    DBuf<float> W32;
+    DBuf<double> cs;
+};
+
+void fp8_row_prepare(Ctx& c, const Geno& g, const double* W, int w, int ldw, Fp8RowPass& rp) {
+    rp.w = w;
+    rp.wp = pad16(w);
+    rp.n_pad = round_up(g.n, 256);  // whole split-FP8 stages (256 codes)
+    const uint64_t tiles = ceil_div(g.p, 128);
+    build_tiles(c, g, false);
+    if (fp8_row_operand(c, g.n, tiles, W, w, ldw, rp.op)) return;
+    rp.W32.alloc(rp.n_pad * rp.wp, c.stream);
+    launch_f64_to_f32_pad(c, W, g.n, w, ldw, rp.W32.get(), rp.n_pad, rp.wp);
+    const Fp8Plan pl = fp8_plan(rp.wp, false, tiles);
+    const int cb = pl.ok ? rp.wp : 64;
+    rp.cs.alloc(rp.wp, c.stream);
+    rp.cs.zero();
+    launch_colsums(c, W, g.n, w, ldw, rp.cs.get());
+    for (int c0 = 0; c0 < w; c0 += cb) {
+        // the epilogue writes pb.wpad columns: the last block is padded only to 16
+        const int wb = std::min(cb, w - c0), bp = std::min(cb, pad16(wb));
+        const Fp8Plan pb = bp == rp.wp ? pl : fp8_plan(bp, false, tiles);
+        DBuf<uint8_t> B((uint64_t)pb.n_total * rp.n_pad, c.stream);
+        DBuf<float> isc(pb.n_total, c.stream);
+        launch_fp8_terms_f64(c, W + c0, ldw, g.n, wb, bp, rp.n_pad, nullptr, 4, 0, B.get(), isc.get());
+        rp.plans.push_back(pb);
+        rp.Bs.push_back(std::move(B));
+        rp.iscs.push_back(std::move(isc));
+        rp.c0s.push_back(c0);
+    }
+    build_missing_lists(c, g);
+}
+
+// rows [r0, r0 + rows) of out (ld wp); err_dev as in launch_tc8_rows.  The
+// tensor-core launches are profiled as "row_contract" (algorithmic bytes:
+// the rows' packed codes, their outputs and the operand).
+void fp8_row_run(Ctx& c, const Geno& g, const SnpStd& s, const Fp8RowPass& rp, uint64_t r0, uint64_t rows,
+                 float* out, int* err_dev) {
+    const double bytes = (double)rows * ceil_div(g.n, 4) + (double)rows * rp.w * 4 + (double)g.n * rp.w * 4;
+    const double flops = 2.0 * g.n * rows * rp.w;
+    if (rp.op.ok) {
+        ProfScope ps(c, "row_contract", bytes, flops);
+        fp8_row_launch(c, g, s, rp.op, r0, rows, out, err_dev);
+        return;
+    }
+    const uint64_t t0 = r0 / 128;
+    const TileView tv{g.tiles.get() + t0 * g.kbt * 4096, g.kbt, g.ntiles - t0};
+    for (size_t b = 0; b < rp.plans.size(); ++b) {
+        const double share = (double)rp.plans[b].wpad / rp.wp;
+        ProfScope ps(c, "row_contract", bytes * share, flops * share);
+        launch_tc8_rows(c, rp.plans[b], tv, rows, g.n, rp.Bs[b].get(), rp.iscs[b].get(), rp.n_pad, 0,
+                        s.mean.get() + r0, s.scale.get() + r0, rp.cs.get(), out + r0 * rp.wp + rp.c0s[b], rp.wp, 1,
+                        0, err_dev);
+    }
+    launch_rowfix_mean(c, out + r0 * rp.wp, rp.wp, rows, rp.w, g.miss_ptr.get() + r0, g.miss_idx.get(),
+                       rp.W32.get(), rp.wp, rp.cs.get(), s.mean.get() + r0, s.scale.get() + r0);
+}
+
 // out (p x wp, FP32) = Y_hat^T W, W = n x w FP64 (leading dim ldw)
 void row_contract_base(Ctx& c, const Geno& g, const SnpStd& s, const double* W, int w, int ldw,
                        DBuf<float>& out, int& wp) {
@@ -354,41 +425,10 @@ void row_contract_base(Ctx& c, const Geno& g, const SnpStd& s, const double* W, 
     const double bytes = (double)g.p * ceil_div(g.n, 4) + (double)g.p * w * 4 + (double)g.n * w * 4;
     if (c.precision == SLFMM_PREC_SPLIT_FP8) {
         // exact E4M3 genotypes x 4 scaled E4M3 terms of W; with the missing-call
-        // indicator operand the epilogue applies out = s_j (P - mu_j (cs - M)).
-        // Operands too wide for TMEM run as column blocks of 64 and a
-        // per-SNP fix over the missing-call lists.
-        const uint64_t tiles = ceil_div(g.p, 128);
-        {
-            Fp8RowOperand op;
-            if (fp8_row_operand(c, g.n, tiles, W, w, ldw, op)) {
-                build_tiles(c, g, false);
-                ProfScope ps(c, "row_contract", bytes, 2.0 * g.n * g.p * w);
-                fp8_row_launch(c, g, s, op, 0, g.p, out.get(), nullptr);
-                return;
-            }
-        }
-        DBuf<float> W32(n_pad * wp, c.stream);
-        launch_f64_to_f32_pad(c, W, g.n, w, ldw, W32.get(), n_pad, wp);
-        const Fp8Plan pl = fp8_plan(wp, false, tiles);
-        const int cb = pl.ok ? wp : 64;
-        DBuf<double> cs(wp, c.stream);
-        cs.zero();
-        launch_colsums(c, W, g.n, w, ldw, cs.get());
-        const TileView tv = build_tiles(c, g, false);
-        for (int c0 = 0; c0 < w; c0 += cb) {
-            // the epilogue writes pb.wpad columns: the last block is padded only to 16
-            const int wb = std::min(cb, w - c0), bp = std::min(cb, pad16(wb));
-            const Fp8Plan pb = bp == wp ? pl : fp8_plan(bp, false, tiles);
-            DBuf<uint8_t> B((uint64_t)pb.n_total * n_pad, c.stream);
-            DBuf<float> isc(pb.n_total, c.stream);
-            launch_fp8_terms_f64(c, W + c0, ldw, g.n, wb, bp, n_pad, nullptr, 4, 0, B.get(), isc.get());
-            ProfScope ps(c, "row_contract", bytes * wb / w, 2.0 * g.n * g.p * wb);
-            launch_tc8_rows(c, pb, tv, g.p, g.n, B.get(), isc.get(), n_pad, 0, s.mean.get(), s.scale.get(),
-                            cs.get(), out.get() + c0, wp, 1, 0);
-        }
-        build_missing_lists(c, g);
-        launch_rowfix_mean(c, out.get(), wp, g.p, w, g.miss_ptr.get(), g.miss_idx.get(), W32.get(), wp, cs.get(),
-                           s.mean.get(), s.scale.get());
+        // indicator operand the epilogue applies out = s_j (P - mu_j (cs - M))
+        Fp8RowPass rp;
+        fp8_row_prepare(c, g, W, w, ldw, rp);
+        fp8_row_run(c, g, s, rp, 0, g.p, out.get(), nullptr);
         return;
     }
     DBuf<float> W32(n_pad * wp, c.stream);
@@ -819,12 +859,6 @@ void assoc(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, const doubl
         for (int jj = 0; jj < d; ++jj)
             for (int k = 1; k < w; ++k) bt[jj * wu + (k - 1)] = (float)Bh[jj * w + k];
     }
-    // u = Q_C[:, 1:]^T y for every SNP
-    DBuf<float> U;
-    int wp = 0;
-    phase(c, "association design");
-    row_contract(c, g, st, QC.get() + 1, wu, w, U, wp);
-    phase(c, "association row pass");
     DBuf<float> thd = upload(c, th.data(), th.size()), btd = upload(c, bt.data(), bt.size());
     DBuf<double> cjjd = upload(c, cjj.data(), cjj.size());
     DBuf<uint8_t> dxd = upload(c, drop_x.data(), drop_x.size());
@@ -834,7 +868,60 @@ void assoc(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, const doubl
     DBuf<float> t32(pp * d, c.stream);
     DBuf<uint32_t> hist((size_t)d * kHistBins, c.stream);
     hist.zero();
-    {
+    phase(c, "association design");
+    // u = Q_C[:, 1:]^T y for every SNP, then the statistics.  With page-locked
+    // host outputs the split-FP8 pass runs in chunks of SNPs: each chunk's
+    // beta and r2 are final after its epilogue and copy out on the copy
+    // stream while later chunks compute (t and p wait for the GIF).
+    DBuf<float> U;
+    int wp = 0;
+    const uint64_t chunk = round_up(ceil_div(p, 8), 128);
+    const bool chunked = c.precision == SLFMM_PREC_SPLIT_FP8 && st.fill.k == 0 && p >= 2 * chunk &&
+                         (out.beta || out.r2) && (!out.beta || is_pinned(out.beta)) &&
+                         (!out.r2 || is_pinned(out.r2));
+    bool copied = false;
+    if (chunked) {
+        Fp8RowPass rp;
+        fp8_row_prepare(c, g, QC.get() + 1, wu, w, rp);
+        wp = rp.wp;
+        U.alloc(pp * wp, c.stream);
+        DBuf<int> err(1, c.stream);
+        err.zero();
+        cudaEvent_t ev;
+        SLFMM_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+        struct EvGuard {
+            cudaEvent_t e;
+            ~EvGuard() { cudaEventDestroy(e); }
+        } evg{ev};
+        for (uint64_t r0 = 0; r0 < p; r0 += chunk) {
+            const uint64_t rows = std::min(chunk, p - r0);
+            fp8_row_run(c, g, st, rp, r0, rows, U.get(), err.get());
+            AssocConsts kc = k;
+            kc.zero_var = k.zero_var ? k.zero_var + r0 : nullptr;
+            {
+                ProfScope ps(c, "assoc_epilogue", (double)rows * (wu * 4 + 8 + d * 12 + 24), 4.0 * rows * d * wu);
+                launch_assoc_epilogue(c, rows, U.get() + r0 * wp, wp, st.tss.get() + r0, kc, beta.get() + r0 * d,
+                                      t32.get() + r0 * d, r2.get() + r0 * 3, hist.get());
+            }
+            SLFMM_CUDA(cudaEventRecord(ev, c.stream));
+            SLFMM_CUDA(cudaStreamWaitEvent(c.copy_stream, ev, 0));
+            if (out.beta)
+                SLFMM_CUDA(cudaMemcpyAsync(out.beta + r0 * d, beta.get() + r0 * d, rows * d * sizeof(double),
+                                           cudaMemcpyDeviceToHost, c.copy_stream));
+            if (out.r2)
+                SLFMM_CUDA(cudaMemcpyAsync(out.r2 + r0 * 3, r2.get() + r0 * 3, rows * 3 * sizeof(double),
+                                           cudaMemcpyDeviceToHost, c.copy_stream));
+        }
+        const int e = fetch(c, err.get(), 1)[0];
+        if (e) {
+            SLFMM_CUDA(cudaStreamSynchronize(c.copy_stream));
+            throw_tc8_timeout(e);
+        }
+        copied = true;
+        phase(c, "association row pass and statistics");
+    } else {
+        row_contract(c, g, st, QC.get() + 1, wu, w, U, wp);
+        phase(c, "association row pass");
         ProfScope ps(c, "assoc_epilogue", (double)p * (wu * 4 + 8 + d * 12 + 24), 4.0 * p * d * wu);
         launch_assoc_epilogue(c, p, U.get(), wp, st.tss.get(), k, beta.get(), t32.get(), r2.get(), hist.get());
     }
@@ -852,11 +939,12 @@ void assoc(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, const doubl
     DBuf<double> gptd = upload(c, gpt.data(), gpt.size());
     launch_calibrate(c, p, d, t32.get(), gptd.get(), t64.get(), pv.get());
     phase(c, "association statistics, GIF");
-    if (out.beta) d2h(c, out.beta, beta.get(), p * d);
+    if (out.beta && !copied) d2h(c, out.beta, beta.get(), p * d);
     if (out.tstat) d2h(c, out.tstat, t64.get(), p * d);
     if (out.pvalue) d2h(c, out.pvalue, pv.get(), p * d);
-    if (out.r2) d2h(c, out.r2, r2.get(), p * 3);
+    if (out.r2 && !copied) d2h(c, out.r2, r2.get(), p * 3);
     sync(c);
+    SLFMM_CUDA(cudaStreamSynchronize(c.copy_stream));
     phase(c, "results to host");
 }
 

@@ -101,3 +101,32 @@ def test_lists_overrun_rebuilt(engines, prec):
     res = sg.fit_lfmm2_host(packed, N, c.x, cfg, omega=omega, engine=engines[prec])
     ref = O.fit_oracle64(raw, raw, c.x, k=3, oversampling=5, norm=O.NORM_EIGENSTRAT, omega=omega)
     _check(res, ref.assoc, ref.u_hat)
+
+
+def _pinned_out(sg, n, p, d, k):
+    out, keep = {}, []
+    for name, shape in (("u_hat", (n, k)), ("beta", (p, d)), ("tstat", (p, d)), ("pvalue", (p, d)),
+                        ("r2", (p, 3)), ("gif_per_trait", (d,))):
+        pa = sg.PinnedArray(shape, np.float64)
+        out[name] = pa.array
+        keep.append(pa)
+    return out, keep
+
+
+@pytest.mark.parametrize("d", [2, 30])
+def test_fit_host_pinned_outputs_chunked(engine, cohort, d):
+    """Page-locked outputs: the association pass runs in SNP chunks and copies
+    beta and r2 while later chunks compute; bit for bit the resident fit.
+    d = 30 takes the association pass without the indicator (missing-call
+    lists per chunk), d = 2 the indicator form."""
+    sg = _sg()
+    c = cohort
+    x = c.x[:, :d]
+    cfg = sg.Lfmm2Config(k=3, oversampling=5, norm=sg.SnpNorm.EIGENSTRAT)
+    omega = O.rng_normal_matrix(5, c.n, 8)
+    out, keep = _pinned_out(sg, c.n, c.p, d, 3)
+    host = sg.fit_lfmm2_host(c.packed, c.n, x, cfg, omega=omega, engine=engine, out=out)
+    geno = engine.upload(c.packed, c.n)
+    res = sg.fit_lfmm2(geno, sg.SubsetSpec.all(), geno, x, cfg, omega=omega, engine=engine)
+    _same(host, res)
+    del keep
