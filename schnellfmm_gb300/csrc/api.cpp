@@ -131,6 +131,8 @@ bool is_pinned(const void* p) {
 // Work run on each chunk of rows [r0, r1) right after it lands (tiles,
 // counts and missing-call offsets of the chunk are ready).
 struct ChunkHook {
+    // device setup, run once while the first chunks are being copied
+    virtual void begin(Ctx& c) {}
     virtual void rows(Ctx& c, const Geno& g, uint64_t r0, uint64_t r1) = 0;
     virtual ~ChunkHook() = default;
 };
@@ -177,36 +179,44 @@ void upload_geno(Ctx& c, Geno& g, const uint8_t* packed, uint64_t n_phys, uint64
         uint64_t cap = 0;  // index capacity, sized from the first chunk's density
         uint64_t first_end = 0;
         const bool direct = is_pinned(packed);
-        DBuf<uint8_t> dstage[2];
-        dstage[0].alloc(rows_per * bps, c.stream);
-        dstage[1].alloc(rows_per * bps, c.stream);
-        uint8_t* hstage[2] = {nullptr, nullptr};
-        cudaEvent_t copied[2], consumed[2];
-        for (int b = 0; b < 2; ++b) {
+        const uint64_t nchunks = ceil_div(g.p, rows_per);
+        // staging depth: two buffers (measured on GB300: deeper staging of a
+        // page-locked payload neither shortens the upload nor hides the hook's
+        // setup better); a pageable payload goes through two pinned buffers
+        const char* ns_env = std::getenv("SLFMM_UPLOAD_STAGES");  // tuning override
+        const uint64_t ns_direct = ns_env && *ns_env ? (uint64_t)std::max(2, std::atoi(ns_env)) : 2;
+        const int NS = (int)std::max<uint64_t>(1, std::min<uint64_t>(direct ? ns_direct : 2, nchunks));
+        std::vector<DBuf<uint8_t>> dstage(NS);
+        for (auto& d : dstage) d.alloc(rows_per * bps, c.stream);
+        std::vector<uint8_t*> hstage(NS, nullptr);
+        std::vector<cudaEvent_t> copied(NS, nullptr), consumed(NS, nullptr);
+        struct Cleanup {
+            std::vector<uint8_t*>& h;
+            std::vector<cudaEvent_t>& a;
+            std::vector<cudaEvent_t>& b;
+            ~Cleanup() {
+                for (size_t i = 0; i < h.size(); ++i) {
+                    if (h[i]) cudaFreeHost(h[i]);
+                    if (a[i]) cudaEventDestroy(a[i]);
+                    if (b[i]) cudaEventDestroy(b[i]);
+                }
+            }
+        } cleanup{hstage, copied, consumed};
+        for (int b = 0; b < NS; ++b) {
             SLFMM_CUDA(cudaEventCreateWithFlags(&copied[b], cudaEventDisableTiming));
             SLFMM_CUDA(cudaEventCreateWithFlags(&consumed[b], cudaEventDisableTiming));
             SLFMM_CUDA(cudaEventRecord(consumed[b], c.stream));
         }
-        struct Cleanup {
-            uint8_t** h; cudaEvent_t* a; cudaEvent_t* b;
-            ~Cleanup() {
-                for (int i = 0; i < 2; ++i) {
-                    if (h[i]) cudaFreeHost(h[i]);
-                    cudaEventDestroy(a[i]);
-                    cudaEventDestroy(b[i]);
-                }
-            }
-        } cleanup{hstage, copied, consumed};
         if (!direct)
-            for (int b = 0; b < 2; ++b) SLFMM_CUDA(cudaMallocHost(&hstage[b], rows_per * bps));
+            for (int b = 0; b < NS; ++b) SLFMM_CUDA(cudaMallocHost(&hstage[b], rows_per * bps));
         SLFMM_CUDA(cudaStreamSynchronize(c.stream));
-        const uint64_t nchunks = ceil_div(g.p, rows_per);
-        for (uint64_t ch = 0; ch < nchunks; ++ch) {
-            const int b = (int)(ch & 1);
+        // copy chunk ch into staging buffer ch % NS once the repack that last
+        // used the buffer is done
+        auto issue = [&](uint64_t ch) {
+            const int b = (int)(ch % NS);
             const uint64_t r0 = ch * rows_per, r1 = std::min(g.p, r0 + rows_per), rows = r1 - r0;
             bool contiguous = true;  // one copy when the rows are consecutive (src/parallel.rs:129-146)
             for (uint64_t r = r0 + 1; r < r1 && contiguous; ++r) contiguous = snps[r] == snps[r - 1] + 1;
-            // wait until the repack that last used buffer b is done
             SLFMM_CUDA(cudaStreamWaitEvent(c.copy_stream, consumed[b], 0));
             if (direct && contiguous) {
                 SLFMM_CUDA(cudaMemcpyAsync(dstage[b].get(), packed + snps[r0] * bps, rows * bps,
@@ -228,9 +238,16 @@ void upload_geno(Ctx& c, Geno& g, const uint8_t* packed, uint64_t n_phys, uint64
                                            c.copy_stream));
             }
             SLFMM_CUDA(cudaEventRecord(copied[b], c.copy_stream));
+        };
+        for (uint64_t ch = 0; ch + 1 < (uint64_t)NS; ++ch) issue(ch);
+        if (hook) hook->begin(c);
+        for (uint64_t ch = 0; ch < nchunks; ++ch) {
+            if (ch + NS - 1 < nchunks) issue(ch + NS - 1);
+            const int b = (int)(ch % NS);
+            const uint64_t r0 = ch * rows_per, r1 = std::min(g.p, r0 + rows_per), rows = r1 - r0;
             if (ch == 1) {
-                // the first chunk's list length sizes the index array (the
-                // second chunk's copy is already in flight); 1.5x its density
+                // the first chunk's list length sizes the index array (later
+                // chunks' copies are already in flight); 1.5x its density
                 // plus slack, and a chunk that overruns it leaves the lists
                 // to be rebuilt after the upload
                 const uint64_t nnz0 = fetch(c, g.miss_ptr.get() + first_end, 1)[0];
@@ -316,13 +333,21 @@ struct Fp8RowOperand {
     DBuf<double> cs;
 };
 
+// whether a width-w row pass has the indicator plan (SLFMM_TC8_ROW_IND=0 turns
+// it off)
+bool fp8_row_indicator_plan(int w, uint64_t tiles) {
+    const int wp = pad16(w);
+    const char* ind_env = std::getenv("SLFMM_TC8_ROW_IND");
+    if (wp > kMaxW || (ind_env && ind_env[0] == '0')) return false;
+    const Fp8Plan pl = fp8_plan(wp, true, tiles);
+    return pl.ok && pl.n_ind != 0;
+}
+
 bool fp8_row_operand(Ctx& c, uint64_t n, uint64_t tiles, const double* W, int w, int ldw, Fp8RowOperand& op) {
     op.wp = pad16(w);
     op.n_pad = round_up(n, 256);  // whole split-FP8 stages (256 codes)
-    const char* ind_env = std::getenv("SLFMM_TC8_ROW_IND");
-    if (op.wp > kMaxW || (ind_env && ind_env[0] == '0')) return false;
+    if (!fp8_row_indicator_plan(w, tiles)) return false;
     op.pl = fp8_plan(op.wp, true, tiles);
-    if (!op.pl.ok || op.pl.n_ind == 0) return false;
     op.cs.alloc(op.wp, c.stream);
     op.cs.zero();
     launch_colsums(c, W, n, w, ldw, op.cs.get());
@@ -1114,12 +1139,35 @@ void check_cfg(const slfmm_config* cfg) {
 // The operands and kernels are those of the pass after the upload, so the
 // sketch is identical; it only moves under the host-link-bound copies.
 struct Presketch : ChunkHook {
+    // inputs of the setup
+    uint64_t n = 0, p = 0;
+    const double* x = nullptr;
+    int d = 0;
+    const slfmm_config* cfg = nullptr;
+    const double* omega = nullptr;
+    // state
     Step0 s0;
     SnpStd se;
     int norm = 0, l = 0;
     Fp8RowOperand op;
     DBuf<float> Z;
     DBuf<int> err;
+    // covariates (Step 0), P Omega and its split-FP8 operand, while the first
+    // chunks are being copied
+    void begin(Ctx& c) override {
+        step0(c, x, n, d, cfg->lambda, cfg->scale_cov != 0, s0);
+        DBuf<double> W;
+        sketch_operand(c, s0, n, l, cfg->seed, omega, W);
+        SLFMM_REQUIRE(fp8_row_operand(c, n, ceil_div(p, 128), W.get(), l, l, op), SLFMM_ERR_CUDA,
+                      "sketch operand plan changed");
+        se.mean.alloc(p, c.stream);
+        se.scale.alloc(p, c.stream);
+        se.tss.alloc(p, c.stream);
+        se.zero_var.alloc(p, c.stream);
+        Z.alloc(p * op.wp, c.stream);
+        err.alloc(1, c.stream);
+        err.zero();
+    }
     void rows(Ctx& c, const Geno& g, uint64_t r0, uint64_t r1) override {
         launch_stats_mean_range(c, g, r0, r1 - r0, norm, se.mean.get(), se.scale.get(), se.tss.get(),
                                 se.zero_var.get());
@@ -1128,25 +1176,22 @@ struct Presketch : ChunkHook {
 };
 
 // true when the estimation and testing matrices are the same upload of p SNPs
-// with mean imputation and the sketch width has an indicator plan
-bool presketch_prepare(Ctx& c, uint64_t n, uint64_t p, const double* x, int d, const slfmm_config* cfg,
-                       const double* omega, Presketch& ps) {
+// with mean imputation and the sketch width has an indicator plan (host-side
+// checks only; the device setup runs in begin())
+bool presketch_eligible(Ctx& c, uint64_t n, uint64_t p, const double* x, int d, const slfmm_config* cfg,
+                        const double* omega, Presketch& ps) {
     if (c.precision != SLFMM_PREC_SPLIT_FP8 || cfg->impute != SLFMM_IMPUTE_MEAN || p == 0) return false;
     check_cfg(cfg);
     ps.l = (int)cfg->k + (int)cfg->oversampling;
     if (ps.l > 64 || p < (uint64_t)ps.l || n < (uint64_t)ps.l) return false;  // the fit reports these
-    step0(c, x, n, d, cfg->lambda, cfg->scale_cov != 0, ps.s0);
-    DBuf<double> W;
-    sketch_operand(c, ps.s0, n, ps.l, cfg->seed, omega, W);
-    if (!fp8_row_operand(c, n, ceil_div(p, 128), W.get(), ps.l, ps.l, ps.op)) return false;
+    if (!fp8_row_indicator_plan(ps.l, ceil_div(p, 128))) return false;
+    ps.n = n;
+    ps.p = p;
+    ps.x = x;
+    ps.d = d;
+    ps.cfg = cfg;
+    ps.omega = omega;
     ps.norm = cfg->norm;
-    ps.se.mean.alloc(p, c.stream);
-    ps.se.scale.alloc(p, c.stream);
-    ps.se.tss.alloc(p, c.stream);
-    ps.se.zero_var.alloc(p, c.stream);
-    ps.Z.alloc(p * ps.op.wp, c.stream);
-    ps.err.alloc(1, c.stream);
-    ps.err.zero();
     return true;
 }
 
@@ -1486,16 +1531,15 @@ int slfmm_fit_host(slfmm_ctx* c, const uint8_t* packed, uint64_t n_physical, uin
     // with every SNP in the estimation, the sketch pass runs under the upload
     Presketch ps;
     phase(*c, "", true);
-    const bool pre = all && cfg && presketch_prepare(*c, sample_keep ? n_keep : n_physical, n_snps, x, (int)d, cfg,
-                                                     omega, ps);
-    if (pre) phase(*c, "covariates, sketch operand");
+    const bool pre = all && cfg && presketch_eligible(*c, sample_keep ? n_keep : n_physical, n_snps, x, (int)d,
+                                                      cfg, omega, ps);
     upload_geno(*c, full, packed, n_physical, n_snps, sample_keep, n_keep, subset_indices(nullptr, n_snps),
                 pre ? &ps : nullptr);
     if (pre) {
         const int e = fetch(*c, ps.err.get(), 1)[0];
         if (e) throw_tc8_timeout(e);
     }
-    phase(*c, pre ? "upload with the sketch pass" : "upload");
+    phase(*c, pre ? "covariates; upload with the sketch pass" : "upload");
     const Geno* ge = &full;
     if (!all) {
         upload_geno(*c, sub, packed, n_physical, n_snps, sample_keep, n_keep, subset_indices(est, n_snps));
