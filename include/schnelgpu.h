@@ -186,6 +186,43 @@ int slfmm_fit_host(slfmm_ctx* ctx, const uint8_t* packed, uint64_t n_physical,
                    const slfmm_subset* est, const double* x, uint32_t d,
                    const slfmm_config* cfg, const double* omega, slfmm_results* res);
 
+/* ---- batched fits --------------------------------------------------------- */
+/* Per-trait models on their own sample sets.  Trait t (of n_traits) uses the
+ * samples i of the resident matrix g with masks[i * n_traits + t] != 0, in
+ * sample order, and is a d = 1 model with x = y[i * n_traits + t] (y is
+ * n x n_traits row-major; values at masked samples are ignored).  This is the
+ * reference's one run per trait with its covariate file holding the trait's
+ * samples and --intersect-samples (src/main.rs:128-138: load_covariates keeps
+ * the matched samples, BedFile::subset_samples (src/bed.rs:155-159)
+ * restricts the genotypes).
+ * res[t] receives trait t's results with u_hat n_t x K (n_t = its sample
+ * count), beta / tstat / pvalue p x 1, r2 p x 3, gif_per_trait 1.  Each
+ * trait's sample subset is extracted on the device from the resident matrix;
+ * nothing is uploaded again. */
+int slfmm_fit_traits(slfmm_ctx* ctx, const slfmm_geno* g, const double* y, const uint8_t* masks,
+                     uint32_t n_traits, const slfmm_config* cfg, slfmm_results* res);
+
+/* One independent problem of slfmm_fit_many: the arguments of slfmm_fit_host
+ * with every SNP in the estimation. */
+typedef struct slfmm_problem {
+    const uint8_t* packed; /* p x ceil(n_physical / 4) PLINK payload (host) */
+    uint64_t n_physical;
+    uint64_t n_snps;
+    const double* x;       /* n_physical x d row-major */
+    uint32_t d;
+    const slfmm_config* cfg;
+    const double* omega;   /* n x (K + oversampling) or NULL */
+    slfmm_results* res;
+} slfmm_problem;
+
+/* Many independent problems of uneven n, p, K and d (the reference runs them
+ * one CLI invocation at a time): they run concurrently on n_streams internal
+ * streams of the context's device (0: 4), each problem's kernels in order on
+ * one stream.  status[i] (may be NULL) receives problem i's status; returns
+ * the first nonzero status, or SLFMM_OK. */
+int slfmm_fit_many(slfmm_ctx* ctx, const slfmm_problem* problems, uint32_t n_problems,
+                   uint32_t n_streams, int* status);
+
 /* ---- synthetic cohorts (plays the role of src/simulate.rs:49-142) ------- */
 /* Draw a structured cohort directly into a device-resident matrix: n
  * samples with admixture proportions admix (n x n_pop, host, rows sum to 1),

@@ -31,7 +31,7 @@ import math
 import os
 from dataclasses import dataclass, field
 from pathlib import Path
-from typing import List, Optional, Sequence
+from typing import List, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -93,6 +93,11 @@ class _Config(C.Structure):
 _dp = C.POINTER(C.c_double)
 
 
+class _Problem(C.Structure):
+    _fields_ = [("packed", C.c_void_p), ("n_physical", C.c_uint64), ("n_snps", C.c_uint64), ("x", C.c_void_p),
+                ("d", C.c_uint32), ("cfg", C.c_void_p), ("omega", C.c_void_p), ("res", C.c_void_p)]
+
+
 class _Results(C.Structure):
     _fields_ = [("u_hat", _dp), ("beta", _dp), ("tstat", _dp), ("pvalue", _dp), ("r2", _dp),
                 ("gif_per_trait", _dp), ("gif", C.c_double), ("nmf_cv", _dp), ("nmf_cv_mean", C.c_double),
@@ -107,7 +112,7 @@ EXPORTED_SYMBOLS = (
     "slfmm_generate_omega", "slfmm_estimate_factors", "slfmm_test_associations", "slfmm_fit",
     "slfmm_fit_host", "slfmm_write_tsv", "slfmm_format_exp6", "slfmm_simulate", "slfmm_geno_download",
     "slfmm_profile_enable", "slfmm_profile_read", "slfmm_host_alloc", "slfmm_host_free", "slfmm_contract_raw",
-    "slfmm_gif_noalloc",
+    "slfmm_gif_noalloc", "slfmm_fit_traits", "slfmm_fit_many",
 )
 
 _lib_handle = None
@@ -155,6 +160,8 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
         "slfmm_host_free": (i32, [vp]),
         "slfmm_contract_raw": (i32, [vp, vp, i32, vp, u32, vp]),
         "slfmm_gif_noalloc": (i32, [vp, vp, u64, u32, vp]),
+        "slfmm_fit_traits": (i32, [vp, vp, vp, vp, u32, C.POINTER(_Config), C.POINTER(_Results)]),
+        "slfmm_fit_many": (i32, [vp, C.POINTER(_Problem), u32, u32, C.POINTER(C.c_int)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -680,6 +687,64 @@ def fit_lfmm2(y_est, est_subset: SubsetSpec, y_full, x: np.ndarray, config: Lfmm
     if output is not None:
         write_tsv(output.path, output.bim, output.cov_names, res)
     return res
+
+
+def fit_lfmm2_traits(y_full: "Genotypes", y: np.ndarray, masks: np.ndarray, config: Lfmm2Config,
+                     engine: Optional[Engine] = None) -> List[TestResults]:
+    """One d = 1 model per trait (column of y, n x T) on the samples where
+    masks[:, t] is nonzero -- the reference run once per trait with that
+    trait's samples and --intersect-samples.  Genotypes stay resident."""
+    eng = engine or default_engine()
+    y = np.ascontiguousarray(y, dtype=np.float64)
+    masks = np.ascontiguousarray(masks, dtype=np.uint8)
+    n, t_count = y.shape
+    if masks.shape != y.shape or n != y_full.n_samples:
+        raise SchnelGpuError(ERR_BAD_ARG, "y and masks must be n_samples x n_traits")
+    p = y_full.n_snps
+    nmf_iter = config.nmf.n_iter if (config.impute == ImputeStrategy.NMF and config.nmf) else 0
+    rs = (_Results * t_count)()
+    arrs = []
+    for t in range(t_count):
+        r, arr = _alloc_results(int(np.count_nonzero(masks[:, t])), p, 1, config.k, nmf_iter)
+        rs[t] = r
+        arrs.append(arr)
+    cfg = config._c()
+    eng.check(eng.lib.slfmm_fit_traits(eng.h, y_full.h, _ptr(y), _ptr(masks), t_count, C.byref(cfg), rs))
+    return [_to_results(rs[t], arrs[t], config) for t in range(t_count)]
+
+
+def fit_lfmm2_many(problems: Sequence[Tuple[np.ndarray, int, np.ndarray, Lfmm2Config]],
+                   engine: Optional[Engine] = None, n_streams: int = 0,
+                   outs: Optional[Sequence[dict]] = None) -> List[TestResults]:
+    """Independent problems (packed payload, n_physical, x, config), run
+    concurrently on n_streams streams of the engine's device (0: 4).
+    ``outs`` may hold preallocated (e.g. pinned) result arrays per problem."""
+    eng = engine or default_engine()
+    keep = []
+    probs = (_Problem * len(problems))()
+    rs = (_Results * len(problems))()
+    arrs = []
+    for i, (packed, n_physical, x, config) in enumerate(problems):
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        bps = (n_physical + 3) // 4
+        n_snps = packed.size // bps
+        if outs is None:
+            nmf_iter = config.nmf.n_iter if (config.impute == ImputeStrategy.NMF and config.nmf) else 0
+            r, arr = _alloc_results(n_physical, n_snps, x.shape[1], config.k, nmf_iter)
+        else:
+            arr = outs[i]
+            r = _Results(_dptr(arr["u_hat"]), _dptr(arr["beta"]), _dptr(arr["tstat"]), _dptr(arr["pvalue"]),
+                         _dptr(arr["r2"]), _dptr(arr["gif_per_trait"]), 0.0, _dptr(arr.get("nmf_cv")), 0.0, 0.0,
+                         0.0, 0)
+        rs[i] = r
+        arrs.append(arr)
+        cfg = config._c()
+        keep += [x, cfg, packed]
+        probs[i] = _Problem(packed.ctypes.data, n_physical, n_snps, x.ctypes.data, x.shape[1],
+                            C.addressof(cfg), None, C.addressof(rs[i]))
+    status = (C.c_int * max(len(problems), 1))()
+    eng.check(eng.lib.slfmm_fit_many(eng.h, probs, len(problems), n_streams, status))
+    return [_to_results(rs[i], arrs[i], problems[i][3]) for i in range(len(problems))]
 
 
 def fit_lfmm2_host(packed: np.ndarray, n_physical: int, x: np.ndarray, config: Lfmm2Config,

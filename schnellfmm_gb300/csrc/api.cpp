@@ -1306,40 +1306,58 @@ using namespace slfmm;
 
 extern "C" {
 
+namespace slfmm {
+namespace {
+// device checks, streams and the memory pool of a context
+void ctx_open(Ctx& c, int device, int precision, int verbose, cudaStream_t stream) {
+    int ndev = 0;
+    SLFMM_CUDA(cudaGetDeviceCount(&ndev));
+    SLFMM_REQUIRE(device >= 0 && device < ndev, SLFMM_ERR_CUDA, "no such CUDA device");
+    SLFMM_CUDA(cudaSetDevice(device));
+    cudaDeviceProp prop{};
+    SLFMM_CUDA(cudaGetDeviceProperties(&prop, device));
+    SLFMM_REQUIRE(prop.major == 10 && prop.minor == 3, SLFMM_ERR_CUDA,
+                  std::string("schnelgpu is built for sm_103a (GB300); device is ") + prop.name);
+    c.device = device;
+    c.sm_count = prop.multiProcessorCount;
+    c.precision = precision;
+    c.verbose = verbose;
+    if (stream) {
+        c.stream = stream;
+    } else {
+        SLFMM_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+        c.own_stream = true;
+    }
+    SLFMM_CUDA(cudaStreamCreateWithFlags(&c.copy_stream, cudaStreamNonBlocking));
+    cudaMemPool_t pool;
+    SLFMM_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+    uint64_t thr = UINT64_MAX;
+    SLFMM_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+    c.dev_flags.alloc(4, c.stream);
+    c.dev_flags.zero();
+    SLFMM_CUDA(cudaStreamSynchronize(c.stream));
+}
+
+void ctx_close(Ctx& c) {
+    cudaSetDevice(c.device);
+    c.dev_flags.release();
+    if (c.stream) cudaStreamSynchronize(c.stream);
+    if (c.copy_stream) cudaStreamDestroy(c.copy_stream);
+    if (c.own_stream && c.stream) cudaStreamDestroy(c.stream);
+    c.copy_stream = nullptr;
+    c.stream = nullptr;
+}
+}  // namespace
+}  // namespace slfmm
+
 int slfmm_create(int device, const slfmm_opts* opts, slfmm_ctx** out) {
     if (!out) return SLFMM_ERR_BAD_ARG;
     *out = nullptr;
     slfmm_ctx* c = new (std::nothrow) slfmm_ctx();
     if (!c) return SLFMM_ERR_NOMEM;
     try {
-        int ndev = 0;
-        SLFMM_CUDA(cudaGetDeviceCount(&ndev));
-        SLFMM_REQUIRE(device >= 0 && device < ndev, SLFMM_ERR_CUDA, "no such CUDA device");
-        SLFMM_CUDA(cudaSetDevice(device));
-        cudaDeviceProp prop{};
-        SLFMM_CUDA(cudaGetDeviceProperties(&prop, device));
-        SLFMM_REQUIRE(prop.major == 10 && prop.minor == 3, SLFMM_ERR_CUDA,
-                      std::string("schnelgpu is built for sm_103a (GB300); device is ") + prop.name);
-        c->device = device;
-        c->sm_count = prop.multiProcessorCount;
-        if (opts) {
-            c->precision = opts->precision;
-            c->verbose = opts->verbose;
-        }
-        if (opts && opts->stream) {
-            c->stream = (cudaStream_t)opts->stream;
-        } else {
-            SLFMM_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-            c->own_stream = true;
-        }
-        SLFMM_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
-        cudaMemPool_t pool;
-        SLFMM_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
-        uint64_t thr = UINT64_MAX;
-        SLFMM_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
-        c->dev_flags.alloc(4, c->stream);
-        c->dev_flags.zero();
-        SLFMM_CUDA(cudaStreamSynchronize(c->stream));
+        ctx_open(*c, device, opts ? opts->precision : SLFMM_PREC_SPLIT_FP8, opts ? opts->verbose : 0,
+                 opts ? (cudaStream_t)opts->stream : nullptr);
     } catch (const slfmm::Error& e) {
         fprintf(stderr, "schnelgpu: %s\n", e.what());
         const int code = e.code;
@@ -1352,11 +1370,7 @@ int slfmm_create(int device, const slfmm_opts* opts, slfmm_ctx** out) {
 
 void slfmm_destroy(slfmm_ctx* c) {
     if (!c) return;
-    cudaSetDevice(c->device);
-    c->dev_flags.release();
-    if (c->stream) cudaStreamSynchronize(c->stream);
-    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
-    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    ctx_close(*c);
     delete c;
 }
 
@@ -1546,6 +1560,130 @@ int slfmm_fit_host(slfmm_ctx* c, const uint8_t* packed, uint64_t n_physical, uin
         ge = &sub;
     }
     fit_impl(*c, *ge, full, x, (int)d, cfg, omega, res, pre ? &ps : nullptr);
+    API_CATCH(c)
+}
+
+namespace slfmm {
+namespace {
+// The samples `keep` (ascending or not, each < src.n) of a resident matrix as
+// a new resident matrix: the padded rows are re-packed on the device from the
+// resident copy (BedFile::subset_samples, src/bed.rs:155-159), then counted.
+// Tile-major copies and missing-call lists are built on first use.
+void geno_subset_samples(Ctx& c, const Geno& src, const std::vector<uint64_t>& keep, Geno& dst) {
+    SLFMM_REQUIRE(!keep.empty(), SLFMM_ERR_BAD_ARG, "empty sample subset");
+    std::vector<uint32_t> k32(keep.size());
+    for (size_t i = 0; i < keep.size(); ++i) {
+        SLFMM_REQUIRE(keep[i] < src.n, SLFMM_ERR_BAD_ARG, "sample index out of range");
+        k32[i] = (uint32_t)keep[i];
+    }
+    DBuf<uint32_t> keep_d = upload(c, k32.data(), k32.size());
+    dst.n = keep.size();
+    dst.p = src.p;
+    dst.stride = round_up(ceil_div(dst.n, 4), 128);
+    dst.packed.alloc(std::max<uint64_t>(dst.p, 1) * dst.stride, c.stream);
+    dst.counts.alloc(std::max<uint64_t>(dst.p, 1) * 4, c.stream);
+    launch_repack(c, src.packed.get(), src.p, src.stride, src.n, keep_d.get(), dst.n, dst.packed.get(), dst.stride);
+    launch_snp_counts(c, dst, nullptr);
+    sync(c);
+}
+
+// one problem of slfmm_fit_many on a worker's context (the body of
+// slfmm_fit_host with every SNP in the estimation)
+void fit_problem(Ctx& c, const slfmm_problem& pr) {
+    SLFMM_REQUIRE(pr.packed && pr.x && pr.cfg, SLFMM_ERR_BAD_ARG, "null problem input");
+    Geno full;
+    Presketch ps;
+    const bool pre = presketch_eligible(c, pr.n_physical, pr.n_snps, pr.x, (int)pr.d, pr.cfg, pr.omega, ps);
+    upload_geno(c, full, pr.packed, pr.n_physical, pr.n_snps, nullptr, 0, subset_indices(nullptr, pr.n_snps),
+                pre ? &ps : nullptr);
+    if (pre) {
+        const int e = fetch(c, ps.err.get(), 1)[0];
+        if (e) throw_tc8_timeout(e);
+    }
+    fit_impl(c, full, full, pr.x, (int)pr.d, pr.cfg, pr.omega, pr.res, pre ? &ps : nullptr);
+}
+}  // namespace
+}  // namespace slfmm
+
+int slfmm_fit_traits(slfmm_ctx* c, const slfmm_geno* g, const double* y, const uint8_t* masks,
+                     uint32_t n_traits, const slfmm_config* cfg, slfmm_results* res) {
+    if (!c || !g || !y || !masks || !cfg || !res) return SLFMM_ERR_BAD_ARG;
+    API_TRY
+    SLFMM_CUDA(cudaSetDevice(c->device));
+    SLFMM_REQUIRE(n_traits >= 1, SLFMM_ERR_BAD_ARG, "no traits");
+    const uint64_t n = g->n;
+    for (uint32_t t = 0; t < n_traits; ++t) {
+        std::vector<uint64_t> keep;
+        std::vector<double> xt;
+        for (uint64_t i = 0; i < n; ++i)
+            if (masks[i * n_traits + t]) {
+                keep.push_back(i);
+                xt.push_back(y[i * n_traits + t]);
+            }
+        try {
+            SLFMM_REQUIRE(!keep.empty(), SLFMM_ERR_BAD_ARG, "no samples");
+            Geno sub;
+            geno_subset_samples(*c, *g, keep, sub);
+            fit_impl(*c, sub, sub, xt.data(), 1, cfg, nullptr, &res[t]);
+        } catch (const Error& e) {
+            throw Error(e.code, "trait " + std::to_string(t) + ": " + e.what());
+        }
+    }
+    API_CATCH(c)
+}
+
+int slfmm_fit_many(slfmm_ctx* c, const slfmm_problem* problems, uint32_t n_problems, uint32_t n_streams,
+                   int* status) {
+    if (!c || (!problems && n_problems)) return SLFMM_ERR_BAD_ARG;
+    API_TRY
+    SLFMM_CUDA(cudaSetDevice(c->device));
+    if (n_problems == 0) return SLFMM_OK;
+    const uint32_t workers = std::max<uint32_t>(1, std::min(n_streams ? n_streams : 4u, n_problems));
+    std::vector<int> st(n_problems, SLFMM_OK);
+    std::vector<std::string> msg(n_problems);
+    std::atomic<uint32_t> next{0};
+    // each worker owns a context (its own streams) on the same device and
+    // takes problems in order; kernels of different workers run concurrently
+    auto work = [&]() {
+        Ctx w;
+        try {
+            ctx_open(w, c->device, c->precision, 0, nullptr);
+        } catch (const Error& e) {
+            for (uint32_t i = next.fetch_add(1); i < n_problems; i = next.fetch_add(1)) {
+                st[i] = e.code;
+                msg[i] = e.what();
+            }
+            return;
+        }
+        for (uint32_t i = next.fetch_add(1); i < n_problems; i = next.fetch_add(1)) {
+            try {
+                fit_problem(w, problems[i]);
+            } catch (const Error& e) {
+                st[i] = e.code;
+                msg[i] = e.what();
+            } catch (const std::bad_alloc&) {
+                st[i] = SLFMM_ERR_NOMEM;
+                msg[i] = "host allocation failed";
+            } catch (const std::exception& e) {
+                st[i] = SLFMM_ERR_CUDA;
+                msg[i] = e.what();
+            }
+        }
+        ctx_close(w);
+    };
+    std::vector<std::thread> pool;
+    for (uint32_t k = 1; k < workers; ++k) pool.emplace_back(work);
+    work();
+    for (auto& th : pool) th.join();
+    int first = SLFMM_OK;
+    for (uint32_t i = 0; i < n_problems; ++i) {
+        if (status) status[i] = st[i];
+        if (st[i] != SLFMM_OK && first == SLFMM_OK) {
+            first = st[i];
+            c->last_error = "problem " + std::to_string(i) + ": " + msg[i];
+        }
+    }
+    return first;
     API_CATCH(c)
 }
 

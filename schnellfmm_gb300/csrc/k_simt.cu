@@ -166,7 +166,7 @@ template <int CPT>
 void row_lut_impl(Ctx& c, const Geno& g, const float* lut, const float* W, float* out) {
     constexpr int WP = CPT * 16;
     const size_t smem = (size_t)kRowSamples * WP * sizeof(float);
-    static bool configured = false;
+    static thread_local bool configured = false;  // per host thread: contexts may run concurrently
     if (!configured) {
         SLFMM_CUDA(cudaFuncSetAttribute(k_row_lut<CPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smem));

@@ -428,15 +428,15 @@ __global__ void k_scale_product(const double* __restrict__ a, const double* __re
 // -------------------------------------------------------------------------
 // host side
 // -------------------------------------------------------------------------
+// thread-safe one-time lookup (contexts may run on several host threads)
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
         void* p = nullptr;
         cudaDriverEntryPointQueryResult q;
         SLFMM_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
         SLFMM_REQUIRE(q == cudaDriverEntryPointSuccess && p, SLFMM_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
-        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
     return fn;
 }
 

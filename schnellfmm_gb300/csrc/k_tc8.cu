@@ -749,15 +749,15 @@ __global__ void k_sub_colterm(double* __restrict__ S, int lds, uint64_t n, int w
     }
 }
 
+// thread-safe one-time lookup (contexts may run on several host threads)
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn8() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
+    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
         void* p = nullptr;
         cudaDriverEntryPointQueryResult q;
         SLFMM_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
         SLFMM_REQUIRE(q == cudaDriverEntryPointSuccess && p, SLFMM_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
-        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
     return fn;
 }
 
