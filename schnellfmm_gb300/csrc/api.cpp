@@ -469,7 +469,7 @@ void row_contract_base(Ctx& c, const Geno& g, const SnpStd& s, const double* W, 
         launch_colsums(c, W, g.n, w, ldw, cs.get());
         {
             ProfScope ps(c, "row_contract", bytes, 2.0 * g.n * g.p * w);
-            launch_tc_rows(c, g.packed.get(), g.stride, g.p, g.n, bs.get(), n_pad, wp, out.get(), wp, 1, 0);
+            launch_tc_rows(c, packed_rows(g), g.stride, g.p, g.n, bs.get(), n_pad, wp, out.get(), wp, 1, 0);
         }
         launch_rowfix_mean(c, out.get(), wp, g.p, w, g.miss_ptr.get(), g.miss_idx.get(), W32.get(), wp, cs.get(),
                            s.mean.get(), s.scale.get());
@@ -1587,6 +1587,20 @@ void geno_subset_samples(Ctx& c, const Geno& src, const std::vector<uint64_t>& k
     sync(c);
 }
 
+// Whether a split-FP8 mean-imputation fit of an n x p matrix with one
+// covariate runs on the tile-major copies alone: every row and column pass
+// (the RSVD sketch width and the test-pass width 1 + K) has an indicator plan,
+// so no pass needs the missing-call lists or the row-major copy.
+bool tiles_only_fit(const Ctx& c, const slfmm_config* cfg, uint64_t n, uint64_t p) {
+    if (c.precision != SLFMM_PREC_SPLIT_FP8 || cfg->impute != SLFMM_IMPUTE_MEAN) return false;
+    const int l = (int)cfg->k + (int)cfg->oversampling;
+    if (l > 64) return false;
+    const uint64_t tp = ceil_div(p, 128), tn = ceil_div(n, 128);
+    if (!fp8_row_indicator_plan(l, tp)) return false;
+    const Fp8Plan col = fp8_plan(pad16(l), true, tn);
+    return col.ok && col.n_ind != 0 && fp8_row_indicator_plan((int)cfg->k + 1, tp);
+}
+
 // one problem of slfmm_fit_many on a worker's context (the body of
 // slfmm_fit_host with every SNP in the estimation)
 void fit_problem(Ctx& c, const slfmm_problem& pr) {
@@ -1623,7 +1637,16 @@ int slfmm_fit_traits(slfmm_ctx* c, const slfmm_geno* g, const double* y, const u
         try {
             SLFMM_REQUIRE(!keep.empty(), SLFMM_ERR_BAD_ARG, "no samples");
             Geno sub;
-            geno_subset_samples(*c, *g, keep, sub);
+            phase(*c, "", true);
+            if (tiles_only_fit(*c, cfg, keep.size(), g->p)) {
+                std::vector<uint32_t> k32(keep.begin(), keep.end());
+                DBuf<uint32_t> keep_d = upload(*c, k32.data(), k32.size());
+                tiles_subset_samples(*c, *g, keep_d.get(), keep.size(), sub);
+                sync(*c);
+            } else {
+                geno_subset_samples(*c, *g, keep, sub);
+            }
+            phase(*c, "trait sample subset");
             fit_impl(*c, sub, sub, xt.data(), 1, cfg, nullptr, &res[t]);
         } catch (const Error& e) {
             throw Error(e.code, "trait " + std::to_string(t) + ": " + e.what());

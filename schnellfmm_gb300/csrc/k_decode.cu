@@ -57,6 +57,49 @@ __global__ void k_repack(const uint8_t* __restrict__ in, uint64_t rows, uint64_t
     }
 }
 
+// Re-pack with a sample subset, one block per row (grid-stride): the row's
+// in_bps bytes and the kept sample indices are staged in shared memory, the
+// indices transposed (ks[k * words + w] = keep[16 w + k]) so that the threads
+// of a warp, one output word each, read consecutive entries.  Host side checks
+// that both arrays fit.
+__global__ void __launch_bounds__(256) k_repack_keep(const uint8_t* __restrict__ in, uint64_t rows, uint64_t in_bps,
+                                                     const uint32_t* __restrict__ keep, uint64_t n_out,
+                                                     uint8_t* __restrict__ out, uint64_t stride) {
+    extern __shared__ __align__(16) uint8_t sm_keep[];
+    const uint64_t words = (n_out + 15) / 16;           // output words holding kept samples
+    uint32_t* ks = reinterpret_cast<uint32_t*>(sm_keep);  // 16 x words indices
+    uint8_t* row_s = sm_keep + ((words * 16 * 4 + 15) / 16) * 16;
+    for (uint64_t e = threadIdx.x; e < words * 16; e += blockDim.x) {
+        const uint64_t w = e / 16, k = e % 16, s = w * 16 + k;
+        ks[k * words + w] = s < n_out ? keep[s] : 0xFFFFFFFFu;
+    }
+    const uint64_t out_words = stride / 4;
+    const bool w4 = in_bps % 4 == 0 && reinterpret_cast<uintptr_t>(in) % 4 == 0;
+    for (uint64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+        __syncthreads();  // the previous row's codes are consumed (and the indices staged)
+        const uint8_t* src = in + r * in_bps;
+        if (w4) {
+            for (uint64_t i = threadIdx.x; i < in_bps / 4; i += blockDim.x)
+                reinterpret_cast<uint32_t*>(row_s)[i] = reinterpret_cast<const uint32_t*>(src)[i];
+        } else {
+            for (uint64_t i = threadIdx.x; i < in_bps; i += blockDim.x) row_s[i] = src[i];
+        }
+        __syncthreads();
+        uint32_t* dst = reinterpret_cast<uint32_t*>(out + r * stride);
+        for (uint64_t w = threadIdx.x; w < out_words; w += blockDim.x) {
+            uint32_t word = 0;
+            if (w < words) {
+#pragma unroll
+                for (int k = 0; k < 16; ++k) {
+                    const uint32_t idx = ks[k * words + w];
+                    if (idx != 0xFFFFFFFFu) word |= (uint32_t)((row_s[idx >> 2] >> ((idx & 3) * 2)) & 3u) << (2 * k);
+                }
+            }
+            dst[w] = word;
+        }
+    }
+}
+
 // Straight copy without a sample subset when the payload rows are V-aligned:
 // rows of in_bps bytes -> rows of `stride` bytes, the payload's last 32-bit
 // word masked to the codes of n_out samples and the rest of the row zero.
@@ -316,6 +359,15 @@ void launch_repack(Ctx& c, const uint8_t* in, uint64_t rows, uint64_t in_bps, ui
         SLFMM_LAUNCHED(c, "k_repack_vec");
         return;
     }
+    const size_t keep_smem = ((ceil_div(n_out, 16) * 16 * 4 + 15) / 16) * 16 + in_bps;
+    if (keep != nullptr && keep_smem <= 200 * 1024) {
+        SLFMM_CUDA(cudaFuncSetAttribute(k_repack_keep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)keep_smem));
+        const uint64_t per_sm = std::max<uint64_t>(1, std::min<uint64_t>(4, (220 * 1024) / keep_smem));
+        const unsigned grid = (unsigned)std::min<uint64_t>(rows, (uint64_t)c.sm_count * per_sm);
+        k_repack_keep<<<grid, 256, keep_smem, c.stream>>>(in, rows, in_bps, keep, n_out, out, stride);
+        SLFMM_LAUNCHED(c, "k_repack_keep");
+        return;
+    }
     const uint64_t work = rows * (stride / 4);
     k_repack<<<grid_for(c, work, 256), 256, 0, c.stream>>>(in, rows, in_bps, keep, n_out, out, stride);
     SLFMM_LAUNCHED(c, "k_repack");
@@ -325,7 +377,7 @@ void launch_snp_counts(Ctx& c, const Geno& g, uint64_t* miss_count_out) {
     if (g.p == 0) return;
     const int block = 256;
     const uint64_t grid = ceil_div(g.p * 32, block);
-    k_snp_counts<<<(unsigned)grid, block, 0, c.stream>>>(g.packed.get(), g.p, g.stride, g.n,
+    k_snp_counts<<<(unsigned)grid, block, 0, c.stream>>>(packed_rows(g), g.p, g.stride, g.n,
                                                          g.counts.get(), miss_count_out);
     SLFMM_LAUNCHED(c, "k_snp_counts");
 }
@@ -334,7 +386,7 @@ void launch_snp_counts_range(Ctx& c, const Geno& g, uint64_t r0, uint64_t rows) 
     if (rows == 0) return;
     const int block = 256;
     const uint64_t grid = ceil_div(rows * 32, block);
-    k_snp_counts<<<(unsigned)grid, block, 0, c.stream>>>(g.packed.get() + r0 * g.stride, rows, g.stride, g.n,
+    k_snp_counts<<<(unsigned)grid, block, 0, c.stream>>>(packed_rows(g) + r0 * g.stride, rows, g.stride, g.n,
                                                          g.counts.get() + r0 * 4, nullptr);
     SLFMM_LAUNCHED(c, "k_snp_counts");
 }
@@ -360,7 +412,7 @@ void build_missing_lists(Ctx& c, const Geno& g) {
     if (nnz && g.p) {
         const int block = 256;
         k_miss_fill<<<(unsigned)ceil_div(g.p * 32, block), block, 0, c.stream>>>(
-            g.packed.get(), g.p, g.stride, g.n, g.miss_ptr.get(), g.miss_idx.get(), nullptr, ~0ull);
+            packed_rows(g), g.p, g.stride, g.n, g.miss_ptr.get(), g.miss_idx.get(), nullptr, ~0ull);
         SLFMM_LAUNCHED(c, "k_miss_fill");
     }
     g.have_csr = true;
@@ -376,7 +428,7 @@ void csr_chunk_fill(Ctx& c, const Geno& g, uint64_t r0, uint64_t rows, uint64_t 
     if (rows == 0 || cap == 0) return;
     const int block = 256;
     k_miss_fill<<<(unsigned)ceil_div(rows * 32, block), block, 0, c.stream>>>(
-        g.packed.get() + r0 * g.stride, rows, g.stride, g.n, g.miss_ptr.get() + r0, g.miss_idx.get(), nullptr, cap);
+        packed_rows(g) + r0 * g.stride, rows, g.stride, g.n, g.miss_ptr.get() + r0, g.miss_idx.get(), nullptr, cap);
     SLFMM_LAUNCHED(c, "k_miss_fill");
 }
 
@@ -391,7 +443,7 @@ void build_missing_csc(Ctx& c, const Geno& g) {
     DBuf<uint32_t> rowid(g.nnz, c.stream), keys_out(g.nnz, c.stream);
     const int block = 256;
     k_miss_fill<<<(unsigned)ceil_div(g.p * 32, block), block, 0, c.stream>>>(
-        g.packed.get(), g.p, g.stride, g.n, g.miss_ptr.get(), keys_out.get(), rowid.get(), ~0ull);
+        packed_rows(g), g.p, g.stride, g.n, g.miss_ptr.get(), keys_out.get(), rowid.get(), ~0ull);
     SLFMM_LAUNCHED(c, "k_miss_fill");
     int end_bit = 1;
     while ((1ull << end_bit) < g.n) ++end_bit;
@@ -447,7 +499,7 @@ void launch_decode_chunk(Ctx& c, const Geno& g, uint64_t snp0, uint64_t ncols, c
                          const double* scale, double* out) {
     if (ncols == 0 || g.n == 0) return;
     k_decode_chunk<<<grid_for(c, g.n * ncols, 256), 256, 0, c.stream>>>(
-        g.packed.get(), g.stride, g.n, snp0, ncols, mean, scale, out);
+        packed_rows(g), g.stride, g.n, snp0, ncols, mean, scale, out);
     SLFMM_LAUNCHED(c, "k_decode_chunk");
 }
 

@@ -550,7 +550,7 @@ void launch_nmf_clamp0_f32(Ctx& c, const float* src, int ld, double* X, uint64_t
 void launch_nmf_cv(Ctx& c, const Geno& g, uint64_t chunk, uint64_t mask_seed, double rate, const float* W,
                    const float* H, int k, double* part) {
     if (!g.p) return;
-    k_nmf_cv<<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(g.packed.get(), g.stride, g.n, g.p, chunk, mask_seed,
+    k_nmf_cv<<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(packed_rows(g), g.stride, g.n, g.p, chunk, mask_seed,
                                                          rate_threshold(rate), W, H, k, g.counts.get(), part);
     SLFMM_LAUNCHED(c, "k_nmf_cv");
 }
@@ -562,7 +562,7 @@ void launch_nmf_gwas_cv(Ctx& c, const Geno& g, uint64_t chunk, uint64_t seed, do
     const uint64_t nchunks = ceil_div(g.p, chunk);
     k_obs_base<<<grid_for(c, nchunks, 64), 64, 0, c.stream>>>(g.counts.get(), g.p, chunk, base.get());
     SLFMM_LAUNCHED(c, "k_obs_base");
-    k_nmf_gwas_cv<<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(g.packed.get(), g.stride, g.n, g.p, chunk, seed,
+    k_nmf_gwas_cv<<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(packed_rows(g), g.stride, g.n, g.p, chunk, seed,
                                                               rate_threshold(rate), W, Wpt, k, base.get(), part);
     SLFMM_LAUNCHED(c, "k_nmf_gwas_cv");
 }

@@ -173,7 +173,7 @@ void row_lut_impl(Ctx& c, const Geno& g, const float* lut, const float* W, float
         configured = true;
     }
     const unsigned grid = (unsigned)ceil_div(g.p, kRowSnps);
-    k_row_lut<CPT><<<grid, 256, smem, c.stream>>>(g.packed.get(), g.stride, g.p, g.n,
+    k_row_lut<CPT><<<grid, 256, smem, c.stream>>>(packed_rows(g), g.stride, g.p, g.n,
                                                   reinterpret_cast<const float4*>(lut), W, out);
     SLFMM_LAUNCHED(c, "k_row_lut");
 }
@@ -192,7 +192,7 @@ void col_lut_impl(Ctx& c, const Geno& g, const float* lut, const float* Q, doubl
     splits = ceil_div(g.p, per_split);
     DBuf<float> part(splits * n_pad * WP, c.stream);
     dim3 grid((unsigned)tiles, (unsigned)splits);
-    k_col_lut<CPT><<<grid, 256, 0, c.stream>>>(g.packed.get(), g.stride, g.p, n_pad,
+    k_col_lut<CPT><<<grid, 256, 0, c.stream>>>(packed_rows(g), g.stride, g.p, n_pad,
                                                reinterpret_cast<const float4*>(lut), Q, per_split,
                                                part.get());
     SLFMM_LAUNCHED(c, "k_col_lut");

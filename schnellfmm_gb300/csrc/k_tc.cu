@@ -526,7 +526,7 @@ void build_transposed(Ctx& c, const Geno& g) {
     g.packedT.alloc(g.n * g.strideT, c.stream);
     SLFMM_CUDA(cudaMemsetAsync(g.packedT.get(), 0, g.n * g.strideT, c.stream));
     dim3 grid((unsigned)ceil_div(g.p, 128), (unsigned)ceil_div(g.n, 128));
-    k_transpose_packed<<<grid, 256, 0, c.stream>>>(g.packed.get(), g.p, g.stride, g.n, g.packedT.get(), g.strideT);
+    k_transpose_packed<<<grid, 256, 0, c.stream>>>(packed_rows(g), g.p, g.stride, g.n, g.packedT.get(), g.strideT);
     SLFMM_LAUNCHED(c, "k_transpose_packed");
     g.have_T = true;
 }

@@ -895,6 +895,65 @@ __global__ void __launch_bounds__(256) k_transpose_tiles(const uint8_t* __restri
     }
 }
 
+// Sample-major tiles of a sample subset: row rr of output sample tile ts
+// (output sample s = 128 ts + rr) is row i % 128 of source tile i / 128, i =
+// keep[s], in every K block; samples past n_keep are zero codes.  One thread
+// per 16 bytes (two per 32-byte tile row).
+__global__ void k_gather_tile_rows(const uint8_t* __restrict__ src, uint64_t kbt, const uint32_t* __restrict__ keep,
+                                   uint64_t n_keep, uint64_t ntiles_dst, uint8_t* __restrict__ dst) {
+    const uint64_t total = ntiles_dst * kbt * 256;
+    const uint4* s4 = reinterpret_cast<const uint4*>(src);
+    uint4* d4 = reinterpret_cast<uint4*>(dst);
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t h = e & 1u, rr = (e >> 1) & 127u, rest = e >> 8;
+        const uint64_t kb = rest % kbt, ts = rest / kbt;
+        const uint64_t sidx = ts * kM + rr;
+        uint4 v = make_uint4(0, 0, 0, 0);
+        if (sidx < n_keep) {
+            const uint64_t i = keep[sidx];
+            v = s4[((i / kM) * kbt + kb) * 256 + (i % kM) * 2 + h];
+        }
+        d4[e] = v;
+    }
+}
+
+// Allele and missing counts of every SNP from the SNP-major tiles (the
+// codes of samples past n are 00 there): one warp per SNP, lanes over the
+// K blocks of its tile row; counts as k_snp_counts (c0 = n - c1 - c2 - cm).
+__global__ void k_snp_counts_tiles(const uint8_t* __restrict__ tiles, uint64_t kbt, uint64_t p, uint64_t n,
+                                   int32_t* __restrict__ counts) {
+    constexpr uint32_t kLo2 = 0x55555555u;
+    const uint64_t j = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x & 31;
+    if (j >= p) return;
+    const uint64_t t = j / kM, r = j % kM;
+    uint32_t c1 = 0, c2 = 0, cm = 0;
+    for (uint64_t kb = lane; kb < kbt; kb += 32) {
+        const uint4* q = reinterpret_cast<const uint4*>(tiles + (t * kbt + kb) * kTileBytes + r * 32);
+        const uint4 a = q[0], b = q[1];
+        const uint32_t ws[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            const uint32_t lo = ws[k] & kLo2, hi = (ws[k] >> 1) & kLo2;
+            c1 += __popc(hi & ~lo);
+            c2 += __popc(hi & lo);
+            cm += __popc(~hi & lo);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        c1 += __shfl_xor_sync(0xffffffffu, c1, o);
+        c2 += __shfl_xor_sync(0xffffffffu, c2, o);
+        cm += __shfl_xor_sync(0xffffffffu, cm, o);
+    }
+    if (lane == 0) {
+        counts[j * 4 + 0] = (int32_t)(n - c1 - c2 - cm);
+        counts[j * 4 + 1] = (int32_t)c1;
+        counts[j * 4 + 2] = (int32_t)c2;
+        counts[j * 4 + 3] = (int32_t)cm;
+    }
+}
+
 static void tile_rows(Ctx& c, const uint8_t* in, uint64_t rows, uint64_t stride, DBuf<uint8_t>& out, uint64_t& kbt,
                       uint64_t& ntiles) {
     SLFMM_REQUIRE(stride % 32 == 0, SLFMM_ERR_BAD_ARG, "packed stride must be a multiple of 32 bytes");
@@ -923,7 +982,7 @@ void tile_chunk(Ctx& c, const Geno& g, uint64_t r0, uint64_t r1, bool last) {
     }
     const uint64_t t0 = r0 / kM, t1 = last ? g.ntiles : ceil_div(r1, kM);
     const uint64_t chunks = (t1 - t0) * g.kbt * (kTileBytes / 16);
-    k_tile_rows<<<grid_for(c, chunks, 256), 256, 0, c.stream>>>(g.packed.get() + r0 * g.stride, r1 - r0, g.stride,
+    k_tile_rows<<<grid_for(c, chunks, 256), 256, 0, c.stream>>>(packed_rows(g) + r0 * g.stride, r1 - r0, g.stride,
                                                                  g.kbt, chunks,
                                                                  g.tiles.get() + t0 * g.kbt * kTileBytes);
     SLFMM_LAUNCHED(c, "k_tile_rows");
@@ -937,10 +996,41 @@ void tile_chunk(Ctx& c, const Geno& g, uint64_t r0, uint64_t r1, bool last) {
     if (last) g.have_tiles = g.have_tilesT = true;
 }
 
+void tiles_subset_samples(Ctx& c, const Geno& full, const uint32_t* keep_dev, uint64_t n_keep, Geno& sub) {
+    SLFMM_REQUIRE(n_keep > 0 && n_keep <= full.n, SLFMM_ERR_BAD_ARG, "bad sample subset");
+    build_tiles(c, full, true);
+    sub.n = n_keep;
+    sub.p = full.p;
+    sub.stride = round_up(ceil_div(n_keep, 4), 128);
+    // sample-major: the kept samples' rows of the full matrix's tiles
+    sub.kbtT = full.kbtT;
+    sub.ntilesT = round_up(std::max<uint64_t>(ceil_div(n_keep, kM), 1), 8);
+    sub.tilesT.alloc(sub.ntilesT * sub.kbtT * kTileBytes, c.stream);
+    const uint64_t rows16 = sub.ntilesT * sub.kbtT * 256;
+    k_gather_tile_rows<<<grid_for(c, rows16, 256), 256, 0, c.stream>>>(full.tilesT.get(), full.kbtT, keep_dev, n_keep,
+                                                                       sub.ntilesT, sub.tilesT.get());
+    SLFMM_LAUNCHED(c, "k_gather_tile_rows");
+    // SNP-major: the 2-bit transpose of those blocks
+    sub.kbt = sub.stride / 32;
+    sub.ntiles = round_up(std::max<uint64_t>(ceil_div(sub.p, kM), 1), 8);
+    sub.tiles.alloc(sub.ntiles * sub.kbt * kTileBytes, c.stream);
+    const uint64_t blocks = std::min<uint64_t>(sub.ntiles * sub.kbt, (uint64_t)c.sm_count * 16);
+    k_transpose_tiles<<<(unsigned)blocks, 256, 0, c.stream>>>(sub.tilesT.get(), sub.kbtT, sub.ntilesT, sub.tiles.get(),
+                                                               sub.kbt, sub.ntiles, 0, sub.kbt);
+    SLFMM_LAUNCHED(c, "k_transpose_tiles");
+    sub.have_tiles = sub.have_tilesT = true;
+    sub.counts.alloc(std::max<uint64_t>(sub.p, 1) * 4, c.stream);
+    if (sub.p) {
+        k_snp_counts_tiles<<<(unsigned)ceil_div(sub.p * 32, 256), 256, 0, c.stream>>>(sub.tiles.get(), sub.kbt, sub.p,
+                                                                                      sub.n, sub.counts.get());
+        SLFMM_LAUNCHED(c, "k_snp_counts_tiles");
+    }
+}
+
 TileView build_tiles(Ctx& c, const Geno& g, bool transposed) {
     if (!transposed) {
         if (!g.have_tiles) {
-            tile_rows(c, g.packed.get(), g.p, g.stride, g.tiles, g.kbt, g.ntiles);
+            tile_rows(c, packed_rows(g), g.p, g.stride, g.tiles, g.kbt, g.ntiles);
             g.have_tiles = true;
         }
         return TileView{g.tiles.get(), g.kbt, g.ntiles};

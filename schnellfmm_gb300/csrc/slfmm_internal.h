@@ -269,11 +269,22 @@ struct Fp8Plan {
 };
 Fp8Plan fp8_plan(int wpad, bool ind, uint64_t tiles);
 // tile-major packed operand (rows = SNPs, or samples when transposed)
+// the row-major packed copy of a matrix (a sample subset built from the
+// tile-major copies has none: the passes that need it must not run on it)
+inline const uint8_t* packed_rows(const Geno& g) {
+    SLFMM_REQUIRE(g.packed.get() != nullptr, SLFMM_ERR_BAD_ARG, "this matrix has no row-major packed copy");
+    return g.packed.get();
+}
+
 struct TileView {
     const uint8_t* base;
     uint64_t kbt, ntiles;
 };
 TileView build_tiles(Ctx& c, const Geno& g, bool transposed);
+// The samples keep_dev[0 .. n_keep) of a matrix as a new matrix holding only
+// the tile-major copies and the counts (no row-major copy): the kept rows of
+// the sample-major tiles, their 2-bit transpose, counts from the tiles.
+void tiles_subset_samples(Ctx& c, const Geno& full, const uint32_t* keep_dev, uint64_t n_keep, Geno& sub);
 void tile_chunk(Ctx& c, const Geno& g, uint64_t r0, uint64_t r1, bool last);
 void launch_fp8_terms_f64(Ctx& c, const double* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
                           const double* kscale, int terms, int row_off, uint8_t* B, float* inv_scale);
