@@ -64,6 +64,9 @@ typedef struct {
     int   precision;   /* SLFMM_PREC_*                                     */
     int   verbose;     /* progress/diagnostics on stderr                   */
     void* stream;      /* optional cudaStream_t to run on (NULL = own)     */
+    int   autotune;    /* time the tensor-core ring depths once per shape
+                          and keep the fastest (results are unchanged);
+                          also switched on by SLFMM_AUTOTUNE=1             */
 } slfmm_opts;
 
 typedef struct {

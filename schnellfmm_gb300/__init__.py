@@ -75,7 +75,7 @@ class Precision(enum.IntEnum):
 # ctypes declarations (must match include/schnelgpu.h)
 # ---------------------------------------------------------------------------
 class _Opts(C.Structure):
-    _fields_ = [("precision", C.c_int), ("verbose", C.c_int), ("stream", C.c_void_p)]
+    _fields_ = [("precision", C.c_int), ("verbose", C.c_int), ("stream", C.c_void_p), ("autotune", C.c_int)]
 
 
 class _Subset(C.Structure):
@@ -309,9 +309,9 @@ class Engine:
     """One CUDA context + stream on one device (replaces the worker pool)."""
 
     def __init__(self, device: int = 0, precision: Precision = Precision.SPLIT_FP8, stream: Optional[int] = None,
-                 verbose: bool = False):
+                 verbose: bool = False, autotune: bool = False):
         self.lib = load_library()
-        opts = _Opts(int(precision), int(verbose), C.c_void_p(stream) if stream else None)
+        opts = _Opts(int(precision), int(verbose), C.c_void_p(stream) if stream else None, int(autotune))
         h = C.c_void_p()
         rc = self.lib.slfmm_create(device, C.byref(opts), C.byref(h))
         if rc != OK:

@@ -7,6 +7,7 @@
 // packed matrix is uploaded once (pinned staging ring, double-buffered) and
 // every pass is a kernel over the resident copy.
 #include <algorithm>
+#include <mutex>
 #include <chrono>
 #include <atomic>
 #include <cmath>
@@ -35,6 +36,19 @@ void profile_collect(Ctx& c) {
         }
         kv.second.pending.clear();
     }
+}
+
+void raise_dynamic_smem(const void* fn, size_t bytes) {
+    if (bytes <= 48 * 1024) return;
+    static std::mutex mu;
+    static std::map<std::pair<int, const void*>, size_t> raised;
+    int dev = 0;
+    SLFMM_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> lock(mu);
+    size_t& cur = raised[{dev, fn}];
+    if (bytes <= cur) return;
+    SLFMM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+    cur = bytes;
 }
 
 void after_launch(Ctx& c, const char* name) {
@@ -1358,6 +1372,8 @@ int slfmm_create(int device, const slfmm_opts* opts, slfmm_ctx** out) {
     try {
         ctx_open(*c, device, opts ? opts->precision : SLFMM_PREC_SPLIT_FP8, opts ? opts->verbose : 0,
                  opts ? (cudaStream_t)opts->stream : nullptr);
+        const char* at = std::getenv("SLFMM_AUTOTUNE");
+        c->autotune = (opts && opts->autotune) || (at && at[0] == '1');
     } catch (const slfmm::Error& e) {
         fprintf(stderr, "schnelgpu: %s\n", e.what());
         const int code = e.code;
@@ -1671,6 +1687,7 @@ int slfmm_fit_many(slfmm_ctx* c, const slfmm_problem* problems, uint32_t n_probl
         Ctx w;
         try {
             ctx_open(w, c->device, c->precision, 0, nullptr);
+            w.autotune = c->autotune;
         } catch (const Error& e) {
             for (uint32_t i = next.fetch_add(1); i < n_problems; i = next.fetch_add(1)) {
                 st[i] = e.code;

@@ -320,9 +320,7 @@ void launch_assoc_epilogue(Ctx& c, uint64_t p, const float* u, int ldu, const do
     if (p == 0) return;
     SLFMM_REQUIRE(k.d <= kTraitPad, SLFMM_ERR_BAD_ARG, "at most 64 traits");
     const size_t smem = (size_t)(2 * k.w * kTraitPad + k.w * kUsStride + 2 * kTileSnps) * sizeof(float);
-    if (smem > 48 * 1024)
-        SLFMM_CUDA(cudaFuncSetAttribute(k_assoc_epilogue, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem));
+    raise_dynamic_smem((const void*)k_assoc_epilogue, smem);
     const uint64_t tiles = ceil_div(p, (uint64_t)kTileSnps);
     const unsigned grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)c.sm_count * 3);
     k_assoc_epilogue<<<grid, 256, smem, c.stream>>>(

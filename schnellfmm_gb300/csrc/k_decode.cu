@@ -361,7 +361,7 @@ void launch_repack(Ctx& c, const uint8_t* in, uint64_t rows, uint64_t in_bps, ui
     }
     const size_t keep_smem = ((ceil_div(n_out, 16) * 16 * 4 + 15) / 16) * 16 + in_bps;
     if (keep != nullptr && keep_smem <= 200 * 1024) {
-        SLFMM_CUDA(cudaFuncSetAttribute(k_repack_keep, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)keep_smem));
+        raise_dynamic_smem((const void*)k_repack_keep, keep_smem);
         const uint64_t per_sm = std::max<uint64_t>(1, std::min<uint64_t>(4, (220 * 1024) / keep_smem));
         const unsigned grid = (unsigned)std::min<uint64_t>(rows, (uint64_t)c.sm_count * per_sm);
         k_repack_keep<<<grid, 256, keep_smem, c.stream>>>(in, rows, in_bps, keep, n_out, out, stride);

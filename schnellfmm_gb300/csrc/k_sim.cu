@@ -112,8 +112,7 @@ void launch_simulate(Ctx& c, uint64_t n, uint64_t p, int n_pop, const float* adm
     const uint64_t per = round_up(ceil_div(p, want), kSimSnps);
     dim3 grid((unsigned)sblocks, (unsigned)ceil_div(p, per));
     const size_t smem = (size_t)(kSimSamples + kSimSnps) * n_pop * sizeof(float);
-    if (smem > 48 * 1024)
-        SLFMM_CUDA(cudaFuncSetAttribute(k_sim_geno, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    raise_dynamic_smem((const void*)k_sim_geno, smem);
     k_sim_geno<<<grid, 256, smem, c.stream>>>(n, p, n_pop, admix_dev, f.get(), miss, inbreeding, key ^ 0x5bd1e995ull,
                                               per, out, stride);
     SLFMM_LAUNCHED(c, "k_sim_geno");

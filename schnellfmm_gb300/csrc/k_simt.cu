@@ -166,12 +166,7 @@ template <int CPT>
 void row_lut_impl(Ctx& c, const Geno& g, const float* lut, const float* W, float* out) {
     constexpr int WP = CPT * 16;
     const size_t smem = (size_t)kRowSamples * WP * sizeof(float);
-    static thread_local bool configured = false;  // per host thread: contexts may run concurrently
-    if (!configured) {
-        SLFMM_CUDA(cudaFuncSetAttribute(k_row_lut<CPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (int)smem));
-        configured = true;
-    }
+    raise_dynamic_smem((const void*)k_row_lut<CPT>, smem);
     const unsigned grid = (unsigned)ceil_div(g.p, kRowSnps);
     k_row_lut<CPT><<<grid, 256, smem, c.stream>>>(packed_rows(g), g.stride, g.p, g.n,
                                                   reinterpret_cast<const float4*>(lut), W, out);

@@ -929,10 +929,7 @@ bool narrow_tiled(const float* A, int lda) {
     return lda % 4 == 0 && lda <= 32 && reinterpret_cast<uintptr_t>(A) % 16 == 0;
 }
 
-void set_smem(const void* fn, size_t bytes) {
-    if (bytes > 48 * 1024)
-        SLFMM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
-}
+void set_smem(const void* fn, size_t bytes) { raise_dynamic_smem(fn, bytes); }
 
 }  // namespace
 

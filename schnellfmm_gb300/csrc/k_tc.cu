@@ -542,11 +542,7 @@ int launch_tc_rows(Ctx& c, const uint8_t* packed, uint64_t stride, uint64_t rows
     SLFMM_REQUIRE(stride % 16 == 0 && stride * 4 >= ceil_div(K, kKB) * kKB, SLFMM_ERR_BAD_ARG, "bad packed stride");
     SLFMM_REQUIRE(rows < (1ull << 31), SLFMM_ERR_BAD_ARG, "too many rows");
     const TcPlan pl = plan((uint32_t)wpad);
-    static thread_local size_t configured = 0;
-    if (configured < pl.smem) {
-        SLFMM_CUDA(cudaFuncSetAttribute(k_tc_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
-        configured = pl.smem;
-    }
+    raise_dynamic_smem((const void*)k_tc_rows, pl.smem);
     const CUtensorMap tp = map_packed(packed, stride, rows);
     const CUtensorMap tb = map_bsplit(bsplit, K_pad, 2 * wpad);
     DBuf<int> err(1, c.stream);

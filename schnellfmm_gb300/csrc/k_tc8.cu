@@ -784,7 +784,10 @@ static int env_int(const char* name, int dflt) {
     return v && *v ? std::atoi(v) : dflt;
 }
 
-Fp8Plan fp8_plan(int wpad, bool ind, uint64_t tiles) {
+// The plan with explicit caps on the packed-code ring (pmax), the W ring
+// (smax) and the MMA wait group (gmax); fp8_plan takes them from the
+// environment (defaults 8, 8, 4).
+Fp8Plan fp8_plan_knobs(int wpad, bool ind, uint64_t tiles, int pmax_in, int smax, int gmax_in) {
     Fp8Plan p{};
     p.wpad = (uint32_t)wpad;
     p.n_main = kMainTerms * wpad;
@@ -804,18 +807,18 @@ Fp8Plan fp8_plan(int wpad, bool ind, uint64_t tiles) {
     p.kcopies = (!ind && 2 * p.d_cols + 3 * p.a_cols <= 512) ? 2 : 1;
     p.a_base = p.kcopies * p.d_cols;
     const uint32_t by_tmem = p.a_base < 512 ? (512 - p.a_base) / p.a_cols : 0;
-    const uint32_t pmax = (uint32_t)std::min(16, std::max(2, env_int("SLFMM_TC8_PSTAGES", 8)));
+    const uint32_t pmax = (uint32_t)std::min(16, std::max(2, pmax_in));
     for (p.pstages = pmax;; p.pstages /= 2) {
         const size_t budget = 225 * 1024 - fixed - (size_t)p.pstages * kStageBytes;
         const uint32_t by_smem = (uint32_t)(budget / p.b_stage_bytes);
-        p.stages = std::min<uint32_t>(std::min(by_tmem, by_smem), (uint32_t)env_int("SLFMM_TC8_STAGES", 8));
+        p.stages = std::min<uint32_t>(std::min(by_tmem, by_smem), (uint32_t)std::max(1, smax));
         if (p.stages >= std::min<uint32_t>(by_tmem, 2) || p.pstages <= 2) break;
     }
     // MMA wait groups: up to 16 MMAs per wait and warp, at least two groups in the ring
     const uint32_t nch = p.n_main > 256 ? 2 : 1;
     const uint32_t per_stage = (kStageK / 32) * (p.nsplit || p.kcopies == 2 ? nch : nch + (ind ? 1 : 0));
     p.group = 1;
-    const uint32_t gmax = (uint32_t)env_int("SLFMM_TC8_GROUP", 4);
+    const uint32_t gmax = (uint32_t)gmax_in;
     for (uint32_t gsz : {4u, 2u})
         if (gsz <= gmax && gsz * per_stage <= 16 && p.stages >= 2 * gsz) {
             p.group = gsz;
@@ -838,6 +841,11 @@ Fp8Plan fp8_plan(int wpad, bool ind, uint64_t tiles) {
     p.ok = p.stages >= 2 && p.n_main % ceil_div(p.n_main, 256) == 0 && (p.n_main / ceil_div(p.n_main, 256)) % 16 == 0 &&
            p.n_ind <= 256;
     return p;
+}
+
+Fp8Plan fp8_plan(int wpad, bool ind, uint64_t tiles) {
+    return fp8_plan_knobs(wpad, ind, tiles, env_int("SLFMM_TC8_PSTAGES", 8), env_int("SLFMM_TC8_STAGES", 8),
+                          env_int("SLFMM_TC8_GROUP", 4));
 }
 
 // row-major packed rows (rows x stride) -> tile-major copy; one thread per
@@ -1110,10 +1118,89 @@ void throw_tc8_timeout(int site) {
                 "split-FP8 contraction: a bounded device wait expired (site " + std::to_string(site) + ")");
 }
 
+static int tc8_launch(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t rows, uint64_t K, const uint8_t* B,
+                      const float* inv_scale, uint64_t K_pad, int mode, const double* row_mean,
+                      const double* row_scale, const double* cs, float* out, int ldo, int splits,
+                      uint64_t split_stride, int* err_dev);
+
+// Autotuner: the ring depths (packed codes, W stages) of a plan, timed on
+// two waves of the real pass and cached per context and shape.  Only knobs
+// that leave the arithmetic alone are tuned: the candidates keep the default
+// plan's MMA wait group and accumulator layout, so every choice gives the
+// same bits.
+static Fp8Plan tc8_tuned_plan(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t rows, uint64_t K,
+                              const uint8_t* B, const float* inv_scale, uint64_t K_pad, int mode,
+                              const double* row_mean, const double* row_scale, const double* cs, int ldo, int splits,
+                              uint64_t split_stride) {
+    const std::string key = std::to_string(pl.wpad) + "/" + std::to_string(pl.n_ind) + "/" + std::to_string(K) +
+                            "/" + std::to_string(splits) + "/" + std::to_string(mode);
+    auto rebuild = [&](int pmax, int smax) {
+        return fp8_plan_knobs((int)pl.wpad, pl.n_ind != 0, ceil_div(rows, (uint64_t)kM), pmax, smax, (int)pl.group);
+    };
+    auto it = c.tuned.find(key);
+    if (it != c.tuned.end()) return rebuild(it->second.first, it->second.second);
+    const uint64_t trial_rows = std::min<uint64_t>(rows, (uint64_t)c.sm_count * 2 * kM);
+    DBuf<float> scratch(std::max<uint64_t>(trial_rows, 1) * (uint64_t)ldo * std::max(splits, 1), c.stream);
+    cudaEvent_t e0, e1;
+    SLFMM_CUDA(cudaEventCreate(&e0));
+    SLFMM_CUDA(cudaEventCreate(&e1));
+    struct EvGuard {
+        cudaEvent_t a, b;
+        ~EvGuard() { cudaEventDestroy(a); cudaEventDestroy(b); }
+    } guard{e0, e1};
+    DBuf<int> err(1, c.stream);
+    err.zero();
+    float best = 1e30f;
+    std::pair<int, int> pick{8, 8};
+    for (int pmax : {2, 4, 8, 16})
+        for (int smax : {2, 3, 4, 8}) {
+            const Fp8Plan q = rebuild(pmax, smax);
+            if (!q.ok || q.group != pl.group || q.kcopies != pl.kcopies || q.nsplit != pl.nsplit) continue;
+            float ms = 1e30f;
+            for (int rep = 0; rep < 2; ++rep) {
+                SLFMM_CUDA(cudaEventRecord(e0, c.stream));
+                tc8_launch(c, q, tv, trial_rows, K, B, inv_scale, K_pad, mode, row_mean, row_scale, cs,
+                           scratch.get(), ldo, splits, trial_rows * (uint64_t)ldo, err.get());
+                SLFMM_CUDA(cudaEventRecord(e1, c.stream));
+                SLFMM_CUDA(cudaEventSynchronize(e1));
+                float t = 0.f;
+                SLFMM_CUDA(cudaEventElapsedTime(&t, e0, e1));
+                ms = std::min(ms, t);
+            }
+            if (ms < best) {
+                best = ms;
+                pick = {pmax, smax};
+            }
+        }
+    int h = 0;
+    SLFMM_CUDA(cudaMemcpyAsync(&h, err.get(), sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    SLFMM_CUDA(cudaStreamSynchronize(c.stream));
+    if (h != 0) throw_tc8_timeout(h);
+    c.tuned[key] = pick;
+    if (c.verbose)
+        fprintf(stderr, "[schnelgpu] autotune %s: packed ring cap %d, W ring cap %d (%.3f ms on %llu rows)\n",
+                key.c_str(), pick.first, pick.second, best, (unsigned long long)trial_rows);
+    return rebuild(pick.first, pick.second);
+}
+
 int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t rows, uint64_t K,
-                     const uint8_t* B, const float* inv_scale, uint64_t K_pad, int mode, const double* row_mean,
-                     const double* row_scale, const double* cs, float* out, int ldo, int splits,
-                     uint64_t split_stride, int* err_dev) {
+                    const uint8_t* B, const float* inv_scale, uint64_t K_pad, int mode, const double* row_mean,
+                    const double* row_scale, const double* cs, float* out, int ldo, int splits,
+                    uint64_t split_stride, int* err_dev) {
+    if (c.autotune && pl.ok && pl.cluster == 1 && rows > 0) {
+        const Fp8Plan tp = tc8_tuned_plan(c, pl, tv, rows, K, B, inv_scale, K_pad, mode, row_mean, row_scale, cs, ldo,
+                                          splits, split_stride);
+        if (tp.ok) return tc8_launch(c, tp, tv, rows, K, B, inv_scale, K_pad, mode, row_mean, row_scale, cs, out, ldo,
+                                     splits, split_stride, err_dev);
+    }
+    return tc8_launch(c, pl, tv, rows, K, B, inv_scale, K_pad, mode, row_mean, row_scale, cs, out, ldo, splits,
+                      split_stride, err_dev);
+}
+
+static int tc8_launch(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t rows, uint64_t K, const uint8_t* B,
+                      const float* inv_scale, uint64_t K_pad, int mode, const double* row_mean,
+                      const double* row_scale, const double* cs, float* out, int ldo, int splits,
+                      uint64_t split_stride, int* err_dev) {
     SLFMM_REQUIRE(pl.ok, SLFMM_ERR_BAD_ARG, "no feasible split-FP8 tile plan for this width");
     SLFMM_REQUIRE(K_pad % kStageK == 0 && K_pad >= ceil_div(K, kStageK) * kStageK, SLFMM_ERR_BAD_ARG,
                   "bad K padding");
@@ -1122,11 +1209,7 @@ int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t rows
     SLFMM_REQUIRE(tv.ntiles >= round_up(ceil_div(rows, kM), pl.cluster), SLFMM_ERR_BAD_ARG,
                   "tile-major operand has too few tiles");
     SLFMM_REQUIRE(mode == 0 || pl.n_ind != 0, SLFMM_ERR_BAD_ARG, "row correction needs the indicator operand");
-    static thread_local size_t configured = 0;
-    if (configured < pl.smem) {
-        SLFMM_CUDA(cudaFuncSetAttribute(k_tc8_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)pl.smem));
-        configured = pl.smem;
-    }
+    raise_dynamic_smem((const void*)k_tc8_rows, pl.smem);
     const CUtensorMap tb = map2d_u8(B, K_pad, pl.n_total, 128, pl.box_rows, true);
     DBuf<int> err;
     if (!err_dev) {
@@ -1180,7 +1263,17 @@ int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t rows
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    SLFMM_CUDA(cudaLaunchKernelEx(&cfg, k_tc8_rows, tb, a));
+    const cudaError_t le = cudaLaunchKernelEx(&cfg, k_tc8_rows, tb, a);
+    if (le != cudaSuccess) {
+        cudaGetLastError();
+        char buf[320];
+        snprintf(buf, sizeof buf,
+                 "split-FP8 contraction launch failed (%s): grid %u x %u, smem %zu, stages %u, pstages %u, group %u, "
+                 "n_total %u, box %u x %u, rows %llu, K %llu",
+                 cudaGetErrorString(le), gx, gy, pl.smem, pl.stages, pl.pstages, pl.group, pl.n_total, 128u,
+                 pl.box_rows, (unsigned long long)rows, (unsigned long long)K);
+        throw Error(SLFMM_ERR_CUDA, buf);
+    }
     SLFMM_LAUNCHED(c, "k_tc8_rows");
     if (err_dev) return (int)gy;
     int h = 0;

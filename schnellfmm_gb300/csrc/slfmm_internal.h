@@ -158,6 +158,8 @@ struct Ctx {
     bool profiling = false;
     std::map<std::string, ProfRec> prof;
     double phase_t0 = 0.0;  // verbose phase log: start of the current phase (ms)
+    bool autotune = false;   // time the tensor-core ring depths per shape once
+    std::map<std::string, std::pair<int, int>> tuned;  // shape -> (packed ring cap, W ring cap)
 };
 
 // bracket a launch with CUDA events when profiling is on
@@ -193,6 +195,12 @@ inline int grid_for(const Ctx& c, uint64_t work, int block) {
     const uint64_t g = want < cap ? want : cap;
     return (int)(g > 0 ? g : 1);
 }
+
+// Raise a kernel's dynamic shared-memory limit to at least `bytes` (no-op up
+// to 48 KiB).  The limit is a process-wide attribute of the function, and
+// contexts may launch from several host threads, so it only ever grows:
+// every launch finds it at least as large as it set it.
+void raise_dynamic_smem(const void* fn, size_t bytes);
 
 // count + check a kernel launch
 void after_launch(Ctx& c, const char* name);
@@ -268,7 +276,7 @@ struct Fp8Plan {
     bool ok;
 };
 Fp8Plan fp8_plan(int wpad, bool ind, uint64_t tiles);
-// tile-major packed operand (rows = SNPs, or samples when transposed)
+Fp8Plan fp8_plan_knobs(int wpad, bool ind, uint64_t tiles, int pmax, int smax, int gmax);
 // the row-major packed copy of a matrix (a sample subset built from the
 // tile-major copies has none: the passes that need it must not run on it)
 inline const uint8_t* packed_rows(const Geno& g) {
@@ -276,6 +284,7 @@ inline const uint8_t* packed_rows(const Geno& g) {
     return g.packed.get();
 }
 
+// tile-major packed operand (rows = SNPs, or samples when transposed)
 struct TileView {
     const uint8_t* base;
     uint64_t kbt, ntiles;

@@ -99,3 +99,25 @@ def test_fit_many_reports_the_problem(engine):
     with pytest.raises(sg.SchnelGpuError) as e:
         sg.fit_lfmm2_many(probs, engine=engine, n_streams=2)
     assert "problem 1" in str(e.value)
+
+
+@pytest.mark.parametrize("case", ["nmf", "wide"])
+def test_fit_traits_row_major_subsets(engine, case):
+    """Fits that need the row-major copy (NMF imputation; a sketch too wide
+    for the indicator plan) take the re-packed subset: still bit for bit the
+    per-trait subset fits."""
+    sg = _sg()
+    c = simdata.simulate(300, 3000, k_pop=3, fst=0.08, miss=0.05, d=1, seed=23)
+    y, masks = _traits(c.n, 2, 8)
+    if case == "nmf":
+        cfg = sg.Lfmm2Config(k=3, oversampling=5, norm=sg.SnpNorm.EIGENSTRAT, impute=sg.ImputeStrategy.NMF,
+                             nmf=sg.NmfConfig(k=4, n_iter=3, cv_rate=0.01))
+    else:
+        cfg = sg.Lfmm2Config(k=40, oversampling=10, norm=sg.SnpNorm.EIGENSTRAT)
+    geno = engine.upload(c.packed, c.n)
+    res = sg.fit_lfmm2_traits(geno, y, masks, cfg, engine=engine)
+    for t in range(2):
+        keep = np.flatnonzero(masks[:, t])
+        sub = engine.upload(c.packed, c.n, sample_keep=keep)
+        ref = sg.fit_lfmm2(sub, sg.SubsetSpec.all(), sub, y[keep, t:t + 1], cfg, engine=engine)
+        _same(res[t], ref)
