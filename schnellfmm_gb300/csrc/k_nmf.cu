@@ -306,12 +306,20 @@ __global__ void __launch_bounds__(256) k_nmf_cv(const uint8_t* __restrict__ pack
         const int64_t c0 = counts[r * 4], c1 = counts[r * 4 + 1], c2 = counts[r * 4 + 2];
         const int64_t nobs = c0 + c1 + c2;
         const double cm = nobs > 0 ? (double)(c1 + 2 * c2) / (double)nobs : 0.0;
-        const uint8_t* row = packed + r * stride;
+        // a lane takes the 16 codes of one 32-bit word at a time; the draw
+        // input key + (ctr + 1) gamma of consecutive samples differs by gamma
+        const uint32_t* row = reinterpret_cast<const uint32_t*>(packed + r * stride);
+        const uint64_t nwords = (n + 15) / 16;
         double e1 = 0.0, e2 = 0.0, cnt = 0.0;
-        for (uint64_t i = lane; i < n; i += 32) {
-            const uint32_t code = code_at(row, i);
-            if (code == 1u) continue;
-            if (draw_below(key, col * n + i, thresh)) {
+        for (uint64_t wd = lane; wd < nwords; wd += 32) {
+            const uint32_t v = row[wd];
+            const uint64_t i0 = wd * 16;
+            uint64_t z = key + (col * n + i0 + 1) * kGamma;
+            const int nb = n - i0 < 16 ? (int)(n - i0) : 16;
+            for (int b = 0; b < nb; ++b, z += kGamma) {
+                const uint32_t code = (v >> (2 * b)) & 3u;
+                if (code == 1u || (mix64(z) >> 11) >= thresh) continue;
+                const uint64_t i = i0 + b;
                 const double g = code == 0 ? 0.0 : (double)(code - 1);
                 e1 += fabs(g - (double)fill_dot(W + i * k, hs[wl], k));
                 e2 += fabs(g - cm);
