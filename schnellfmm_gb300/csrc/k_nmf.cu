@@ -184,14 +184,16 @@ __global__ void __launch_bounds__(256) k_fill_row_correct(float* __restrict__ ou
 // segments of kColSeg calls, one warp per (sample, segment), and the segment
 // sums are added into S with FP64 atomics.
 constexpr uint64_t kColSeg = 1024;
-template <int CG>
+// sm[r] = (s_r, mu_r) in FP32 (the values the correction uses), one 8-byte
+// gather per call; with H4 the H row (k % 4 == 0, 16-byte aligned) is read as
+// 16-byte loads, the products summed in the same order as fill_dot.
+template <int CG, bool H4>
 __global__ void __launch_bounds__(256) k_fill_col_correct(double* __restrict__ S, int lds, uint64_t n, int w,
                                                           uint64_t nseg, const uint64_t* __restrict__ cptr,
                                                           const uint32_t* __restrict__ cidx,
                                                           const float* __restrict__ Qop, int ldq,
                                                           const float* __restrict__ Wn, const float* __restrict__ H,
-                                                          int k, const double* __restrict__ mean,
-                                                          const double* __restrict__ scale) {
+                                                          int k, const float2* __restrict__ sm) {
     __shared__ float ws[8][kMaxNmfK];
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     const uint64_t nw = (uint64_t)gridDim.x * 8;
@@ -208,8 +210,24 @@ __global__ void __launch_bounds__(256) k_fill_col_correct(double* __restrict__ S
             float dm = 0.f;
             if (b + lane < e1) {
                 my = cidx[b + lane];
-                const float f = fill_dot(H + (uint64_t)my * k, ws[wl], k);
-                dm = (float)scale[my] * (f - (float)mean[my]);
+                float f = 0.f;
+                if constexpr (H4) {
+                    const float4* h4 = reinterpret_cast<const float4*>(H + (uint64_t)my * k);
+#pragma unroll
+                    for (int q = 0; q < kMaxNmfK / 4; ++q) {
+                        if (4 * q < k) {
+                            const float4 v = h4[q];
+                            f = fmaf(v.x, ws[wl][4 * q], f);
+                            f = fmaf(v.y, ws[wl][4 * q + 1], f);
+                            f = fmaf(v.z, ws[wl][4 * q + 2], f);
+                            f = fmaf(v.w, ws[wl][4 * q + 3], f);
+                        }
+                    }
+                } else {
+                    f = fill_dot(H + (uint64_t)my * k, ws[wl], k);
+                }
+                const float2 smv = sm[my];
+                dm = smv.x * (f - smv.y);
             }
             round_accum<CG>(acc, my, dm, (int)(e1 - b < 32 ? e1 - b : 32), Qop, ldq, w, lane);
         }
@@ -489,31 +507,46 @@ void launch_fill_row_correct(Ctx& c, const Geno& g, float* out, int ldo, int w, 
     SLFMM_LAUNCHED(c, "k_fill_row_correct");
 }
 
+__global__ void k_scale_mean_f32(const double* __restrict__ mean, const double* __restrict__ scale, uint64_t p,
+                                 float2* __restrict__ out) {
+    for (uint64_t r = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; r < p; r += (uint64_t)gridDim.x * blockDim.x)
+        out[r] = make_float2((float)scale[r], (float)mean[r]);
+}
+
+template <bool H4>
+static void fill_col_correct_launch(Ctx& c, const Geno& g, unsigned grid, uint64_t nseg, double* S, int lds, int w,
+                                    const float* Qop, int ldq, const float* Wn, const float* H, int k,
+                                    const float2* sm) {
+    const uint64_t* cp = g.missT_ptr.get();
+    const uint32_t* ci = g.missT_idx.get();
+    switch (narrow_group(w)) {
+        case 8:
+            k_fill_col_correct<8, H4><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, sm);
+            break;
+        case 16:
+            k_fill_col_correct<16, H4><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, sm);
+            break;
+        case 32:
+            k_fill_col_correct<32, H4><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, sm);
+            break;
+        default:
+            k_fill_col_correct<0, H4><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, sm);
+    }
+}
+
 void launch_fill_col_correct(Ctx& c, const Geno& g, double* S, int lds, int w, const float* Qop, int ldq,
                              const float* Wn, const float* H, int k, const double* mean, const double* scale) {
     if (!g.n || !w) return;
     SLFMM_REQUIRE(w <= 128 && k >= 1 && k <= kMaxNmfK, SLFMM_ERR_BAD_ARG, "NMF correction shape");
     const uint64_t nseg = std::max<uint64_t>(1, ceil_div(g.missT_max, kColSeg));
     const unsigned grid = (unsigned)grid_for(c, g.n * nseg, 8);
-    const uint64_t* cp = g.missT_ptr.get();
-    const uint32_t* ci = g.missT_idx.get();
-    switch (narrow_group(w)) {
-        case 8:
-            k_fill_col_correct<8><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, mean,
-                                                              scale);
-            break;
-        case 16:
-            k_fill_col_correct<16><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, mean,
-                                                               scale);
-            break;
-        case 32:
-            k_fill_col_correct<32><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, mean,
-                                                               scale);
-            break;
-        default:
-            k_fill_col_correct<0><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, mean,
-                                                              scale);
-    }
+    DBuf<float2> sm(std::max<uint64_t>(g.p, 1), c.stream);
+    k_scale_mean_f32<<<grid_for(c, g.p, 256), 256, 0, c.stream>>>(mean, scale, g.p, sm.get());
+    SLFMM_LAUNCHED(c, "k_scale_mean_f32");
+    if (k % 4 == 0 && reinterpret_cast<uintptr_t>(H) % 16 == 0)
+        fill_col_correct_launch<true>(c, g, grid, nseg, S, lds, w, Qop, ldq, Wn, H, k, sm.get());
+    else
+        fill_col_correct_launch<false>(c, g, grid, nseg, S, lds, w, Qop, ldq, Wn, H, k, sm.get());
     SLFMM_LAUNCHED(c, "k_fill_col_correct");
 }
 
