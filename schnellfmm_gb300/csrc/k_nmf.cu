@@ -139,7 +139,7 @@ __device__ __forceinline__ void round_finish(float (&acc)[4]) {
 // Row pass correction: out[r, c] += s_r * sum_{i in miss(r)} (f_ir - mu_r) Wop[i, c]
 // (the base pass counted the missing calls at the mean).  One warp per SNP;
 // 32 missing indices and their fills are formed per round and broadcast.
-template <int CG>
+template <int CG, bool W4>
 __global__ void __launch_bounds__(256) k_fill_row_correct(float* __restrict__ out, int ldo, uint64_t p, int w,
                                                           const uint64_t* __restrict__ ptr,
                                                           const uint32_t* __restrict__ idx, const float* __restrict__ Wop,
@@ -163,7 +163,23 @@ __global__ void __launch_bounds__(256) k_fill_row_correct(float* __restrict__ ou
             float dm = 0.f;
             if (b + lane < e1) {
                 my = idx[b + lane];
-                dm = fill_dot(Wn + (uint64_t)my * k, hs[wl], k) - mu;
+                float f = 0.f;
+                if constexpr (W4) {  // 16-byte loads of the W row, summed in fill_dot's order
+                    const float4* w4 = reinterpret_cast<const float4*>(Wn + (uint64_t)my * k);
+#pragma unroll
+                    for (int q = 0; q < kMaxNmfK / 4; ++q) {
+                        if (4 * q < k) {
+                            const float4 v = w4[q];
+                            f = fmaf(v.x, hs[wl][4 * q], f);
+                            f = fmaf(v.y, hs[wl][4 * q + 1], f);
+                            f = fmaf(v.z, hs[wl][4 * q + 2], f);
+                            f = fmaf(v.w, hs[wl][4 * q + 3], f);
+                        }
+                    }
+                } else {
+                    f = fill_dot(Wn + (uint64_t)my * k, hs[wl], k);
+                }
+                dm = f - mu;
             }
             round_accum<CG>(acc, my, dm, (int)(e1 - b < 32 ? e1 - b : 32), Wop, ldw, w, lane);
         }
@@ -482,28 +498,40 @@ void launch_fill_stats(Ctx& c, const Geno& g, int norm, const float* W, const fl
 // narrow operand group size: the smallest of 8, 16, 32 that holds w, else 0
 static int narrow_group(int w) { return w <= 8 ? 8 : w <= 16 ? 16 : w <= 32 ? 32 : 0; }
 
+template <bool W4>
+static void fill_row_correct_launch(Ctx& c, const Geno& g, unsigned grid, float* out, int ldo, int w,
+                                    const float* Wop, int ldw, const float* Wn, const float* H, int k,
+                                    const double* mean, const double* scale) {
+    const uint64_t* mp = g.miss_ptr.get();
+    const uint32_t* mi = g.miss_idx.get();
+    switch (narrow_group(w)) {
+        case 8:
+            k_fill_row_correct<8, W4><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, mp, mi, Wop, ldw, Wn, H, k, mean,
+                                                                  scale);
+            break;
+        case 16:
+            k_fill_row_correct<16, W4><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, mp, mi, Wop, ldw, Wn, H, k, mean,
+                                                                   scale);
+            break;
+        case 32:
+            k_fill_row_correct<32, W4><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, mp, mi, Wop, ldw, Wn, H, k, mean,
+                                                                   scale);
+            break;
+        default:
+            k_fill_row_correct<0, W4><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, mp, mi, Wop, ldw, Wn, H, k, mean,
+                                                                  scale);
+    }
+}
+
 void launch_fill_row_correct(Ctx& c, const Geno& g, float* out, int ldo, int w, const float* Wop, int ldw,
                              const float* Wn, const float* H, int k, const double* mean, const double* scale) {
     if (!g.p || !w) return;
     SLFMM_REQUIRE(w <= 128 && k >= 1 && k <= kMaxNmfK, SLFMM_ERR_BAD_ARG, "NMF correction shape");
     const unsigned grid = (unsigned)grid_for(c, g.p, 8);
-    switch (narrow_group(w)) {
-        case 8:
-            k_fill_row_correct<8><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, g.miss_ptr.get(), g.miss_idx.get(),
-                                                              Wop, ldw, Wn, H, k, mean, scale);
-            break;
-        case 16:
-            k_fill_row_correct<16><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, g.miss_ptr.get(), g.miss_idx.get(),
-                                                               Wop, ldw, Wn, H, k, mean, scale);
-            break;
-        case 32:
-            k_fill_row_correct<32><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, g.miss_ptr.get(), g.miss_idx.get(),
-                                                               Wop, ldw, Wn, H, k, mean, scale);
-            break;
-        default:
-            k_fill_row_correct<0><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, g.miss_ptr.get(), g.miss_idx.get(),
-                                                              Wop, ldw, Wn, H, k, mean, scale);
-    }
+    if (k % 4 == 0 && reinterpret_cast<uintptr_t>(Wn) % 16 == 0)
+        fill_row_correct_launch<true>(c, g, grid, out, ldo, w, Wop, ldw, Wn, H, k, mean, scale);
+    else
+        fill_row_correct_launch<false>(c, g, grid, out, ldo, w, Wop, ldw, Wn, H, k, mean, scale);
     SLFMM_LAUNCHED(c, "k_fill_row_correct");
 }
 
