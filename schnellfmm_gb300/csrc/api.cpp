@@ -151,14 +151,16 @@ struct ChunkHook {
     virtual ~ChunkHook() = default;
 };
 
+// snps: the payload rows to take, in order (nullptr: all n_snps rows)
 void upload_geno(Ctx& c, Geno& g, const uint8_t* packed, uint64_t n_phys, uint64_t n_snps,
-                 const uint64_t* keep, uint64_t n_keep, const std::vector<uint64_t>& snps,
+                 const uint64_t* keep, uint64_t n_keep, const std::vector<uint64_t>* snps,
                  ChunkHook* hook = nullptr) {
     SLFMM_REQUIRE(packed != nullptr || n_snps == 0, SLFMM_ERR_BAD_ARG, "null genotype payload");
     SLFMM_REQUIRE(n_phys > 0, SLFMM_ERR_BAD_ARG, "no samples");
     const uint64_t bps = ceil_div(n_phys, 4);
     g.n = keep ? n_keep : n_phys;
-    g.p = snps.size();
+    g.p = snps ? snps->size() : n_snps;
+    auto row_of = [snps](uint64_t r) { return snps ? (*snps)[r] : r; };
     SLFMM_REQUIRE(g.n > 0, SLFMM_ERR_BAD_ARG, "empty sample subset");
     SLFMM_REQUIRE(g.n < (1ull << 31), SLFMM_ERR_BAD_ARG, "too many samples");
     g.stride = round_up(ceil_div(g.n, 4), 128);
@@ -230,23 +232,24 @@ void upload_geno(Ctx& c, Geno& g, const uint8_t* packed, uint64_t n_phys, uint64
             const int b = (int)(ch % NS);
             const uint64_t r0 = ch * rows_per, r1 = std::min(g.p, r0 + rows_per), rows = r1 - r0;
             bool contiguous = true;  // one copy when the rows are consecutive (src/parallel.rs:129-146)
-            for (uint64_t r = r0 + 1; r < r1 && contiguous; ++r) contiguous = snps[r] == snps[r - 1] + 1;
+            if (snps)
+                for (uint64_t r = r0 + 1; r < r1 && contiguous; ++r) contiguous = (*snps)[r] == (*snps)[r - 1] + 1;
             SLFMM_CUDA(cudaStreamWaitEvent(c.copy_stream, consumed[b], 0));
             if (direct && contiguous) {
-                SLFMM_CUDA(cudaMemcpyAsync(dstage[b].get(), packed + snps[r0] * bps, rows * bps,
+                SLFMM_CUDA(cudaMemcpyAsync(dstage[b].get(), packed + row_of(r0) * bps, rows * bps,
                                            cudaMemcpyHostToDevice, c.copy_stream));
             } else if (direct) {
                 for (uint64_t r = r0; r < r1; ++r)
-                    SLFMM_CUDA(cudaMemcpyAsync(dstage[b].get() + (r - r0) * bps, packed + snps[r] * bps, bps,
+                    SLFMM_CUDA(cudaMemcpyAsync(dstage[b].get() + (r - r0) * bps, packed + row_of(r) * bps, bps,
                                                cudaMemcpyHostToDevice, c.copy_stream));
             } else {
                 // the pinned buffer b is reused only after its previous H2D finished
                 SLFMM_CUDA(cudaEventSynchronize(copied[b]));
                 if (contiguous) {
-                    std::memcpy(hstage[b], packed + snps[r0] * bps, rows * bps);
+                    std::memcpy(hstage[b], packed + row_of(r0) * bps, rows * bps);
                 } else {
                     for (uint64_t r = r0; r < r1; ++r)
-                        std::memcpy(hstage[b] + (r - r0) * bps, packed + snps[r] * bps, bps);
+                        std::memcpy(hstage[b] + (r - r0) * bps, packed + row_of(r) * bps, bps);
                 }
                 SLFMM_CUDA(cudaMemcpyAsync(dstage[b].get(), hstage[b], rows * bps, cudaMemcpyHostToDevice,
                                            c.copy_stream));
@@ -1429,8 +1432,12 @@ int slfmm_geno_upload(slfmm_ctx* c, const uint8_t* packed, uint64_t n_physical, 
     API_TRY
     SLFMM_CUDA(cudaSetDevice(c->device));
     std::unique_ptr<slfmm_geno> g(new slfmm_geno());
-    std::vector<uint64_t> idx = subset_indices(snps, n_snps);
-    upload_geno(*c, *g, packed, n_physical, n_snps, sample_keep, n_keep, idx);
+    if (!snps || snps->kind == SLFMM_SUBSET_ALL) {
+        upload_geno(*c, *g, packed, n_physical, n_snps, sample_keep, n_keep, nullptr);
+    } else {
+        const std::vector<uint64_t> idx = subset_indices(snps, n_snps);
+        upload_geno(*c, *g, packed, n_physical, n_snps, sample_keep, n_keep, &idx);
+    }
     *out = g.release();
     API_CATCH(c)
 }
@@ -1563,7 +1570,7 @@ int slfmm_fit_host(slfmm_ctx* c, const uint8_t* packed, uint64_t n_physical, uin
     phase(*c, "", true);
     const bool pre = all && cfg && presketch_eligible(*c, sample_keep ? n_keep : n_physical, n_snps, x, (int)d,
                                                       cfg, omega, ps);
-    upload_geno(*c, full, packed, n_physical, n_snps, sample_keep, n_keep, subset_indices(nullptr, n_snps),
+    upload_geno(*c, full, packed, n_physical, n_snps, sample_keep, n_keep, nullptr,
                 pre ? &ps : nullptr);
     if (pre) {
         const int e = fetch(*c, ps.err.get(), 1)[0];
@@ -1572,7 +1579,8 @@ int slfmm_fit_host(slfmm_ctx* c, const uint8_t* packed, uint64_t n_physical, uin
     phase(*c, pre ? "covariates; upload with the sketch pass" : "upload");
     const Geno* ge = &full;
     if (!all) {
-        upload_geno(*c, sub, packed, n_physical, n_snps, sample_keep, n_keep, subset_indices(est, n_snps));
+        const std::vector<uint64_t> est_idx = subset_indices(est, n_snps);
+        upload_geno(*c, sub, packed, n_physical, n_snps, sample_keep, n_keep, &est_idx);
         ge = &sub;
     }
     fit_impl(*c, *ge, full, x, (int)d, cfg, omega, res, pre ? &ps : nullptr);
@@ -1624,7 +1632,7 @@ void fit_problem(Ctx& c, const slfmm_problem& pr) {
     Geno full;
     Presketch ps;
     const bool pre = presketch_eligible(c, pr.n_physical, pr.n_snps, pr.x, (int)pr.d, pr.cfg, pr.omega, ps);
-    upload_geno(c, full, pr.packed, pr.n_physical, pr.n_snps, nullptr, 0, subset_indices(nullptr, pr.n_snps),
+    upload_geno(c, full, pr.packed, pr.n_physical, pr.n_snps, nullptr, 0, nullptr,
                 pre ? &ps : nullptr);
     if (pre) {
         const int e = fetch(c, ps.err.get(), 1)[0];
