@@ -1,6 +1,6 @@
 """CPU oracle for the streaming LFMM2 hot path -- TEST INFRASTRUCTURE ONLY.
 
-This module is the checker, never the product.  Only ``tests/``,
+This module is the oracle, never the product.  Only ``tests/``,
 ``__graft_entry__.smoke()`` and ``bench.py`` (its ``cpu_baseline`` leg and
 its ``--impl reference`` arm) may import it.  The product path lives in
 ``schnellfmm_gb300`` and runs on the GPU only.

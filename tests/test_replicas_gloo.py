@@ -1,5 +1,5 @@
-"""The N > 1 form of the benchmark runs independent replicas (the fit does
-not shard on one-GPU machines): the job time is the slowest rank's and the job
+"""The N > 1 form of the benchmark runs independent replicas (the fit is not
+sharded across GPUs): the job time is the slowest rank's and the job
 rate counts every rank's SNPs.  Checked with two gloo ranks on the CPU."""
 import os
 import socket
