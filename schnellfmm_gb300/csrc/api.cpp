@@ -1,7 +1,7 @@
 // C ABI and host orchestration of the GB300 streaming LFMM2 engine.
 //
 // Mirrors the library surface of schnelLFMM (src/lib.rs:102-263) and the
-// stage drivers estimate_factors_streaming (src/rsvd.rs:26-177) and
+// stage functions estimate_factors_streaming (src/rsvd.rs:26-177) and
 // test_associations_fused (src/testing.rs:252-528).  The reference streams
 // the memory-mapped .bed through a thread pool for every pass; here the
 // packed matrix is uploaded once (pinned staging ring, double-buffered) and
