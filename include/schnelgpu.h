@@ -53,6 +53,14 @@ extern "C" {
 #define SLFMM_IMPUTE_MEAN      0      /* ImputeStrategy::Mean (src/lib.rs:39-44) */
 #define SLFMM_IMPUTE_NMF       1      /* ImputeStrategy::Nmf                     */
 
+/* Stream the Gaussian sketches (Omega of src/rsvd.rs:44-46, the NMF probe of
+ * src/nmf.rs:291-293) are drawn from. */
+#define SLFMM_RNG_COUNTER      0      /* SplitMix64 counter stream, drawn on the
+                                         device (default)                        */
+#define SLFMM_RNG_CHACHA8      1      /* ChaCha8Rng::seed_from_u64(seed) sampled
+                                         by Normal(0, 1) in row-major order, the
+                                         reference's stream, drawn on the host   */
+
 #define SLFMM_SUBSET_ALL       0      /* SubsetSpec::All     (src/bed.rs:50-57)  */
 #define SLFMM_SUBSET_RATE      1      /* SubsetSpec::Rate(r)                     */
 #define SLFMM_SUBSET_INDICES   2      /* SubsetSpec::Indices(v)                  */
@@ -67,6 +75,7 @@ typedef struct {
     int   autotune;    /* time the tensor-core ring depths once per shape
                           and keep the fastest (results are unchanged);
                           also switched on by SLFMM_AUTOTUNE=1             */
+    int   rng;         /* SLFMM_RNG_* stream of the sketch matrices        */
 } slfmm_opts;
 
 typedef struct {
@@ -169,6 +178,12 @@ int slfmm_center_covariates(slfmm_ctx* ctx, const double* x, uint64_t n, uint32_
 /* Random sketch Omega (n x l) the engine uses for a given seed. */
 int slfmm_generate_omega(slfmm_ctx* ctx, uint64_t seed, uint64_t n, uint32_t l,
                          double* out);
+/* Host-only (no context, no device): the rows x cols row-major matrix of
+ * Normal(0, 1) draws from ChaCha8Rng::seed_from_u64(seed), i.e.
+ * Array2::from_shape_fn((rows, cols), |_| normal.sample(&mut rng)) of
+ * src/rsvd.rs:44-46 (seed = config.seed) and src/nmf.rs:291-293
+ * (seed = config.seed + 1 000 000).  The SLFMM_RNG_CHACHA8 stream. */
+int slfmm_reference_normal(uint64_t seed, uint64_t rows, uint32_t cols, double* out);
 /* estimate_factors (src/lib.rs:127-136): Step 0 + RSVD of M Y_est.
  * omega: n x (K+oversampling) or NULL (engine RNG).  u_hat: n x K. */
 int slfmm_estimate_factors(slfmm_ctx* ctx, const slfmm_geno* y_est, const double* x,

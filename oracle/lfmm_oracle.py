@@ -20,10 +20,14 @@ reference file:line it follows.  Two forms are provided:
 Parity status: the decode, counting, mean/scale, subset, histogram/median,
 GIF and covariate-centring rules are pinned by the reference's own unit-test
 known answers (``tests/golden/reference_kats.json`` and the CPU tests).  The
-random streams (ChaCha8 + rand_distr in the reference) are NOT reproduced: a
-counter-based SplitMix64 generator is used by both this oracle and the GPU,
-so RNG-dependent quantities (Omega, CV masks) are "parity unpinned" against
-the reference and compared at the subspace / statistical level instead.
+engine's default random streams are a counter-based SplitMix64 generator
+shared by this oracle and the GPU.  The reference's sketch stream
+(ChaCha8Rng::seed_from_u64 + Normal(0, 1)) is restated in
+``chacha8_normal_matrix`` from the published algorithms; its ChaCha block
+function is pinned by the RFC 8439 test vector, the rest is "parity
+unpinned" (no test of the reference checks Omega values).  CV masks use the
+counter stream only.  RNG-dependent quantities are compared at the subspace /
+statistical level.
 """
 from __future__ import annotations
 
@@ -245,6 +249,169 @@ def rng_normal_matrix(seed: int, rows: int, cols: int) -> np.ndarray:
     u2 = (rng_u64(seed, 2 * idx + np.uint64(1)) >> np.uint64(11)).astype(np.float64) * (2.0 ** -53)
     z = np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
     return z.reshape(rows, cols)
+
+
+# ---------------------------------------------------------------------------
+# The reference's sketch stream (src/rsvd.rs:44-46, src/nmf.rs:291-293):
+# ChaCha8Rng::seed_from_u64(seed) sampled by rand_distr's Normal(0, 1) into an
+# Array2 in row-major order.  Restated from the published algorithms (the
+# crates, rand_core 0.6.4 / rand_chacha 0.3.1 / rand_distr 0.4.3 per
+# Cargo.lock, are not in the reference tree):
+#   ChaCha block function -- Bernstein 2008 / RFC 8439 s2.3, 64-bit block
+#     counter in words 12-13, 64-bit stream id in words 14-15;
+#   seed_from_u64 -- 8 PCG32 XSH-RR outputs (O'Neill 2014) as the key words;
+#   Normal -- ZIGNOR ziggurat, 256 strips (Doornik 2005).
+# ---------------------------------------------------------------------------
+
+_CHACHA_CONST = (0x61707865, 0x3320646E, 0x79622D32, 0x6B206574)   # "expand 32-byte k"
+_MASK32 = 0xFFFFFFFF
+
+
+def chacha_blocks(state: np.ndarray, rounds: int) -> np.ndarray:
+    """ChaCha block function over B input states at once: ``state`` is
+    (B, 16) uint32, the result (B, 16) uint32 is rounds/2 double rounds
+    (columns, then diagonals) plus the input state (RFC 8439 s2.3)."""
+    x = [state[:, i].astype(np.uint32) for i in range(16)]
+
+    def rotl(v, r):
+        return (v << np.uint32(r)) | (v >> np.uint32(32 - r))
+
+    def qr(a, b, c, d):
+        x[a] = x[a] + x[b]; x[d] = rotl(x[d] ^ x[a], 16)
+        x[c] = x[c] + x[d]; x[b] = rotl(x[b] ^ x[c], 12)
+        x[a] = x[a] + x[b]; x[d] = rotl(x[d] ^ x[a], 8)
+        x[c] = x[c] + x[d]; x[b] = rotl(x[b] ^ x[c], 7)
+
+    with np.errstate(over="ignore"):
+        for _ in range(rounds // 2):
+            qr(0, 4, 8, 12); qr(1, 5, 9, 13); qr(2, 6, 10, 14); qr(3, 7, 11, 15)
+            qr(0, 5, 10, 15); qr(1, 6, 11, 12); qr(2, 7, 8, 13); qr(3, 4, 9, 14)
+        return np.stack(x, axis=1) + state.astype(np.uint32)
+
+
+def pcg32_seed_words(seed: int) -> List[int]:
+    """seed_from_u64: the LCG state is stepped (multiplier
+    6364136223846793005, increment 11634580027462260723) before each of 8
+    XSH-RR outputs, which become the 8 little-endian key words."""
+    s = seed & 0xFFFFFFFFFFFFFFFF
+    words = []
+    for _ in range(8):
+        s = (s * 6364136223846793005 + 11634580027462260723) & 0xFFFFFFFFFFFFFFFF
+        xorshifted = (((s >> 18) ^ s) >> 27) & _MASK32
+        rot = s >> 59
+        words.append(((xorshifted >> rot) | (xorshifted << ((32 - rot) & 31))) & _MASK32)
+    return words
+
+
+def chacha8_u64(seed: int, count: int, start_block: int = 0) -> np.ndarray:
+    """``count`` consecutive 64-bit outputs of ChaCha8Rng::seed_from_u64(seed)
+    from block ``start_block`` on: the keystream's 32-bit words in order, two
+    per output, low word first."""
+    blocks = (2 * count + 15) // 16
+    st = np.zeros((blocks, 16), dtype=np.uint32)
+    st[:, 0:4] = _CHACHA_CONST
+    st[:, 4:12] = pcg32_seed_words(seed)
+    ctr = np.arange(start_block, start_block + blocks, dtype=np.uint64)
+    st[:, 12] = (ctr & np.uint64(_MASK32)).astype(np.uint32)
+    st[:, 13] = (ctr >> np.uint64(32)).astype(np.uint32)
+    words = chacha_blocks(st, 8).reshape(-1).astype(np.uint64)
+    return (words[0::2] | (words[1::2] << np.uint64(32)))[:count]
+
+
+ZIG_R = 3.6541528853610088
+ZIG_V = 0.00492867323399
+
+
+def _gauss_pdf(x: float) -> float:
+    return math.exp(-x * x / 2.0)
+
+
+def ziggurat_tables() -> Tuple[List[float], List[float]]:
+    """Strip edges x_0..x_256 and f(x_i) of the 256-strip ziggurat:
+    x_0 = V / f(R) (the base strip's equivalent width), x_1 = R,
+    x_{i+1} = f^-1(V / x_i + f(x_i)), x_256 = 0 (Doornik 2005)."""
+    x = [0.0] * 257
+    x[0] = ZIG_V / _gauss_pdf(ZIG_R)
+    x[1] = ZIG_R
+    for i in range(2, 256):
+        x[i] = math.sqrt(-2.0 * math.log(ZIG_V / x[i - 1] + _gauss_pdf(x[i - 1])))
+    x[256] = 0.0
+    return x, [_gauss_pdf(v) for v in x]
+
+
+class _U64Stream:
+    def __init__(self, seed: int, hint: int):
+        self.seed, self.pos, self.block = seed, 0, 0
+        self.buf = np.zeros(0, dtype=np.uint64)
+        self._more(max(hint, 8))
+
+    def _more(self, count: int):
+        count = (count + 7) // 8 * 8                     # whole blocks
+        nxt = chacha8_u64(self.seed, count, self.block)
+        self.block += count // 8
+        self.buf = np.concatenate([self.buf[self.pos:], nxt])
+        self.pos = 0
+
+    def next(self) -> int:
+        if self.pos == self.buf.size:
+            self._more(max(1024, self.buf.size // 4))
+        v = int(self.buf[self.pos])
+        self.pos += 1
+        return v
+
+
+def _bits_to_f64(b: int) -> float:
+    return float(np.array([b], dtype=np.uint64).view(np.float64)[0])
+
+
+def chacha8_normal_matrix(seed: int, rows: int, cols: int, stats: Optional[dict] = None) -> np.ndarray:
+    """Array2::from_shape_fn((rows, cols), |_| Normal::new(0, 1).sample(&mut
+    ChaCha8Rng::seed_from_u64(seed))) (src/rsvd.rs:44-46).  Per draw: a u64
+    gives strip i (low 8 bits) and u in [-1, 1) (top 52 bits as the mantissa
+    of [2, 4), minus 3); x = u x_i is accepted if |x| < x_{i+1}; strip 0 falls
+    back to the tail beyond R (two open (0, 1) uniforms per try, top 52 bits
+    in [1, 2) minus 1 - 2^-53, until -2 ln b >= (ln a / R)^2); other strips
+    accept if f_{i+1} + (f_i - f_{i+1}) U < f(x), U = (u64 >> 11) 2^-53.
+    ``stats`` (optional) counts the tail and wedge branches taken."""
+    xt, ft = ziggurat_tables()
+    rng = _U64Stream(seed, rows * cols + rows * cols // 64 + 16)
+    out = np.empty(rows * cols)
+    tails = wedges = 0
+    for e in range(rows * cols):
+        while True:
+            bits = rng.next()
+            i = bits & 0xFF
+            u = _bits_to_f64((1024 << 52) | (bits >> 12)) - 3.0
+            x = u * xt[i]
+            if abs(x) < xt[i + 1]:
+                break
+            if i == 0:
+                tails += 1
+                tx, ty = 1.0, 0.0
+                while -2.0 * ty < tx * tx:
+                    a = _bits_to_f64((1023 << 52) | (rng.next() >> 12)) - (1.0 - 2.0 ** -53)
+                    b = _bits_to_f64((1023 << 52) | (rng.next() >> 12)) - (1.0 - 2.0 ** -53)
+                    tx = math.log(a) / ZIG_R
+                    ty = math.log(b)
+                x = tx - ZIG_R if u < 0.0 else ZIG_R - tx
+                break
+            wedges += 1
+            if ft[i + 1] + (ft[i] - ft[i + 1]) * ((rng.next() >> 11) * 2.0 ** -53) < _gauss_pdf(x):
+                break
+        out[e] = 0.0 + 1.0 * x
+    if stats is not None:
+        stats.update(tails=tails, wedges=wedges)
+    return out.reshape(rows, cols)
+
+
+def sketch_normal(rng: str, seed: int, rows: int, cols: int) -> np.ndarray:
+    """Gaussian sketch from the named stream: "counter" (the engine's
+    default) or "chacha8" (the reference's)."""
+    if rng == "counter":
+        return rng_normal_matrix(seed, rows, cols)
+    if rng == "chacha8":
+        return chacha8_normal_matrix(seed, rows, cols)
+    raise ValueError(f"unknown stream {rng!r}")
 
 
 # ---------------------------------------------------------------------------
@@ -606,12 +773,12 @@ def normalize_w(w: np.ndarray, h: np.ndarray, eps: float) -> None:
                 h[j, :] *= col_norm
 
 
-def nmf_init_from_random_probe(raw_est: np.ndarray, k: int, seed: int):
-    """src/nmf.rs:279-362 with the shared counter RNG: Omega' from seed+1e6,
+def nmf_init_from_random_probe(raw_est: np.ndarray, k: int, seed: int, rng: str = "counter"):
+    """src/nmf.rs:279-362: Omega' from seed+1e6 (``rng`` names the stream),
     Z = Y_meanraw^T Omega', W = |Omega' Vt[:k]^T|, H = max(0, W^+ Y_meanraw)."""
     n, p = raw_est.shape
     l = k + 10
-    omega = rng_normal_matrix(seed + 1_000_000, n, l)
+    omega = sketch_normal(rng, seed + 1_000_000, n, l)
     y = fill_missing_with_column_means(raw_est)
     z = y.T @ omega
     _, _, vt = np.linalg.svd(z, full_matrices=False)
@@ -658,9 +825,9 @@ class NmfResult:
 
 
 def nmf_impute_estimation(raw_est: np.ndarray, k: int, n_iter: int, eps: float, cv_rate: float,
-                          seed: int, chunk: int) -> NmfResult:
+                          seed: int, chunk: int, rng: str = "counter") -> NmfResult:
     """src/nmf.rs:80-249 on a raw (n, p_est) matrix with NaNs."""
-    w, h = nmf_init_from_random_probe(raw_est, k, seed)
+    w, h = nmf_init_from_random_probe(raw_est, k, seed, rng)
     w = np.maximum(w, eps)
     h = np.maximum(h, eps)
     normalize_w(w, h, eps)
@@ -749,22 +916,24 @@ def fit_oracle64(raw_est: np.ndarray, raw_full: np.ndarray, x: np.ndarray, *, k:
                  lam: float = 1e-5, oversampling: int = 10, power_iter: int = 2,
                  seed: int = 42, norm: int = NORM_EIGENSTRAT, scale_cov: bool = False,
                  omega: Optional[np.ndarray] = None, nmf: Optional[dict] = None,
-                 chunk: int = 10_000) -> FitResult:
+                 chunk: int = 10_000, rng: str = "counter") -> FitResult:
     """fit_lfmm2 (src/lib.rs:162-263) in the thin FP64 formulation.
 
     ``raw_est``/``raw_full`` are raw (n, p) matrices with NaN for missing.
-    ``nmf`` = dict(k=, n_iter=, eps=, cv_rate=) switches on NMF imputation."""
+    ``nmf`` = dict(k=, n_iter=, eps=, cv_rate=) switches on NMF imputation.
+    ``rng`` ("counter" or "chacha8") names the stream of the Gaussian
+    sketches that are not given (Omega, the NMF probe)."""
     xs = center_covariates(x, scale_cov)
     n, d = xs.shape
     pre = precompute_thin(xs, lam)
     l = k + oversampling
     if omega is None:
-        omega = rng_normal_matrix(seed, n, l)
+        omega = sketch_normal(rng, seed, n, l)
     nmf_res = None
     gwas_cv = None
     if nmf is not None:
         nmf_res = nmf_impute_estimation(raw_est, nmf["k"], nmf["n_iter"], nmf.get("eps", 1e-16),
-                                        nmf["cv_rate"], seed, chunk)
+                                        nmf["cv_rate"], seed, chunk, rng)
         w = nmf_res.w
         inv_wtw, _ = safe_inv(w.T @ w, "W^T W for NMF pinv")
         w_pinv = inv_wtw @ w.T

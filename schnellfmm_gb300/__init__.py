@@ -71,11 +71,20 @@ class Precision(enum.IntEnum):
     SPLIT_FP8 = 2
 
 
+class SketchRng(enum.IntEnum):
+    """Stream the Gaussian sketches (src/rsvd.rs:44-46, src/nmf.rs:291-293)
+    are drawn from: the device counter stream, or the reference's
+    ChaCha8Rng::seed_from_u64 + Normal(0, 1) stream drawn on the host."""
+    COUNTER = 0
+    CHACHA8 = 1
+
+
 # ---------------------------------------------------------------------------
 # ctypes declarations (must match include/schnelgpu.h)
 # ---------------------------------------------------------------------------
 class _Opts(C.Structure):
-    _fields_ = [("precision", C.c_int), ("verbose", C.c_int), ("stream", C.c_void_p), ("autotune", C.c_int)]
+    _fields_ = [("precision", C.c_int), ("verbose", C.c_int), ("stream", C.c_void_p), ("autotune", C.c_int),
+                ("rng", C.c_int)]
 
 
 class _Subset(C.Structure):
@@ -112,7 +121,7 @@ EXPORTED_SYMBOLS = (
     "slfmm_generate_omega", "slfmm_estimate_factors", "slfmm_test_associations", "slfmm_fit",
     "slfmm_fit_host", "slfmm_write_tsv", "slfmm_format_exp6", "slfmm_simulate", "slfmm_geno_download",
     "slfmm_profile_enable", "slfmm_profile_read", "slfmm_host_alloc", "slfmm_host_free", "slfmm_contract_raw",
-    "slfmm_gif_noalloc", "slfmm_fit_traits", "slfmm_fit_many",
+    "slfmm_gif_noalloc", "slfmm_fit_traits", "slfmm_fit_many", "slfmm_reference_normal",
 )
 
 _lib_handle = None
@@ -162,6 +171,7 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
         "slfmm_gif_noalloc": (i32, [vp, vp, u64, u32, vp]),
         "slfmm_fit_traits": (i32, [vp, vp, vp, vp, u32, C.POINTER(_Config), C.POINTER(_Results)]),
         "slfmm_fit_many": (i32, [vp, C.POINTER(_Problem), u32, u32, C.POINTER(C.c_int)]),
+        "slfmm_reference_normal": (i32, [u64, u64, u32, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -170,6 +180,19 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
     if path is None:
         _lib_handle = lib
     return lib
+
+
+def reference_normal(seed: int, rows: int, cols: int) -> np.ndarray:
+    """rows x cols Normal(0, 1) draws from ChaCha8Rng::seed_from_u64(seed) in
+    row-major order, the reference's sketch Omega (src/rsvd.rs:44-46; the NMF
+    probe uses seed + 1 000 000, src/nmf.rs:291-293).  Host only: needs the
+    built library, not a GPU.  Pass it as ``omega=`` or create the engine
+    with ``rng=SketchRng.CHACHA8`` to draw every sketch this way."""
+    out = np.empty((rows, cols))
+    rc = load_library().slfmm_reference_normal(seed & 0xFFFFFFFFFFFFFFFF, rows, cols, _ptr(out))
+    if rc != OK:
+        raise SchnelGpuError(rc, f"slfmm_reference_normal failed ({rc})")
+    return out
 
 
 class PinnedArray:
@@ -309,9 +332,10 @@ class Engine:
     """One CUDA context + stream on one device (replaces the worker pool)."""
 
     def __init__(self, device: int = 0, precision: Precision = Precision.SPLIT_FP8, stream: Optional[int] = None,
-                 verbose: bool = False, autotune: bool = False):
+                 verbose: bool = False, autotune: bool = False, rng: SketchRng = SketchRng.COUNTER):
         self.lib = load_library()
-        opts = _Opts(int(precision), int(verbose), C.c_void_p(stream) if stream else None, int(autotune))
+        opts = _Opts(int(precision), int(verbose), C.c_void_p(stream) if stream else None, int(autotune),
+                     int(rng))
         h = C.c_void_p()
         rc = self.lib.slfmm_create(device, C.byref(opts), C.byref(h))
         if rc != OK:

@@ -20,6 +20,9 @@ LIB = HERE / "libschnelgpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
           "-I", str(HERE.parent / "include")]
+# the host sketch stream must round like the reference's (no fused multiply-add
+# contraction, which GCC does by default for C++ on aarch64)
+PER_FILE = {"host_rng.cpp": ["-Xcompiler", "-ffp-contract=off"]}
 
 
 def nvcc() -> str:
@@ -35,7 +38,7 @@ def sources():
 
 def _compile(src: Path, verbose: bool) -> Path:
     obj = BUILD / (src.stem + ".o")
-    cmd = [nvcc(), *ARCH, *COMMON, "-c", str(src), "-o", str(obj)]
+    cmd = [nvcc(), *ARCH, *COMMON, *PER_FILE.get(src.name, []), "-c", str(src), "-o", str(obj)]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
     r = subprocess.run(cmd, capture_output=True, text=True)

@@ -752,7 +752,7 @@ void sketch_operand(Ctx& c, const Step0& s0, uint64_t n, int l, uint64_t seed, c
                     DBuf<double>& W) {
     W.alloc(n * l, c.stream);
     if (omega_host) h2d(c, W.get(), omega_host, n * l);
-    else launch_normal(c, seed, n, l, W.get());
+    else draw_normal(c, seed, n, l, W.get());
     apply_p(c, s0, W.get(), l, l, false);                    // M^T Omega analogue (:51)
     center_columns(c, W.get(), n, l, l);
 }
@@ -1071,7 +1071,7 @@ void nmf_estimate(Ctx& c, const Geno& g, const slfmm_config* cfg, NmfModel& m) {
     // init_from_random_probe (src/nmf.rs:279-362): Z = Y_meanraw^T Omega',
     // W = |Omega' V_k| with V the right singular vectors of Z, H = max(0, W^+ Y)
     DBuf<double> Om(n * l, c.stream);
-    launch_normal(c, cfg->seed + 1000000ull, n, l, Om.get());
+    draw_normal(c, cfg->seed + 1000000ull, n, l, Om.get());
     DBuf<float> Z;
     int zp = 0;
     row_contract(c, g, rawm, Om.get(), l, l, Z, zp);
@@ -1370,6 +1370,7 @@ void ctx_close(Ctx& c) {
 int slfmm_create(int device, const slfmm_opts* opts, slfmm_ctx** out) {
     if (!out) return SLFMM_ERR_BAD_ARG;
     *out = nullptr;
+    if (opts && opts->rng != SLFMM_RNG_COUNTER && opts->rng != SLFMM_RNG_CHACHA8) return SLFMM_ERR_BAD_ARG;
     slfmm_ctx* c = new (std::nothrow) slfmm_ctx();
     if (!c) return SLFMM_ERR_NOMEM;
     try {
@@ -1377,6 +1378,7 @@ int slfmm_create(int device, const slfmm_opts* opts, slfmm_ctx** out) {
                  opts ? (cudaStream_t)opts->stream : nullptr);
         const char* at = std::getenv("SLFMM_AUTOTUNE");
         c->autotune = (opts && opts->autotune) || (at && at[0] == '1');
+        c->rng = opts ? opts->rng : SLFMM_RNG_COUNTER;
     } catch (const slfmm::Error& e) {
         fprintf(stderr, "schnelgpu: %s\n", e.what());
         const int code = e.code;
@@ -1503,7 +1505,7 @@ int slfmm_generate_omega(slfmm_ctx* c, uint64_t seed, uint64_t n, uint32_t l, do
     API_TRY
     SLFMM_CUDA(cudaSetDevice(c->device));
     DBuf<double> o(std::max<uint64_t>(n * l, 1), c->stream);
-    launch_normal(*c, seed, n, (int)l, o.get());
+    draw_normal(*c, seed, n, (int)l, o.get());
     d2h(*c, out, o.get(), n * l);
     sync(*c);
     API_CATCH(c)
@@ -1696,6 +1698,7 @@ int slfmm_fit_many(slfmm_ctx* c, const slfmm_problem* problems, uint32_t n_probl
         try {
             ctx_open(w, c->device, c->precision, 0, nullptr);
             w.autotune = c->autotune;
+            w.rng = c->rng;
         } catch (const Error& e) {
             for (uint32_t i = next.fetch_add(1); i < n_problems; i = next.fetch_add(1)) {
                 st[i] = e.code;

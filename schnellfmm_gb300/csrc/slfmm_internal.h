@@ -158,6 +158,7 @@ struct Ctx {
     bool profiling = false;
     std::map<std::string, ProfRec> prof;
     double phase_t0 = 0.0;  // verbose phase log: start of the current phase (ms)
+    int rng = SLFMM_RNG_COUNTER;  // stream of the Gaussian sketches
     bool autotune = false;   // time the tensor-core ring depths per shape once
     std::map<std::string, std::pair<int, int>> tuned;  // shape -> (packed ring cap, W ring cap)
 };
@@ -367,6 +368,11 @@ void launch_inverse(Ctx& c, const double* A, int a, double* Ainv, int* status, d
 // (descending) written
 void launch_jacobi_svd(Ctx& c, const double* A, int a, double* V, double* sig);
 void launch_normal(Ctx& c, uint64_t seed, uint64_t rows, int cols, double* out);
+// rows x cols Normal(0, 1) sketch into device memory from the context's
+// stream: the device counter stream (launch_normal) or the reference's ChaCha8
+// stream drawn on the host (reference_normal) and copied
+void draw_normal(Ctx& c, uint64_t seed, uint64_t rows, int cols, double* out);
+void reference_normal(uint64_t seed, uint64_t rows, uint64_t cols, double* out);
 void launch_f64_to_f32_pad(Ctx& c, const double* A, uint64_t m, int a, int lda, float* out,
                            uint64_t m_pad, int ldo);
 void launch_f32_to_f64(Ctx& c, const float* A, uint64_t m, int a, int lda, double* out, int ldo);

@@ -1,7 +1,8 @@
 """The C-ABI library on a machine without a GPU: it builds, loads, exports
 every entry point the header declares, its host-only entry points (number
-formatting, TSV writer, .bed validation) match the oracle, and every call that
-needs the device fails loudly instead of falling back to the CPU."""
+formatting, TSV writer, .bed validation, the reference's sketch stream) match
+the oracle, and every call that needs the device fails loudly instead of
+falling back to the CPU."""
 import ctypes as C
 import re
 from pathlib import Path
@@ -89,6 +90,35 @@ def test_bed_validate(lib, tmp_path):
     assert lib.slfmm_bed_validate(str(short).encode(), n, p, None, err, 256) == -2
     missing = tmp_path / "nope.bed"
     assert lib.slfmm_bed_validate(str(missing).encode(), n, p, None, err, 256) in (-2, -7)
+
+
+@pytest.mark.parametrize("seed,rows,cols", [(42, 2000, 30), (1_000_042, 300, 14), (0, 7, 3),
+                                             (2**64 - 1, 1, 1), (9, 5, 0)])
+def test_reference_normal_matches_oracle(lib, seed, rows, cols):
+    """slfmm_reference_normal (ChaCha8Rng::seed_from_u64 + Normal(0, 1), the
+    SLFMM_RNG_CHACHA8 stream) equals the oracle's restatement bit for bit;
+    the (2000, 30) case takes the tail and wedge branches."""
+    import schnellfmm_gb300 as sg
+    stats = {}
+    ref = O.chacha8_normal_matrix(seed, rows, cols, stats)
+    got = sg.reference_normal(seed, rows, cols)
+    assert got.shape == (rows, cols)
+    np.testing.assert_array_equal(got, ref)
+    if rows * cols >= 60_000:
+        assert stats["tails"] > 0 and stats["wedges"] > 0
+
+
+def test_reference_normal_bad_args(lib):
+    assert lib.slfmm_reference_normal(1, 4, 4, None) == -1
+    assert lib.slfmm_reference_normal(1, 0, 4, None) == 0
+    assert lib.slfmm_reference_normal(1, 2**63, 4, C.c_void_p(8)) == -1   # rows x cols overflows
+
+
+def test_create_rejects_unknown_rng(lib):
+    import schnellfmm_gb300 as sg
+    opts = sg._Opts(int(sg.Precision.SPLIT_FP8), 0, None, 0, 7)
+    h = C.c_void_p()
+    assert lib.slfmm_create(0, C.byref(opts), C.byref(h)) == -1 and not h.value
 
 
 def test_no_gpu_fails_loudly(lib):

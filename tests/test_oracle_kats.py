@@ -162,3 +162,60 @@ def test_rng_stream_definition():
     z = O.rng_normal_matrix(42, 2000, 5)
     assert abs(z.mean()) < 0.05 and abs(z.std() - 1) < 0.05
     np.testing.assert_array_equal(z, O.rng_normal_matrix(42, 2000, 5))
+
+
+# RFC 8439 s2.3.2: ChaCha20 block function, key 00 01 .. 1f, nonce
+# 00 00 00 09 00 00 00 4a 00 00 00 00, block count 1 -> output state words.
+RFC8439_BLOCK_OUT = [0xE4E7F110, 0x15593BD1, 0x1FDD0F50, 0xC47120A3, 0xC7F4D1C7, 0x0368C033, 0x9AAA2204,
+                     0x4E6CD4C3, 0x466482D2, 0x09AA9F07, 0x05D7C214, 0xA2028BD9, 0xD19C12B5, 0xB94E16DE,
+                     0xE883D0CB, 0x4E3C50A2]
+
+
+def test_chacha_block_rfc8439():
+    st = np.zeros((2, 16), dtype=np.uint32)
+    st[:, :4] = O._CHACHA_CONST
+    st[:, 4:12] = np.frombuffer(bytes(range(32)), dtype="<u4")
+    st[:, 12] = [1, 2]
+    st[:, 13], st[:, 14] = 0x09000000, 0x4A000000
+    out = O.chacha_blocks(st, 20)
+    assert out[0].tolist() == RFC8439_BLOCK_OUT
+    assert out[1].tolist() != RFC8439_BLOCK_OUT
+
+
+def test_chacha8_stream_layout():
+    """Consecutive 64-bit outputs, blocks in counter order: any split of the
+    stream at a block boundary concatenates back; the key depends on the seed."""
+    a = O.chacha8_u64(42, 40)
+    np.testing.assert_array_equal(a, np.concatenate([O.chacha8_u64(42, 16, 0), O.chacha8_u64(42, 24, 2)]))
+    assert O.pcg32_seed_words(42) != O.pcg32_seed_words(43)
+    assert not np.array_equal(a, O.chacha8_u64(43, 40))
+    assert len(set(O.pcg32_seed_words(0))) == 8       # seed 0 still gives a full key
+
+
+def test_ziggurat_tables_consistent():
+    """(R, V) of the 256-strip ziggurat: V is the base strip's area
+    R f(R) + int_R^inf f, and the recursion closes at the top strip
+    (V / x_255 + f(x_255) = f(0) = 1)."""
+    from scipy.special import erfc
+    x, f = O.ziggurat_tables()
+    r = O.ZIG_R
+    tail = math.sqrt(math.pi / 2.0) * erfc(r / math.sqrt(2.0))
+    assert r * math.exp(-r * r / 2.0) + tail == pytest.approx(O.ZIG_V, rel=1e-11)
+    assert O.ZIG_V / x[255] + f[255] == pytest.approx(1.0, abs=1e-9)
+    assert all(x[i] > x[i + 1] for i in range(256)) and x[256] == 0.0 and f[256] == 1.0
+    for i in range(1, 255):                           # every strip has area V
+        assert x[i] * (f[i + 1] - f[i]) == pytest.approx(O.ZIG_V, rel=1e-9)
+
+
+def test_chacha8_normal_matrix():
+    stats = {}
+    z = O.chacha8_normal_matrix(42, 4000, 25, stats)
+    assert abs(z.mean()) < 0.02 and abs(z.std() - 1.0) < 0.02
+    assert stats["tails"] > 0 and stats["wedges"] > 0   # both fall-back branches taken
+    assert np.abs(z).max() > O.ZIG_R                    # tail draws beyond R
+    # row-major draw order: fewer rows is a prefix of the same stream
+    np.testing.assert_array_equal(O.chacha8_normal_matrix(42, 7, 25), z[:7])
+    np.testing.assert_array_equal(O.chacha8_normal_matrix(42, 4000, 25), z)
+    assert not np.array_equal(O.chacha8_normal_matrix(43, 7, 25), z[:7])
+    np.testing.assert_array_equal(O.sketch_normal("chacha8", 5, 3, 4), O.chacha8_normal_matrix(5, 3, 4))
+    np.testing.assert_array_equal(O.sketch_normal("counter", 5, 3, 4), O.rng_normal_matrix(5, 3, 4))
