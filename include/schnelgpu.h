@@ -54,12 +54,16 @@ extern "C" {
 #define SLFMM_IMPUTE_NMF       1      /* ImputeStrategy::Nmf                     */
 
 /* Stream the Gaussian sketches (Omega of src/rsvd.rs:44-46, the NMF probe of
- * src/nmf.rs:291-293) are drawn from. */
-#define SLFMM_RNG_COUNTER      0      /* SplitMix64 counter stream, drawn on the
+ * src/nmf.rs:291-293) and the NMF CV hold-out masks (src/nmf.rs:433-448,
+ * src/testing.rs:437-452) are drawn from. */
+#define SLFMM_RNG_COUNTER      0      /* SplitMix64 counter streams, drawn on the
                                          device (default)                        */
-#define SLFMM_RNG_CHACHA8      1      /* ChaCha8Rng::seed_from_u64(seed) sampled
-                                         by Normal(0, 1) in row-major order, the
-                                         reference's stream, drawn on the host   */
+#define SLFMM_RNG_CHACHA8      1      /* the reference's streams:
+                                         ChaCha8Rng::seed_from_u64(seed) sampled
+                                         by Normal(0, 1) in row-major order for
+                                         the sketches (on the host) and by
+                                         Uniform(0, 1) for the masks (on the
+                                         device)                                 */
 
 #define SLFMM_SUBSET_ALL       0      /* SubsetSpec::All     (src/bed.rs:50-57)  */
 #define SLFMM_SUBSET_RATE      1      /* SubsetSpec::Rate(r)                     */

@@ -21,13 +21,13 @@ Parity status: the decode, counting, mean/scale, subset, histogram/median,
 GIF and covariate-centring rules are pinned by the reference's own unit-test
 known answers (``tests/golden/reference_kats.json`` and the CPU tests).  The
 engine's default random streams are a counter-based SplitMix64 generator
-shared by this oracle and the GPU.  The reference's sketch stream
-(ChaCha8Rng::seed_from_u64 + Normal(0, 1)) is restated in
-``chacha8_normal_matrix`` from the published algorithms; its ChaCha block
-function is pinned by the RFC 8439 test vector, the rest is "parity
-unpinned" (no test of the reference checks Omega values).  CV masks use the
-counter stream only.  RNG-dependent quantities are compared at the subspace /
-statistical level.
+shared by this oracle and the GPU.  The reference's streams
+(ChaCha8Rng::seed_from_u64 sampled by Normal(0, 1) for the sketches and by
+Uniform(0, 1) for the CV masks) are restated in ``chacha8_normal_matrix`` and
+``mask_uniform`` from the published algorithms; the ChaCha block function is
+pinned by the RFC 8439 test vector, the rest is "parity unpinned" (no test of
+the reference checks Omega or mask values).  RNG-dependent quantities are
+compared at the subspace / statistical level.
 """
 from __future__ import annotations
 
@@ -789,8 +789,25 @@ def nmf_init_from_random_probe(raw_est: np.ndarray, k: int, seed: int, rng: str 
     return w, h
 
 
+def mask_uniform(rng: str, seed: int, ctr: np.ndarray) -> np.ndarray:
+    """Hold-out uniforms: draw ``ctr`` of the stream keyed by ``seed``.
+    "counter": (u64 >> 11) 2^-53 of the SplitMix64 counter stream;
+    "chacha8": rand_distr's Uniform(0, 1) on ChaCha8Rng::seed_from_u64(seed),
+    (u64 >> 12) 2^-52 of output ``ctr`` (src/nmf.rs:433-434,
+    src/testing.rs:437-438)."""
+    ctr = np.asarray(ctr, dtype=np.uint64)
+    if rng == "counter":
+        return rng_uniform(seed, ctr)
+    if rng != "chacha8":
+        raise ValueError(f"unknown stream {rng!r}")
+    if ctr.size == 0:
+        return np.zeros(ctr.shape)
+    draws = chacha8_u64(seed, int(ctr.max()) + 1)
+    return (draws[ctr] >> np.uint64(12)).astype(np.float64) * (2.0 ** -52)
+
+
 def nmf_cv_error_masked(raw_est: np.ndarray, w: np.ndarray, h: np.ndarray, mask_seed: int,
-                        cv_rate: float, chunk: int) -> Tuple[float, float, int]:
+                        cv_rate: float, chunk: int, rng: str = "counter") -> Tuple[float, float, int]:
     """src/nmf.rs:379-455: per chunk, one uniform per (col,row) in
     column-major order (missing included) from stream mask_seed+chunk_seq;
     masked iff u < cv_rate and observed."""
@@ -805,7 +822,7 @@ def nmf_cv_error_masked(raw_est: np.ndarray, w: np.ndarray, h: np.ndarray, mask_
         col_mean = np.where(n_obs > 0, np.where(obs, y, 0.0).sum(axis=0) / np.maximum(n_obs, 1), 0.0)
         recon = w @ h[:, s:e]
         ctr = np.arange((e - s) * n, dtype=np.uint64).reshape(e - s, n).T   # counter = col*n + row
-        u = rng_uniform(mask_seed + seq, ctr)
+        u = mask_uniform(rng, mask_seed + seq, ctr)
         m = (u < cv_rate) & obs
         nmf_err += float(np.abs(y[m] - recon[m]).sum())
         mean_err += float(np.abs(y[m] - np.broadcast_to(col_mean, y.shape)[m]).sum())
@@ -852,7 +869,7 @@ def nmf_impute_estimation(raw_est: np.ndarray, k: int, n_iter: int, eps: float, 
         h = np.where(upd, h * np.divide(num_h, denom_h, out=np.ones_like(denom_h), where=upd), h)
         h = np.maximum(h, eps)
         normalize_w(w, h, eps)
-        mae, mmae, c = nmf_cv_error_masked(raw_est, w, h, seed + it, cv_rate, chunk)
+        mae, mmae, c = nmf_cv_error_masked(raw_est, w, h, seed + it, cv_rate, chunk, rng)
         cv.append(mae)
         mean_mae = mmae
         total += c
@@ -868,7 +885,7 @@ def nmf_onthefly_fill(raw: np.ndarray, w: np.ndarray, w_pinv: np.ndarray) -> np.
 
 
 def nmf_gwas_cv(raw: np.ndarray, w: np.ndarray, w_pinv: np.ndarray, cv_rate: float, seed: int,
-                chunk: int) -> Tuple[float, float, int]:
+                chunk: int, rng: str = "counter") -> Tuple[float, float, int]:
     """GWAS-phase CV (src/testing.rs:423-487): per block, one draw per
     OBSERVED entry in column-major order from stream seed+seq (the k-th
     observed entry uses counter k); leave-out mean fill; H = max(0, W^+ Y);
@@ -882,7 +899,8 @@ def nmf_gwas_cv(raw: np.ndarray, w: np.ndarray, w_pinv: np.ndarray, cv_rate: flo
         obs = ~np.isnan(y)
         obs_cm = obs.T.reshape(-1)                     # column-major order
         rank = np.cumsum(obs_cm) - 1
-        u = rng_uniform(seed + seq, rank.astype(np.uint64))
+        u = np.ones(obs_cm.shape)
+        u[obs_cm] = mask_uniform(rng, seed + seq, rank[obs_cm].astype(np.uint64))
         m_cm = obs_cm & (u < cv_rate)
         mask = m_cm.reshape(e - s, n).T
         if not mask.any():
@@ -922,7 +940,8 @@ def fit_oracle64(raw_est: np.ndarray, raw_full: np.ndarray, x: np.ndarray, *, k:
     ``raw_est``/``raw_full`` are raw (n, p) matrices with NaN for missing.
     ``nmf`` = dict(k=, n_iter=, eps=, cv_rate=) switches on NMF imputation.
     ``rng`` ("counter" or "chacha8") names the stream of the Gaussian
-    sketches that are not given (Omega, the NMF probe)."""
+    sketches that are not given (Omega, the NMF probe) and of the CV
+    hold-out masks."""
     xs = center_covariates(x, scale_cov)
     n, d = xs.shape
     pre = precompute_thin(xs, lam)
@@ -941,7 +960,7 @@ def fit_oracle64(raw_est: np.ndarray, raw_full: np.ndarray, x: np.ndarray, *, k:
         y_est, _, _ = decode_standardized(raw_est, norm, fill_est)
         fill_full = nmf_onthefly_fill(raw_full, w, w_pinv)           # NmfOnTheFly
         y_full, _, _ = decode_standardized(raw_full, norm, fill_full)
-        gwas_cv = nmf_gwas_cv(raw_full, w, w_pinv, nmf["cv_rate"], seed, chunk)
+        gwas_cv = nmf_gwas_cv(raw_full, w, w_pinv, nmf["cv_rate"], seed, chunk, rng)
     else:
         y_est, _, _ = decode_standardized(raw_est, norm)
         y_full, _, _ = decode_standardized(raw_full, norm)

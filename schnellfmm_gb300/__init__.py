@@ -72,9 +72,11 @@ class Precision(enum.IntEnum):
 
 
 class SketchRng(enum.IntEnum):
-    """Stream the Gaussian sketches (src/rsvd.rs:44-46, src/nmf.rs:291-293)
-    are drawn from: the device counter stream, or the reference's
-    ChaCha8Rng::seed_from_u64 + Normal(0, 1) stream drawn on the host."""
+    """Streams of the Gaussian sketches (src/rsvd.rs:44-46,
+    src/nmf.rs:291-293) and the NMF CV hold-out masks (src/nmf.rs:433-448,
+    src/testing.rs:437-452): the device counter streams, or the reference's
+    ChaCha8Rng::seed_from_u64 streams (Normal(0, 1) sketches drawn on the
+    host, Uniform(0, 1) masks drawn on the device)."""
     COUNTER = 0
     CHACHA8 = 1
 

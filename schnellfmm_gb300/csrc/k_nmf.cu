@@ -31,6 +31,69 @@ __device__ __forceinline__ bool draw_below(uint64_t key, uint64_t ctr, uint64_t 
     return (mix64(key + (ctr + 1) * kGamma) >> 11) < thresh;
 }
 
+// The reference's mask stream (src/nmf.rs:433-434, src/testing.rs:437-438):
+// ChaCha8Rng::seed_from_u64(seed) sampled by Uniform(0, 1).  Output `ctr` is
+// keystream words 2 ctr and 2 ctr + 1 (block ctr / 8: 64-bit block counter in
+// state words 12-13, stream id 0), the key 8 PCG32 XSH-RR outputs of the seed
+// (the same stream host_rng.cpp draws for the sketches), and the uniform
+// (u64 >> 12) 2^-52, below `rate` iff (u64 >> 12) < ceil(rate 2^52).  The
+// last block stays in registers, so consecutive counters reuse it.
+__device__ __forceinline__ void chacha_quarter(uint32_t& a, uint32_t& b, uint32_t& c, uint32_t& d) {
+    a += b; d ^= a; d = __funnelshift_l(d, d, 16);
+    c += d; b ^= c; b = __funnelshift_l(b, b, 12);
+    a += b; d ^= a; d = __funnelshift_l(d, d, 8);
+    c += d; b ^= c; b = __funnelshift_l(b, b, 7);
+}
+
+struct ChaCha8Draws {
+    uint32_t key[8];
+    uint32_t x[16];
+    uint64_t blk;
+    __device__ explicit ChaCha8Draws(uint64_t seed) : blk(~0ull) {
+        uint64_t s = seed;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) {
+            s = s * 6364136223846793005ull + 11634580027462260723ull;
+            const uint32_t xs = (uint32_t)(((s >> 18) ^ s) >> 27);
+            key[j] = __funnelshift_r(xs, xs, (uint32_t)(s >> 59));
+        }
+    }
+    __device__ void refill() {
+        const uint32_t in[16] = {0x61707865u, 0x3320646eu, 0x79622d32u, 0x6b206574u, key[0], key[1], key[2], key[3],
+                                 key[4], key[5], key[6], key[7], (uint32_t)blk, (uint32_t)(blk >> 32), 0u, 0u};
+#pragma unroll
+        for (int i = 0; i < 16; ++i) x[i] = in[i];
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            chacha_quarter(x[0], x[4], x[8], x[12]);
+            chacha_quarter(x[1], x[5], x[9], x[13]);
+            chacha_quarter(x[2], x[6], x[10], x[14]);
+            chacha_quarter(x[3], x[7], x[11], x[15]);
+            chacha_quarter(x[0], x[5], x[10], x[15]);
+            chacha_quarter(x[1], x[6], x[11], x[12]);
+            chacha_quarter(x[2], x[7], x[8], x[13]);
+            chacha_quarter(x[3], x[4], x[9], x[14]);
+        }
+#pragma unroll
+        for (int i = 0; i < 16; ++i) x[i] += in[i];
+    }
+    __device__ uint64_t at(uint64_t ctr) {
+        if ((ctr >> 3) != blk) {
+            blk = ctr >> 3;
+            refill();
+        }
+        const int j = (int)(ctr & 7);
+        uint32_t lo = x[0], hi = x[1];
+#pragma unroll
+        for (int w = 1; w < 8; ++w)
+            if (w == j) {
+                lo = x[2 * w];
+                hi = x[2 * w + 1];
+            }
+        return (uint64_t)lo | ((uint64_t)hi << 32);
+    }
+};
+
 __device__ __forceinline__ uint32_t code_at(const uint8_t* row, uint64_t s) {
     return (row[s >> 2] >> ((s & 3) * 2)) & 3u;
 }
@@ -320,10 +383,12 @@ __global__ void k_nmf_sign(const TS* __restrict__ src, int ldsrc, double* __rest
 }
 
 // Estimation-phase CV (compute_cv_error_masked, src/nmf.rs:379-455).  Chunk
-// `seq` of `chunk` SNPs uses the stream of mask_seed + seq; entry (i, r) draws
-// counter (r - chunk start) n + i (column-major, missing calls included) and
-// is held out iff the draw is below `rate` and the call is observed.  Per SNP:
+// `seq` of `chunk` SNPs uses the stream of mask_seed + seq (the counter
+// stream, or ChaCha8 with kChaCha); entry (i, r) draws counter
+// (r - chunk start) n + i (column-major, missing calls included) and is held
+// out iff the draw is below `rate` and the call is observed.  Per SNP:
 // sum |g - W_i.H_r|, sum |g - mean_r|, count.
+template <bool kChaCha>
 __global__ void __launch_bounds__(256) k_nmf_cv(const uint8_t* __restrict__ packed, uint64_t stride, uint64_t n,
                                                 uint64_t p, uint64_t chunk, uint64_t mask_seed, uint64_t thresh,
                                                 const float* __restrict__ W, const float* __restrict__ H, int k,
@@ -337,6 +402,7 @@ __global__ void __launch_bounds__(256) k_nmf_cv(const uint8_t* __restrict__ pack
         __syncwarp();
         const uint64_t seq = r / chunk, col = r - seq * chunk;
         const uint64_t key = mix64(mask_seed + seq + kGamma);
+        ChaCha8Draws cc(mask_seed + seq);
         const int64_t c0 = counts[r * 4], c1 = counts[r * 4 + 1], c2 = counts[r * 4 + 2];
         const int64_t nobs = c0 + c1 + c2;
         const double cm = nobs > 0 ? (double)(c1 + 2 * c2) / (double)nobs : 0.0;
@@ -352,7 +418,12 @@ __global__ void __launch_bounds__(256) k_nmf_cv(const uint8_t* __restrict__ pack
             const int nb = n - i0 < 16 ? (int)(n - i0) : 16;
             for (int b = 0; b < nb; ++b, z += kGamma) {
                 const uint32_t code = (v >> (2 * b)) & 3u;
-                if (code == 1u || (mix64(z) >> 11) >= thresh) continue;
+                if (code == 1u) continue;
+                if constexpr (kChaCha) {
+                    if ((cc.at(col * n + i0 + b) >> 12) >= thresh) continue;
+                } else {
+                    if ((mix64(z) >> 11) >= thresh) continue;
+                }
                 const uint64_t i = i0 + b;
                 const double g = code == 0 ? 0.0 : (double)(code - 1);
                 e1 += fabs(g - (double)fill_dot(W + i * k, hs[wl], k));
@@ -392,7 +463,9 @@ __global__ void k_obs_base(const int32_t* __restrict__ counts, uint64_t p, uint6
 // its leave-out mean mu', H = max(0, W+ y~) and the MAE of W_i.H and of mu'
 // over the held-out calls accumulate.  W+ y~ = A + mu' B with A = sum over
 // kept observed calls of W+_i g, B = sum over missing and held-out calls of
-// W+_i.  One warp per SNP, two passes over its codes.
+// W+_i.  One warp per SNP, two passes over its codes.  kChaCha draws from the
+// reference's ChaCha8 stream instead of the counter stream.
+template <bool kChaCha>
 __global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__ packed, uint64_t stride, uint64_t n,
                                                      uint64_t p, uint64_t chunk, uint64_t seed, uint64_t thresh,
                                                      const float* __restrict__ W, const float* __restrict__ Wpt, int k,
@@ -404,6 +477,7 @@ __global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__
     for (uint64_t r = (uint64_t)blockIdx.x * 8 + wl; r < p; r += nw) {
         const uint64_t seq = r / chunk;
         const uint64_t key = mix64(seed + seq + kGamma);
+        ChaCha8Draws cc(seed + seq);
         const uint8_t* row = packed + r * stride;
         float A[kMaxNmfK], B[kMaxNmfK];
 #pragma unroll
@@ -417,7 +491,11 @@ __global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__
             const bool obs = i < n && code != 1u;
             const unsigned bal = __ballot_sync(0xffffffffu, obs);
             bool held = false;
-            if (obs) held = draw_below(key, before + __popc(bal & lt), thresh);
+            if (obs) {
+                const uint64_t ctr = before + __popc(bal & lt);
+                if constexpr (kChaCha) held = (cc.at(ctr) >> 12) < thresh;
+                else held = draw_below(key, ctr, thresh);
+            }
             before += __popc(bal);
             if (i < n) {
                 const float* wp = Wpt + i * k;
@@ -459,7 +537,13 @@ __global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__
             const uint32_t code = i < n ? code_at(row, i) : 1u;
             const bool obs = i < n && code != 1u;
             const unsigned bal = __ballot_sync(0xffffffffu, obs);
-            if (obs && draw_below(key, before + __popc(bal & lt), thresh)) {
+            bool held = false;
+            if (obs) {
+                const uint64_t ctr = before + __popc(bal & lt);
+                if constexpr (kChaCha) held = (cc.at(ctr) >> 12) < thresh;
+                else held = draw_below(key, ctr, thresh);
+            }
+            if (held) {
                 const double g = code == 0 ? 0.0 : (double)(code - 1);
                 e1 += fabs(g - (double)fill_dot(W + i * k, hh[wl], k));
                 e2 += fabs(g - mu);
@@ -479,11 +563,12 @@ __global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__
 
 }  // namespace
 
-// ceil(rate 2^53), the integer threshold of draw_below
-static uint64_t rate_threshold(double rate) {
+// ceil(rate 2^bits): u < rate for u = m 2^-bits iff m < this (bits = 53 for
+// the counter stream's uniforms, 52 for the ChaCha8 stream's)
+static uint64_t rate_threshold(double rate, int bits = 53) {
     if (!(rate > 0.0)) return 0;
-    if (rate >= 1.0) return 1ull << 53;
-    return (uint64_t)std::ceil(std::ldexp(rate, 53));
+    if (rate >= 1.0) return 1ull << bits;
+    return (uint64_t)std::ceil(std::ldexp(rate, bits));
 }
 
 void launch_fill_stats(Ctx& c, const Geno& g, int norm, const float* W, const float* H, int k, double* mean,
@@ -619,8 +704,14 @@ void launch_nmf_clamp0_f32(Ctx& c, const float* src, int ld, double* X, uint64_t
 void launch_nmf_cv(Ctx& c, const Geno& g, uint64_t chunk, uint64_t mask_seed, double rate, const float* W,
                    const float* H, int k, double* part) {
     if (!g.p) return;
-    k_nmf_cv<<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(packed_rows(g), g.stride, g.n, g.p, chunk, mask_seed,
-                                                         rate_threshold(rate), W, H, k, g.counts.get(), part);
+    if (c.rng == SLFMM_RNG_CHACHA8)
+        k_nmf_cv<true><<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(packed_rows(g), g.stride, g.n, g.p, chunk,
+                                                                  mask_seed, rate_threshold(rate, 52), W, H, k,
+                                                                  g.counts.get(), part);
+    else
+        k_nmf_cv<false><<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(packed_rows(g), g.stride, g.n, g.p, chunk,
+                                                                   mask_seed, rate_threshold(rate), W, H, k,
+                                                                   g.counts.get(), part);
     SLFMM_LAUNCHED(c, "k_nmf_cv");
 }
 
@@ -631,8 +722,14 @@ void launch_nmf_gwas_cv(Ctx& c, const Geno& g, uint64_t chunk, uint64_t seed, do
     const uint64_t nchunks = ceil_div(g.p, chunk);
     k_obs_base<<<grid_for(c, nchunks, 64), 64, 0, c.stream>>>(g.counts.get(), g.p, chunk, base.get());
     SLFMM_LAUNCHED(c, "k_obs_base");
-    k_nmf_gwas_cv<<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(packed_rows(g), g.stride, g.n, g.p, chunk, seed,
-                                                              rate_threshold(rate), W, Wpt, k, base.get(), part);
+    if (c.rng == SLFMM_RNG_CHACHA8)
+        k_nmf_gwas_cv<true><<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(packed_rows(g), g.stride, g.n, g.p, chunk,
+                                                                       seed, rate_threshold(rate, 52), W, Wpt, k,
+                                                                       base.get(), part);
+    else
+        k_nmf_gwas_cv<false><<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(packed_rows(g), g.stride, g.n, g.p, chunk,
+                                                                        seed, rate_threshold(rate), W, Wpt, k,
+                                                                        base.get(), part);
     SLFMM_LAUNCHED(c, "k_nmf_gwas_cv");
 }
 

@@ -1,9 +1,11 @@
-"""The reference's sketch stream on the engine (SLFMM_RNG_CHACHA8): every
+"""The reference's random streams on the engine (SLFMM_RNG_CHACHA8): every
 Gaussian sketch a fit draws -- Omega (src/rsvd.rs:44-46) and the NMF probe
 (src/nmf.rs:291-293, seed + 1 000 000) -- is ChaCha8Rng::seed_from_u64 +
-Normal(0, 1).  The engine's Omega equals the host draw, a fit equals the
-counter-stream engine's fit with that Omega passed in, bit for bit, and the
-NMF fit agrees with the FP64 oracle drawing the same streams."""
+Normal(0, 1), and the CV hold-out masks (src/nmf.rs:433-448,
+src/testing.rs:437-452) are ChaCha8Rng::seed_from_u64 + Uniform(0, 1).  The
+engine's Omega equals the host draw, a fit equals the counter-stream engine's
+fit with that Omega passed in, bit for bit, and the NMF fit holds out the
+same calls as the FP64 oracle drawing the same streams."""
 import numpy as np
 import pytest
 
@@ -53,8 +55,9 @@ def test_fit_chacha_equals_injected_omega(engine, chacha_engine, host):
 
 
 def test_nmf_fit_chacha_matches_oracle(chacha_engine):
-    """The NMF probe from seed + 1 000 000 on the reference's stream (CV
-    masks stay on the counter stream in both)."""
+    """The NMF probe from seed + 1 000 000 and both CV masks on the
+    reference's streams: the held-out calls are the oracle's (count and
+    mean-fill error exact), the errors and the fit within tolerance."""
     import schnellfmm_gb300 as sg
     from test_gpu_nmf import _cohort
     raw, packed, x = _cohort()
@@ -68,8 +71,15 @@ def test_nmf_fit_chacha_matches_oracle(chacha_engine):
     ref = O.fit_oracle64(raw, raw, x, k=3, lam=1e-5, oversampling=10, seed=seed, norm=O.NORM_EIGENSTRAT,
                          nmf=dict(k=k, n_iter=it, eps=1e-16, cv_rate=rate), chunk=chunk, rng="chacha8")
     np.testing.assert_allclose(res.nmf_cv, ref.nmf.cv_mae_per_iter, rtol=2e-3, atol=0)
+    assert res.nmf_cv_mean == pytest.approx(ref.nmf.cv_mae_mean_impute, rel=1e-9)
     mae, mmae, cnt = ref.gwas_cv
     assert res.nmf_gwas_cv_count == cnt > 0
+    assert res.nmf_gwas_cv_mean_mae == pytest.approx(mmae, rel=1e-9)
+    assert res.nmf_gwas_cv_mae == pytest.approx(mae, rel=2e-3)
+    # a different stream than the counter one: other calls are held out
+    ctr = O.fit_oracle64(raw, raw, x, k=3, lam=1e-5, oversampling=10, seed=seed, norm=O.NORM_EIGENSTRAT,
+                         nmf=dict(k=k, n_iter=it, eps=1e-16, cv_rate=rate), chunk=chunk)
+    assert ctr.nmf.cv_mae_mean_impute != ref.nmf.cv_mae_mean_impute
     assert O.principal_angles_sin_max(res.u_hat, ref.u_hat) < 2e-3
     dt = np.abs(res.tstat - ref.assoc.tstat).max()
     assert dt <= 1e-3, f"max|dt| = {dt}"

@@ -219,3 +219,18 @@ def test_chacha8_normal_matrix():
     assert not np.array_equal(O.chacha8_normal_matrix(43, 7, 25), z[:7])
     np.testing.assert_array_equal(O.sketch_normal("chacha8", 5, 3, 4), O.chacha8_normal_matrix(5, 3, 4))
     np.testing.assert_array_equal(O.sketch_normal("counter", 5, 3, 4), O.rng_normal_matrix(5, 3, 4))
+
+
+def test_mask_uniform_streams():
+    """Hold-out uniforms: the ChaCha8 stream's Uniform(0, 1) is the top 52
+    bits of each output (rand_distr's [1, 2) mantissa minus 1); the counter
+    stream's the top 53; both hold out about `rate` of the calls."""
+    ctr = np.arange(200_000, dtype=np.uint64)
+    u = O.mask_uniform("chacha8", 7, ctr)
+    np.testing.assert_array_equal(u, (O.chacha8_u64(7, 200_000) >> np.uint64(12)).astype(np.float64) * 2.0 ** -52)
+    np.testing.assert_array_equal(O.mask_uniform("chacha8", 7, ctr[[5, 3, 99]]), u[[5, 3, 99]])
+    assert abs((u < 0.01).mean() - 0.01) < 1e-3 and u.min() >= 0.0 and u.max() < 1.0
+    c = O.mask_uniform("counter", 7, ctr)
+    np.testing.assert_array_equal(c, O.rng_uniform(7, ctr))
+    assert abs((c < 0.01).mean() - 0.01) < 1e-3
+    assert O.mask_uniform("chacha8", 7, np.zeros(0, dtype=np.uint64)).size == 0
