@@ -232,6 +232,26 @@ def _dptr(a: Optional[np.ndarray]):
     return None if a is None else a.ctypes.data_as(_dp)
 
 
+def _check_shape(name: str, a: Optional[np.ndarray], rows: int, cols: Optional[int] = None) -> None:
+    """The library reads host matrices with the shapes a call implies; a
+    mismatch is an argument error here, never a read past the buffer."""
+    if a is None:
+        return
+    if a.ndim != 2 or a.shape[0] != rows or (cols is not None and a.shape[1] != cols):
+        want = f"({rows}, {'d' if cols is None else cols})"
+        raise SchnelGpuError(ERR_BAD_ARG, f"{name} has shape {a.shape}, expected {want}")
+
+
+def _payload(packed: np.ndarray, n_physical: int) -> Tuple[np.ndarray, int]:
+    """The SNP-major .bed payload as contiguous bytes and its SNP count."""
+    packed = np.ascontiguousarray(packed, dtype=np.uint8)
+    bps = (n_physical + 3) // 4
+    n_snps = packed.size // bps if bps else 0
+    if packed.size != n_snps * bps:
+        raise SchnelGpuError(ERR_BAD_BED, "payload size is not a multiple of ceil(n/4)")
+    return packed, n_snps
+
+
 # ---------------------------------------------------------------------------
 # configuration mirrors
 # ---------------------------------------------------------------------------
@@ -380,11 +400,7 @@ class Engine:
 
     def upload(self, packed: np.ndarray, n_physical: int, sample_keep: Optional[Sequence[int]] = None,
                snps: Optional[SubsetSpec] = None) -> "Genotypes":
-        packed = np.ascontiguousarray(packed, dtype=np.uint8)
-        bps = (n_physical + 3) // 4
-        n_snps = packed.size // bps if bps else 0
-        if packed.size != n_snps * bps:
-            raise SchnelGpuError(ERR_BAD_BED, "payload size is not a multiple of ceil(n/4)")
+        packed, n_snps = _payload(packed, n_physical)
         keep = None if sample_keep is None else np.ascontiguousarray(sample_keep, dtype=np.uint64)
         sub = (snps or SubsetSpec.all())._c()
         h = C.c_void_p()
@@ -625,6 +641,8 @@ def estimate_factors(y_est, subset: SubsetSpec, x: np.ndarray, config: Lfmm2Conf
     x = np.ascontiguousarray(x, dtype=np.float64)
     u = np.empty((g.n_samples, config.k))
     om = None if omega is None else np.ascontiguousarray(omega, dtype=np.float64)
+    _check_shape("x", x, g.n_samples)
+    _check_shape("omega", om, g.n_samples, config.k + config.oversampling)
     cfg = config._c()
     eng.check(eng.lib.slfmm_estimate_factors(eng.h, g.h, _ptr(x), x.shape[1], C.byref(cfg), _ptr(om), _ptr(u)))
     return u
@@ -657,6 +675,8 @@ def test_associations(y_full, x: np.ndarray, u_hat: np.ndarray, config: Lfmm2Con
     g = _as_geno(y_full, eng)
     x = np.ascontiguousarray(x, dtype=np.float64)
     u_hat = np.ascontiguousarray(u_hat, dtype=np.float64)
+    _check_shape("x", x, g.n_samples)
+    _check_shape("u_hat", u_hat, g.n_samples, config.k)
     r, arr = _alloc_results(g.n_samples, g.n_snps, x.shape[1], config.k, 0)
     cfg = config._c()
     eng.check(eng.lib.slfmm_test_associations(eng.h, g.h, _ptr(x), x.shape[1], _ptr(u_hat), C.byref(cfg),
@@ -704,9 +724,11 @@ def fit_lfmm2(y_est, est_subset: SubsetSpec, y_full, x: np.ndarray, config: Lfmm
     else:
         ge = _as_geno(y_est, eng, est_subset)
     x = np.ascontiguousarray(x, dtype=np.float64)
+    om = None if omega is None else np.ascontiguousarray(omega, dtype=np.float64)
+    _check_shape("x", x, gf.n_samples)
+    _check_shape("omega", om, gf.n_samples, config.k + config.oversampling)
     nmf_iter = (config.nmf.n_iter if config.nmf else 0) if config.impute == ImputeStrategy.NMF else 0
     r, arr = _alloc_results(gf.n_samples, gf.n_snps, x.shape[1], config.k, nmf_iter)
-    om = None if omega is None else np.ascontiguousarray(omega, dtype=np.float64)
     cfg = config._c()
     eng.check(eng.lib.slfmm_fit(eng.h, ge.h, gf.h, _ptr(x), x.shape[1], C.byref(cfg), _ptr(om), C.byref(r)))
     res = _to_results(r, arr, config)
@@ -752,8 +774,8 @@ def fit_lfmm2_many(problems: Sequence[Tuple[np.ndarray, int, np.ndarray, Lfmm2Co
     arrs = []
     for i, (packed, n_physical, x, config) in enumerate(problems):
         x = np.ascontiguousarray(x, dtype=np.float64)
-        bps = (n_physical + 3) // 4
-        n_snps = packed.size // bps
+        packed, n_snps = _payload(packed, n_physical)
+        _check_shape(f"problem {i}: x", x, n_physical)
         if outs is None:
             nmf_iter = config.nmf.n_iter if (config.impute == ImputeStrategy.NMF and config.nmf) else 0
             r, arr = _alloc_results(n_physical, n_snps, x.shape[1], config.k, nmf_iter)
@@ -780,10 +802,12 @@ def fit_lfmm2_host(packed: np.ndarray, n_physical: int, x: np.ndarray, config: L
     """fit_lfmm2 from a HOST payload (upload, fit, copy back) in one C-ABI call.
     ``out`` may hold preallocated (e.g. pinned) result arrays."""
     eng = engine or default_engine()
-    bps = (n_physical + 3) // 4
-    n_snps = packed.size // bps
+    packed, n_snps = _payload(packed, n_physical)
     n = n_physical if sample_keep is None else len(sample_keep)
     x = np.ascontiguousarray(x, dtype=np.float64)
+    _check_shape("x", x, n)
+    if omega is not None:
+        _check_shape("omega", np.asarray(omega), n, config.k + config.oversampling)
     d = x.shape[1]
     if out is None:
         r, arr = _alloc_results(n, n_snps, d, config.k, config.nmf.n_iter if config.nmf else 0)

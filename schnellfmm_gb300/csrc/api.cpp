@@ -1479,7 +1479,9 @@ int slfmm_decode_chunk(slfmm_ctx* c, const slfmm_geno* g, uint64_t snp0, uint64_
     if (!c || !g || !out) return SLFMM_ERR_BAD_ARG;
     API_TRY
     SLFMM_CUDA(cudaSetDevice(c->device));
-    SLFMM_REQUIRE(snp0 + ncols <= g->p, SLFMM_ERR_BAD_ARG, "SNP range out of bounds");
+    SLFMM_REQUIRE(snp0 <= g->p && ncols <= g->p - snp0, SLFMM_ERR_BAD_ARG, "SNP range out of bounds");
+    SLFMM_REQUIRE(norm == SLFMM_NORM_CENTER_ONLY || norm == SLFMM_NORM_EIGENSTRAT, SLFMM_ERR_BAD_ARG,
+                  "unknown normalisation");
     SnpStd s;
     std_mean(*c, *g, norm, s);
     DBuf<double> o(std::max<uint64_t>(g->n * ncols, 1), c->stream);
@@ -1504,6 +1506,7 @@ int slfmm_generate_omega(slfmm_ctx* c, uint64_t seed, uint64_t n, uint32_t l, do
     if (!c || !out) return SLFMM_ERR_BAD_ARG;
     API_TRY
     SLFMM_CUDA(cudaSetDevice(c->device));
+    SLFMM_REQUIRE(l <= 4096, SLFMM_ERR_BAD_ARG, "sketch width above 4096");
     DBuf<double> o(std::max<uint64_t>(n * l, 1), c->stream);
     draw_normal(*c, seed, n, (int)l, o.get());
     d2h(*c, out, o.get(), n * l);

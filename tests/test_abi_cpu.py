@@ -114,6 +114,25 @@ def test_reference_normal_bad_args(lib):
     assert lib.slfmm_reference_normal(1, 2**63, 4, C.c_void_p(8)) == -1   # rows x cols overflows
 
 
+def test_host_array_shapes_checked():
+    """Host matrices whose shape does not match the call are argument errors
+    before the library is called (it would read them with the implied shape)."""
+    import schnellfmm_gb300 as sg
+    sg._check_shape("x", np.zeros((5, 2)), 5)
+    sg._check_shape("omega", None, 5, 13)
+    for a, rows, cols in [(np.zeros(5), 5, None), (np.zeros((4, 2)), 5, None), (np.zeros((5, 12)), 5, 13)]:
+        with pytest.raises(sg.SchnelGpuError) as e:
+            sg._check_shape("x", a, rows, cols)
+        assert e.value.code == sg.ERR_BAD_ARG and "expected" in str(e.value)
+    packed, p = sg._payload(np.zeros((7, 3), dtype=np.uint8), 10)
+    assert p == 7 and packed.flags.c_contiguous and packed.dtype == np.uint8
+    pinned = np.zeros(12, dtype=np.uint8)
+    assert sg._payload(pinned, 4)[0].ctypes.data == pinned.ctypes.data   # no copy of a usable payload
+    with pytest.raises(sg.SchnelGpuError) as e:
+        sg._payload(np.zeros(10, dtype=np.uint8), 10)
+    assert e.value.code == sg.ERR_BAD_BED
+
+
 def test_create_rejects_unknown_rng(lib):
     import schnellfmm_gb300 as sg
     opts = sg._Opts(int(sg.Precision.SPLIT_FP8), 0, None, 0, 7)

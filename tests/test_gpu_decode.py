@@ -84,3 +84,19 @@ def test_bad_arguments(engine):
         engine.upload(c.packed, 20, sample_keep=[0, 25])
     with pytest.raises(sg.SchnelGpuError):
         engine.upload(c.packed, 20, snps=sg.SubsetSpec.from_indices([10]))
+
+
+def test_decode_chunk_rejects_bad_ranges(engine):
+    """A SNP range past the end (also one whose end wraps around 2^64) and an
+    unknown normalisation are argument errors, not device accesses."""
+    sg = _sg()
+    c = simdata.simulate(40, 50, seed=5)
+    geno = engine.upload(c.packed, 40)
+    np.testing.assert_array_equal(geno.decode_chunk(45, 5, 1), geno.decode_chunk(0, 50, 1)[:, 45:])
+    for snp0, ncols in [(45, 6), (51, 0), (2**64 - 2, 3)]:
+        with pytest.raises(sg.SchnelGpuError) as e:
+            geno.decode_chunk(snp0, ncols, 1)
+        assert e.value.code == sg.ERR_BAD_ARG
+    with pytest.raises(sg.SchnelGpuError) as e:
+        geno.decode_chunk(0, 5, 7)
+    assert e.value.code == sg.ERR_BAD_ARG
