@@ -364,6 +364,8 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--out", default=None, help="also write the JSON line to this file")
     ap.add_argument("--autotune", action="store_true", help="let the engine tune its ring depths (warm-up does it)")
+    ap.add_argument("--rng", choices=["counter", "chacha8"], default="counter",
+                    help="random streams of the sketches and CV masks (chacha8: the reference's)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -383,7 +385,7 @@ def main():
                           f"l={w['k'] + w['oversampling']} q={w['power_iter']}",
               "n_samples": w["n"], "n_snps": w["p"], "K": w["k"], "d": w["d"], "oversampling": w["oversampling"],
               "power_iter": w["power_iter"], "est_rate": w["est_rate"], "precision": args.precision,
-              "autotune": bool(args.autotune),
+              "autotune": bool(args.autotune), "rng": args.rng,
               "l2": "inputs larger than L2 (packed genotypes %.1f GB vs 129 MB L2)" % (w["p"] * ((w["n"] + 3) // 4) / 1e9)}
 
     if args.impl == "reference":
@@ -417,7 +419,8 @@ def main():
     torch_stream = torch.cuda.current_stream()
     prec = {"split_fp8": sg.Precision.SPLIT_FP8, "split_bf16": sg.Precision.SPLIT_BF16,
             "fp32": sg.Precision.FP32}[args.precision]
-    eng = sg.Engine(dev, prec, stream=torch_stream.cuda_stream, autotune=args.autotune)
+    eng = sg.Engine(dev, prec, stream=torch_stream.cuda_stream, autotune=args.autotune,
+                    rng=sg.SketchRng.CHACHA8 if args.rng == "chacha8" else sg.SketchRng.COUNTER)
     n, p, d, k = w["n"], w["p"], w["d"], w["k"]
     rng = np.random.default_rng(100 + rank)
     q = rng.dirichlet(np.full(w["n_pop"], w["alpha"]), size=n).astype(np.float32)
