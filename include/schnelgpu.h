@@ -294,7 +294,7 @@ int slfmm_profile_read(slfmm_ctx* ctx, const char* kernel, double* total_ms, uin
  * make that first call before any stream capture begins. */
 int slfmm_gif_noalloc(slfmm_ctx* ctx, const float* t_dev, uint64_t p, uint32_t d, double* gif_dev);
 
-/* ---- output (src/testing.rs:740-801) ------------------------------------ */
+/* ---- output (src/testing.rs:740-801, 818-983) --------------------------- */
 /* Write <out>.tsv: header chr pos snp_id {p_,beta_,t_}xcov r2_cov r2_latent
  * r2_resid, numbers in Rust "{:.6e}" form.  chrom/snp_id are arrays of p
  * C strings, cov_names d C strings.  Formatting runs on n_threads host
@@ -302,6 +302,21 @@ int slfmm_gif_noalloc(slfmm_ctx* ctx, const float* t_dev, uint64_t p, uint32_t d
 int slfmm_write_tsv(const char* path, uint64_t p, uint32_t d, const char* const* chrom,
                     const uint64_t* pos, const char* const* snp_id,
                     const char* const* cov_names, const slfmm_results* res, int n_threads);
+
+#define SLFMM_PARQUET_UNCOMPRESSED 0  /* CompressionCodec::UNCOMPRESSED          */
+#define SLFMM_PARQUET_ZSTD         6  /* CompressionCodec::ZSTD (the reference's);
+                                         libzstd.so.1 is loaded at run time      */
+/* Write <out>.parquet, the --format parquet output (coalesce_output_parquet,
+ * src/testing.rs:818-983): columns chr, pos, snp_id, p_<cov>...,
+ * beta_<cov>..., t_<cov>..., r2_cov, r2_latent, r2_resid, all required
+ * (build_calibrated_schema, src/testing.rs:620-640), rows in SNP order, row
+ * groups of 2^18 rows encoded on n_threads host threads (0 = all).
+ * SLFMM_ERR_IO if the file cannot be written or ZSTD is asked for and libzstd
+ * cannot be loaded. */
+int slfmm_write_parquet(const char* path, uint64_t p, uint32_t d, const char* const* chrom,
+                        const uint64_t* pos, const char* const* snp_id,
+                        const char* const* cov_names, const slfmm_results* res,
+                        int compression, int n_threads);
 /* Format one value like Rust "{:.6e}"; returns the length written. */
 int slfmm_format_exp6(double v, char* buf, size_t buf_len);
 

@@ -123,7 +123,7 @@ EXPORTED_SYMBOLS = (
     "slfmm_generate_omega", "slfmm_estimate_factors", "slfmm_test_associations", "slfmm_fit",
     "slfmm_fit_host", "slfmm_write_tsv", "slfmm_format_exp6", "slfmm_simulate", "slfmm_geno_download",
     "slfmm_profile_enable", "slfmm_profile_read", "slfmm_host_alloc", "slfmm_host_free", "slfmm_contract_raw",
-    "slfmm_gif_noalloc", "slfmm_fit_traits", "slfmm_fit_many", "slfmm_reference_normal",
+    "slfmm_gif_noalloc", "slfmm_fit_traits", "slfmm_fit_many", "slfmm_reference_normal", "slfmm_write_parquet",
 )
 
 _lib_handle = None
@@ -174,6 +174,8 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
         "slfmm_fit_traits": (i32, [vp, vp, vp, vp, u32, C.POINTER(_Config), C.POINTER(_Results)]),
         "slfmm_fit_many": (i32, [vp, C.POINTER(_Problem), u32, u32, C.POINTER(C.c_int)]),
         "slfmm_reference_normal": (i32, [u64, u64, u32, vp]),
+        "slfmm_write_parquet": (i32, [C.c_char_p, u64, u32, C.POINTER(C.c_char_p), C.POINTER(u64),
+                                      C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), C.POINTER(_Results), i32, i32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -687,12 +689,19 @@ def test_associations(y_full, x: np.ndarray, u_hat: np.ndarray, config: Lfmm2Con
 test_associations.__test__ = False  # keep pytest from collecting the API function
 
 
+class OutputFormat(enum.Enum):
+    """src/testing.rs:35-48."""
+    TSV = "tsv"
+    PARQUET = "parquet"
+
+
 @dataclass
 class OutputConfig:
-    """src/testing.rs:68-73 (TSV only)."""
+    """src/testing.rs:68-73."""
     path: Path
     bim: Sequence[BimRecord]
     cov_names: Sequence[str]
+    format: OutputFormat = OutputFormat.TSV
 
 
 def write_tsv(path: os.PathLike, bim: Sequence[BimRecord], cov_names: Sequence[str], res: TestResults,
@@ -708,6 +717,33 @@ def write_tsv(path: os.PathLike, bim: Sequence[BimRecord], cov_names: Sequence[s
                  0.0, 0.0, 0.0, 0)
     rc = lib.slfmm_write_tsv(str(path).encode(), p, d, chrom, pos.ctypes.data_as(C.POINTER(C.c_uint64)), sid,
                              names, C.byref(r), n_threads)
+    if rc != OK:
+        raise SchnelGpuError(rc, f"Failed to create {path}")
+
+
+PARQUET_UNCOMPRESSED = 0
+PARQUET_ZSTD = 6
+
+
+def write_parquet(path: os.PathLike, bim: Sequence[BimRecord], cov_names: Sequence[str], res: TestResults,
+                  compression: int = PARQUET_ZSTD, n_threads: int = 0) -> None:
+    """<out>.parquet as coalesce_output_parquet (src/testing.rs:818-983):
+    chr, pos, snp_id, p_*, beta_*, t_*, r2_cov, r2_latent, r2_resid; rows in
+    SNP order; ZSTD (the reference's codec) or uncompressed."""
+    lib = load_library()
+    p, d = res.beta.shape
+    if len(bim) != p or len(cov_names) != d:
+        raise SchnelGpuError(ERR_BAD_ARG, "bim must have one record per SNP and cov_names one name per trait")
+    enc = lambda xs: (C.c_char_p * max(len(xs), 1))(*[s.encode() for s in xs])
+    chrom = enc([b.chrom for b in bim])
+    sid = enc([b.snp_id for b in bim])
+    pos = np.ascontiguousarray([b.pos for b in bim], dtype=np.uint64)
+    names = enc(list(cov_names))
+    cols = {k: np.ascontiguousarray(getattr(res, k), dtype=np.float64) for k in ("beta", "tstat", "pvalue", "r2")}
+    r = _Results(None, _dptr(cols["beta"]), _dptr(cols["tstat"]), _dptr(cols["pvalue"]), _dptr(cols["r2"]), None,
+                 res.gif, None, 0.0, 0.0, 0.0, 0)
+    rc = lib.slfmm_write_parquet(str(path).encode(), p, d, chrom, pos.ctypes.data_as(C.POINTER(C.c_uint64)), sid,
+                                 names, C.byref(r), compression, n_threads)
     if rc != OK:
         raise SchnelGpuError(rc, f"Failed to create {path}")
 
@@ -733,7 +769,8 @@ def fit_lfmm2(y_est, est_subset: SubsetSpec, y_full, x: np.ndarray, config: Lfmm
     eng.check(eng.lib.slfmm_fit(eng.h, ge.h, gf.h, _ptr(x), x.shape[1], C.byref(cfg), _ptr(om), C.byref(r)))
     res = _to_results(r, arr, config)
     if output is not None:
-        write_tsv(output.path, output.bim, output.cov_names, res)
+        (write_parquet if output.format == OutputFormat.PARQUET else write_tsv)(output.path, output.bim,
+                                                                                 output.cov_names, res)
     return res
 
 

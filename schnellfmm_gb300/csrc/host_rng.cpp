@@ -182,8 +182,8 @@ void draw_normal(Ctx& c, uint64_t seed, uint64_t rows, int cols, double* out) {
 }  // namespace slfmm
 
 extern "C" int slfmm_reference_normal(uint64_t seed, uint64_t rows, uint32_t cols, double* out) {
-    if (!out && rows * (uint64_t)cols) return SLFMM_ERR_BAD_ARG;
     if (rows && cols && rows > UINT64_MAX / cols) return SLFMM_ERR_BAD_ARG;
+    if (!out && rows && cols) return SLFMM_ERR_BAD_ARG;
     slfmm::reference_normal(seed, rows, cols, out);
     return SLFMM_OK;
 }

@@ -1,7 +1,7 @@
 """The C-ABI library on a machine without a GPU: it builds, loads, exports
 every entry point the header declares, its host-only entry points (number
-formatting, TSV writer, .bed validation, the reference's sketch stream) match
-the oracle, and every call that needs the device fails loudly instead of
+formatting, TSV and Parquet writers, .bed validation, the reference's sketch
+stream) match the oracle or an independent reader, and every call that needs the device fails loudly instead of
 falling back to the CPU."""
 import ctypes as C
 import re
@@ -64,6 +64,67 @@ def test_write_tsv_matches_oracle(lib, tmp_path):
     rows = O.tsv_rows([b.chrom for b in bim], [b.pos for b in bim], [b.snp_id for b in bim], ref)
     want = O.tsv_header(names) + "\n" + "".join(r + "\n" for r in rows)
     assert out.read_text() == want
+
+
+def _results(sg, p, d, seed):
+    rng = np.random.default_rng(seed)
+    res = sg.TestResults(u_hat=np.zeros((4, 2)), gif=1.0, gif_per_trait=np.ones(d),
+                         beta=rng.standard_normal((p, d)), tstat=rng.standard_normal((p, d)) * 3,
+                         pvalue=rng.uniform(1e-12, 1, (p, d)), r2=rng.uniform(0, 1, (p, 3)))
+    if p and d:
+        res.pvalue[0, 0] = np.nan
+        res.beta[-1, -1] = -0.0
+    bim = [sg.BimRecord(str(1 + i // 20), f"rs{i}_\u00e9", 0.0, 1000 + 7 * i, "A", "G") for i in range(p)]
+    return res, bim
+
+
+@pytest.mark.parametrize("p,d", [(57, 3), (300_000, 2), (0, 1), (9, 0)])
+@pytest.mark.parametrize("codec", ["zstd", "none"])
+def test_write_parquet_reads_back(lib, tmp_path, p, d, codec):
+    """<out>.parquet (coalesce_output_parquet, src/testing.rs:818-983) read
+    back by an independent Parquet reader: the calibrated schema
+    (src/testing.rs:620-640) with every field required, the values bit for
+    bit, row groups of 2^18 rows, the requested codec."""
+    pq = pytest.importorskip("pyarrow.parquet")
+    import schnellfmm_gb300 as sg
+    res, bim = _results(sg, p, d, 11)
+    names = [f"cov{j}" for j in range(d)]
+    out = tmp_path / "res.parquet"
+    sg.write_parquet(out, bim, names, res, compression=sg.PARQUET_ZSTD if codec == "zstd" else sg.PARQUET_UNCOMPRESSED,
+                     n_threads=3)
+    f = pq.ParquetFile(out)
+    tab = f.read()
+    want = (["chr", "pos", "snp_id"] + [f"p_{n}" for n in names] + [f"beta_{n}" for n in names]
+            + [f"t_{n}" for n in names] + ["r2_cov", "r2_latent", "r2_resid"])
+    assert tab.column_names == want and tab.num_rows == p
+    assert all(not fld.nullable for fld in tab.schema)
+    assert str(tab.schema.field("chr").type) == "string" and str(tab.schema.field("pos").type) == "int64"
+    assert f.metadata.num_row_groups == -(-p // (1 << 18))
+    if p:
+        assert f.metadata.row_group(0).column(3).compression == ("ZSTD" if codec == "zstd" else "UNCOMPRESSED")
+    assert tab.column("chr").to_pylist() == [b.chrom for b in bim]
+    assert tab.column("pos").to_pylist() == [b.pos for b in bim]
+    assert tab.column("snp_id").to_pylist() == [b.snp_id for b in bim]
+    bits = lambda a: np.ascontiguousarray(a, dtype=np.float64).view(np.uint64)
+    for j, n in enumerate(names):
+        for pre, arr in (("p_", res.pvalue), ("beta_", res.beta), ("t_", res.tstat)):
+            np.testing.assert_array_equal(bits(tab.column(pre + n).to_numpy()), bits(arr[:, j]))
+    for k, n in enumerate(["r2_cov", "r2_latent", "r2_resid"]):
+        np.testing.assert_array_equal(bits(tab.column(n).to_numpy()), bits(res.r2[:, k]))
+
+
+def test_write_parquet_bad_args(lib, tmp_path):
+    import schnellfmm_gb300 as sg
+    res, bim = _results(sg, 5, 1, 2)
+    with pytest.raises(sg.SchnelGpuError) as e:
+        sg.write_parquet(tmp_path / "x.parquet", bim, ["a"], res, compression=1)   # SNAPPY: not written
+    assert e.value.code == sg.ERR_BAD_ARG
+    with pytest.raises(sg.SchnelGpuError) as e:
+        sg.write_parquet(tmp_path / "x.parquet", bim[:4], ["a"], res)
+    assert e.value.code == sg.ERR_BAD_ARG
+    with pytest.raises(sg.SchnelGpuError) as e:
+        sg.write_parquet(tmp_path / "no_such_dir" / "x.parquet", bim, ["a"], res)
+    assert e.value.code == sg.ERR_IO
 
 
 def _write_bed(path, payload, magic=bytes([0x6C, 0x1B, 0x01])):
