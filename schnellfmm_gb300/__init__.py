@@ -12,6 +12,7 @@ reference (src/lib.rs, ...)    here
 ``SubsetSpec``                 :class:`SubsetSpec`   (src/bed.rs:50-57)
 ``SnpNorm``                    :class:`SnpNorm`      (src/bed.rs:19-26)
 ``Lfmm2Config`` / ``NmfConfig``:class:`Lfmm2Config` / :class:`NmfConfig`
+``load_covariates`` (CLI)      :func:`load_covariates`   (src/main.rs:339-571)
 ``center_covariates``          :func:`center_covariates` (src/lib.rs:102-117)
 ``estimate_factors``           :func:`estimate_factors`  (src/lib.rs:127-136)
 ``test_associations``          :func:`test_associations` (src/lib.rs:144-154)
@@ -29,6 +30,7 @@ import enum
 import weakref
 import math
 import os
+import sys
 from dataclasses import dataclass, field
 from pathlib import Path
 from typing import List, Optional, Sequence, Tuple
@@ -609,6 +611,122 @@ class BedFile:
 
     def upload(self, eng: Engine, snps: Optional[SubsetSpec] = None) -> Genotypes:
         return eng.upload(np.asarray(self.payload), self.n_physical_samples, self.sample_keep, snps)
+
+
+_MISSING_COV = (".",)
+
+
+def _cov_value(text: str, name: str, line: int, sample: str) -> float:
+    """One covariate cell: empty, '.' and NA (any case) are missing; anything
+    else must parse as a finite number (src/main.rs:413-440)."""
+    t = text.strip()
+    if not t or t in _MISSING_COV or t.lower() == "na":
+        return math.nan
+    try:
+        if "_" in t:               # digit separators: not a number to the reference's parser
+            raise ValueError
+        v = float(t)
+    except ValueError:
+        raise SchnelGpuError(ERR_BAD_ARG, f"Failed to parse value '{t}' for covariate '{name}' on line {line} "
+                                          f"(sample '{sample}')")
+    if math.isinf(v):
+        raise SchnelGpuError(ERR_BAD_ARG, f"Infinite value ({t}) for covariate '{name}' on line {line} "
+                                          f"(sample '{sample}'): Inf values will propagate through all matrix "
+                                          f"operations")
+    return v
+
+
+def load_covariates(path: os.PathLike, fam: Sequence[FamRecord], intersect: bool = False,
+                    verbose: bool = False) -> Tuple[List[str], np.ndarray, List[int]]:
+    """Covariate / phenotype table matched to .fam order (load_covariates,
+    src/main.rs:339-571).
+
+    Comma-delimited for a ``.csv`` extension, tab-delimited otherwise.  The
+    header's first cell names the sample-ID column (may be blank), the rest
+    name the covariates; each row is a sample ID (matched against the .fam
+    IIDs) and one value per covariate.  Blank lines are skipped; duplicate IDs,
+    ragged rows, unparsable or infinite values are errors.  Samples of the
+    .fam absent from the table are an error unless ``intersect`` (then they
+    are dropped).  Missing values are imputed per column with the mean of
+    the observed ones (0 if none).  Returns (names, x kept x d, kept .fam
+    row indices)."""
+    path = Path(path)
+    delim = "," if path.suffix == ".csv" else "\t"
+    if verbose:
+        sys.stderr.write(f"  Detected {'CSV' if delim == ',' else 'TSV'} format (delimiter: {delim!r})\n")
+    try:
+        with open(path, newline="") as f:
+            lines = f.read().split("\n")
+    except OSError:
+        raise SchnelGpuError(ERR_IO, f"Failed to open covariate file: {path}")
+    if lines and lines[-1] == "":
+        lines.pop()                                   # the final newline ends the last line
+    lines = [ln[:-1] if ln.endswith("\r") else ln for ln in lines]
+    if not lines:
+        raise SchnelGpuError(ERR_BAD_ARG, "Covariate file is empty")
+    header = lines[0].split(delim)
+    if len(header) < 2:
+        raise SchnelGpuError(ERR_BAD_ARG, f"Covariate file header has only {len(header)} field(s) - expected at "
+                                          f"least a sample ID column and one covariate column (delimiter: "
+                                          f"{delim!r})")
+    names = [h.strip() for h in header[1:]]
+    d = len(names)
+    data, order = {}, []
+    for i, line in enumerate(lines[1:]):
+        if not line.strip():
+            continue
+        fields = line.split(delim)
+        if len(fields) != d + 1:
+            raise SchnelGpuError(ERR_BAD_ARG, f"Line {i + 2} has {len(fields)} fields, expected {d + 1} "
+                                              f"(1 sample ID + {d} covariates)")
+        sid = fields[0].strip()
+        vals = [_cov_value(s, names[j], i + 2, sid) for j, s in enumerate(fields[1:])]
+        if sid in data:
+            raise SchnelGpuError(ERR_BAD_ARG, f"Duplicate sample ID '{sid}' in covariate file (line {i + 2})")
+        data[sid] = vals
+        order.append(sid)
+    if not data:
+        raise SchnelGpuError(ERR_BAD_ARG, "Covariate file has no data rows")
+    sys.stderr.write(f"  Read {len(data)} samples from covariate file\n")
+    kept, rows = [], []
+    for r, rec in enumerate(fam):
+        vals = data.get(rec.iid)
+        if vals is not None:
+            kept.append(r)
+            rows.append(vals)
+        elif not intersect:
+            raise SchnelGpuError(ERR_BAD_ARG, f"Sample '{rec.iid}' (FID='{rec.fid}') from .fam file not found in "
+                                              f"covariate file.\n.fam has {len(fam)} samples, covariate file has "
+                                              f"{len(data)}.\nFirst few covariate sample IDs: "
+                                              f"[{', '.join(order[:5])}]\nHint: use --intersect-samples to use "
+                                              f"only samples present in both files.")
+    if not kept:
+        raise SchnelGpuError(ERR_BAD_ARG, f"No samples in common between .fam file ({len(fam)} samples) and "
+                                          f"covariate file ({len(data)} samples).\nFirst few .fam IIDs: "
+                                          f"[{', '.join(r.iid for r in fam[:5])}]\nFirst few covariate IDs: "
+                                          f"[{', '.join(order[:5])}]")
+    if len(data) > len(kept):
+        sys.stderr.write(f"  Warning: {len(data) - len(kept)} sample(s) in covariate file not present in .fam "
+                         f"file (ignored)\n")
+    if len(fam) > len(kept):
+        sys.stderr.write(f"  Warning: {len(fam) - len(kept)} sample(s) in .fam file not present in covariate "
+                         f"file (dropped with --intersect-samples)\n")
+    sys.stderr.write(f"  Matched {len(kept)} samples to .fam order\n")
+    x = np.array(rows, dtype=np.float64).reshape(len(kept), d)
+    for j in range(d):
+        col = x[:, j]
+        miss = np.isnan(col)
+        if not miss.any():
+            continue
+        total, n_obs = 0.0, 0
+        for v in col[~miss]:                      # in row order, like the reference's running sum
+            total += float(v)
+            n_obs += 1
+        mean = total / n_obs if n_obs else 0.0
+        col[miss] = mean
+        sys.stderr.write(f"  Warning: covariate '{names[j]}' has {int(miss.sum())} missing value(s) ('.', 'NA', "
+                         f"or empty), imputed to column mean ({mean:.6f})\n")
+    return names, x, kept
 
 
 # ---------------------------------------------------------------------------

@@ -1,0 +1,83 @@
+"""The covariate loader (load_covariates, src/main.rs:339-571) on the host:
+the reference's own known answer (its test at src/main.rs:589-641, restated in
+tests/golden/reference_kats.json) plus the delimiter, matching, intersection
+and error rules of the same function."""
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+KATS = json.loads((Path(__file__).parent / "golden" / "reference_kats.json").read_text())
+
+
+def _sg():
+    import schnellfmm_gb300 as sg
+    return sg
+
+
+def _fam(sg, iids):
+    return [sg.FamRecord("FAM", iid, "0", "0", 0, "-9") for iid in iids]
+
+
+def test_covariate_na_imputation_kat(tmp_path):
+    sg = _sg()
+    k = KATS["covariate_na_imputation"]
+    path = tmp_path / "cov.tsv"
+    path.write_text(k["tsv"])
+    names, x, kept = sg.load_covariates(path, _fam(sg, [f"IND{i}" for i in range(5)]))
+    assert names == ["env_0", "env_1"] and kept == [0, 1, 2, 3, 4]
+    np.testing.assert_allclose(x, np.array(k["expected"]), rtol=0, atol=k["tol"])
+    assert x[1, 1] == (0.5 + 3.5 + 4.5) / 3.0 and x[0, 0] == 4.0
+
+
+def test_csv_fam_order_and_extra_samples(tmp_path):
+    sg = _sg()
+    path = tmp_path / "cov.csv"
+    path.write_text(",a,b\r\nS3,3,30\r\n\r\nS1,1,10\r\nS9,9,90\r\nS2,2,nan\r\n")
+    names, x, kept = sg.load_covariates(path, _fam(sg, ["S1", "S2", "S3"]))
+    assert names == ["a", "b"] and kept == [0, 1, 2]
+    np.testing.assert_array_equal(x, [[1, 10], [2, 20], [3, 30]])   # 'nan' is missing: mean of 10 and 30
+
+
+def test_intersect_samples(tmp_path):
+    sg = _sg()
+    path = tmp_path / "cov.tsv"
+    path.write_text("id\tv\nB\t2\nD\t4\n")
+    fam = _fam(sg, ["A", "B", "C", "D"])
+    with pytest.raises(sg.SchnelGpuError, match="--intersect-samples"):
+        sg.load_covariates(path, fam)
+    names, x, kept = sg.load_covariates(path, fam, intersect=True)
+    assert kept == [1, 3] and x[:, 0].tolist() == [2.0, 4.0]
+    with pytest.raises(sg.SchnelGpuError, match="No samples in common"):
+        sg.load_covariates(path, _fam(sg, ["X", "Y"]), intersect=True)
+
+
+@pytest.mark.parametrize("text,match", [
+    ("", "empty"),
+    ("id\n", "header has only 1 field"),
+    ("id\tv\n\n", "no data rows"),
+    ("id\tv\nA\t1\nA\t2\n", "Duplicate sample ID 'A'"),
+    ("id\tv\nA\t1\n\nB\t1\t2\n", "Line 4 has 3 fields"),
+    ("id\tv\nA\tinf\n", "Infinite value"),
+    ("id\tv\nA\t1_0\n", "Failed to parse value '1_0'"),
+    ("id\tv\nA\tabc\n", "Failed to parse value 'abc' for covariate 'v' on line 2"),
+])
+def test_errors(tmp_path, text, match):
+    sg = _sg()
+    path = tmp_path / "cov.tsv"
+    path.write_text(text)
+    with pytest.raises(sg.SchnelGpuError, match=match) as e:
+        sg.load_covariates(path, _fam(sg, ["A", "B"]))
+    assert e.value.code == sg.ERR_BAD_ARG
+
+
+def test_all_missing_column_and_missing_file(tmp_path):
+    sg = _sg()
+    path = tmp_path / "cov.tsv"
+    path.write_text("id\tv\tw\nA\tNA\t1\nB\t.\t\n")
+    names, x, _ = sg.load_covariates(path, _fam(sg, ["A", "B"]))
+    np.testing.assert_array_equal(x, [[0.0, 1.0], [0.0, 1.0]])     # no observed value: 0
+    with pytest.raises(sg.SchnelGpuError) as e:
+        sg.load_covariates(tmp_path / "none.tsv", _fam(sg, ["A"]))
+    assert e.value.code == sg.ERR_IO
