@@ -613,6 +613,28 @@ class BedFile:
         return eng.upload(np.asarray(self.payload), self.n_physical_samples, self.sample_keep, snps)
 
 
+def align_est_bed_samples(est_bed: BedFile, main_bed: BedFile) -> None:
+    """--est-bed alignment (align_est_bed_samples, src/main.rs:282-331): the
+    estimation .bed takes the main .bed's samples in the main .bed's order
+    (matched by IID; a repeated IID in the estimation .fam resolves to its
+    last row), via subset_samples when the order or the count differs; an
+    estimation .bed without some main-.bed sample is an error."""
+    index = {r.iid: i for i, r in enumerate(est_bed.fam_records)}
+    idx, missing = [], []
+    for r in main_bed.fam_records:
+        if r.iid in index:
+            idx.append(index[r.iid])
+        else:
+            missing.append(r.iid)
+    if missing:
+        raise SchnelGpuError(ERR_BAD_ARG, f"est-bed is missing {len(missing)} sample(s) that are in the main BED "
+                                          f"file: [{', '.join(missing[:5])}]{', ...' if len(missing) > 5 else ''}")
+    if len(idx) != est_bed.n_samples or any(i != j for i, j in enumerate(idx)):
+        sys.stderr.write(f"  Reordering/subsetting est-bed samples to match main BED ({est_bed.n_samples} → "
+                         f"{len(idx)} samples)\n")
+        est_bed.subset_samples(idx)
+
+
 _MISSING_COV = (".",)
 
 

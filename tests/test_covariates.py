@@ -1,7 +1,9 @@
-"""The covariate loader (load_covariates, src/main.rs:339-571) on the host:
-the reference's own known answer (its test at src/main.rs:589-641, restated in
+"""Sample-side host logic of the command line: the covariate loader
+(load_covariates, src/main.rs:339-571) on the reference's own known answer
+(its test at src/main.rs:589-641, restated in
 tests/golden/reference_kats.json) plus the delimiter, matching, intersection
-and error rules of the same function."""
+and error rules of the same function, and the --est-bed sample alignment
+(src/main.rs:282-331)."""
 import json
 from pathlib import Path
 
@@ -81,3 +83,24 @@ def test_all_missing_column_and_missing_file(tmp_path):
     with pytest.raises(sg.SchnelGpuError) as e:
         sg.load_covariates(tmp_path / "none.tsv", _fam(sg, ["A"]))
     assert e.value.code == sg.ERR_IO
+
+
+def _bed(sg, iids):
+    return sg.BedFile(Path("x.bed"), _fam(sg, iids), [], np.zeros(0, np.uint8))
+
+
+def test_align_est_bed_samples():
+    """--est-bed alignment (src/main.rs:282-331): the estimation .bed follows
+    the main .bed's samples and order; a missing sample is an error."""
+    sg = _sg()
+    est = _bed(sg, ["A", "B", "C"])
+    sg.align_est_bed_samples(est, _bed(sg, ["A", "B", "C"]))
+    assert est.sample_keep is None and est.n_samples == 3            # already aligned: untouched
+    est = _bed(sg, ["A", "B", "C", "D"])
+    sg.align_est_bed_samples(est, _bed(sg, ["C", "A", "D"]))
+    assert est.sample_keep.tolist() == [2, 0, 3] and [r.iid for r in est.fam_records] == ["C", "A", "D"]
+    assert est.n_samples == 3 and est.n_physical_samples == 4
+    est = _bed(sg, ["A", "B"])
+    with pytest.raises(sg.SchnelGpuError, match=r"missing 6 sample\(s\) .*\[C, D, E, F, G\], \.\.\.") as e:
+        sg.align_est_bed_samples(est, _bed(sg, ["A", "C", "D", "E", "F", "G", "H"]))
+    assert e.value.code == sg.ERR_BAD_ARG
