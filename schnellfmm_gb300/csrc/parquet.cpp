@@ -22,6 +22,7 @@
 #include <atomic>
 #include <cstdio>
 #include <cstring>
+#include <new>
 #include <string>
 #include <thread>
 #include <vector>
@@ -219,26 +220,16 @@ struct ChunkMeta {
     int64_t offset, uncompressed, compressed;
 };
 
-}  // namespace
-}  // namespace slfmm
-
-extern "C" int slfmm_write_parquet(const char* path, uint64_t p, uint32_t d, const char* const* chrom,
-                                   const uint64_t* pos, const char* const* snp_id, const char* const* cov_names,
-                                   const slfmm_results* res, int compression, int n_threads) {
-    using namespace slfmm;
-    if (!path || !res || (p && (!chrom || !pos || !snp_id)) || (d && !cov_names)) return SLFMM_ERR_BAD_ARG;
-    if (p && (!res->pvalue || !res->beta || !res->tstat || !res->r2)) return SLFMM_ERR_BAD_ARG;
-    if (compression != SLFMM_PARQUET_UNCOMPRESSED && compression != SLFMM_PARQUET_ZSTD) return SLFMM_ERR_BAD_ARG;
-    if (compression == SLFMM_PARQUET_ZSTD && !zstd().ok) return SLFMM_ERR_IO;
-
+// the file body after a successful fopen: magic, row groups, footer
+bool write_parquet_file(FILE* f, uint64_t p, uint32_t d, const char* const* chrom, const uint64_t* pos,
+                        const char* const* snp_id, const char* const* cov_names, const slfmm_results* res,
+                        int compression, int n_threads) {
     std::vector<Column> cols = {{"chr", kByteArrayT, true}, {"pos", kInt64T, false}, {"snp_id", kByteArrayT, true}};
     for (const char* pre : {"p_", "beta_", "t_"})
         for (uint32_t j = 0; j < d; ++j) cols.push_back({std::string(pre) + cov_names[j], kDoubleT, false});
     for (const char* nm : {"r2_cov", "r2_latent", "r2_resid"}) cols.push_back({nm, kDoubleT, false});
     const uint32_t nc = (uint32_t)cols.size();
 
-    FILE* f = std::fopen(path, "wb");
-    if (!f) return SLFMM_ERR_IO;
     bool ok = std::fwrite("PAR1", 1, 4, f) == 4;
     int64_t off = 4;
     const Table t{p, d, chrom, pos, snp_id, res};
@@ -251,10 +242,20 @@ extern "C" int slfmm_write_parquet(const char* path, uint64_t p, uint32_t d, con
         std::vector<ColumnChunk> chunks(nc);
         std::atomic<uint32_t> next{0};
         auto work = [&]() {
-            for (uint32_t c = next++; c < nc; c = next++) chunks[c] = encode_chunk(t, c, r0, r1, compression);
+            for (uint32_t c = next++; c < nc; c = next++) {
+                try {
+                    chunks[c] = encode_chunk(t, c, r0, r1, compression);
+                } catch (...) {
+                    chunks[c].ok = false;
+                }
+            }
         };
         std::vector<std::thread> th;
-        for (int i = 1; i < std::min<int>(nt, (int)nc); ++i) th.emplace_back(work);
+        try {
+            for (int i = 1; i < std::min<int>(nt, (int)nc); ++i) th.emplace_back(work);
+        } catch (...) {
+            // fewer threads: those started and this one take the columns
+        }
         work();
         for (auto& x : th) x.join();
         std::vector<ChunkMeta> meta(nc);
@@ -324,6 +325,32 @@ extern "C" int slfmm_write_parquet(const char* path, uint64_t p, uint32_t d, con
         tail += "PAR1";
         ok = std::fwrite(tail.data(), 1, tail.size(), f) == tail.size();
     }
-    if (std::fclose(f) != 0) ok = false;
-    return ok ? SLFMM_OK : SLFMM_ERR_IO;
+    return ok;
+}
+
+}  // namespace
+}  // namespace slfmm
+
+extern "C" int slfmm_write_parquet(const char* path, uint64_t p, uint32_t d, const char* const* chrom,
+                                   const uint64_t* pos, const char* const* snp_id, const char* const* cov_names,
+                                   const slfmm_results* res, int compression, int n_threads) {
+    using namespace slfmm;
+    if (!path || !res || (p && (!chrom || !pos || !snp_id)) || (d && !cov_names)) return SLFMM_ERR_BAD_ARG;
+    if (p && (!res->pvalue || !res->beta || !res->tstat || !res->r2)) return SLFMM_ERR_BAD_ARG;
+    if (compression != SLFMM_PARQUET_UNCOMPRESSED && compression != SLFMM_PARQUET_ZSTD) return SLFMM_ERR_BAD_ARG;
+    if (compression == SLFMM_PARQUET_ZSTD && !zstd().ok) return SLFMM_ERR_IO;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return SLFMM_ERR_IO;
+    int rc = SLFMM_OK;
+    try {
+        rc = write_parquet_file(f, p, d, chrom, pos, snp_id, cov_names, res, compression, n_threads)
+                 ? SLFMM_OK
+                 : SLFMM_ERR_IO;
+    } catch (const std::bad_alloc&) {
+        rc = SLFMM_ERR_NOMEM;
+    } catch (...) {
+        rc = SLFMM_ERR_IO;
+    }
+    if (std::fclose(f) != 0 && rc == SLFMM_OK) rc = SLFMM_ERR_IO;
+    return rc;
 }
