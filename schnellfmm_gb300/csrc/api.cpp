@@ -1297,6 +1297,10 @@ int format_exp6(double v, char* buf, size_t len) {
 }
 
 }  // namespace
+
+bool write_tsv_body(FILE* f, uint64_t p, uint32_t d, const char* const* chrom, const uint64_t* pos,
+                    const char* const* snp_id, const char* const* cov_names, const slfmm_results* res,
+                    int n_threads);
 }  // namespace slfmm
 
 // ===========================================================================
@@ -1878,6 +1882,26 @@ int slfmm_write_tsv(const char* path, uint64_t p, uint32_t d, const char* const*
     if (!res->pvalue || !res->beta || !res->tstat || !res->r2) return SLFMM_ERR_BAD_ARG;
     FILE* f = std::fopen(path, "wb");
     if (!f) return SLFMM_ERR_IO;
+    int rc = SLFMM_OK;
+    try {
+        rc = write_tsv_body(f, p, d, chrom, pos, snp_id, cov_names, res, n_threads) ? SLFMM_OK : SLFMM_ERR_IO;
+    } catch (const std::bad_alloc&) {
+        rc = SLFMM_ERR_NOMEM;
+    } catch (...) {
+        rc = SLFMM_ERR_IO;
+    }
+    if (std::fclose(f) != 0 && rc == SLFMM_OK) rc = SLFMM_ERR_IO;
+    return rc;
+}
+
+}  // extern "C"
+
+namespace slfmm {
+// the TSV rows after the file is open: header, then blocks of rows formatted
+// on n_threads threads and written in order
+bool write_tsv_body(FILE* f, uint64_t p, uint32_t d, const char* const* chrom, const uint64_t* pos,
+                    const char* const* snp_id, const char* const* cov_names, const slfmm_results* res,
+                    int n_threads) {
     std::string head = "chr\tpos\tsnp_id";
     for (uint32_t j = 0; j < d; ++j) {
         const std::string nm = cov_names[j];
@@ -1891,8 +1915,9 @@ int slfmm_write_tsv(const char* path, uint64_t p, uint32_t d, const char* const*
     for (uint64_t b0 = 0; b0 < p && ok; b0 += block * nt) {
         std::vector<std::string> parts(nt);
         std::vector<std::thread> th;
-        for (int t = 0; t < nt; ++t) {
-            th.emplace_back([&, t]() {
+        std::vector<char> failed(nt, 0);
+        auto fmt = [&](int t) {
+            try {
                 const uint64_t r0 = b0 + t * block, r1 = std::min(p, r0 + block);
                 std::string& s = parts[t];
                 char buf[64];
@@ -1915,14 +1940,23 @@ int slfmm_write_tsv(const char* path, uint64_t p, uint32_t d, const char* const*
                     }
                     s += '\n';
                 }
-            });
+            } catch (...) {
+                failed[t] = 1;
+            }
+        };
+        int started = 1;
+        try {
+            for (; started < nt; ++started) th.emplace_back(fmt, started);
+        } catch (...) {
+            // threads that did not start: their blocks are formatted below
         }
+        fmt(0);
+        for (int t = started; t < nt; ++t) fmt(t);
         for (auto& x : th) x.join();
+        for (int t = 0; t < nt; ++t) ok = ok && !failed[t];
         for (auto& s : parts)
-            if (!s.empty() && std::fwrite(s.data(), 1, s.size(), f) != s.size()) ok = false;
+            if (ok && !s.empty() && std::fwrite(s.data(), 1, s.size(), f) != s.size()) ok = false;
     }
-    if (std::fclose(f) != 0) ok = false;
-    return ok ? SLFMM_OK : SLFMM_ERR_IO;
+    return ok;
 }
-
-}  // extern "C"
+}  // namespace slfmm
