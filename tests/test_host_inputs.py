@@ -1,9 +1,9 @@
-"""Sample-side host logic of the command line: the covariate loader
-(load_covariates, src/main.rs:339-571) on the reference's own known answer
-(its test at src/main.rs:589-641, restated in
-tests/golden/reference_kats.json) plus the delimiter, matching, intersection
-and error rules of the same function, and the --est-bed sample alignment
-(src/main.rs:282-331)."""
+"""Host-side input logic: the covariate loader (load_covariates,
+src/main.rs:339-571) on the reference's own known answer (its test at
+src/main.rs:589-641, restated in tests/golden/reference_kats.json) plus the
+delimiter, matching, intersection and error rules of the same function; the
+--est-bed sample alignment (src/main.rs:282-331); the PLINK triplet reader
+(BedFile::open, src/bed.rs:60-135) and SNP subset counts."""
 import json
 from pathlib import Path
 
@@ -104,3 +104,62 @@ def test_align_est_bed_samples():
     with pytest.raises(sg.SchnelGpuError, match=r"missing 6 sample\(s\) .*\[C, D, E, F, G\], \.\.\.") as e:
         sg.align_est_bed_samples(est, _bed(sg, ["A", "C", "D", "E", "F", "G", "H"]))
     assert e.value.code == sg.ERR_BAD_ARG
+
+
+def _triplet(tmp_path, n, p, fam_lines=None, bim_lines=None, payload=None):
+    from oracle import lfmm_oracle as O
+    rng = np.random.default_rng(n * 1000 + p)
+    codes = rng.integers(0, 4, size=(p, n), dtype=np.uint8)
+    packed = O.pack_codes(codes) if payload is None else payload
+    (tmp_path / "t.bed").write_bytes(bytes([0x6C, 0x1B, 0x01]) + packed.tobytes())
+    (tmp_path / "t.fam").write_text("".join(fam_lines if fam_lines is not None else
+                                            [f"F{i} I{i} 0 0 {i % 3} -9\n" for i in range(n)]))
+    (tmp_path / "t.bim").write_text("".join(bim_lines if bim_lines is not None else
+                                            [f"{1 + i // 4}\trs{i}\t0.5\t{100 + i}\tA\tG\n" for i in range(p)]))
+    return tmp_path / "t.bed", packed
+
+
+def test_bed_file_open(tmp_path):
+    """BedFile::open (src/bed.rs:60-135): .fam / .bim parsed, the .bed's magic
+    and size checked, the payload mapped; subset_samples (:155-159) keeps the
+    physical layout."""
+    sg = _sg()
+    path, packed = _triplet(tmp_path, 10, 7)
+    bed = sg.BedFile.open(path)
+    assert bed.n_samples == bed.n_physical_samples == 10 and bed.n_snps == 7 and bed.bytes_per_snp() == 3
+    assert bed.fam_records[3] == sg.FamRecord("F3", "I3", "0", "0", 0, "-9")
+    assert bed.bim_records[5] == sg.BimRecord("2", "rs5", 0.5, 105, "A", "G")
+    np.testing.assert_array_equal(np.asarray(bed.payload).reshape(7, 3), packed)
+    bed.subset_samples([9, 0, 4])
+    assert bed.n_samples == 3 and bed.n_physical_samples == 10 and bed.bytes_per_snp() == 3
+    assert [r.iid for r in bed.fam_records] == ["I9", "I0", "I4"] and bed.sample_keep.tolist() == [9, 0, 4]
+
+
+def test_bed_file_open_errors(tmp_path):
+    sg = _sg()
+    path, _ = _triplet(tmp_path, 10, 7, payload=np.zeros((6, 3), np.uint8))   # one SNP short
+    with pytest.raises(sg.SchnelGpuError) as e:
+        sg.BedFile.open(path)
+    assert e.value.code == sg.ERR_BAD_BED
+    path, _ = _triplet(tmp_path, 4, 2, fam_lines=["F0 I0 0 0 1\n"] * 4)
+    with pytest.raises(sg.SchnelGpuError, match="FAM line 1 has 5 fields"):
+        sg.BedFile.open(path)
+    path, _ = _triplet(tmp_path, 4, 2, bim_lines=["1 rs0 0 x A G\n", "1 rs1 0 5 A G\n"])
+    with pytest.raises(sg.SchnelGpuError, match="BIM line 1: invalid position 'x'"):
+        sg.BedFile.open(path)
+    with pytest.raises(sg.SchnelGpuError) as e:
+        sg.BedFile.open(tmp_path / "absent.bed")
+    assert e.value.code == sg.ERR_IO
+
+
+def test_subset_spec_counts():
+    """SubsetSpec counts (src/bed.rs:162-171) against the oracle's index lists
+    and the reference's subset known answers."""
+    sg = _sg()
+    from oracle import lfmm_oracle as O
+    for n_snps in (0, 1, 99, 100, 101, 10_000):
+        assert sg.SubsetSpec.all().count(n_snps) == n_snps
+        for rate in (0.01, 0.1, 0.37, 0.5, 1.0):
+            assert sg.SubsetSpec.from_rate(rate).count(n_snps) == len(O.subset_indices(n_snps, rate=rate))
+    k = KATS["subset_count_consistency"]
+    assert sg.SubsetSpec.from_indices(k["indices"]).count(k["n"]) == k["indices_count"]
