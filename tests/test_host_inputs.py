@@ -163,3 +163,19 @@ def test_subset_spec_counts():
             assert sg.SubsetSpec.from_rate(rate).count(n_snps) == len(O.subset_indices(n_snps, rate=rate))
     k = KATS["subset_count_consistency"]
     assert sg.SubsetSpec.from_indices(k["indices"]).count(k["n"]) == k["indices_count"]
+
+
+def test_imputation_warnings_and_na_case(tmp_path, capsys):
+    """NA tokens in any case count as missing, and the warning names each
+    covariate with its missing count (the expectations of the reference's
+    tests/integration.rs:278-350)."""
+    sg = _sg()
+    path = tmp_path / "cov.tsv"
+    rows = ["IND0\t.\t0.5", "IND1\t1.0\tNA", "IND2\t2.0\tna", "IND3\t3.0\tNa", "IND4\t\t1.5", "IND5\t4.0\t2.5"]
+    path.write_text("sample_id\tenv_0\tenv_1\n" + "\n".join(rows) + "\n")
+    names, x, _ = sg.load_covariates(path, _fam(sg, [f"IND{i}" for i in range(6)]))
+    err = capsys.readouterr().err
+    assert "imputed to column mean" in err
+    assert "covariate 'env_0' has 2 missing value(s)" in err and "covariate 'env_1' has 3 missing value(s)" in err
+    assert x[0, 0] == x[4, 0] == (1.0 + 2.0 + 3.0 + 4.0) / 4.0
+    assert x[1, 1] == x[2, 1] == x[3, 1] == (0.5 + 1.5 + 2.5) / 3.0
