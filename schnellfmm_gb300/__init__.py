@@ -308,6 +308,8 @@ class SubsetSpec:
 
     @staticmethod
     def from_rate(rate: float) -> "SubsetSpec":
+        if not 0.0 < rate <= 1.0:       # src/main.rs:169-172
+            raise SchnelGpuError(ERR_BAD_ARG, f"--est-rate must be in (0.0, 1.0], got {rate}")
         return SubsetSpec("rate", rate=rate)
 
     @staticmethod

@@ -163,6 +163,9 @@ def test_subset_spec_counts():
             assert sg.SubsetSpec.from_rate(rate).count(n_snps) == len(O.subset_indices(n_snps, rate=rate))
     k = KATS["subset_count_consistency"]
     assert sg.SubsetSpec.from_indices(k["indices"]).count(k["n"]) == k["indices_count"]
+    for bad in (0.0, -0.1, 5.0, float("nan")):
+        with pytest.raises(sg.SchnelGpuError, match="est-rate must be in"):
+            sg.SubsetSpec.from_rate(bad)
 
 
 def test_imputation_warnings_and_na_case(tmp_path, capsys):
