@@ -87,7 +87,7 @@ def test_bad_arguments(engine):
 
 
 def test_decode_chunk_rejects_bad_ranges(engine):
-    """A SNP range past the end (also one whose end wraps around 2^64) and an
+    """A SNP range past the end (also one whose end overflows 64 bits) and an
     unknown normalisation are argument errors, not device accesses."""
     sg = _sg()
     c = simdata.simulate(40, 50, seed=5)
