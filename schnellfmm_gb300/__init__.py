@@ -846,19 +846,52 @@ class OutputConfig:
     format: OutputFormat = OutputFormat.TSV
 
 
+class _CStrings:
+    """Strings as one NUL-separated UTF-8 buffer and a char* per string (the
+    buffer lives as long as this object)."""
+
+    def __init__(self, strs: Sequence[str]):
+        strs = list(strs)
+        self.blob = np.frombuffer(("\0".join(strs) + "\0").encode(), dtype=np.uint8)
+        ends = np.flatnonzero(self.blob == 0)
+        if strs and ends.size != len(strs):
+            raise SchnelGpuError(ERR_BAD_ARG, "a name contains a NUL character")
+        self.ptrs = np.zeros(max(len(strs), 1), dtype=np.uint64)
+        if strs:
+            self.ptrs[1:] = ends[:-1] + 1
+            self.ptrs += np.uint64(self.blob.ctypes.data)
+
+    def arg(self):
+        return self.ptrs.ctypes.data_as(C.POINTER(C.c_char_p))
+
+
+def _output_args(bim: Sequence[BimRecord], cov_names: Sequence[str], res: TestResults):
+    """The writers' arguments: per-SNP names, positions, covariate names and
+    the result columns as contiguous FP64, checked against each other."""
+    p, d = res.beta.shape
+    if len(bim) != p or len(cov_names) != d:
+        raise SchnelGpuError(ERR_BAD_ARG, "bim must have one record per SNP and cov_names one name per trait")
+    cols = {k: np.ascontiguousarray(getattr(res, k), dtype=np.float64) for k in ("beta", "tstat", "pvalue", "r2")}
+    for k, shape in (("beta", (p, d)), ("tstat", (p, d)), ("pvalue", (p, d)), ("r2", (p, 3))):
+        if cols[k].shape != shape:
+            raise SchnelGpuError(ERR_BAD_ARG, f"{k} has shape {cols[k].shape}, expected {shape}")
+    chrom = _CStrings(b.chrom for b in bim)
+    sid = _CStrings(b.snp_id for b in bim)
+    names = _CStrings(cov_names)
+    pos = np.ascontiguousarray([b.pos for b in bim] or [0], dtype=np.uint64)
+    r = _Results(None, _dptr(cols["beta"]), _dptr(cols["tstat"]), _dptr(cols["pvalue"]), _dptr(cols["r2"]), None,
+                 res.gif, None, 0.0, 0.0, 0.0, 0)
+    keep = (cols, chrom, sid, names, pos)
+    return p, d, chrom.arg(), pos.ctypes.data_as(C.POINTER(C.c_uint64)), sid.arg(), names.arg(), r, keep
+
+
 def write_tsv(path: os.PathLike, bim: Sequence[BimRecord], cov_names: Sequence[str], res: TestResults,
               n_threads: int = 0) -> None:
+    """<out>.tsv as coalesce_output_tsv (src/testing.rs:740-801)."""
     lib = load_library()
-    p, d = res.beta.shape
-    enc = lambda xs: (C.c_char_p * len(xs))(*[s.encode() for s in xs])
-    chrom = enc([b.chrom for b in bim])
-    sid = enc([b.snp_id for b in bim])
-    pos = np.ascontiguousarray([b.pos for b in bim], dtype=np.uint64)
-    names = enc(list(cov_names))
-    r = _Results(None, _dptr(res.beta), _dptr(res.tstat), _dptr(res.pvalue), _dptr(res.r2), None, res.gif, None,
-                 0.0, 0.0, 0.0, 0)
-    rc = lib.slfmm_write_tsv(str(path).encode(), p, d, chrom, pos.ctypes.data_as(C.POINTER(C.c_uint64)), sid,
-                             names, C.byref(r), n_threads)
+    p, d, chrom, pos, sid, names, r, keep = _output_args(bim, cov_names, res)
+    rc = lib.slfmm_write_tsv(str(path).encode(), p, d, chrom, pos, sid, names, C.byref(r), n_threads)
+    del keep
     if rc != OK:
         raise SchnelGpuError(rc, f"Failed to create {path}")
 
@@ -873,19 +906,9 @@ def write_parquet(path: os.PathLike, bim: Sequence[BimRecord], cov_names: Sequen
     chr, pos, snp_id, p_*, beta_*, t_*, r2_cov, r2_latent, r2_resid; rows in
     SNP order; ZSTD (the reference's codec) or uncompressed."""
     lib = load_library()
-    p, d = res.beta.shape
-    if len(bim) != p or len(cov_names) != d:
-        raise SchnelGpuError(ERR_BAD_ARG, "bim must have one record per SNP and cov_names one name per trait")
-    enc = lambda xs: (C.c_char_p * max(len(xs), 1))(*[s.encode() for s in xs])
-    chrom = enc([b.chrom for b in bim])
-    sid = enc([b.snp_id for b in bim])
-    pos = np.ascontiguousarray([b.pos for b in bim], dtype=np.uint64)
-    names = enc(list(cov_names))
-    cols = {k: np.ascontiguousarray(getattr(res, k), dtype=np.float64) for k in ("beta", "tstat", "pvalue", "r2")}
-    r = _Results(None, _dptr(cols["beta"]), _dptr(cols["tstat"]), _dptr(cols["pvalue"]), _dptr(cols["r2"]), None,
-                 res.gif, None, 0.0, 0.0, 0.0, 0)
-    rc = lib.slfmm_write_parquet(str(path).encode(), p, d, chrom, pos.ctypes.data_as(C.POINTER(C.c_uint64)), sid,
-                                 names, C.byref(r), compression, n_threads)
+    p, d, chrom, pos, sid, names, r, keep = _output_args(bim, cov_names, res)
+    rc = lib.slfmm_write_parquet(str(path).encode(), p, d, chrom, pos, sid, names, C.byref(r), compression, n_threads)
+    del keep
     if rc != OK:
         raise SchnelGpuError(rc, f"Failed to create {path}")
 
