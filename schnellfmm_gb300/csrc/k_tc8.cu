@@ -13,10 +13,8 @@
 // second set of terms, which makes the mean-imputation correction of missing
 // calls exact without any gather over the missing-call lists.
 //
-// W tiles are shared by the CTAs of a cluster through TMA multicast: each of
-// the C CTAs loads 1/C of the rows of every W stage into all C CTAs.  A stage
-// is reloaded only after every CTA of the cluster has finished its MMAs on it
-// (per-stage "B empty" barriers counting C multicast commits).
+// Every CTA streams its own W stages with TMA; a stage is reloaded only after
+// the CTA's MMAs on it have completed (per-stage "B empty" barriers).
 //
 // Replaces the reference's per-chunk FP64 dgemms (src/rsvd.rs:61-69, :88-97,
 // :117-125, :144-153; src/testing.rs:355-374) and, through the indicator
@@ -65,7 +63,6 @@ struct Tc8Args {
     uint32_t usets;         // unpack sets in use: at most `stages`, so that a set never waits on a stage
                             // two uses ahead (an mbarrier parity wait cannot tell those apart)
     uint32_t b_stage_bytes; // n_total * 128
-    uint32_t cluster;       // CTAs sharing W through multicast
     uint32_t box_rows;      // rows per W TMA box
     uint32_t loads;         // W boxes this CTA issues per stage
     const float* inv_scale; // n_total: 2^-(e0 + 4t) per B row
@@ -130,7 +127,7 @@ struct Ring {
 template <int NCH, bool MAIN, bool IND, int G>
 __device__ __forceinline__ void tc8_mma_loop(const Tc8Args& a, uint32_t tmem, uint32_t d_main, uint32_t bsm_addr,
                                              uint64_t* full_b, uint64_t* full_a, uint64_t* a_empty,
-                                             uint64_t* b_empty, uint32_t nkb, uint16_t mask, uint32_t start,
+                                             uint64_t* b_empty, uint32_t nkb, uint32_t start,
                                              uint32_t len0, uint32_t skip) {
     const uint32_t S = a.stages;
     const uint32_t chunk = a.n_main / NCH;
@@ -174,8 +171,7 @@ __device__ __forceinline__ void tc8_mma_loop(const Tc8Args& a, uint32_t tmem, ui
                     if (IND) mma_ts_f8(d_ind, ad + kStageK / 4 + kk * 8, bk + indoff, id_ind, acc);
                 }
                 mma_commit(a_empty + st.slot);
-                if (mask != 1) mma_commit_mc(b_empty + st.slot, mask);
-                else mma_commit(b_empty + st.slot);
+                mma_commit(b_empty + st.slot);
                 st.advance(1, S);
             }
         }
@@ -188,16 +184,16 @@ __device__ __forceinline__ void tc8_mma_loop(const Tc8Args& a, uint32_t tmem, ui
 template <int NCH, bool MAIN, bool IND>
 __device__ __forceinline__ void tc8_mma_dispatch(const Tc8Args& a, uint32_t tmem, uint32_t d_main, uint32_t bsm_addr,
                                                  uint64_t* full_b, uint64_t* full_a, uint64_t* a_empty,
-                                                 uint64_t* b_empty, uint32_t nkb, uint16_t mask, uint32_t start,
+                                                 uint64_t* b_empty, uint32_t nkb, uint32_t start,
                                                  uint32_t len0, uint32_t skip) {
     if (a.group == 4)
-        tc8_mma_loop<NCH, MAIN, IND, 4>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty, nkb, mask, start,
+        tc8_mma_loop<NCH, MAIN, IND, 4>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty, nkb,start,
                                         len0, skip);
     else if (a.group == 2)
-        tc8_mma_loop<NCH, MAIN, IND, 2>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty, nkb, mask, start,
+        tc8_mma_loop<NCH, MAIN, IND, 2>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty, nkb,start,
                                         len0, skip);
     else
-        tc8_mma_loop<NCH, MAIN, IND, 1>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty, nkb, mask, start,
+        tc8_mma_loop<NCH, MAIN, IND, 1>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty, nkb,start,
                                         len0, skip);
 }
 
@@ -213,16 +209,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     uint64_t* full_b = bars;                 // [S] W tile landed (TMA tx)
     uint64_t* full_a = bars + S;             // [S] A operand written to TMEM (128 arrivals)
     uint64_t* a_empty = bars + 2 * S;        // [S] own MMAs on the stage done
-    uint64_t* b_empty = bars + 3 * S;        // [S] MMAs of every cluster CTA on the stage done
+    uint64_t* b_empty = bars + 3 * S;        // [S] every MMA warp's MMAs on the W stage done
     uint64_t* p_full = bars + 4 * S;         // [P] packed codes landed (TMA tx)
     uint64_t* p_empty = bars + 4 * S + P;    // [P] packed codes consumed (4 warp arrivals)
     uint64_t* tmem_full = bars + 4 * S + 2 * P;
     uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(tmem_full + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t C = a.cluster;
-    const uint32_t rank = C > 1 ? cluster_ctarank() : 0;
-    const uint16_t mask = (uint16_t)((1u << C) - 1u);
     const uint32_t row0 = blockIdx.x * kM;
     const uint32_t kb0 = blockIdx.y * a.kb_per_split;
     const uint32_t kb1 = min(a.kb_total, kb0 + a.kb_per_split);
@@ -234,7 +227,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             mbar_init(full_b + s, 1);
             mbar_init(full_a + s, 4);     // one arrival per unpack warp
             mbar_init(a_empty + s, a.nsplit ? 2 : 1);   // every MMA warp that reads the stage commits
-            mbar_init(b_empty + s, a.nsplit ? 2 * C : C);
+            mbar_init(b_empty + s, a.nsplit ? 2 : 1);
         }
         for (uint32_t p = 0; p < P; ++p) {
             mbar_init(p_full + p, 1);
@@ -253,7 +246,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     fence_before();
     __syncthreads();
     fence_after();
-    cluster_sync();  // every peer's barriers exist before any multicast lands
     const uint32_t tmem = *tmem_holder;
 
     if (warp == 0) {
@@ -277,8 +269,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         // each spinning role has a warp of its own: lanes of one warp that
         // spin in different loops starve each other
         if (lane == 0) {
-            // W producer: this CTA's share of every W stage, multicast to the cluster
-            const uint32_t y_begin = rank * a.box_rows * a.loads;
+            // W producer: every W stage in boxes of box_rows rows
             Ring wr{0, 0};
             uint32_t issued = 0;
             for (uint32_t i = 0; i < nkb; ++i) {
@@ -287,11 +278,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                 const int kb = (int)(kb0 + i);
                 for (int h = 0; h < kHalves; ++h)
                     for (uint32_t l = 0; l < a.loads; ++l) {
-                        const uint32_t y = y_begin + l * a.box_rows;
+                        const uint32_t y = l * a.box_rows;
                         uint8_t* dst = bsm + wr.slot * a.b_stage_bytes + (h * a.n_total + y) * 128;
                         const int x = kb * kStageK + h * kTileK;
-                        if (C > 1) tma_2d_mc(dst, &tm_b, x, (int)y, full_b + wr.slot, mask);
-                        else tma_2d(dst, &tm_b, x, (int)y, full_b + wr.slot);
+                        tma_2d(dst, &tm_b, x, (int)y, full_b + wr.slot);
                     }
                 issued = i + 1;
                 wr.advance(1, S);
@@ -310,39 +300,39 @@ __global__ void __launch_bounds__(kThreads, 1)
                 if (m == 0) {
                     if (nch == 1)
                         tc8_mma_dispatch<1, true, false>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty,
-                                                         nkb, mask, 0, G, 0);
+                                                         nkb,0, G, 0);
                     else
                         tc8_mma_dispatch<2, true, false>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty,
-                                                         nkb, mask, 0, G, 0);
+                                                         nkb,0, G, 0);
                 } else {
                     tc8_mma_dispatch<1, false, true>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty, nkb,
-                                                     mask, 0, G > 1 ? G / 2 : 1, 0);
+                                                     0, G > 1 ? G / 2 : 1, 0);
                 }
             } else if (a.kcopies == 2) {
                 // alternate groups of G K blocks into accumulator copies m
                 const uint32_t d_main = tmem + m * a.d_cols;
                 if (nch == 1)
                     tc8_mma_dispatch<1, true, false>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty,
-                                                     nkb, mask, m * G, G, G);
+                                                     nkb,m * G, G, G);
                 else
                     tc8_mma_dispatch<2, true, false>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty,
-                                                     nkb, mask, m * G, G, G);
+                                                     nkb,m * G, G, G);
             } else if (m == 0) {
                 // one MMA warp does everything
                 if (nch == 1) {
                     if (ind)
                         tc8_mma_dispatch<1, true, true>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty,
-                                                        nkb, mask, 0, G, 0);
+                                                        nkb,0, G, 0);
                     else
                         tc8_mma_dispatch<1, true, false>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty,
-                                                         nkb, mask, 0, G, 0);
+                                                         nkb,0, G, 0);
                 } else {
                     if (ind)
                         tc8_mma_dispatch<2, true, true>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty,
-                                                        nkb, mask, 0, G, 0);
+                                                        nkb,0, G, 0);
                     else
                         tc8_mma_dispatch<2, true, false>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty,
-                                                         nkb, mask, 0, G, 0);
+                                                         nkb,0, G, 0);
                 }
             }
             mma_commit(tmem_full);  // both MMA warps arrive (an idle one at once)
@@ -476,7 +466,6 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     fence_before();
     __syncthreads();
-    cluster_sync();  // no peer multicasts or commits into this CTA after this point
     if (warp == 1) {
         fence_after();
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(a.tmem_cols)
@@ -778,7 +767,7 @@ CUtensorMap map2d_u8(const uint8_t* base, uint64_t inner, uint64_t rows, uint32_
 
 }  // namespace
 
-// Tuning overrides (autotuner / experiments): SLFMM_TC8_CLUSTER, _STAGES, _PSTAGES.
+// Tuning overrides (autotuner / experiments): SLFMM_TC8_STAGES, _PSTAGES, _GROUP.
 static int env_int(const char* name, int dflt) {
     const char* v = std::getenv(name);
     return v && *v ? std::atoi(v) : dflt;
@@ -826,15 +815,8 @@ Fp8Plan fp8_plan_knobs(int wpad, bool ind, uint64_t tiles, int pmax_in, int smax
         }
     p.stages -= p.stages % p.group;
     p.smem = fixed + (size_t)p.pstages * kStageBytes + (size_t)p.stages * p.b_stage_bytes;
-    // cluster multicast of W when there are enough tiles and rows split evenly
-    p.cluster = 1;
-    const uint32_t cmax = (uint32_t)env_int("SLFMM_TC8_CLUSTER", 1);  // co-scheduling a cluster idles SMs: off by default
-    for (uint32_t c : {8u, 4u, 2u})
-        if (c <= cmax && tiles >= 2 * c && p.n_total % (8 * c) == 0) {
-            p.cluster = c;
-            break;
-        }
-    const uint32_t rows_mine = p.n_total / p.cluster;
+    (void)tiles;
+    const uint32_t rows_mine = p.n_total;
     p.loads = (uint32_t)ceil_div(rows_mine, 256);
     while (rows_mine % p.loads != 0 || (rows_mine / p.loads) % 8 != 0) ++p.loads;
     p.box_rows = rows_mine / p.loads;
@@ -1187,7 +1169,7 @@ int launch_tc8_rows(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t rows
                     const uint8_t* B, const float* inv_scale, uint64_t K_pad, int mode, const double* row_mean,
                     const double* row_scale, const double* cs, float* out, int ldo, int splits,
                     uint64_t split_stride, int* err_dev) {
-    if (c.autotune && pl.ok && pl.cluster == 1 && rows > 0) {
+    if (c.autotune && pl.ok && rows > 0) {
         const Fp8Plan tp = tc8_tuned_plan(c, pl, tv, rows, K, B, inv_scale, K_pad, mode, row_mean, row_scale, cs, ldo,
                                           splits, split_stride);
         if (tp.ok) return tc8_launch(c, tp, tv, rows, K, B, inv_scale, K_pad, mode, row_mean, row_scale, cs, out, ldo,
@@ -1206,7 +1188,7 @@ static int tc8_launch(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t ro
                   "bad K padding");
     SLFMM_REQUIRE(tv.base && tv.kbt % kHalves == 0 && tv.kbt >= ceil_div(K, kStageK) * kHalves, SLFMM_ERR_BAD_ARG,
                   "tile-major operand too short in K");
-    SLFMM_REQUIRE(tv.ntiles >= round_up(ceil_div(rows, kM), pl.cluster), SLFMM_ERR_BAD_ARG,
+    SLFMM_REQUIRE(tv.ntiles >= ceil_div(rows, kM), SLFMM_ERR_BAD_ARG,
                   "tile-major operand has too few tiles");
     SLFMM_REQUIRE(mode == 0 || pl.n_ind != 0, SLFMM_ERR_BAD_ARG, "row correction needs the indicator operand");
     raise_dynamic_smem((const void*)k_tc8_rows, pl.smem);
@@ -1235,7 +1217,6 @@ static int tc8_launch(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t ro
     a.usets = std::min<uint32_t>(kUnpackSets, std::min(pl.stages, pl.pstages));
     a.tmem_cols = pl.tmem_cols;
     a.b_stage_bytes = pl.b_stage_bytes;
-    a.cluster = pl.cluster;
     a.box_rows = pl.box_rows;
     a.loads = pl.loads;
     a.inv_scale = inv_scale;
@@ -1250,19 +1231,12 @@ static int tc8_launch(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t ro
     a.tile_bytes = tv.kbt * (uint64_t)kTileBytes;
     a.err = err_dev ? err_dev : err.get();
     const unsigned gy = (unsigned)ceil_div(a.kb_total, a.kb_per_split);
-    const unsigned gx = (unsigned)round_up(ceil_div(rows, kM), pl.cluster);
+    const unsigned gx = (unsigned)ceil_div(rows, kM);
     cudaLaunchConfig_t cfg{};
     cfg.gridDim = dim3(gx, gy, 1);
     cfg.blockDim = dim3(kThreads, 1, 1);
     cfg.dynamicSmemBytes = pl.smem;
     cfg.stream = c.stream;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = pl.cluster;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
     const cudaError_t le = cudaLaunchKernelEx(&cfg, k_tc8_rows, tb, a);
     if (le != cudaSuccess) {
         cudaGetLastError();

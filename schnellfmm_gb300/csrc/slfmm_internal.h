@@ -268,11 +268,11 @@ void launch_weighted_colsum(Ctx& c, const float* Q, int ldq, uint64_t p, int w, 
 void launch_scale_product(Ctx& c, const double* a, const double* b, uint64_t n, double* out);
 
 // k_tc8.cu : split-FP8 tcgen05 contractions with optional missing-call
-// indicator operand and cluster-multicast W tiles
+// indicator operand
 struct Fp8Plan {
     uint32_t wpad, n_main, n_ind, n_total, d_cols, a_cols, stages, pstages, group, tmem_cols, b_stage_bytes;
     uint32_t kcopies, nsplit, a_base;
-    uint32_t cluster, box_rows, loads;
+    uint32_t box_rows, loads;
     size_t smem;
     bool ok;
 };
