@@ -350,6 +350,151 @@ def run_many(args, w):
             "clocks": clk.summary()}
 
 
+def _compare(res_t, res_beta, res_r2, ref) -> dict:
+    """Per-SNP agreement of GPU results with an oracle AssocResults."""
+    scale = float(np.abs(ref.beta).max()) or 1.0
+    return {"max_abs_dt": float(np.abs(res_t - ref.tstat).max()),
+            "max_abs_dbeta_over_max_beta": float(np.abs(res_beta - ref.beta).max() / scale),
+            "max_abs_dr2": float(np.abs(res_r2 - ref.r2).max())}
+
+
+def _top_overlap(t_gpu: np.ndarray, t_ref: np.ndarray, top: int = 100) -> float:
+    """Smallest share, over traits, of the oracle's top-`top` |t| SNPs that
+    are also in the GPU's top `top`."""
+    worst = 1.0
+    for j in range(t_ref.shape[1]):
+        a = set(np.argsort(-np.abs(t_ref[:, j]))[:top].tolist())
+        b = set(np.argsort(-np.abs(t_gpu[:, j]))[:top].tolist())
+        worst = min(worst, len(a & b) / float(top))
+    return worst
+
+
+def link_probe(host_u8: np.ndarray, stream) -> dict:
+    """Page-locked host<->device copy rates of this machine: 2 GB of the pinned
+    payload to the device and back, as one copy each (CUDA events)."""
+    import torch
+    nbytes = int(min(host_u8.nbytes, 2 << 30))
+    src = torch.from_numpy(host_u8.reshape(-1)[:nbytes])
+    dev = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    out = {}
+    for name, fn in (("h2d_gbs", lambda: dev.copy_(src, non_blocking=True)),
+                     ("d2h_gbs", lambda: src.copy_(dev, non_blocking=True))):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[name] = nbytes / (e0.elapsed_time(e1) / 1e3) / 1e9
+    del dev
+    return out
+
+
+def run_to_tsv(args, sg, eng, host_packed, n, x, cfg, est, out, p, d) -> dict:
+    """The end-to-end path to the reference's output file: slfmm_fit_host
+    from the page-locked payload, then <out>.tsv written and closed on local
+    disk (coalesce_output_tsv's layout and "{:.6e}" numbers).  The .bim names
+    are marshalled once, before timing; the file is deleted afterwards."""
+    import ctypes
+    import tempfile
+    lib = sg.load_library()
+    chrom = sg._CStrings(str(1 + j // 100_000) for j in range(p))
+    sid = sg._CStrings(f"rs{j}" for j in range(p))
+    names = sg._CStrings(f"trait{j}" for j in range(d))
+    pos = np.ascontiguousarray(1000 + 10 * np.arange(p, dtype=np.uint64))
+    r = sg._Results(None, sg._dptr(out["beta"]), sg._dptr(out["tstat"]), sg._dptr(out["pvalue"]),
+                    sg._dptr(out["r2"]), None, 0.0, None, 0.0, 0.0, 0.0, 0)
+    fd, path = tempfile.mkstemp(suffix=".tsv")
+    os.close(fd)
+    fit_ms, write_ms, size = [], [], 0
+    try:
+        for _ in range(args.tsv_steps):
+            t0 = time.perf_counter()
+            sg.fit_lfmm2_host(host_packed, n, x, cfg, est_subset=est, engine=eng, out=out)
+            t1 = time.perf_counter()
+            rc = lib.slfmm_write_tsv(path.encode(), p, d, chrom.arg(), pos.ctypes.data_as(ctypes.POINTER(ctypes.c_uint64)),
+                                     sid.arg(), names.arg(), ctypes.byref(r), 0)
+            t2 = time.perf_counter()
+            if rc != 0:
+                raise RuntimeError(f"slfmm_write_tsv failed ({rc})")
+            fit_ms.append((t1 - t0) * 1e3)
+            write_ms.append((t2 - t1) * 1e3)
+        size = os.path.getsize(path)
+    finally:
+        os.remove(path)
+    total = min(a + b for a, b in zip(fit_ms, write_ms))
+    return {"value": p / (total / 1e3), "unit": "SNPs/s", "ms_per_step": total, "fit_host_ms": min(fit_ms),
+            "write_tsv_ms": min(write_ms), "tsv_bytes": int(size), "steps": args.tsv_steps,
+            "host_threads": os.cpu_count()}
+
+
+def run_parity(args, w, eng, geno_est, geno, est, host_packed, x, cfg):
+    """Accuracy of the benchmarked configuration against the FP64 oracle
+    (outside the timed region).
+
+    * ``full``: one fit of the benchmarked matrix with host outputs; the
+      oracle tests a fixed sample of 20 000 of its SNPs with the GPU's U_hat
+      (the association pass at the full n, d and K), and the GIF of all p SNPs
+      is recomputed from the GPU's t statistics by the oracle's histogram.
+    * ``slice``: the same cohort generator at p = 100 000 SNPs, fitted end to
+      end on the GPU (engine sketch stream) and by the oracle (same stream,
+      streamed from the same packed matrix): U_hat subspace, t, beta, r2, GIF,
+      top-100 overlap."""
+    import schnellfmm_gb300 as sg
+    from oracle import lfmm_oracle as O
+    t0 = time.perf_counter()
+    n, p, d, k = w["n"], w["p"], w["d"], w["k"]
+    out = {"tolerance": {"max_abs_dt": 1e-3, "sin_theta_u": 1e-3}}
+    res = sg.fit_lfmm2(geno_est, est, geno, x, cfg, engine=eng)
+    xs = O.center_covariates(x, False)
+    pre = O.precompute_thin(xs, w["lam"])
+    rs = np.random.default_rng(9)
+    idx = np.sort(rs.choice(p, size=min(p, args.parity_snps), replace=False))
+    ysub = O.PackedMatrix(np.asarray(host_packed), n, O.NORM_EIGENSTRAT, snps=idx)
+    ref = O.assoc_oracle64_packed(ysub, xs, res.u_hat, pre.ridge_inv)
+    full = _compare(res.tstat[idx], res.beta[idx], res.r2[idx], ref)
+    hist = O.TsqHistogram(d)
+    for s in range(0, p, 1 << 18):
+        hist.add_chunk(res.tstat[s:s + (1 << 18)])
+    gif_per, gif = hist.compute_gif()
+    full.update({"snps_checked": int(len(idx)), "gif_gpu": float(res.gif), "gif_oracle_histogram": gif,
+                 "max_abs_dgif_per_trait": float(np.abs(np.asarray(res.gif_per_trait) - gif_per).max())})
+    out["full"] = full
+    del res
+    if w.get("nmf") is None and args.parity_slice_snps > 0:
+        ps = args.parity_slice_snps
+        rng = np.random.default_rng(300)
+        q = rng.dirichlet(np.full(w["n_pop"], w["alpha"]), size=n).astype(np.float32)
+        xsl = make_covariates(n, d, q.astype(np.float64), w["mask_max"], 17)
+        g2 = eng.simulate(q, ps, fst=w["fst"], f_lo=w["f_lo"], f_hi=w["f_hi"], miss=w["miss"],
+                          inbreeding=w["inbreeding"], seed=4242)
+        pk = np.empty((ps, (n + 3) // 4), dtype=np.uint8)
+        g2.download(pk)
+        est_idx = O.subset_indices(ps, rate=w["est_rate"]) if w["est_rate"] else None
+        g2e = eng.upload(pk, n, snps=sg.SubsetSpec.from_rate(w["est_rate"])) if w["est_rate"] else g2
+        r2 = sg.fit_lfmm2(g2e, sg.SubsetSpec.all(), g2, xsl, cfg, engine=eng)
+        l = k + w["oversampling"]
+        omega = O.sketch_normal(args.rng, cfg.seed, n, l)
+        ref2 = O.fit_oracle64_packed(pk, n, xsl, k=k, lam=w["lam"], oversampling=w["oversampling"],
+                                     power_iter=w["power_iter"], norm=O.NORM_EIGENSTRAT, omega=omega,
+                                     est_snps=est_idx)
+        sl = _compare(r2.tstat, r2.beta, r2.r2, ref2.assoc)
+        sl.update({"workload": f"n={n} p={ps} K={k} d={d} (same generator, seed 4242)",
+                   "sin_theta_u": O.principal_angles_sin_max(r2.u_hat, ref2.u_hat),
+                   "gif_gpu": float(r2.gif), "gif_oracle": float(ref2.assoc.gif),
+                   "top100_overlap_min_over_traits": _top_overlap(r2.tstat, ref2.assoc.tstat)})
+        out["slice"] = sl
+        if g2e is not g2:
+            g2e.free()
+        g2.free()
+    worst_dt = max(out["full"]["max_abs_dt"], out.get("slice", {}).get("max_abs_dt", 0.0))
+    out["max_abs_dt"] = worst_dt
+    out["within_tolerance"] = bool(worst_dt <= 1e-3 and out.get("slice", {}).get("sin_theta_u", 0.0) < 1e-3)
+    out["oracle_seconds"] = time.perf_counter() - t0
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -364,8 +509,14 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--out", default=None, help="also write the JSON line to this file")
     ap.add_argument("--autotune", action="store_true", help="let the engine tune its ring depths (warm-up does it)")
-    ap.add_argument("--rng", choices=["counter", "chacha8"], default="counter",
-                    help="random streams of the sketches and CV masks (chacha8: the reference's)")
+    ap.add_argument("--rng", choices=["counter", "chacha8"], default="chacha8",
+                    help="random streams of the sketches and CV masks (chacha8: the reference's, the default)")
+    ap.add_argument("--no-parity", action="store_true", help="skip the accuracy check against the FP64 oracle")
+    ap.add_argument("--tsv-steps", type=int, default=1,
+                    help="end-to-end steps that also write <out>.tsv to local disk (0: none)")
+    ap.add_argument("--parity-snps", type=int, default=20_000, help="SNPs of the full fit checked by the oracle")
+    ap.add_argument("--parity-slice-snps", type=int, default=100_000,
+                    help="SNPs of the separately fitted slice checked end to end (0: none)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -502,12 +653,26 @@ def main():
         h2d = p * bps + (int(p * (w["est_rate"] or 0) + 1) * bps if w["est_rate"] else 0) + x.nbytes
         d2h = sum(a.nbytes for a in out.values())
         e2e = {"value": job_rate(p, world, e2e_ms), "unit": "SNPs/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms}
+               "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
+               "per_step_ms": [e0.elapsed_time(e1) / args.steps, wall]}
+        # where one call's time goes (after the timed loop): device time per
+        # phase from events on the engine's stream, host wall time per phase,
+        # and this box's page-locked copy rates
+        eng.profile(True)
+        t0 = time.perf_counter()
+        sg.fit_lfmm2_host(host_packed, n, x, cfg, est_subset=est, engine=eng, out=out)
+        e2e["one_call_wall_ms"] = (time.perf_counter() - t0) * 1e3
+        e2e["phases_of_one_call"] = eng.phases()
+        eng.profile(False)
+        e2e["link_probe"] = link_probe(host_packed, torch_stream)
+        if args.tsv_steps > 0:
+            e2e["to_tsv"] = run_to_tsv(args, sg, eng, host_packed, n, x, cfg, est, out, p, d)
 
     # ---- plain FP32 GPU path, same resident inputs ----
     fp32 = None
     if not args.no_fp32_path and prec != sg.Precision.FP32:
-        eng32 = sg.Engine(dev, sg.Precision.FP32, stream=torch_stream.cuda_stream)
+        eng32 = sg.Engine(dev, sg.Precision.FP32, stream=torch_stream.cuda_stream,
+                          rng=sg.SketchRng.CHACHA8 if args.rng == "chacha8" else sg.SketchRng.COUNTER)
         _fit_device_only(eng32)
         barrier()
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -520,6 +685,19 @@ def main():
         ms32 = maxover(f0.elapsed_time(f1) / reps)
         fp32 = {"value": job_rate(p, world, ms32), "unit": "SNPs/s", "ms_per_step": ms32,
                 "speedup_of_headline": ms32 / ms_step}
+        if e2e is not None:
+            # the same host-to-host call on the FP32 engine
+            sg.fit_lfmm2_host(host_packed, n, x, cfg, est_subset=est, engine=eng32, out=out)
+            barrier()
+            t0 = time.perf_counter()
+            f0.record(torch_stream)
+            for _ in range(reps):
+                sg.fit_lfmm2_host(host_packed, n, x, cfg, est_subset=est, engine=eng32, out=out)
+            f1.record(torch_stream)
+            barrier()
+            ms32e = maxover(max(f0.elapsed_time(f1) / reps, (time.perf_counter() - t0) * 1e3 / reps))
+            fp32["e2e"] = {"value": job_rate(p, world, ms32e), "unit": "SNPs/s", "ms_per_step": ms32e}
+            fp32["e2e_speedup_of_headline"] = ms32e / e2e["ms_per_step"]
         eng32.close()
 
     # ---- roofline of the dominant kernel class ----
@@ -548,8 +726,15 @@ def main():
                          f"restatement of the reference (numpy FP64), extrapolated to p={p}",
                "extrapolated_total_s": info["extrapolated_total_s"]}
 
+    parity = None
+    if rank == 0 and not args.no_parity:
+        parity = run_parity(args, w, eng, geno_est, geno, est, host_packed, x, cfg)
+
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": "SNPs/s", "n_gpus": world, "steps": args.steps,
+        line = {"metric": METRIC, "value": value,
+                "value_kind": "resident: packed genotypes already in HBM when the timed region starts "
+                              "(the host-to-host number through the C ABI is e2e)",
+                "unit": "SNPs/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms_step,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": {sg.Precision.SPLIT_FP8: "e4m3x4 split (exact e4m3 genotypes, fp32 accumulate)",
@@ -557,7 +742,7 @@ def main():
                           sg.Precision.FP32: "fp32"}[prec],
                 "data": "synthetic (seeded structured cohort drawn on the device)",
                 "config": config, "e2e": e2e, "gpu_launches": int(launches), "roofline": roof,
-                "cpu_baseline": cpu, "fp32_gpu_path": fp32, "clocks": clk.summary()}
+                "cpu_baseline": cpu, "fp32_gpu_path": fp32, "parity": parity, "clocks": clk.summary()}
         s = json.dumps(line)
         print(s)
         if args.out:

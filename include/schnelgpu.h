@@ -56,14 +56,14 @@ extern "C" {
 /* Stream the Gaussian sketches (Omega of src/rsvd.rs:44-46, the NMF probe of
  * src/nmf.rs:291-293) and the NMF CV hold-out masks (src/nmf.rs:433-448,
  * src/testing.rs:437-452) are drawn from. */
-#define SLFMM_RNG_COUNTER      0      /* SplitMix64 counter streams, drawn on the
-                                         device (default)                        */
-#define SLFMM_RNG_CHACHA8      1      /* the reference's streams:
+#define SLFMM_RNG_CHACHA8      0      /* the reference's streams (default):
                                          ChaCha8Rng::seed_from_u64(seed) sampled
                                          by Normal(0, 1) in row-major order for
-                                         the sketches (on the host) and by
+                                         the sketches (on the host threads) and by
                                          Uniform(0, 1) for the masks (on the
                                          device)                                 */
+#define SLFMM_RNG_COUNTER      1      /* SplitMix64 counter streams, drawn on the
+                                         device                                  */
 
 #define SLFMM_SUBSET_ALL       0      /* SubsetSpec::All     (src/bed.rs:50-57)  */
 #define SLFMM_SUBSET_RATE      1      /* SubsetSpec::Rate(r)                     */
@@ -270,6 +270,24 @@ int slfmm_host_free(void* p);
 int slfmm_profile_enable(slfmm_ctx* ctx, int on);
 int slfmm_profile_read(slfmm_ctx* ctx, const char* kernel, double* total_ms, uint64_t* launches,
                        double* algo_bytes, double* algo_flops);
+/* Phases of the last fit run while profiling is on (slfmm_fit_host: upload
+ * with the sketch pass, randomized SVD, association design, row pass and
+ * statistics, GIF, results to host).  Each phase has its device time
+ * (events on the context's stream, recorded without synchronising) and
+ * the host wall time between its marks.  slfmm_phase_count returns the
+ * number of phases; slfmm_phase_read fills phase i (0-based). */
+int slfmm_phase_count(const slfmm_ctx* ctx);
+int slfmm_phase_read(slfmm_ctx* ctx, int i, char* name, size_t name_len, double* device_ms, double* host_ms);
+
+/* ---- failure-detection test hook ---------------------------------------- */
+/* The next split-FP8 contraction this context launches starts with a wait
+ * on a barrier that nothing completes, bounded by `cycles` SM cycles
+ * (1 .. 8e9), before it issues any copy or MMA: the wait expires, the kernel
+ * frees its tensor memory and returns, and the call that launched it fails
+ * with SLFMM_ERR_DEVICE_TIMEOUT.  Later calls run normally.  Exercises the
+ * bounded-wait path of the device pipeline (no counterpart in the
+ * reference, whose CPU workers cannot stall on a device). */
+int slfmm_debug_expire_next_wait(slfmm_ctx* ctx, uint64_t cycles);
 
 /* ---- allocation-free entry point ----------------------------------------- */
 /* Raw genomic inflation factor of each trait from device-resident t
@@ -289,9 +307,12 @@ int slfmm_profile_read(slfmm_ctx* ctx, const char* kernel, double* total_ms, uin
  * device, so at most 8 traits per call (more returns SLFMM_ERR_BAD_ARG).
  * Every call on a device shares that array and zeroes the rows it uses at its
  * start: calls that overlap in time on one device (other streams, other
- * threads) race on it and must be serialised by the caller.  The first call
- * on each device looks up the array's address (cudaGetSymbolAddress) once;
- * make that first call before any stream capture begins. */
+ * threads) race on it and must be serialised by the caller.  slfmm_create
+ * does the set-up on its device: it looks up the array's address
+ * (cudaGetSymbolAddress) and loads the module of the two kernels (CUDA loads
+ * modules lazily, and a load allocates device memory for the code and the
+ * array).  So only context creation may load or allocate; a call does
+ * neither. */
 int slfmm_gif_noalloc(slfmm_ctx* ctx, const float* t_dev, uint64_t p, uint32_t d, double* gif_dev);
 
 /* ---- output (src/testing.rs:740-801, 818-983) --------------------------- */

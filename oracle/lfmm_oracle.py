@@ -32,7 +32,9 @@ compared at the subspace / statistical level.
 from __future__ import annotations
 
 import math
+import os
 from dataclasses import dataclass, field
+from pathlib import Path
 from typing import List, Optional, Sequence, Tuple
 
 import numpy as np
@@ -594,7 +596,7 @@ class TsqHistogram:
             v = t_sq[:, j]
             v = v[np.isfinite(v)]
             b = np.minimum(np.floor(v / HIST_WIDTH), HIST_BINS - 1).astype(np.int64)
-            np.add.at(self.counts[j], b, 1)
+            self.counts[j] += np.bincount(b, minlength=HIST_BINS).astype(np.uint64)
             self.total[j] += np.uint64(v.size)
 
     def median_for_trait(self, j: int) -> float:
@@ -969,6 +971,178 @@ def fit_oracle64(raw_est: np.ndarray, raw_full: np.ndarray, x: np.ndarray, *, k:
     return FitResult(u_hat, assoc, nmf_res, gwas_cv)
 
 
+# ---------------------------------------------------------------------------
+# The same thin FP64 fit streamed from the packed payload, for shapes whose
+# dense (n, p) matrix does not fit in host memory (n = 20 000 and more)
+# ---------------------------------------------------------------------------
+
+_DECODE_LIB = []
+
+
+def _decode_helper():
+    """The oracle's C decode helper (oracle/liboracle.so, built by
+    oracle/build_oracle.py) when present; the NumPy decode otherwise."""
+    if not _DECODE_LIB:
+        import ctypes
+        path = Path(__file__).resolve().parent / "liboracle.so"
+        lib = None
+        if path.exists():
+            try:
+                lib = ctypes.CDLL(str(path))
+                lib.oracle_decode_rows.restype = ctypes.c_int
+            except OSError:
+                lib = None
+        _DECODE_LIB.append(lib)
+    return _DECODE_LIB[0]
+
+
+class PackedMatrix:
+    """A PLINK payload (p, ceil(n/4)) read as standardised SNP chunks
+    (decode_single_snp, src/bed.rs:300-379, mean imputation): per-SNP mean
+    and scale come from the integer allele counts (bit-identical to the
+    reference's FP64 sums), and each code maps to (g - mean) * scale, a
+    missing call to 0."""
+
+    def __init__(self, packed: np.ndarray, n: int, norm: int, snps: Optional[np.ndarray] = None,
+                 chunk: int = 4096):
+        self.packed = np.asarray(packed, dtype=np.uint8)
+        self.n = int(n)
+        self.norm = norm
+        self.snps = np.arange(self.packed.shape[0]) if snps is None else np.asarray(snps, dtype=np.int64)
+        self.chunk = int(chunk)
+        self.p = len(self.snps)
+        self.mean = np.empty(self.p)
+        self.scale = np.empty(self.p)
+        self.counts = np.empty((self.p, 4), dtype=np.int64)
+        for s, e in self.ranges():
+            codes = unpack_codes(self.packed[self.snps[s:e]], self.n)
+            cnt = np.stack([(codes == c).sum(axis=1) for c in (0, 2, 3, 1)], axis=1)
+            self.counts[s:e] = cnt
+        c0, c1, c2 = self.counts[:, 0], self.counts[:, 1], self.counts[:, 2]
+        nobs = c0 + c1 + c2
+        s1 = c1 + 2 * c2
+        self.mean[:] = np.where(nobs > 0, s1.astype(np.float64) / np.maximum(nobs, 1).astype(np.float64), 0.0)
+        self.scale[:] = compute_scale(self.mean, norm)
+        # ||y||^2 of each standardised column, as snp_stats
+        num = nobs * (c1 + 4 * c2) - s1 * s1
+        css = np.where(nobs > 0, num.astype(np.float64) / np.maximum(nobs, 1), 0.0)
+        self.tss = self.scale * self.scale * css
+
+    def ranges(self):
+        return [(s, min(s + self.chunk, self.p)) for s in range(0, self.p, self.chunk)]
+
+    _BYTE_CODES = ((np.arange(256)[:, None] >> (2 * np.arange(4))[None, :]) & 3).astype(np.intp)
+
+    def block(self, s: int, e: int) -> np.ndarray:
+        """Standardised SNPs [s, e) as an (n, e - s) FP64 block."""
+        lib = _decode_helper()
+        if lib is not None:
+            import ctypes
+            rows = np.ascontiguousarray(self.snps[s:e], dtype=np.int64)
+            out = np.empty((e - s, self.n))
+            mean = np.ascontiguousarray(self.mean[s:e])
+            scale = np.ascontiguousarray(self.scale[s:e])
+            vp = ctypes.c_void_p
+            rc = lib.oracle_decode_rows(self.packed.ctypes.data_as(vp), ctypes.c_uint64(self.packed.shape[1]),
+                                        rows.ctypes.data_as(vp), ctypes.c_uint64(e - s), ctypes.c_uint64(self.n),
+                                        mean.ctypes.data_as(vp), scale.ctypes.data_as(vp), out.ctypes.data_as(vp),
+                                        ctypes.c_int(os.cpu_count() or 1))
+            if rc == 0:
+                return out.T
+        m, sc = self.mean[s:e, None], self.scale[s:e, None]
+        vals = np.concatenate([(0.0 - m) * sc, np.zeros_like(m), (1.0 - m) * sc, (2.0 - m) * sc], axis=1)
+        # per SNP: the four values of each possible byte (4 samples per byte)
+        lut = vals[:, self._BYTE_CODES]                      # (c, 256, 4)
+        rows = self.packed[self.snps[s:e]]                   # (c, bps)
+        out = lut[np.arange(e - s)[:, None], rows]           # (c, bps, 4)
+        return out.reshape(e - s, -1)[:, :self.n].T
+
+    def t_mul(self, w: np.ndarray) -> np.ndarray:
+        """Y^T W (p, w)."""
+        out = np.empty((self.p, w.shape[1]))
+        for s, e in self.ranges():
+            out[s:e] = self.block(s, e).T @ w
+        return out
+
+    def mul(self, q: np.ndarray) -> np.ndarray:
+        """Y Q (n, w) for Q (p, w)."""
+        acc = np.zeros((self.n, q.shape[1]))
+        for s, e in self.ranges():
+            acc += self.block(s, e) @ q[s:e]
+        return acc
+
+
+def rsvd_thin_packed(y: PackedMatrix, pre: PrecomputedThin, k: int, l: int, q_iter: int,
+                     omega: np.ndarray) -> np.ndarray:
+    """rsvd_thin on a PackedMatrix: the same passes (src/rsvd.rs:26-177), each
+    streamed over SNP chunks."""
+    z = y.t_mul(pre.apply_p(omega))
+    q_z = _qr_q(z)
+    for _ in range(q_iter):
+        q_s = _qr_q(pre.apply_p(y.mul(q_z)))
+        q_z = _qr_q(y.t_mul(pre.apply_p(q_s)))
+    u_b, _, _ = np.linalg.svd(pre.apply_p(y.mul(q_z)), full_matrices=False)
+    return pre.apply_pinv(u_b[:, :k])
+
+
+def assoc_oracle64_packed(y: PackedMatrix, xs: np.ndarray, u_hat: np.ndarray,
+                          ridge_inv: np.ndarray) -> AssocResults:
+    """assoc_oracle64 with the SNP chunks decoded from a PackedMatrix.  Every
+    per-SNP statistic follows from T = C^T y (one FP64 product per chunk):
+    coefs = (C^T C)^-1 T; RSS = ||y||^2 - coefs^T T (= ||y - C coefs||^2 for
+    the least-squares coefs, src/testing.rs:365-371); SS_cov = (X^T y)^T
+    (X^T X)^-1 (X^T y) (:374-377); beta = R (X^T y - X^T U (U^T U)^-1 U^T y)
+    (:360-362); ||y||^2 from the SNP's allele counts (exact integers).  At
+    n = 20 000 the residual matrix of the dense form would be rebuilt for
+    every chunk; the forms are equal in exact arithmetic and agree to FP64
+    rounding (RSS keeps > 90 % of TSS in these cohorts)."""
+    n, d = xs.shape
+    k = u_hat.shape[1]
+    df = check_df(n, d, k)
+    utu_inv, _ = safe_inv(u_hat.T @ u_hat, "U_hat^T U_hat")
+    c = np.hstack([np.ones((n, 1)), xs, u_hat])
+    ctc_inv, _ = safe_inv(c.T @ c, "C^T C")
+    xtx_inv, _ = safe_inv(xs.T @ xs, "X^T X")
+    xtu = xs.T @ u_hat
+    ctc_inv_diag = np.array([ctc_inv[1 + j, 1 + j] for j in range(d)])
+    hist = TsqHistogram(d)
+    beta = np.empty((y.p, d))
+    tstat = np.empty((y.p, d))
+    r2 = np.empty((y.p, 3))
+    for s, e in y.ranges():
+        ch = y.block(s, e)
+        ct = c.T @ ch
+        coefs = ctc_inv @ ct
+        tss = y.tss[s:e]
+        rss = tss - np.einsum("ij,ij->j", coefs, ct)
+        xty = ct[1:1 + d]
+        ss_cov = np.einsum("ij,ij->j", xty, xtx_inv @ xty)
+        b = ridge_inv @ (xty - xtu @ (utu_inv @ ct[1 + d:]))
+        t, r2c = _per_snp_stats(ch, coefs, rss, ss_cov, tss, ctc_inv_diag, df, d)
+        hist.add_chunk(t)
+        beta[s:e] = b.T
+        tstat[s:e] = t
+        r2[s:e] = r2c
+    gif_per_trait, gif = hist.compute_gif()
+    return AssocResults(beta, tstat, calibrate_p(tstat, gif_per_trait), r2, gif_per_trait, gif, hist)
+
+
+def fit_oracle64_packed(packed: np.ndarray, n: int, x: np.ndarray, *, k: int, lam: float = 1e-5,
+                        oversampling: int = 10, power_iter: int = 2, norm: int = NORM_EIGENSTRAT,
+                        scale_cov: bool = False, omega: np.ndarray, est_snps: Optional[np.ndarray] = None,
+                        chunk: int = 4096) -> FitResult:
+    """fit_oracle64 (mean imputation) from a packed payload, streamed in SNP
+    chunks so that no (n, p) matrix exists; ``est_snps`` selects the
+    estimation rows (SubsetSpec)."""
+    xs = center_covariates(x, scale_cov)
+    pre = precompute_thin(xs, lam)
+    l = k + oversampling
+    y_est = PackedMatrix(packed, n, norm, est_snps, chunk)
+    u_hat = rsvd_thin_packed(y_est, pre, k, l, power_iter, omega)
+    y_full = y_est if est_snps is None else PackedMatrix(packed, n, norm, None, chunk)
+    return FitResult(u_hat, assoc_oracle64_packed(y_full, xs, u_hat, pre.ridge_inv))
+
+
 def principal_angles_sin_max(a: np.ndarray, b: np.ndarray) -> float:
     """sin of the largest principal angle between span(a) and span(b)."""
     qa, _ = np.linalg.qr(a)
@@ -980,6 +1154,14 @@ def principal_angles_sin_max(a: np.ndarray, b: np.ndarray) -> float:
 # ---------------------------------------------------------------------------
 # Output formatting  (src/testing.rs:740-801)
 # ---------------------------------------------------------------------------
+
+def rust_exp(v: float, prec: int) -> str:
+    """Rust ``format!("{:.prec$e}", v)`` of a finite value (the safe_inv
+    warning's ``{:.2e}``, src/testing.rs:1006-1009): exponent without '+' or
+    zero padding."""
+    mant, exp = ("%.*e" % (prec, v)).split("e")
+    return f"{mant}e{int(exp)}"
+
 
 def rust_lower_exp6(v: float) -> str:
     """Rust ``format!("{:.6e}", v)``: 7 significant digits, exponent without

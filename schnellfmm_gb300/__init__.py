@@ -78,9 +78,9 @@ class SketchRng(enum.IntEnum):
     src/nmf.rs:291-293) and the NMF CV hold-out masks (src/nmf.rs:433-448,
     src/testing.rs:437-452): the device counter streams, or the reference's
     ChaCha8Rng::seed_from_u64 streams (Normal(0, 1) sketches drawn on the
-    host, Uniform(0, 1) masks drawn on the device)."""
-    COUNTER = 0
-    CHACHA8 = 1
+    host threads, Uniform(0, 1) masks drawn on the device), the default."""
+    CHACHA8 = 0
+    COUNTER = 1
 
 
 # ---------------------------------------------------------------------------
@@ -126,6 +126,7 @@ EXPORTED_SYMBOLS = (
     "slfmm_fit_host", "slfmm_write_tsv", "slfmm_format_exp6", "slfmm_simulate", "slfmm_geno_download",
     "slfmm_profile_enable", "slfmm_profile_read", "slfmm_host_alloc", "slfmm_host_free", "slfmm_contract_raw",
     "slfmm_gif_noalloc", "slfmm_fit_traits", "slfmm_fit_many", "slfmm_reference_normal", "slfmm_write_parquet",
+    "slfmm_phase_count", "slfmm_phase_read", "slfmm_debug_expire_next_wait",
 )
 
 _lib_handle = None
@@ -169,6 +170,9 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
         "slfmm_geno_download": (i32, [vp, vp, vp]),
         "slfmm_profile_enable": (i32, [vp, i32]),
         "slfmm_profile_read": (i32, [vp, C.c_char_p, _dp, C.POINTER(u64), _dp, _dp]),
+        "slfmm_phase_count": (i32, [vp]),
+        "slfmm_debug_expire_next_wait": (i32, [vp, u64]),
+        "slfmm_phase_read": (i32, [vp, i32, C.c_char_p, C.c_size_t, _dp, _dp]),
         "slfmm_host_alloc": (i32, [C.c_size_t, C.POINTER(vp)]),
         "slfmm_host_free": (i32, [vp]),
         "slfmm_contract_raw": (i32, [vp, vp, i32, vp, u32, vp]),
@@ -360,7 +364,7 @@ class Engine:
     """One CUDA context + stream on one device (replaces the worker pool)."""
 
     def __init__(self, device: int = 0, precision: Precision = Precision.SPLIT_FP8, stream: Optional[int] = None,
-                 verbose: bool = False, autotune: bool = False, rng: SketchRng = SketchRng.COUNTER):
+                 verbose: bool = False, autotune: bool = False, rng: SketchRng = SketchRng.CHACHA8):
         self.lib = load_library()
         opts = _Opts(int(precision), int(verbose), C.c_void_p(stream) if stream else None, int(autotune),
                      int(rng))
@@ -434,6 +438,17 @@ class Engine:
         self.check(self.lib.slfmm_profile_read(self.h, kernel.encode(), C.byref(ms), C.byref(n), C.byref(b),
                                                C.byref(f)))
         return {"ms": ms.value, "launches": n.value, "bytes": b.value, "flops": f.value}
+
+    def phases(self) -> List[dict]:
+        """Phases of the last fit run with profiling on: name, device time
+        (events on the stream) and host wall time, in ms."""
+        out = []
+        for i in range(self.lib.slfmm_phase_count(self.h)):
+            name = C.create_string_buffer(96)
+            dev, host = C.c_double(), C.c_double()
+            self.check(self.lib.slfmm_phase_read(self.h, i, name, 96, C.byref(dev), C.byref(host)))
+            out.append({"phase": name.value.decode(), "device_ms": dev.value, "host_ms": host.value})
+        return out
 
     def generate_omega(self, seed: int, n: int, l: int) -> np.ndarray:
         out = np.empty((n, l))
@@ -654,7 +669,9 @@ def _cov_value(text: str, name: str, line: int, sample: str) -> float:
         raise SchnelGpuError(ERR_BAD_ARG, f"Failed to parse value '{t}' for covariate '{name}' on line {line} "
                                           f"(sample '{sample}')")
     if math.isinf(v):
-        raise SchnelGpuError(ERR_BAD_ARG, f"Infinite value ({t}) for covariate '{name}' on line {line} "
+        # the parsed value as Rust displays it ("inf" / "-inf"), not the input text
+        shown = "inf" if v > 0 else "-inf"
+        raise SchnelGpuError(ERR_BAD_ARG, f"Infinite value ({shown}) for covariate '{name}' on line {line} "
                                           f"(sample '{sample}'): Inf values will propagate through all matrix "
                                           f"operations")
     return v

@@ -91,13 +91,57 @@ void log(Ctx& c, const std::string& s) {
     if (c.verbose) fprintf(stderr, "[schnelgpu] %s\n", s.c_str());
 }
 
-// Verbose mode: wall time of each phase of a fit.  The stream is
-// synchronised at every mark, so a phase's time covers its device work.
+// Rust "{:.Ne}" of a finite double: C's %.*e without the exponent's sign
+// and zero padding (1.00e-8, not 1.00e-08).
+std::string rust_exp(double v, int prec) {
+    char tmp[64];
+    snprintf(tmp, sizeof tmp, "%.*e", prec, v);
+    char* e = std::strchr(tmp, 'e');
+    if (!e) return tmp;
+    *e = '\0';
+    return std::string(tmp) + "e" + std::to_string(std::atoi(e + 1));
+}
+
+// The outcome of a safe_inv-style inversion (k_inverse status: 0 inverted,
+// 1 inverted after adding eps to the diagonal, 2 failed even then), reported
+// with the reference's stderr warning and error texts (src/testing.rs:996-1024).
+void safe_inv_report(int status, double eps, const char* name) {
+    if (status == 2)
+        throw Error(SLFMM_ERR_SINGULAR,
+                    std::string(name) + " inversion failed even with epsilon=" + rust_exp(eps, 2) + " regularization");
+    if (status == 1)
+        fprintf(stderr, "Warning: %s is singular, adding epsilon=%s diagonal regularization\n", name,
+                rust_exp(eps, 2).c_str());
+}
+
+double host_now_ms() {
+    return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+void clear_phase_marks(Ctx& c) {
+    for (auto& m : c.phase_marks) cudaEventDestroy(m.ev);
+    c.phase_marks.clear();
+}
+
+// Phase marks of a fit.  With profiling on, each mark records an event on
+// the stream and the host clock (no synchronisation; slfmm_phase_read gives
+// both per phase).  Verbose mode logs the wall time of each phase, with the
+// stream synchronised at every mark so that a phase's time covers its
+// device work.
 void phase(Ctx& c, const char* what, bool start = false) {
+    if (c.profiling) {
+        if (start) clear_phase_marks(c);
+        cudaEvent_t e = nullptr;
+        if (cudaEventCreate(&e) == cudaSuccess) {
+            if (cudaEventRecord(e, c.stream) == cudaSuccess)
+                c.phase_marks.push_back({start ? std::string() : std::string(what), e, host_now_ms()});
+            else
+                cudaEventDestroy(e);
+        }
+    }
     if (!c.verbose) return;
     sync(c);
-    const double t = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch())
-                         .count();
+    const double t = host_now_ms();
     if (!start) {
         char buf[160];
         snprintf(buf, sizeof buf, "%-36s %9.2f ms", what, t - c.phase_t0);
@@ -461,7 +505,22 @@ void fp8_row_run(Ctx& c, const Geno& g, const SnpStd& s, const Fp8RowPass& rp, u
 void row_contract_base(Ctx& c, const Geno& g, const SnpStd& s, const double* W, int w, int ldw,
                        DBuf<float>& out, int& wp) {
     wp = pad16(w);
-    SLFMM_REQUIRE(wp <= kMaxW, SLFMM_ERR_BAD_ARG, "operand wider than 128 columns");
+    if (wp > kMaxW) {
+        // wider operands (association designs with many covariates): blocks
+        // of 128 columns, each contracted as above and placed in its columns
+        out.alloc(std::max<uint64_t>(g.p, 1) * wp, c.stream);
+        for (int c0 = 0; c0 < w; c0 += kMaxW) {
+            const int wb = std::min(kMaxW, w - c0);
+            DBuf<float> part;
+            int wpb = 0;
+            row_contract_base(c, g, s, W + c0, wb, ldw, part, wpb);
+            if (g.p)
+                SLFMM_CUDA(cudaMemcpy2DAsync(out.get() + c0, (size_t)wp * sizeof(float), part.get(),
+                                             (size_t)wpb * sizeof(float), (size_t)wpb * sizeof(float), g.p,
+                                             cudaMemcpyDeviceToDevice, c.stream));
+        }
+        return;
+    }
     const uint64_t n_pad = round_up(g.n, 256);  // whole split-FP8 stages (256 codes)
     out.alloc(std::max<uint64_t>(g.p, 1) * wp, c.stream);
     const double bytes = (double)g.p * ceil_div(g.n, 4) + (double)g.p * w * 4 + (double)g.n * w * 4;
@@ -664,11 +723,7 @@ void step0(Ctx& c, const double* x_host, uint64_t n, int d, double lambda, bool 
     launch_inverse(c, gl.get(), d, s.ridge_inv.get(), st.get(), eps.get());
     std::vector<double> Vh = fetch(c, V.get(), (size_t)d * d);
     std::vector<double> ev = fetch(c, sig.get(), (size_t)d);
-    const int status = fetch(c, st.get(), 1)[0];
-    if (status == 2) throw Error(SLFMM_ERR_SINGULAR, "X^T X + lambda I (ridge) inversion failed even with regularization");
-    if (status == 1)
-        fprintf(stderr, "Warning: X^T X + lambda I (ridge) is singular, adding epsilon=%.2e diagonal regularization\n",
-                fetch(c, eps.get(), 1)[0]);
+    safe_inv_report(fetch(c, st.get(), 1)[0], fetch(c, eps.get(), 1)[0], "X^T X + \u03bbI (ridge)");
     // kept directions: sigma_j^2 = eigenvalue of X^T X
     std::vector<int> keep;
     const double emax = ev.empty() ? 0.0 : ev[0];
@@ -831,13 +886,41 @@ void assoc(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, const doubl
                     "Insufficient degrees of freedom: n=" + std::to_string(n) + " samples but 1+d+K=1+" +
                         std::to_string(d) + "+" + std::to_string(K) + "=" + std::to_string(1 + d + K) +
                         ". Need n > 1 + d + K for valid t-tests. Reduce K or add more samples.");
-    SLFMM_REQUIRE(w <= kMaxSmall, SLFMM_ERR_BAD_ARG, "1 + d + K must be <= 128");
+    SLFMM_REQUIRE(w <= kMaxDesign, SLFMM_ERR_BAD_ARG,
+                  "1 + d + K must be <= " + std::to_string(kMaxDesign) + " (got " + std::to_string(w) + ")");
     const double df = (double)(n - 1 - d - K);
     // design C = [1 | X | U_hat], unit-norm columns
     DBuf<double> C(n * w, c.stream), G(w * w, c.stream);
     launch_build_design(c, s0.xs.get(), d, u_hat_dev, K, n, C.get());
     launch_atb(c, C.get(), w, C.get(), w, n, w, w, G.get());
+    // safe_inv of C^T C and X^T X (src/testing.rs:306, :316): an exactly
+    // singular matrix (a zero LU pivot, e.g. a duplicated covariate) gets
+    // eps = 1e-8 max|diag| on its diagonal, with the reference's warning.
+    // The reference then uses (C^T C + eps I)^-1.  Its limit for small eps,
+    // with N an orthonormal basis of the null space of C, is theta = the
+    // minimum-norm least-squares solution (I - N N^T) theta_any and c_jj =
+    // [(C^T C)^+]_jj + (N N^T)_jj / eps; that form is used below (applying
+    // (C^T C + eps I)^-1 directly would multiply the contraction's rounding
+    // by 1/sqrt(eps)).  RSS, SS_cov and beta depend only on span(C), which
+    // the column-dropping factorisation spans exactly.
+    double ctc_eps = 0.0;
+    {
+        DBuf<double> inv((size_t)w * w, c.stream), epsd(1, c.stream);
+        DBuf<int> sti(1, c.stream);
+        if (d > 0) {
+            DBuf<double> xtx((size_t)d * d, c.stream);
+            launch_atb(c, s0.xs.get(), d, s0.xs.get(), d, n, d, d, xtx.get());
+            launch_inverse(c, xtx.get(), d, inv.get(), sti.get(), epsd.get());
+            safe_inv_report(fetch(c, sti.get(), 1)[0], fetch(c, epsd.get(), 1)[0], "X^T X for sequential R^2");
+        }
+        launch_inverse(c, G.get(), w, inv.get(), sti.get(), epsd.get());
+        const int status = fetch(c, sti.get(), 1)[0];
+        const double eps = fetch(c, epsd.get(), 1)[0];
+        safe_inv_report(status, eps, "C^T C  where C = [1 | X | U_hat]");
+        if (status == 1) ctc_eps = eps;
+    }
     std::vector<double> Gh = fetch(c, G.get(), (size_t)w * w);
+    const std::vector<double> Graw = Gh;  // unnormalised C^T C
     std::vector<double> f(w);
     for (int k = 0; k < w; ++k) f[k] = Gh[k * w + k] > 0 ? 1.0 / std::sqrt(Gh[k * w + k]) : 0.0;
     DBuf<double> fd = upload(c, f.data(), w);
@@ -868,15 +951,77 @@ void assoc(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, const doubl
     std::vector<float> th((size_t)d * wu, 0.f), bt((size_t)d * wu, 0.f);
     std::vector<double> cjj(d, 0.0);
     std::vector<uint8_t> drop_x(d, 0);
-    for (int jj = 0; jj < d; ++jj) {
-        const int col = 1 + jj;
-        drop_x[jj] = (uint8_t)(dr[col] != 0);
-        double s = 0.0;
-        for (int k = col; k < w; ++k) {
-            th[jj * wu + (k - 1)] = (float)Li[k * w + col];
-            s += Li[k * w + col] * Li[k * w + col];
+    bool any_dropped = false;
+    for (int k = 0; k < w; ++k) any_dropped = any_dropped || dr[k] != 0;
+    if (ctc_eps > 0.0 && any_dropped) {
+        // exactly singular C^T C: the limit of the reference's regularised
+        // solve, in unnormalised coordinates (theta_i = f_i theta~_i)
+        std::vector<double> Ginv((size_t)w * w, 0.0);  // generalised inverse on the kept columns
+        for (int i = 0; i < w; ++i)
+            for (int j = 0; j < w; ++j) {
+                double acc = 0.0;
+                for (int k = std::max(i, j); k < w; ++k) acc += Li[k * w + i] * Li[k * w + j];
+                Ginv[i * w + j] = f[i] * acc * f[j];
+            }
+        // null vectors n_b = e_b - alpha, alpha = (C_K^T C_K)^-1 C_K^T c_b, one
+        // per dropped column b, orthonormalised (modified Gram-Schmidt)
+        std::vector<std::vector<double>> nv;
+        for (int b = 0; b < w; ++b) {
+            if (!dr[b]) continue;
+            std::vector<double> v(w, 0.0);
+            v[b] = 1.0;
+            for (int i = 0; i < w; ++i) {
+                if (dr[i]) continue;
+                double a = 0.0;
+                for (int j = 0; j < w; ++j)
+                    if (!dr[j]) a += Ginv[i * w + j] * Graw[j * w + b];
+                v[i] -= a;
+            }
+            for (const auto& q : nv) {
+                double dot = 0.0;
+                for (int i = 0; i < w; ++i) dot += q[i] * v[i];
+                for (int i = 0; i < w; ++i) v[i] -= dot * q[i];
+            }
+            double nn = 0.0;
+            for (int i = 0; i < w; ++i) nn += v[i] * v[i];
+            if (nn > 0.0) {
+                nn = 1.0 / std::sqrt(nn);
+                for (int i = 0; i < w; ++i) v[i] *= nn;
+                nv.push_back(std::move(v));
+            }
         }
-        cjj[jj] = s;
+        // theta = M u with M_jk = sum_i (I - N N^T)_ji f_i Li_ki
+        for (int jj = 0; jj < d; ++jj) {
+            const int j = 1 + jj;
+            std::vector<double> pj(w);
+            for (int i = 0; i < w; ++i) {
+                double nn = 0.0;
+                for (const auto& q : nv) nn += q[j] * q[i];
+                pj[i] = (i == j ? 1.0 : 0.0) - nn;
+            }
+            double s = 0.0;
+            for (int k = 0; k < w; ++k) {
+                double m = 0.0;
+                for (int i = 0; i <= k; ++i) m += pj[i] * f[i] * Li[k * w + i];
+                if (k > 0) th[jj * wu + (k - 1)] = (float)m;
+                s += m * m;
+            }
+            double njj = 0.0;
+            for (const auto& q : nv) njj += q[j] * q[j];
+            cjj[jj] = s + njj / ctc_eps;
+            drop_x[jj] = 0;
+        }
+    } else {
+        for (int jj = 0; jj < d; ++jj) {
+            const int col = 1 + jj;
+            drop_x[jj] = (uint8_t)(dr[col] != 0);
+            double s = 0.0;
+            for (int k = col; k < w; ++k) {
+                th[jj * wu + (k - 1)] = (float)Li[k * w + col];
+                s += Li[k * w + col] * Li[k * w + col];
+            }
+            cjj[jj] = s;
+        }
     }
     // beta rows: R ((I - P_U) X)^T Q_C  (src/testing.rs:285-296, 360-362)
     {
@@ -892,11 +1037,7 @@ void assoc(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, const doubl
         launch_gemm_small(c, u_hat_dev, K, n, K, M2.get(), d, d, -1.0, 1.0, F.get(), d);
         launch_atb(c, F.get(), d, QC.get(), w, n, d, w, FtQ.get());
         launch_gemm_small(c, s0.ridge_inv.get(), d, d, d, FtQ.get(), w, w, 1.0, 0.0, Bpp.get(), w);
-        const int sst = fetch(c, sti.get(), 1)[0];
-        if (sst == 2) throw Error(SLFMM_ERR_SINGULAR, "U_hat^T U_hat inversion failed even with regularization");
-        if (sst == 1)
-            fprintf(stderr, "Warning: U_hat^T U_hat is singular, adding epsilon=%.2e diagonal regularization\n",
-                    fetch(c, epsd.get(), 1)[0]);
+        safe_inv_report(fetch(c, sti.get(), 1)[0], fetch(c, epsd.get(), 1)[0], "U_hat^T U_hat");
         std::vector<double> Bh = fetch(c, Bpp.get(), (size_t)d * w);
         for (int jj = 0; jj < d; ++jj)
             for (int k = 1; k < w; ++k) bt[jj * wu + (k - 1)] = (float)Bh[jj * w + k];
@@ -1009,11 +1150,7 @@ void nmf_pinv_t(Ctx& c, const double* W, uint64_t n, int k, DBuf<double>& out, c
     DBuf<int> st(1, c.stream);
     launch_atb(c, W, k, W, k, n, k, k, wtw.get());
     launch_inverse(c, wtw.get(), k, inv.get(), st.get(), eps.get());
-    const int status = fetch(c, st.get(), 1)[0];
-    if (status == 2) throw Error(SLFMM_ERR_SINGULAR, std::string(what) + " inversion failed even with regularization");
-    if (status == 1)
-        fprintf(stderr, "Warning: %s is singular, adding epsilon=%.2e diagonal regularization\n", what,
-                fetch(c, eps.get(), 1)[0]);
+    safe_inv_report(fetch(c, st.get(), 1)[0], fetch(c, eps.get(), 1)[0], what);
     out.alloc(std::max<uint64_t>(n, 1) * k, c.stream);
     launch_gemm_small(c, W, k, n, k, inv.get(), k, k, 1.0, 0.0, out.get(), k);
 }
@@ -1198,6 +1335,8 @@ struct Presketch : ChunkHook {
 bool presketch_eligible(Ctx& c, uint64_t n, uint64_t p, const double* x, int d, const slfmm_config* cfg,
                         const double* omega, Presketch& ps) {
     if (c.precision != SLFMM_PREC_SPLIT_FP8 || cfg->impute != SLFMM_IMPUTE_MEAN || p == 0) return false;
+    const char* env = std::getenv("SLFMM_PRESKETCH");  // tuning override: 0 runs the sketch after the upload
+    if (env && env[0] == '0') return false;
     check_cfg(cfg);
     ps.l = (int)cfg->k + (int)cfg->oversampling;
     if (ps.l > 64 || p < (uint64_t)ps.l || n < (uint64_t)ps.l) return false;  // the fit reports these
@@ -1284,9 +1423,8 @@ void fit_impl(Ctx& c, const Geno& ge, const Geno& gf, const double* x, int d, co
 // ---------------------------------------------------------------------------
 // Rust "{:.6e}" formatting (src/testing.rs:780-797)
 // ---------------------------------------------------------------------------
-int format_exp6(double v, char* buf, size_t len) {
-    if (std::isnan(v)) return snprintf(buf, len, "NaN");
-    if (std::isinf(v)) return snprintf(buf, len, v > 0 ? "inf" : "-inf");
+// C's %.6e re-spelt: exponent without '+' or zero padding (the slow path).
+int format_exp6_printf(double v, char* buf, size_t len) {
     char tmp[48];
     snprintf(tmp, sizeof tmp, "%.6e", v);
     char* e = std::strchr(tmp, 'e');
@@ -1294,6 +1432,127 @@ int format_exp6(double v, char* buf, size_t len) {
     *e = '\0';
     const int ex = std::atoi(e + 1);
     return snprintf(buf, len, "%se%d", tmp, ex);
+}
+
+// Seven significant digits of |v| = m 2^e, correctly rounded (ties to even,
+// like Rust's exact formatting, glibc's printf and Python's %): q =
+// round(m 2^e 10^(6 - e10)) in exact 128-bit integer arithmetic, for decimal
+// exponents whose power of five fits in 64 bits (|6 - e10| <= 27, which
+// covers |v| in about [1e-21, 1e33]).  Returns false outside that range.
+bool exp6_digits(uint64_t m, int e, int e10, uint64_t& q) {
+    using u128 = unsigned __int128;
+    static const uint64_t kPow5[28] = {
+        1ull, 5ull, 25ull, 125ull, 625ull, 3125ull, 15625ull, 78125ull, 390625ull, 1953125ull, 9765625ull,
+        48828125ull, 244140625ull, 1220703125ull, 6103515625ull, 30517578125ull, 152587890625ull,
+        762939453125ull, 3814697265625ull, 19073486328125ull, 95367431640625ull, 476837158203125ull,
+        2384185791015625ull, 11920928955078125ull, 59604644775390625ull, 298023223876953125ull,
+        1490116119384765625ull, 7450580596923828125ull};
+    const int sdec = 6 - e10;
+    if (sdec > 27 || sdec < -27) return false;
+    auto round_div = [](u128 num, u128 den, uint64_t& out) {
+        u128 qq = num / den, rem = num - qq * den;
+        const u128 twice = rem << 1;   // rem < den < 2^127
+        if (twice > den || (twice == den && (qq & 1))) ++qq;
+        if (qq > (u128)UINT64_MAX) return false;
+        out = (uint64_t)qq;
+        return true;
+    };
+    if (sdec >= 0) {
+        const u128 x = (u128)m * kPow5[sdec];  // < 2^53 * 5^27 < 2^116
+        const int k2 = e + sdec;               // value = x 2^k2
+        if (k2 >= 0) {
+            if (k2 > 40 || (x >> (127 - k2)) != 0) return false;
+            const u128 r = x << k2;
+            if (r > (u128)UINT64_MAX) return false;
+            q = (uint64_t)r;
+            return true;
+        }
+        const int sh = -k2;
+        if (sh >= 127) {
+            q = 0;
+            return true;
+        }
+        u128 qq = x >> sh;
+        const u128 rem = x - (qq << sh), half = (u128)1 << (sh - 1);
+        if (rem > half || (rem == half && (qq & 1))) ++qq;
+        if (qq > (u128)UINT64_MAX) return false;
+        q = (uint64_t)qq;
+        return true;
+    }
+    const uint64_t d5 = kPow5[-sdec];          // value = m 2^(e + sdec) / 5^-sdec
+    const int k2 = e + sdec;
+    if (k2 >= 0) {
+        if (k2 > 70) return false;
+        return round_div((u128)m << k2, d5, q);
+    }
+    if (-k2 > 64) {
+        q = 0;
+        return true;
+    }
+    return round_div(m, (u128)d5 << (-k2), q);
+}
+
+// Rust "{:.6e}": NaN, inf, -inf; otherwise d.dddddde<exp> with the sign of
+// negative values (and of -0.0), no '+' and no zero padding in the exponent.
+int format_exp6(double v, char* buf, size_t len) {
+    if (std::isnan(v)) return snprintf(buf, len, "NaN");
+    if (std::isinf(v)) return snprintf(buf, len, v > 0 ? "inf" : "-inf");
+    if (len < 32) return format_exp6_printf(v, buf, len);
+    uint64_t bits;
+    std::memcpy(&bits, &v, sizeof bits);
+    const bool neg = (bits >> 63) != 0;
+    const int bexp = (int)((bits >> 52) & 0x7ff);
+    uint64_t m = bits & ((1ull << 52) - 1);
+    int e;
+    if (bexp == 0) {
+        e = -1074;
+    } else {
+        m |= 1ull << 52;
+        e = bexp - 1075;
+    }
+    char* o = buf;
+    if (neg) *o++ = '-';
+    if (m == 0) {
+        std::memcpy(o, "0.000000e0", 10);
+        return (int)(o - buf) + 10;
+    }
+    // floor(log10 |v|) is floor(log10(2) floor(log2 |v|)) or one more: start
+    // at the lower estimate and step up while the rounded digits reach 10^7
+    const int l2 = e + 63 - __builtin_clzll(m);           // floor(log2 |v|)
+    int e10 = (int)std::floor(l2 * 0.30102999566398120);
+    uint64_t q = 0;
+    for (int attempt = 0;; ++attempt) {
+        if (attempt > 3 || !exp6_digits(m, e, e10, q)) return format_exp6_printf(v, buf, len);
+        if (q >= 10000000ull) {
+            ++e10;
+            continue;
+        }
+        if (q < 1000000ull) return format_exp6_printf(v, buf, len);
+        break;
+    }
+    char dig[7];
+    for (int i = 6; i >= 0; --i) {
+        dig[i] = (char)('0' + q % 10);
+        q /= 10;
+    }
+    *o++ = dig[0];
+    *o++ = '.';
+    std::memcpy(o, dig + 1, 6);
+    o += 6;
+    *o++ = 'e';
+    int x = e10;
+    if (x < 0) {
+        *o++ = '-';
+        x = -x;
+    }
+    char eb[8];
+    int n = 0;
+    do {
+        eb[n++] = (char)('0' + x % 10);
+        x /= 10;
+    } while (x);
+    while (n) *o++ = eb[--n];
+    return (int)(o - buf);
 }
 
 }  // namespace
@@ -1356,11 +1615,14 @@ void ctx_open(Ctx& c, int device, int precision, int verbose, cudaStream_t strea
     SLFMM_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
     c.dev_flags.alloc(4, c.stream);
     c.dev_flags.zero();
+    // slfmm_gif_noalloc allocates nothing after this point on this device
+    gif_noalloc_prepare(device);
     SLFMM_CUDA(cudaStreamSynchronize(c.stream));
 }
 
 void ctx_close(Ctx& c) {
     cudaSetDevice(c.device);
+    clear_phase_marks(c);
     c.dev_flags.release();
     if (c.stream) cudaStreamSynchronize(c.stream);
     if (c.copy_stream) cudaStreamDestroy(c.copy_stream);
@@ -1382,7 +1644,7 @@ int slfmm_create(int device, const slfmm_opts* opts, slfmm_ctx** out) {
                  opts ? (cudaStream_t)opts->stream : nullptr);
         const char* at = std::getenv("SLFMM_AUTOTUNE");
         c->autotune = (opts && opts->autotune) || (at && at[0] == '1');
-        c->rng = opts ? opts->rng : SLFMM_RNG_COUNTER;
+        c->rng = opts ? opts->rng : SLFMM_RNG_CHACHA8;
     } catch (const slfmm::Error& e) {
         fprintf(stderr, "schnelgpu: %s\n", e.what());
         const int code = e.code;
@@ -1801,6 +2063,7 @@ int slfmm_profile_enable(slfmm_ctx* c, int on) {
     API_TRY
     profile_collect(*c);
     c->prof.clear();
+    clear_phase_marks(*c);
     c->profiling = on != 0;
     API_CATCH(c)
 }
@@ -1817,6 +2080,32 @@ int slfmm_profile_read(slfmm_ctx* c, const char* kernel, double* total_ms, uint6
     if (launches) *launches = r.launches;
     if (bytes) *bytes = r.bytes;
     if (flops) *flops = r.flops;
+    API_CATCH(c)
+}
+
+int slfmm_debug_expire_next_wait(slfmm_ctx* c, uint64_t cycles) {
+    if (!c || cycles == 0 || cycles > (uint64_t)kWaitCyclesMax) return SLFMM_ERR_BAD_ARG;
+    c->expire_next_wait = (long long)cycles;
+    return SLFMM_OK;
+}
+
+int slfmm_phase_count(const slfmm_ctx* c) {
+    return c && c->phase_marks.size() > 1 ? (int)c->phase_marks.size() - 1 : 0;
+}
+
+int slfmm_phase_read(slfmm_ctx* c, int i, char* name, size_t name_len, double* device_ms, double* host_ms) {
+    if (!c || i < 0 || (size_t)i + 1 >= c->phase_marks.size()) return SLFMM_ERR_BAD_ARG;
+    API_TRY
+    const auto& a = c->phase_marks[(size_t)i];
+    const auto& b = c->phase_marks[(size_t)i + 1];
+    if (name && name_len) snprintf(name, name_len, "%s", b.name.c_str());
+    if (device_ms) {
+        float ms = 0.f;
+        SLFMM_CUDA(cudaEventSynchronize(b.ev));
+        SLFMM_CUDA(cudaEventElapsedTime(&ms, a.ev, b.ev));
+        *device_ms = ms;
+    }
+    if (host_ms) *host_ms = b.host_ms - a.host_ms;
     API_CATCH(c)
 }
 
@@ -1869,7 +2158,11 @@ int slfmm_gif_noalloc(slfmm_ctx* c, const float* t_dev, uint64_t p, uint32_t d, 
     if (!c) return SLFMM_ERR_BAD_ARG;
     API_TRY
     SLFMM_CUDA(cudaSetDevice(c->device));
-    launch_gif_noalloc(*c, t_dev, p, (int)std::min<uint32_t>(d, 1u << 30), gif_dev);
+    SLFMM_REQUIRE(d <= (uint32_t)kGifNoAllocMaxTraits, SLFMM_ERR_BAD_ARG,
+                  "slfmm_gif_noalloc handles at most " + std::to_string(kGifNoAllocMaxTraits) +
+                      " traits (its static histogram holds " + std::to_string(kGifNoAllocMaxTraits) +
+                      " x 100000 counters); got " + std::to_string(d));
+    launch_gif_noalloc(*c, t_dev, p, (int)d, gif_dev);
     API_CATCH(c)
 }
 
@@ -1899,6 +2192,45 @@ int slfmm_write_tsv(const char* path, uint64_t p, uint32_t d, const char* const*
 namespace slfmm {
 // the TSV rows after the file is open: header, then blocks of rows formatted
 // on n_threads threads and written in order
+// Rows [r0, r1) of <out>.tsv appended to s: chr, pos, snp_id, then
+// p/beta/t per covariate and the three r2 columns, each "{:.6e}".  The
+// buffer is sized from the row bound (14 characters per number at most).
+void format_tsv_rows(uint64_t r0, uint64_t r1, uint32_t d, const char* const* chrom, const uint64_t* pos,
+                     const char* const* snp_id, const slfmm_results* res, std::string& s) {
+    size_t cap = 0;
+    for (uint64_t i = r0; i < r1; ++i) cap += std::strlen(chrom[i]) + std::strlen(snp_id[i]);
+    cap += (r1 - r0) * (24 + (size_t)(3 * d + 3) * 16);
+    s.resize(cap);
+    char* o = &s[0];
+    for (uint64_t i = r0; i < r1; ++i) {
+        for (const char* c = chrom[i]; *c; ++c) *o++ = *c;
+        *o++ = '\t';
+        char dig[24];
+        int n = 0;
+        uint64_t x = pos[i];
+        do {
+            dig[n++] = (char)('0' + x % 10);
+            x /= 10;
+        } while (x);
+        while (n) *o++ = dig[--n];
+        *o++ = '\t';
+        for (const char* c = snp_id[i]; *c; ++c) *o++ = *c;
+        for (uint32_t j = 0; j < d; ++j) {
+            const double vals[3] = {res->pvalue[i * d + j], res->beta[i * d + j], res->tstat[i * d + j]};
+            for (double v : vals) {
+                *o++ = '\t';
+                o += format_exp6(v, o, 32);
+            }
+        }
+        for (int k = 0; k < 3; ++k) {
+            *o++ = '\t';
+            o += format_exp6(res->r2[i * 3 + k], o, 32);
+        }
+        *o++ = '\n';
+    }
+    s.resize((size_t)(o - &s[0]));
+}
+
 bool write_tsv_body(FILE* f, uint64_t p, uint32_t d, const char* const* chrom, const uint64_t* pos,
                     const char* const* snp_id, const char* const* cov_names, const slfmm_results* res,
                     int n_threads) {
@@ -1908,38 +2240,23 @@ bool write_tsv_body(FILE* f, uint64_t p, uint32_t d, const char* const* chrom, c
         head += "\tp_" + nm + "\tbeta_" + nm + "\tt_" + nm;
     }
     head += "\tr2_cov\tr2_latent\tr2_resid\n";
-    std::fwrite(head.data(), 1, head.size(), f);
-    int nt = n_threads > 0 ? n_threads : (int)std::max(1u, std::thread::hardware_concurrency());
-    const uint64_t block = 65536;
-    bool ok = true;
-    for (uint64_t b0 = 0; b0 < p && ok; b0 += block * nt) {
-        std::vector<std::string> parts(nt);
+    if (std::fwrite(head.data(), 1, head.size(), f) != head.size()) return false;
+    const int nt = n_threads > 0 ? n_threads : (int)std::max(1u, std::thread::hardware_concurrency());
+    // batches of nt blocks: the threads format batch k + 1 while one thread
+    // writes batch k (the file is written in row order)
+    const uint64_t block = std::max<uint64_t>(1024, std::min<uint64_t>(32768, ceil_div(p, 4 * (uint64_t)nt)));
+    const uint64_t batch = block * (uint64_t)nt;
+    std::vector<std::string> cur(nt), next(nt);
+    std::atomic<bool> ok{true};
+    std::thread writer;
+    auto format_batch = [&](uint64_t b0, std::vector<std::string>& parts) {
         std::vector<std::thread> th;
         std::vector<char> failed(nt, 0);
         auto fmt = [&](int t) {
             try {
-                const uint64_t r0 = b0 + t * block, r1 = std::min(p, r0 + block);
-                std::string& s = parts[t];
-                char buf[64];
-                for (uint64_t i = r0; i < r1; ++i) {
-                    s += chrom[i];
-                    s += '\t';
-                    s += std::to_string(pos[i]);
-                    s += '\t';
-                    s += snp_id[i];
-                    for (uint32_t j = 0; j < d; ++j) {
-                        const double vals[3] = {res->pvalue[i * d + j], res->beta[i * d + j], res->tstat[i * d + j]};
-                        for (double v : vals) {
-                            s += '\t';
-                            s.append(buf, (size_t)format_exp6(v, buf, sizeof buf));
-                        }
-                    }
-                    for (int k = 0; k < 3; ++k) {
-                        s += '\t';
-                        s.append(buf, (size_t)format_exp6(res->r2[i * 3 + k], buf, sizeof buf));
-                    }
-                    s += '\n';
-                }
+                const uint64_t r0 = std::min(p, b0 + (uint64_t)t * block), r1 = std::min(p, r0 + block);
+                parts[t].clear();
+                if (r1 > r0) format_tsv_rows(r0, r1, d, chrom, pos, snp_id, res, parts[t]);
             } catch (...) {
                 failed[t] = 1;
             }
@@ -1953,10 +2270,25 @@ bool write_tsv_body(FILE* f, uint64_t p, uint32_t d, const char* const* chrom, c
         fmt(0);
         for (int t = started; t < nt; ++t) fmt(t);
         for (auto& x : th) x.join();
-        for (int t = 0; t < nt; ++t) ok = ok && !failed[t];
-        for (auto& s : parts)
-            if (ok && !s.empty() && std::fwrite(s.data(), 1, s.size(), f) != s.size()) ok = false;
+        for (int t = 0; t < nt; ++t)
+            if (failed[t]) ok = false;
+    };
+    try {
+        for (uint64_t b0 = 0; b0 < p && ok; b0 += batch) {
+            format_batch(b0, next);
+            if (writer.joinable()) writer.join();
+            if (!ok) break;
+            std::swap(cur, next);
+            writer = std::thread([&] {
+                for (auto& s : cur)
+                    if (ok && !s.empty() && std::fwrite(s.data(), 1, s.size(), f) != s.size()) ok = false;
+            });
+        }
+    } catch (...) {
+        if (writer.joinable()) writer.join();
+        throw;
     }
+    if (writer.joinable()) writer.join();
     return ok;
 }
 }  // namespace slfmm

@@ -30,8 +30,12 @@
 // The block function is pinned by the RFC 8439 test vector; the seed
 // expansion, the output order and the sampler follow the crates' published
 // descriptions and cannot be run against the crates here.
+#include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <memory>
+#include <thread>
+#include <vector>
 
 #include "slfmm_internal.h"
 
@@ -66,21 +70,37 @@ void chacha_block(const uint32_t in[16], int rounds, uint32_t out[16]) {
     for (int i = 0; i < 16; ++i) out[i] = x[i] + in[i];
 }
 
+// Input state of ChaCha8Rng::seed_from_u64(seed) at block 0.
+void chacha8_key_state(uint64_t seed, uint32_t st[16]) {
+    st[0] = 0x61707865u;   // "expand 32-byte k"
+    st[1] = 0x3320646eu;
+    st[2] = 0x79622d32u;
+    st[3] = 0x6b206574u;
+    uint64_t s = seed;
+    for (int j = 0; j < 8; ++j) {
+        s = s * 6364136223846793005ull + 11634580027462260723ull;
+        const uint32_t xorshifted = (uint32_t)(((s >> 18) ^ s) >> 27);
+        st[4 + j] = rotr32(xorshifted, (int)(s >> 59));
+    }
+    st[12] = st[13] = st[14] = st[15] = 0;
+}
+
+// 64-bit output number `pos` of the stream: block pos / 8, words 2 (pos % 8)
+// (low) and 2 (pos % 8) + 1 (high); the stream is counter-addressable.
+inline uint64_t chacha8_u64_at(const uint32_t key[16], uint64_t pos) {
+    uint32_t in[16], out[16];
+    std::memcpy(in, key, sizeof(in));
+    const uint64_t b = pos / 8;
+    in[12] = (uint32_t)b;
+    in[13] = (uint32_t)(b >> 32);
+    chacha_block(in, 8, out);
+    const int w = (int)(pos % 8);
+    return (uint64_t)out[2 * w] | ((uint64_t)out[2 * w + 1] << 32);
+}
+
 class ChaCha8Stream {
 public:
-    explicit ChaCha8Stream(uint64_t seed) {
-        st_[0] = 0x61707865u;   // "expand 32-byte k"
-        st_[1] = 0x3320646eu;
-        st_[2] = 0x79622d32u;
-        st_[3] = 0x6b206574u;
-        uint64_t s = seed;
-        for (int j = 0; j < 8; ++j) {
-            s = s * 6364136223846793005ull + 11634580027462260723ull;
-            const uint32_t xorshifted = (uint32_t)(((s >> 18) ^ s) >> 27);
-            st_[4 + j] = rotr32(xorshifted, (int)(s >> 59));
-        }
-        st_[12] = st_[13] = st_[14] = st_[15] = 0;
-    }
+    explicit ChaCha8Stream(uint64_t seed) { chacha8_key_state(seed, st_); }
     uint64_t next_u64() {
         const uint64_t lo = next_u32();
         const uint64_t hi = next_u32();
@@ -131,12 +151,24 @@ const ZigTables& zig_tables() {
     return t;
 }
 
-inline double unit_closed_open(ChaCha8Stream& r) { return (double)(r.next_u64() >> 11) * (1.0 / 9007199254740992.0); }
-inline double unit_open(ChaCha8Stream& r) {
+template <class Stream>
+inline double unit_closed_open(Stream& r) { return (double)(r.next_u64() >> 11) * (1.0 / 9007199254740992.0); }
+template <class Stream>
+inline double unit_open(Stream& r) {
     return from_bits((1023ull << 52) | (r.next_u64() >> 12)) - (1.0 - 1.0 / 9007199254740992.0);
 }
 
-double standard_normal(ChaCha8Stream& r, const ZigTables& t) {
+// The ziggurat's first test on one 64-bit draw: true (and x) when the draw
+// is accepted at once, without further draws.
+inline bool zig_fast(uint64_t bits, const ZigTables& t, double& x) {
+    const int i = (int)(bits & 0xff);
+    const double u = from_bits((1024ull << 52) | (bits >> 12)) - 3.0;
+    x = u * t.x[i];
+    return std::fabs(x) < t.x[i + 1];
+}
+
+template <class Stream>
+double standard_normal(Stream& r, const ZigTables& t) {
     for (;;) {
         const uint64_t bits = r.next_u64();
         const int i = (int)(bits & 0xff);
@@ -157,14 +189,121 @@ double standard_normal(ChaCha8Stream& r, const ZigTables& t) {
     }
 }
 
+// The stream from output `pos` on, read from a precomputed run of outputs
+// [0, n) and computed block by block past its end.
+struct BufferedStream {
+    const uint64_t* buf;
+    uint64_t n;
+    const uint32_t* key;
+    uint64_t pos;
+    uint64_t next_u64() { return pos < n ? buf[pos++] : chacha8_u64_at(key, pos++); }
+};
+
+template <class F>
+void parallel_for(uint64_t n, int threads, F&& fn) {
+    std::vector<std::thread> pool;
+    for (int t = 1; t < threads; ++t)
+        pool.emplace_back([&, t] { fn(n * (uint64_t)t / threads, n * (uint64_t)(t + 1) / threads); });
+    fn(0, n / (uint64_t)threads);
+    for (auto& th : pool) th.join();
+}
+
+// The same draws as the sequential loop, on host threads.  Draw e starts at
+// some 64-bit output s_e; most draws take one output (the ziggurat's first
+// test accepts), so s_{e+1} = s_e + 1 except after a draw that goes on to
+// the wedge or tail tests.  The outputs are generated and tested in
+// parallel (the stream is counter-addressable); one thread then walks only
+// the outputs whose first test fails, in order, running the full sampler
+// from each one that is a draw start (an output inside an earlier draw's
+// extra draws is not), which fixes every s_e; the values are copied out in
+// parallel.
+void reference_normal_parallel(uint64_t seed, uint64_t count, double* out, int threads) {
+    const ZigTables& t = zig_tables();
+    uint32_t key[16];
+    chacha8_key_state(seed, key);
+    uint64_t npos = count + count / 32 + 4096;
+    for (;;) {
+        const uint64_t nb = (npos + 7) / 8;
+        npos = nb * 8;
+        std::unique_ptr<uint64_t[]> bits(new uint64_t[npos]);  // no zero fill: every entry is written
+        std::unique_ptr<double[]> val(new double[npos]);
+        std::vector<std::vector<uint64_t>> slow(threads);
+        const uint64_t per = (nb + threads - 1) / threads;
+        std::vector<std::thread> pool;
+        auto gen = [&](int th) {
+            const uint64_t b0 = std::min(nb, per * th), b1 = std::min(nb, b0 + per);
+            uint32_t in[16], o[16];
+            std::memcpy(in, key, sizeof(in));
+            for (uint64_t b = b0; b < b1; ++b) {
+                in[12] = (uint32_t)b;
+                in[13] = (uint32_t)(b >> 32);
+                chacha_block(in, 8, o);
+                for (int w = 0; w < 8; ++w) {
+                    const uint64_t j = b * 8 + w;
+                    bits[j] = (uint64_t)o[2 * w] | ((uint64_t)o[2 * w + 1] << 32);
+                    double x;
+                    if (zig_fast(bits[j], t, x)) val[j] = x;
+                    else slow[th].push_back(j);
+                }
+            }
+        };
+        for (int th = 1; th < threads; ++th) pool.emplace_back(gen, th);
+        gen(0);
+        for (auto& th : pool) th.join();
+        // walk: runs of one-output draws between the draw starts that need
+        // more outputs
+        struct Run { uint64_t pos, out, len; };
+        std::vector<Run> runs;
+        std::vector<std::pair<uint64_t, double>> singles;  // (output index, value)
+        uint64_t cur = 0, produced = 0;
+        bool done = false;
+        for (int th = 0; th < threads && !done; ++th)
+            for (uint64_t e : slow[th]) {
+                if (e < cur) continue;                   // inside an earlier draw
+                const uint64_t len = std::min(e - cur, count - produced);
+                if (len) runs.push_back({cur, produced, len});
+                produced += len;
+                if (produced == count) { done = true; break; }
+                BufferedStream bs{bits.get(), npos, key, e};
+                singles.emplace_back(produced, standard_normal(bs, t));
+                ++produced;
+                cur = bs.pos;
+                if (produced == count) { done = true; break; }
+            }
+        if (!done && cur < npos) {
+            const uint64_t len = std::min(npos - cur, count - produced);
+            runs.push_back({cur, produced, len});
+            produced += len;
+        }
+        if (produced < count) {  // more outputs needed than generated (rare)
+            npos *= 2;
+            continue;
+        }
+        const double mean = 0.0, sd = 1.0;
+        parallel_for(runs.size(), threads, [&](uint64_t r0, uint64_t r1) {
+            for (uint64_t r = r0; r < r1; ++r)
+                for (uint64_t k = 0; k < runs[r].len; ++k) out[runs[r].out + k] = mean + sd * val[runs[r].pos + k];
+        });
+        for (const auto& sv : singles) out[sv.first] = mean + sd * sv.second;
+        return;
+    }
+}
+
 }  // namespace
 
 void reference_normal(uint64_t seed, uint64_t rows, uint64_t cols, double* out) {
+    const uint64_t count = rows * cols;
+    const int hw = (int)std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    if (count >= (1u << 16) && hw > 1) {
+        reference_normal_parallel(seed, count, out, hw);
+        return;
+    }
     const ZigTables& t = zig_tables();
     ChaCha8Stream r(seed);
     const double mean = 0.0, sd = 1.0;
-    for (uint64_t e = 0; e < rows * cols; ++e) out[e] = mean + sd * standard_normal(r, t);
+    for (uint64_t e = 0; e < count; ++e) out[e] = mean + sd * standard_normal(r, t);
 }
+
 
 void draw_normal(Ctx& c, uint64_t seed, uint64_t rows, int cols, double* out) {
     if (c.rng != SLFMM_RNG_CHACHA8) {

@@ -27,11 +27,35 @@ namespace {
 // k-major, so one k step is three 16-byte loads and 32 FMAs per thread.
 constexpr int kTileSnps = 64;
 constexpr int kTraitPad = 64;
+
+// Histogram bin of one FP32 t statistic by the reference's rule applied to
+// that value: t_sq = t * t in FP64, skipped when not finite, bin =
+// min(floor(t_sq / 0.001), last) (src/testing.rs:135-149); -1 when skipped.
+// t * t * 1000 in FP32 is within 1.2e-7 relative of t_sq / 0.001, so its
+// floor is the bin unless it lies within that distance of a bin edge (about
+// one value in 4000 near t^2 = 1); those values, and any whose FP32 square
+// overflows, take the FP64 division.
+__device__ __forceinline__ int tsq_bin(float t) {
+    if (!isfinite(t)) return -1;
+    const float xf = t * t * 1000.0f;
+    const float fl = floorf(xf);
+    const float fr = xf - fl;                 // exact while xf < 2^23
+    const float tol = xf * 2.5e-7f;
+    if (xf < 8388608.0f && fr > tol && fr < 1.0f - tol)
+        return fl >= (float)(kHistBins - 1) ? kHistBins - 1 : (int)fl;
+    const double q = floor(((double)t * (double)t) / kHistWidth);
+    return q >= (double)(kHistBins - 1) ? kHistBins - 1 : (int)q;
+}
 constexpr int kUsStride = kTileSnps + 4;  // 16-byte rows, staggered banks
 
+// One block of up to 64 traits per launch: traits [t0, t0 + d) of a model
+// with d_model covariates (the first d_model coordinates of u are the
+// covariate ones, so SS_cov always sums over d_model); beta and t32 rows
+// have d_model entries and point at trait t0; r2 may be null (written by the
+// launch of the first block).
 __global__ void __launch_bounds__(256) k_assoc_epilogue(
     uint64_t p, const float* __restrict__ u, int ldu, const double* __restrict__ tss,
-    const uint8_t* __restrict__ zero_var, int d, int w, double df,
+    const uint8_t* __restrict__ zero_var, int d, int d_model, int w, double df,
     const float* __restrict__ theta_rows, const float* __restrict__ beta_rows,
     const double* __restrict__ cjj, const uint8_t* __restrict__ dropped,
     double* __restrict__ beta, float* __restrict__ t32, double* __restrict__ r2,
@@ -71,7 +95,7 @@ __global__ void __launch_bounds__(256) k_assoc_epilogue(
             for (int k = l8; k < w; k += 8) {
                 const float v = us[k * kUsStride + sn];
                 ss = fmaf(v, v, ss);
-                if (k < d) sc = fmaf(v, v, sc);
+                if (k < d_model) sc = fmaf(v, v, sc);
             }
 #pragma unroll
             for (int o = 4; o > 0; o >>= 1) {
@@ -95,9 +119,11 @@ __global__ void __launch_bounds__(256) k_assoc_epilogue(
                         b = fmax(T - rss - ssc, 0.0) / T;
                         c = rss / T;
                     }
-                    r2[j * 3 + 0] = a;
-                    r2[j * 3 + 1] = b;
-                    r2[j * 3 + 2] = c;
+                    if (r2) {
+                        r2[j * 3 + 0] = a;
+                        r2[j * 3 + 1] = b;
+                        r2[j * 3 + 2] = c;
+                    }
                 }
                 s2s[sn] = s2f;
                 zvs[sn] = zv;
@@ -148,14 +174,10 @@ __global__ void __launch_bounds__(256) k_assoc_epilogue(
                     t = th[a][b] * rsqrtf(var);
                     if (!isfinite(t)) t = 0.f;
                 }
-                beta[j * d + jj] = zv ? 0.0 : (double)bb[a][b];
-                t32[j * d + jj] = t;
-                const float t2 = t * t;
-                if (isfinite(t2)) {
-                    unsigned bin = (unsigned)fminf(t2 * 1000.0f, (float)(kHistBins - 1));
-                    if (bin > (unsigned)(kHistBins - 1)) bin = kHistBins - 1;
-                    atomicAdd(&hist[(uint64_t)jj * kHistBins + bin], 1u);
-                }
+                beta[j * d_model + jj] = zv ? 0.0 : (double)bb[a][b];
+                t32[j * d_model + jj] = t;
+                const int bin = tsq_bin(t);
+                if (bin >= 0) atomicAdd(&hist[(uint64_t)jj * kHistBins + bin], 1u);
             }
         }
     }
@@ -258,20 +280,14 @@ __global__ void k_calibrate(uint64_t p, int d, const float* __restrict__ t32,
 // Every call on a device shares it; each call zeroes the rows it uses first.
 static __device__ __align__(256) uint32_t g_noalloc_hist[kGifNoAllocMaxTraits * kHistBins];
 
-// Same binning as the association epilogue: bin = min(t^2 * 1000, last) for
-// every finite t^2 of trait j.
+// Same binning as the association epilogue (tsq_bin) for every t of trait j.
 __global__ void k_tsq_hist(const float* __restrict__ t, uint64_t p, int d, uint32_t* __restrict__ hist) {
     const uint64_t total = p * (uint64_t)d;
     for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < total;
          e += (uint64_t)gridDim.x * blockDim.x) {
         const int jj = (int)(e % d);
-        const float tv = t[e];
-        const float t2 = tv * tv;
-        if (isfinite(t2)) {
-            unsigned bin = (unsigned)fminf(t2 * 1000.0f, (float)(kHistBins - 1));
-            if (bin > (unsigned)(kHistBins - 1)) bin = kHistBins - 1;
-            atomicAdd(&hist[(uint64_t)jj * kHistBins + bin], 1u);
-        }
+        const int bin = tsq_bin(t[e]);
+        if (bin >= 0) atomicAdd(&hist[(uint64_t)jj * kHistBins + bin], 1u);
     }
 }
 
@@ -297,6 +313,17 @@ static uint32_t* noalloc_hist_address(int device) {
     return addr[device];
 }
 
+// Context set-up for slfmm_gif_noalloc: the histogram's device address on
+// this device, and the module of its two kernels loaded (CUDA loads modules
+// lazily, at a kernel's first use; loading allocates device memory for the
+// code and for the static histogram).  After this, a call allocates nothing.
+void gif_noalloc_prepare(int device) {
+    noalloc_hist_address(device);
+    cudaFuncAttributes fa{};
+    SLFMM_CUDA(cudaFuncGetAttributes(&fa, (const void*)k_tsq_hist));
+    SLFMM_CUDA(cudaFuncGetAttributes(&fa, (const void*)k_gif));
+}
+
 void launch_gif_noalloc(Ctx& c, const float* t, uint64_t p, int d, double* gif_raw) {
     SLFMM_REQUIRE(d >= 0 && d <= kGifNoAllocMaxTraits, SLFMM_ERR_BAD_ARG,
                   "slfmm_gif_noalloc handles at most " + std::to_string(kGifNoAllocMaxTraits) +
@@ -318,15 +345,21 @@ void launch_assoc_epilogue(Ctx& c, uint64_t p, const float* u, int ldu, const do
                            const AssocConsts& k, double* beta, float* t32, double* r2,
                            uint32_t* hist) {
     if (p == 0) return;
-    SLFMM_REQUIRE(k.d <= kTraitPad, SLFMM_ERR_BAD_ARG, "at most 64 traits");
     const size_t smem = (size_t)(2 * k.w * kTraitPad + k.w * kUsStride + 2 * kTileSnps) * sizeof(float);
+    SLFMM_REQUIRE(smem <= 227 * 1024, SLFMM_ERR_BAD_ARG, "association design too wide for the epilogue");
     raise_dynamic_smem((const void*)k_assoc_epilogue, smem);
     const uint64_t tiles = ceil_div(p, (uint64_t)kTileSnps);
     const unsigned grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)c.sm_count * 3);
-    k_assoc_epilogue<<<grid, 256, smem, c.stream>>>(
-        p, u, ldu, tss, k.zero_var, k.d, k.w, k.df, k.theta_rows, k.beta_rows, k.cjj, k.dropped,
-        beta, t32, r2, hist);
-    SLFMM_LAUNCHED(c, "k_assoc_epilogue");
+    // traits in blocks of 64 (the coefficient tables of one block stay in
+    // shared memory); every block reads the same u rows
+    for (int t0 = 0; t0 < k.d; t0 += kTraitPad) {
+        const int db = std::min(kTraitPad, k.d - t0);
+        k_assoc_epilogue<<<grid, 256, smem, c.stream>>>(
+            p, u, ldu, tss, k.zero_var, db, k.d, k.w, k.df, k.theta_rows + (size_t)t0 * k.w,
+            k.beta_rows + (size_t)t0 * k.w, k.cjj + t0, k.dropped + t0, beta + t0, t32 + t0, t0 == 0 ? r2 : nullptr,
+            hist + (size_t)t0 * kHistBins);
+        SLFMM_LAUNCHED(c, "k_assoc_epilogue");
+    }
 }
 
 void launch_gif(Ctx& c, const uint32_t* hist, int d, double* gif_raw) {

@@ -483,8 +483,9 @@ __global__ void __launch_bounds__(128) k_trmul_f32(float* __restrict__ A, int ld
 // original diagonal is dropped instead: L_kk = 1, L_ik = 0, dropped[k] = 1
 // (rank-deficient design columns).  status[0] counts replaced/dropped pivots.
 __global__ void k_cholesky(double* __restrict__ G, int a, int* __restrict__ status,
-                           double drop_tol, int* __restrict__ dropped) {
-    extern __shared__ double S[];
+                           double drop_tol, int* __restrict__ dropped, double* __restrict__ work) {
+    extern __shared__ double S_sm[];
+    double* S = work ? work : S_sm;   // global scratch for matrices wider than kMaxSmall
     __shared__ double piv;
     __shared__ int bad;
     __shared__ int drop_k;
@@ -525,10 +526,13 @@ __global__ void k_cholesky(double* __restrict__ G, int a, int* __restrict__ stat
 }
 
 // Inverse of a lower-triangular matrix: one thread per column.
-__global__ void k_tri_inv_lower(const double* __restrict__ L, int a, double* __restrict__ X) {
-    extern __shared__ double S[];
-    for (int e = threadIdx.x; e < a * a; e += blockDim.x) S[e] = L[e];
-    __syncthreads();
+__global__ void k_tri_inv_lower(const double* __restrict__ L, int a, double* __restrict__ X, int in_smem) {
+    extern __shared__ double S_sm[];
+    const double* S = in_smem ? S_sm : L;   // matrices wider than kMaxSmall are read in place
+    if (in_smem) {
+        for (int e = threadIdx.x; e < a * a; e += blockDim.x) S_sm[e] = L[e];
+        __syncthreads();
+    }
     for (int cc = threadIdx.x; cc < a; cc += blockDim.x) {
         for (int i = 0; i < cc; ++i) X[i * a + cc] = 0.0;
         for (int i = cc; i < a; ++i) {
@@ -583,10 +587,14 @@ __device__ bool lu_smem(double* S, int* piv, int a) {
 // safe_inv (src/testing.rs:996-1024): invert; on an exactly zero pivot add
 // eps = 1e-8 * max(max|diag|, 1e-300) to the diagonal and retry.
 // status: 0 ok, 1 regularised, 2 failed.  eps_used[0] = eps (0 if none).
+// Matrices wider than kMaxSmall work in `work` (a x a doubles then a ints,
+// global memory) instead of shared memory.
 __global__ void k_inverse(const double* __restrict__ A, int a, double* __restrict__ X,
-                          int* __restrict__ status, double* __restrict__ eps_used) {
-    extern __shared__ double S[];
-    __shared__ int piv[kMaxSmall];
+                          int* __restrict__ status, double* __restrict__ eps_used, double* __restrict__ work) {
+    extern __shared__ double S_sm[];
+    __shared__ int piv_sm[kMaxSmall];
+    double* S = work ? work : S_sm;
+    int* piv = work ? reinterpret_cast<int*>(work + (size_t)a * a) : piv_sm;
     __shared__ double eps;
     for (int attempt = 0; attempt < 2; ++attempt) {
         if (threadIdx.x == 0) {
@@ -1050,11 +1058,16 @@ void launch_gram_f32(Ctx& c, const float* A, int lda, uint64_t m, int a, double*
 void launch_gemm_small(Ctx& c, const double* A, int lda, uint64_t m, int a, const double* B, int ldb,
                        int b, double alpha, double beta, double* C, int ldc) {
     if (m == 0 || b == 0) return;
-    const size_t sm = (size_t)a * b * sizeof(double);
-    set_smem((const void*)k_gemm_small<double>, sm);
-    k_gemm_small<double><<<grid_for(c, m * b, 256), 256, sm, c.stream>>>(A, lda, m, a, B, ldb, b, alpha,
-                                                                         beta, C, ldc);
-    SLFMM_LAUNCHED(c, "k_gemm_small");
+    // B in shared memory: column blocks of B (and C) for wide products
+    const int bb = std::max(1, std::min(b, (int)((200 * 1024) / (sizeof(double) * (size_t)std::max(a, 1)))));
+    for (int c0 = 0; c0 < b; c0 += bb) {
+        const int nb = std::min(bb, b - c0);
+        const size_t sm = (size_t)a * nb * sizeof(double);
+        set_smem((const void*)k_gemm_small<double>, sm);
+        k_gemm_small<double><<<grid_for(c, m * nb, 256), 256, sm, c.stream>>>(A, lda, m, a, B + c0, ldb, nb, alpha,
+                                                                              beta, C + c0, ldc);
+        SLFMM_LAUNCHED(c, "k_gemm_small");
+    }
 }
 
 void launch_gemm_small_f32out(Ctx& c, const double* A, int lda, uint64_t m, int a, const double* B,
@@ -1091,24 +1104,37 @@ void launch_trmul_f32(Ctx& c, float* A, int lda, uint64_t m, int a, const double
     SLFMM_LAUNCHED(c, "k_trmul_f32");
 }
 
+// The small dense solvers keep the matrix in shared memory up to kMaxSmall
+// columns and work in global memory (L2-resident) up to kMaxDesign.
 void launch_cholesky(Ctx& c, double* A, int a, int* status, double drop_tol, int* dropped) {
-    SLFMM_REQUIRE(a <= kMaxSmall, SLFMM_ERR_BAD_ARG, "matrix too large for the small Cholesky");
-    set_smem((const void*)k_cholesky, smem_sq(a));
-    k_cholesky<<<1, 512, smem_sq(a), c.stream>>>(A, a, status, drop_tol, dropped);
+    SLFMM_REQUIRE(a <= kMaxDesign, SLFMM_ERR_BAD_ARG, "matrix too large for the small Cholesky");
+    if (a <= kMaxSmall) {
+        set_smem((const void*)k_cholesky, smem_sq(a));
+        k_cholesky<<<1, 512, smem_sq(a), c.stream>>>(A, a, status, drop_tol, dropped, nullptr);
+    } else {
+        DBuf<double> work((size_t)a * a, c.stream);
+        k_cholesky<<<1, 1024, 0, c.stream>>>(A, a, status, drop_tol, dropped, work.get());
+    }
     SLFMM_LAUNCHED(c, "k_cholesky");
 }
 
 void launch_tri_inv_lower(Ctx& c, const double* L, int a, double* Linv) {
-    SLFMM_REQUIRE(a <= kMaxSmall, SLFMM_ERR_BAD_ARG, "matrix too large for the triangular inverse");
-    set_smem((const void*)k_tri_inv_lower, smem_sq(a));
-    k_tri_inv_lower<<<1, 128, smem_sq(a), c.stream>>>(L, a, Linv);
+    SLFMM_REQUIRE(a <= kMaxDesign, SLFMM_ERR_BAD_ARG, "matrix too large for the triangular inverse");
+    const bool sm = a <= kMaxSmall;
+    if (sm) set_smem((const void*)k_tri_inv_lower, smem_sq(a));
+    k_tri_inv_lower<<<1, sm ? 128 : 256, sm ? smem_sq(a) : 0, c.stream>>>(L, a, Linv, sm ? 1 : 0);
     SLFMM_LAUNCHED(c, "k_tri_inv_lower");
 }
 
 void launch_inverse(Ctx& c, const double* A, int a, double* Ainv, int* status, double* eps_used) {
-    SLFMM_REQUIRE(a <= kMaxSmall, SLFMM_ERR_BAD_ARG, "matrix too large for the small inverse");
-    set_smem((const void*)k_inverse, smem_sq(a));
-    k_inverse<<<1, 256, smem_sq(a), c.stream>>>(A, a, Ainv, status, eps_used);
+    SLFMM_REQUIRE(a <= kMaxDesign, SLFMM_ERR_BAD_ARG, "matrix too large for the small inverse");
+    if (a <= kMaxSmall) {
+        set_smem((const void*)k_inverse, smem_sq(a));
+        k_inverse<<<1, 256, smem_sq(a), c.stream>>>(A, a, Ainv, status, eps_used, nullptr);
+    } else {
+        DBuf<double> work((size_t)a * a + (size_t)(a + 1) / 2, c.stream);  // matrix, then a pivot ints
+        k_inverse<<<1, 1024, 0, c.stream>>>(A, a, Ainv, status, eps_used, work.get());
+    }
     SLFMM_LAUNCHED(c, "k_inverse");
 }
 

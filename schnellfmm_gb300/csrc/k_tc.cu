@@ -580,9 +580,12 @@ int tc_split_count(Ctx& c, uint64_t rows, uint64_t K) {
 void launch_rowfix_mean(Ctx& c, float* P, int ldp, uint64_t rows, int w, const uint64_t* ptr, const uint32_t* idx,
                         const float* W, int ldw, const double* cs, const double* mean, const double* scale) {
     if (!rows) return;
-    k_rowfix_mean<<<(unsigned)ceil_div(rows * 32, 256), 256, 0, c.stream>>>(P, ldp, rows, w, ptr, idx, W, ldw, cs,
-                                                                           mean, scale);
-    SLFMM_LAUNCHED(c, "k_rowfix_mean");
+    // a warp covers 128 columns (4 per lane): wider operands in column blocks
+    for (int c0 = 0; c0 < w; c0 += 128) {
+        k_rowfix_mean<<<(unsigned)ceil_div(rows * 32, 256), 256, 0, c.stream>>>(
+            P + c0, ldp, rows, std::min(128, w - c0), ptr, idx, W + c0, ldw, cs + c0, mean, scale);
+        SLFMM_LAUNCHED(c, "k_rowfix_mean");
+    }
 }
 
 void launch_colfix_mean(Ctx& c, double* S, int lds, uint64_t n, int w, const uint64_t* ptr, const uint32_t* idx,

@@ -54,7 +54,8 @@ struct Tc8Args {
     uint32_t n_total;       // B rows / D columns in use
     uint32_t d_cols;        // TMEM columns reserved for D
     uint32_t a_cols;        // TMEM columns per A stage (32, or 64 with the indicator)
-    uint32_t stages, tmem_cols;
+    uint32_t stages, tmem_cols;  // stages: A operand ring depth (TMEM)
+    uint32_t wstages;       // W operand ring depth (shared memory), >= stages
     uint32_t pstages;       // packed-code prefetch depth
     uint32_t group;         // K blocks an MMA warp waits for at once (1, 2, 4; divides stages)
     uint32_t kcopies;       // accumulator copies (2: MMA warps take alternate K groups)
@@ -67,6 +68,7 @@ struct Tc8Args {
     uint32_t loads;         // W boxes this CTA issues per stage
     const float* inv_scale; // n_total: 2^-(e0 + 4t) per B row
     int mode;               // 0: out = P + M; 1: out = s_r (P - mu_r (cs_c - M))
+    long long expire_cycles;  // > 0: test hook, see below
     const double* row_mean;
     const double* row_scale;
     const double* cs;
@@ -129,7 +131,7 @@ __device__ __forceinline__ void tc8_mma_loop(const Tc8Args& a, uint32_t tmem, ui
                                              uint64_t* full_b, uint64_t* full_a, uint64_t* a_empty,
                                              uint64_t* b_empty, uint32_t nkb, uint32_t start,
                                              uint32_t len0, uint32_t skip) {
-    const uint32_t S = a.stages;
+    const uint32_t S = a.stages, SW = a.wstages;
     const uint32_t chunk = a.n_main / NCH;
     const uint32_t id_main = instr_desc_e4m3(chunk);
     const uint32_t id_ind = IND ? instr_desc_e4m3(a.n_ind) : 0u;
@@ -140,23 +142,25 @@ __device__ __forceinline__ void tc8_mma_loop(const Tc8Args& a, uint32_t tmem, ui
     const uint64_t hstep = (uint64_t)a.n_total * (128 >> 4);  // next 128-sample half of the stage
     const uint32_t d_ind = tmem + a.n_main;
     const uint32_t a0 = tmem + a.a_base;
-    Ring st{0, 0};
+    Ring st{0, 0}, sw{0, 0};  // A ring (TMEM) and W ring (shared memory) positions
     st.advance(start, S);
+    sw.advance(start, SW);
     uint32_t i = start, len = len0;
     while (i < nkb) {
         const uint32_t g = min(len, nkb - i);
         bool ok = true;
-        Ring w = st;
+        Ring w = st, wb = sw;
         for (uint32_t j = 0; j < g && ok; ++j) {
-            ok = mbar_wait(full_b + w.slot, w.phase, a.err, 25) && mbar_wait(full_a + w.slot, w.phase, a.err, 26);
+            ok = mbar_wait(full_b + wb.slot, wb.phase, a.err, 25) && mbar_wait(full_a + w.slot, w.phase, a.err, 26);
             w.advance(1, S);
+            wb.advance(1, SW);
         }
         if (!ok) break;
         fence_after();
 #pragma unroll
         for (int j = 0; j < G; ++j) {
             if ((uint32_t)j < g) {
-                const uint64_t bd = bdesc0 + st.slot * bstep;
+                const uint64_t bd = bdesc0 + sw.slot * bstep;
                 const uint32_t ad = a0 + st.slot * a.a_cols;
                 const uint32_t acc0 = (i + j) > start ? 1u : 0u;
 #pragma unroll
@@ -171,12 +175,14 @@ __device__ __forceinline__ void tc8_mma_loop(const Tc8Args& a, uint32_t tmem, ui
                     if (IND) mma_ts_f8(d_ind, ad + kStageK / 4 + kk * 8, bk + indoff, id_ind, acc);
                 }
                 mma_commit(a_empty + st.slot);
-                mma_commit(b_empty + st.slot);
+                mma_commit(b_empty + sw.slot);
                 st.advance(1, S);
+                sw.advance(1, SW);
             }
         }
         i += g + skip;
         st.advance(skip, S);
+        sw.advance(skip, SW);
         len = G;
     }
 }
@@ -201,19 +207,20 @@ __global__ void __launch_bounds__(kThreads, 1)
     k_tc8_rows(const __grid_constant__ CUtensorMap tm_b, Tc8Args a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-    const uint32_t S = a.stages, P = a.pstages;
+    const uint32_t S = a.stages, SW = a.wstages, P = a.pstages;
     uint8_t* bsm = smem;
-    uint8_t* psm = bsm + S * a.b_stage_bytes;
+    uint8_t* psm = bsm + SW * a.b_stage_bytes;
     float* scl = reinterpret_cast<float*>(psm + P * kStageBytes);             // up to 512 floats
     uint64_t* bars = reinterpret_cast<uint64_t*>(reinterpret_cast<uint8_t*>(scl) + 2048);
-    uint64_t* full_b = bars;                 // [S] W tile landed (TMA tx)
-    uint64_t* full_a = bars + S;             // [S] A operand written to TMEM (128 arrivals)
-    uint64_t* a_empty = bars + 2 * S;        // [S] own MMAs on the stage done
-    uint64_t* b_empty = bars + 3 * S;        // [S] every MMA warp's MMAs on the W stage done
-    uint64_t* p_full = bars + 4 * S;         // [P] packed codes landed (TMA tx)
-    uint64_t* p_empty = bars + 4 * S + P;    // [P] packed codes consumed (4 warp arrivals)
-    uint64_t* tmem_full = bars + 4 * S + 2 * P;
-    uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(tmem_full + 1);
+    uint64_t* full_b = bars;                 // [SW] W stage landed (TMA tx)
+    uint64_t* b_empty = bars + SW;           // [SW] every MMA warp's MMAs on the W stage done
+    uint64_t* full_a = bars + 2 * SW;        // [S] A operand written to TMEM (128 arrivals)
+    uint64_t* a_empty = full_a + S;          // [S] the MMAs reading the A stage done
+    uint64_t* p_full = a_empty + S;          // [P] packed codes landed (TMA tx)
+    uint64_t* p_empty = p_full + P;          // [P] packed codes consumed (4 warp arrivals)
+    uint64_t* tmem_full = p_empty + P;
+    uint64_t* never = tmem_full + 1;         // test hook: a barrier nothing arrives at
+    uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(never + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t row0 = blockIdx.x * kM;
@@ -223,17 +230,20 @@ __global__ void __launch_bounds__(kThreads, 1)
     const bool ind = a.n_ind != 0;
 
     if (threadIdx.x == 0) {
-        for (uint32_t s = 0; s < S; ++s) {
+        for (uint32_t s = 0; s < SW; ++s) {
             mbar_init(full_b + s, 1);
+            mbar_init(b_empty + s, a.nsplit ? 2 : 1);   // every MMA warp that reads the stage commits
+        }
+        for (uint32_t s = 0; s < S; ++s) {
             mbar_init(full_a + s, 4);     // one arrival per unpack warp
-            mbar_init(a_empty + s, a.nsplit ? 2 : 1);   // every MMA warp that reads the stage commits
-            mbar_init(b_empty + s, a.nsplit ? 2 : 1);
+            mbar_init(a_empty + s, a.nsplit ? 2 : 1);
         }
         for (uint32_t p = 0; p < P; ++p) {
             mbar_init(p_full + p, 1);
             mbar_init(p_empty + p, 4);
         }
         mbar_init(tmem_full, 2);
+        mbar_init(never, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 1) {
@@ -248,7 +258,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     fence_after();
     const uint32_t tmem = *tmem_holder;
 
-    if (warp == 0) {
+    // Test hook (slfmm_debug_expire_next_wait): before any copy or MMA is
+    // issued, thread 0 waits on a barrier that nothing completes, bounded by
+    // expire_cycles; the wait expires, sets the error flag (site 30), and the
+    // CTA skips its work and frees its TMEM.  Nothing is in flight, so the
+    // context stays usable.
+    if (a.expire_cycles > 0) {
+        if (threadIdx.x == 0) mbar_wait_for(never, 0, a.err, 30, a.expire_cycles);
+    } else if (warp == 0) {
         if (lane == 0) {
             // packed-code producer: runs up to P stages ahead of the unpackers;
             // each (tile, stage) operand is one contiguous bulk copy
@@ -273,7 +290,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             Ring wr{0, 0};
             uint32_t issued = 0;
             for (uint32_t i = 0; i < nkb; ++i) {
-                if (i >= S && !mbar_wait(b_empty + wr.slot, wr.phase ^ 1u, a.err, 23)) break;
+                if (i >= SW && !mbar_wait(b_empty + wr.slot, wr.phase ^ 1u, a.err, 23)) break;
                 mbar_arrive_tx(full_b + wr.slot, a.b_stage_bytes);
                 const int kb = (int)(kb0 + i);
                 for (int h = 0; h < kHalves; ++h)
@@ -284,10 +301,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                         tma_2d(dst, &tm_b, x, (int)y, full_b + wr.slot);
                     }
                 issued = i + 1;
-                wr.advance(1, S);
+                wr.advance(1, SW);
             }
-            for (uint32_t i = issued > S ? issued - S : 0; i < issued; ++i)
-                mbar_wait(full_b + i % S, (i / S) & 1, a.err, 24);
+            for (uint32_t i = issued > SW ? issued - SW : 0; i < issued; ++i)
+                mbar_wait(full_b + i % SW, (i / SW) & 1, a.err, 24);
         }
     } else if (warp == 1 || warp == 3) {
         if (lane == 0) {
@@ -776,7 +793,7 @@ static int env_int(const char* name, int dflt) {
 // The plan with explicit caps on the packed-code ring (pmax), the W ring
 // (smax) and the MMA wait group (gmax); fp8_plan takes them from the
 // environment (defaults 8, 8, 4).
-Fp8Plan fp8_plan_knobs(int wpad, bool ind, uint64_t tiles, int pmax_in, int smax, int gmax_in) {
+Fp8Plan fp8_plan_knobs(int wpad, bool ind, uint64_t tiles, int pmax_in, int smax, int gmax_in, int wmax) {
     Fp8Plan p{};
     p.wpad = (uint32_t)wpad;
     p.n_main = kMainTerms * wpad;
@@ -796,13 +813,23 @@ Fp8Plan fp8_plan_knobs(int wpad, bool ind, uint64_t tiles, int pmax_in, int smax
     p.kcopies = (!ind && 2 * p.d_cols + 3 * p.a_cols <= 512) ? 2 : 1;
     p.a_base = p.kcopies * p.d_cols;
     const uint32_t by_tmem = p.a_base < 512 ? (512 - p.a_base) / p.a_cols : 0;
+    // A ring: as deep as TMEM allows (cap smax).  W ring: its own depth in
+    // shared memory, at least one stage more than the A ring and at least 3
+    // where it fits (cap wmax): a W stage is refilled only after the MMAs on
+    // it complete, and the refill comes from L2 (the same W for every CTA).
+    // The packed-code ring gives up depth (pmax, halving down to 2) for it.
+    p.stages = std::min<uint32_t>(by_tmem, (uint32_t)std::max(1, smax));
     const uint32_t pmax = (uint32_t)std::min(16, std::max(2, pmax_in));
+    const uint32_t wcap = (uint32_t)std::max(1, std::min(16, wmax));
+    const uint32_t wwant = std::min(wcap, std::max(p.stages + 1, 3u));
+    uint32_t by_smem = 0;
     for (p.pstages = pmax;; p.pstages /= 2) {
         const size_t budget = 225 * 1024 - fixed - (size_t)p.pstages * kStageBytes;
-        const uint32_t by_smem = (uint32_t)(budget / p.b_stage_bytes);
-        p.stages = std::min<uint32_t>(std::min(by_tmem, by_smem), (uint32_t)std::max(1, smax));
-        if (p.stages >= std::min<uint32_t>(by_tmem, 2) || p.pstages <= 2) break;
+        by_smem = (uint32_t)(budget / p.b_stage_bytes);
+        if (by_smem >= wwant || p.pstages <= 2) break;
     }
+    p.wstages = std::min(by_smem, wcap);
+    p.stages = std::min(p.stages, p.wstages);
     // MMA wait groups: up to 16 MMAs per wait and warp, at least two groups in the ring
     const uint32_t nch = p.n_main > 256 ? 2 : 1;
     const uint32_t per_stage = (kStageK / 32) * (p.nsplit || p.kcopies == 2 ? nch : nch + (ind ? 1 : 0));
@@ -814,7 +841,7 @@ Fp8Plan fp8_plan_knobs(int wpad, bool ind, uint64_t tiles, int pmax_in, int smax
             break;
         }
     p.stages -= p.stages % p.group;
-    p.smem = fixed + (size_t)p.pstages * kStageBytes + (size_t)p.stages * p.b_stage_bytes;
+    p.smem = fixed + (size_t)p.pstages * kStageBytes + (size_t)p.wstages * p.b_stage_bytes;
     (void)tiles;
     const uint32_t rows_mine = p.n_total;
     p.loads = (uint32_t)ceil_div(rows_mine, 256);
@@ -827,7 +854,7 @@ Fp8Plan fp8_plan_knobs(int wpad, bool ind, uint64_t tiles, int pmax_in, int smax
 
 Fp8Plan fp8_plan(int wpad, bool ind, uint64_t tiles) {
     return fp8_plan_knobs(wpad, ind, tiles, env_int("SLFMM_TC8_PSTAGES", 8), env_int("SLFMM_TC8_STAGES", 8),
-                          env_int("SLFMM_TC8_GROUP", 4));
+                          env_int("SLFMM_TC8_GROUP", 4), env_int("SLFMM_TC8_WSTAGES", 8));
 }
 
 // row-major packed rows (rows x stride) -> tile-major copy; one thread per
@@ -1117,7 +1144,8 @@ static Fp8Plan tc8_tuned_plan(Ctx& c, const Fp8Plan& pl, const TileView& tv, uin
     const std::string key = std::to_string(pl.wpad) + "/" + std::to_string(pl.n_ind) + "/" + std::to_string(K) +
                             "/" + std::to_string(splits) + "/" + std::to_string(mode);
     auto rebuild = [&](int pmax, int smax) {
-        return fp8_plan_knobs((int)pl.wpad, pl.n_ind != 0, ceil_div(rows, (uint64_t)kM), pmax, smax, (int)pl.group);
+        return fp8_plan_knobs((int)pl.wpad, pl.n_ind != 0, ceil_div(rows, (uint64_t)kM), pmax, smax, (int)pl.group,
+                              env_int("SLFMM_TC8_WSTAGES", 8));
     };
     auto it = c.tuned.find(key);
     if (it != c.tuned.end()) return rebuild(it->second.first, it->second.second);
@@ -1209,6 +1237,7 @@ static int tc8_launch(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t ro
     a.d_cols = pl.d_cols;
     a.a_cols = pl.a_cols;
     a.stages = pl.stages;
+    a.wstages = pl.wstages;
     a.pstages = pl.pstages;
     a.group = pl.group;
     a.kcopies = pl.kcopies;
@@ -1220,6 +1249,8 @@ static int tc8_launch(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t ro
     a.box_rows = pl.box_rows;
     a.loads = pl.loads;
     a.inv_scale = inv_scale;
+    a.expire_cycles = c.expire_next_wait;
+    c.expire_next_wait = 0;
     a.mode = mode;
     a.row_mean = row_mean;
     a.row_scale = row_scale;
@@ -1242,9 +1273,9 @@ static int tc8_launch(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t ro
         cudaGetLastError();
         char buf[320];
         snprintf(buf, sizeof buf,
-                 "split-FP8 contraction launch failed (%s): grid %u x %u, smem %zu, stages %u, pstages %u, group %u, "
+                 "split-FP8 contraction launch failed (%s): grid %u x %u, smem %zu, stages %u/%u, pstages %u, group %u, "
                  "n_total %u, box %u x %u, rows %llu, K %llu",
-                 cudaGetErrorString(le), gx, gy, pl.smem, pl.stages, pl.pstages, pl.group, pl.n_total, 128u,
+                 cudaGetErrorString(le), gx, gy, pl.smem, pl.stages, pl.wstages, pl.pstages, pl.group, pl.n_total, 128u,
                  pl.box_rows, (unsigned long long)rows, (unsigned long long)K);
         throw Error(SLFMM_ERR_CUDA, buf);
     }

@@ -39,12 +39,14 @@ struct Error : std::runtime_error {
 // constants shared by host and device
 // ---------------------------------------------------------------------------
 constexpr int kHistBins = 100000;      // src/testing.rs:124
+constexpr long long kWaitCyclesMax = 8000000000ll;  // the device waits' own limit (~4 s at 2 GHz)
 constexpr int kGifNoAllocMaxTraits = 8; // traits the static histogram of slfmm_gif_noalloc holds
 constexpr int kMaxNmfK = 16;            // NMF rank limit of the imputation kernels
 constexpr double kHistWidth = 0.001;   // src/testing.rs:125
 constexpr double kGifDivisor = 0.4549; // src/testing.rs:169
 constexpr int kMaxW = 128;             // widest GEMM operand (columns)
-constexpr int kMaxSmall = 128;         // largest small dense matrix (w x w)
+constexpr int kMaxSmall = 128;         // largest small dense matrix (w x w) in shared memory
+constexpr int kMaxDesign = 256;        // widest association design C = [1 | X | U_hat] (1 + d + K)
 
 inline uint64_t round_up(uint64_t x, uint64_t m) { return (x + m - 1) / m * m; }
 inline uint64_t ceil_div(uint64_t x, uint64_t m) { return (x + m - 1) / m; }
@@ -158,7 +160,16 @@ struct Ctx {
     bool profiling = false;
     std::map<std::string, ProfRec> prof;
     double phase_t0 = 0.0;  // verbose phase log: start of the current phase (ms)
-    int rng = SLFMM_RNG_COUNTER;  // stream of the Gaussian sketches
+    // with profiling on: an event on the stream and the host clock at every
+    // phase mark of the last fit (no synchronisation)
+    struct PhaseMark {
+        std::string name;
+        cudaEvent_t ev;
+        double host_ms;
+    };
+    std::vector<PhaseMark> phase_marks;
+    int rng = SLFMM_RNG_CHACHA8;  // stream of the Gaussian sketches
+    long long expire_next_wait = 0;  // test hook: next split-FP8 launch's wait limit (SM cycles)
     bool autotune = false;   // time the tensor-core ring depths per shape once
     std::map<std::string, std::pair<int, int>> tuned;  // shape -> (packed ring cap, W ring cap)
 };
@@ -270,14 +281,14 @@ void launch_scale_product(Ctx& c, const double* a, const double* b, uint64_t n, 
 // k_tc8.cu : split-FP8 tcgen05 contractions with optional missing-call
 // indicator operand
 struct Fp8Plan {
-    uint32_t wpad, n_main, n_ind, n_total, d_cols, a_cols, stages, pstages, group, tmem_cols, b_stage_bytes;
+    uint32_t wpad, n_main, n_ind, n_total, d_cols, a_cols, stages, wstages, pstages, group, tmem_cols, b_stage_bytes;
     uint32_t kcopies, nsplit, a_base;
     uint32_t box_rows, loads;
     size_t smem;
     bool ok;
 };
 Fp8Plan fp8_plan(int wpad, bool ind, uint64_t tiles);
-Fp8Plan fp8_plan_knobs(int wpad, bool ind, uint64_t tiles, int pmax, int smax, int gmax);
+Fp8Plan fp8_plan_knobs(int wpad, bool ind, uint64_t tiles, int pmax, int smax, int gmax, int wmax);
 // the row-major packed copy of a matrix (a sample subset built from the
 // tile-major copies has none: the passes that need it must not run on it)
 inline const uint8_t* packed_rows(const Geno& g) {
@@ -394,6 +405,7 @@ void launch_gif(Ctx& c, const uint32_t* hist, int d, double* gif_raw);
 // raw GIF per trait from p x d FP32 t statistics using the static per-device
 // histogram (allocates nothing)
 void launch_gif_noalloc(Ctx& c, const float* t, uint64_t p, int d, double* gif_raw);
+void gif_noalloc_prepare(int device);
 void launch_calibrate(Ctx& c, uint64_t p, int d, const float* t32, const double* gif_per_trait,
                       double* t64, double* pval);
 

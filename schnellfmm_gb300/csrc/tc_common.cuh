@@ -44,19 +44,24 @@ __device__ __forceinline__ bool mbar_try(uint32_t addr, uint32_t parity) {
 // round trip on every wait that is not already complete.
 constexpr long long kWaitCycles = 8000000000ll;  // ~4 s at 2 GHz
 
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+__device__ __forceinline__ bool mbar_wait_for(uint64_t* bar, uint32_t parity, int* err, int code,
+                                              long long limit_cycles) {
     const uint32_t addr = smem_u32(bar);
     if (mbar_try(addr, parity)) return true;
     const long long t0 = clock64();
     for (uint32_t it = 1;; ++it) {
         if (mbar_try(addr, parity)) return true;
         if ((it & 1023u) == 0) {
-            if (*(volatile int*)err != 0 || clock64() - t0 > kWaitCycles) {
+            if (*(volatile int*)err != 0 || clock64() - t0 > limit_cycles) {
                 atomicCAS(err, 0, code);
                 return false;
             }
         }
     }
+}
+
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+    return mbar_wait_for(bar, parity, err, code, kWaitCycles);
 }
 
 __device__ __forceinline__ void tma_2d(void* dst, const CUtensorMap* tm, int x, int y, uint64_t* bar) {

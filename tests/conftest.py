@@ -26,9 +26,11 @@ def _gpu_available() -> bool:
 
 @pytest.fixture(scope="session")
 def engine():
-    """Default engine: split-FP8 tensor-core path."""
+    """Split-FP8 tensor-core engine on the counter sketch stream (the tests
+    that compare with the oracle's counter stream use it; test_gpu_rng covers
+    the default ChaCha8 stream)."""
     import schnellfmm_gb300 as sg
-    eng = sg.Engine(precision=sg.Precision.SPLIT_FP8)
+    eng = sg.Engine(precision=sg.Precision.SPLIT_FP8, rng=sg.SketchRng.COUNTER)
     yield eng
     eng.close()
 
@@ -36,7 +38,7 @@ def engine():
 @pytest.fixture(scope="session")
 def engine_bf16():
     import schnellfmm_gb300 as sg
-    eng = sg.Engine(precision=sg.Precision.SPLIT_BF16)
+    eng = sg.Engine(precision=sg.Precision.SPLIT_BF16, rng=sg.SketchRng.COUNTER)
     yield eng
     eng.close()
 
@@ -49,6 +51,6 @@ def engines(engine, engine_bf16, engine_fp32):
 @pytest.fixture(scope="session")
 def engine_fp32():
     import schnellfmm_gb300 as sg
-    eng = sg.Engine(precision=sg.Precision.FP32)
+    eng = sg.Engine(precision=sg.Precision.FP32, rng=sg.SketchRng.COUNTER)
     yield eng
     eng.close()

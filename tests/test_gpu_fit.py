@@ -6,6 +6,7 @@ import numpy as np
 import pytest
 
 from oracle import lfmm_oracle as O
+from parity import check_fit
 import simdata
 
 pytestmark = pytest.mark.gpu
@@ -19,24 +20,7 @@ def _sg():
 
 
 def _check(res, ref, u_ref, t_tol=T_TOL):
-    assert O.principal_angles_sin_max(res.u_hat, u_ref) < 1e-3
-    dt = np.abs(res.tstat - ref.tstat).max()
-    assert dt <= t_tol, f"max|dt| = {dt}"
-    scale = np.abs(ref.beta).max()
-    assert np.abs(res.beta - ref.beta).max() <= 1e-3 * scale + 1e-12
-    assert np.abs(res.r2 - ref.r2).max() <= 1e-4
-    # GIF can move by one histogram bin (0.001 in t^2) at a bin edge
-    assert abs(res.gif - ref.gif) <= 0.0023
-    # p-values follow from t and GIF.  Calibration evaluates erfc in FP32 (the
-    # statistic itself is FP32): relative error ~ 2e-6 (1 + z^2) in the tail
-    p_expect = O.calibrate_p(res.tstat, res.gif_per_trait)
-    z = np.abs(res.tstat) / np.sqrt(res.gif_per_trait)[None, :]
-    rel = np.abs(res.pvalue - p_expect) / np.maximum(p_expect, 1e-300)
-    assert np.all(rel <= 2e-6 * (1.0 + z * z)), float((rel / (1 + z * z)).max())
-    # top hits keep their order
-    top = np.argsort(-np.abs(ref.tstat[:, 0]))[:10]
-    top_gpu = np.argsort(-np.abs(res.tstat[:, 0]))[:10]
-    assert set(top[:5]) <= set(top_gpu)
+    check_fit(res, ref, u_ref, t_tol)
 
 
 @pytest.mark.parametrize("prec", ["fp32", "bf16", "fp8"])
@@ -157,4 +141,80 @@ def test_high_missingness(engines, prec):
     cfg = sg.Lfmm2Config(k=4, norm=sg.SnpNorm.EIGENSTRAT)
     res = sg.fit_lfmm2(geno, sg.SubsetSpec.all(), geno, c.x, cfg, omega=omega, engine=engines[prec])
     ref = O.fit_oracle64(c.raw, c.raw, c.x, k=4, norm=O.NORM_EIGENSTRAT, omega=omega)
+    _check(res, ref.assoc, ref.u_hat)
+
+
+def test_duplicated_covariate_safe_inv(engine, capfd):
+    """A duplicated covariate makes C^T C and X^T X exactly singular: the
+    reference's safe_inv adds eps = 1e-8 max|diag| and warns on stderr
+    (src/testing.rs:996-1024); both copies then share the coefficient and
+    get near-zero t.  The GPU fit follows the same regularised algebra."""
+    sg = _sg()
+    c = simdata.simulate(300, 2000, k_pop=3, fst=0.1, miss=0.01, d=3, n_causal=20, seed=12)
+    x = 0.5 * c.x
+    x[:, 2] = x[:, 0]
+    omega = O.rng_normal_matrix(5, c.n, 13)
+    geno = engine.upload(c.packed, c.n)
+    capfd.readouterr()
+    res = sg.fit_lfmm2(geno, sg.SubsetSpec.all(), geno, x, sg.Lfmm2Config(k=3, norm=sg.SnpNorm.EIGENSTRAT),
+                       omega=omega, engine=engine)
+    err = capfd.readouterr().err
+    ref = O.fit_oracle64(c.raw, c.raw, x, k=3, norm=O.NORM_EIGENSTRAT, omega=omega)
+    _check(res, ref.assoc, ref.u_hat)
+    # the oracle's safe_inv regularises the same two matrices
+    xs = O.center_covariates(x, False)
+    cmat = np.hstack([np.ones((c.n, 1)), xs, ref.u_hat])
+    ctc = cmat.T @ cmat
+    _, reg = O.safe_inv(ctc)
+    assert reg
+    eps_c = 1e-8 * np.abs(np.diag(ctc)).max()
+    eps_x = 1e-8 * np.abs(np.diag(xs.T @ xs)).max()
+    assert (f"Warning: C^T C  where C = [1 | X | U_hat] is singular, adding epsilon="
+            f"{O.rust_exp(eps_c, 2)} diagonal regularization") in err, err
+    assert (f"Warning: X^T X for sequential R^2 is singular, adding epsilon="
+            f"{O.rust_exp(eps_x, 2)} diagonal regularization") in err, err
+    # both copies of the covariate: near-zero t, half the single-copy effect each
+    assert np.abs(res.tstat[:, [0, 2]]).max() < 1e-2
+    np.testing.assert_allclose(res.tstat[:, 0], res.tstat[:, 2], atol=1e-4)
+
+
+def test_bounded_wait_expiry_leaves_context_usable():
+    """Failure detection on the device without a fault: a split-FP8
+    contraction whose first wait is on a barrier nothing completes gives
+    SLFMM_ERR_DEVICE_TIMEOUT after the bound; the same context then fits
+    normally, with the same bits as before."""
+    sg = _sg()
+    eng = sg.Engine(precision=sg.Precision.SPLIT_FP8)
+    try:
+        c = simdata.simulate(300, 2000, k_pop=3, fst=0.1, miss=0.01, d=2, seed=13)
+        omega = O.rng_normal_matrix(6, c.n, 13)
+        geno = eng.upload(c.packed, c.n)
+        cfg = sg.Lfmm2Config(k=3, norm=sg.SnpNorm.EIGENSTRAT)
+        before = sg.fit_lfmm2(geno, sg.SubsetSpec.all(), geno, c.x, cfg, omega=omega, engine=eng)
+        assert eng.lib.slfmm_debug_expire_next_wait(eng.h, 0) == sg.ERR_BAD_ARG
+        eng.check(eng.lib.slfmm_debug_expire_next_wait(eng.h, 2_000_000))     # ~1 ms at 2 GHz
+        with pytest.raises(sg.SchnelGpuError) as e:
+            sg.fit_lfmm2(geno, sg.SubsetSpec.all(), geno, c.x, cfg, omega=omega, engine=eng)
+        assert e.value.code == sg.ERR_DEVICE_TIMEOUT and "bounded device wait expired (site 30)" in str(e.value)
+        after = sg.fit_lfmm2(geno, sg.SubsetSpec.all(), geno, c.x, cfg, omega=omega, engine=eng)
+        for k in ("tstat", "beta", "r2", "u_hat"):
+            assert np.array_equal(getattr(after, k), getattr(before, k)), k
+        geno.free()
+    finally:
+        eng.close()
+
+
+@pytest.mark.parametrize("prec", ["fp32", "bf16", "fp8"])
+def test_wide_design_d100_k30(engines, prec):
+    """More covariates than one 64-trait epilogue block and a design wider
+    than 128 columns (1 + d + K = 131): the reference puts no limit on d
+    (C = [1 | X | U_hat], src/testing.rs:296-304)."""
+    sg = _sg()
+    c = simdata.simulate(900, 3000, k_pop=4, fst=0.08, miss=0.01, d=100, n_causal=15, seed=19)
+    omega = O.rng_normal_matrix(8, c.n, 40)
+    geno = engines[prec].upload(c.packed, c.n)
+    cfg = sg.Lfmm2Config(k=30, oversampling=10, norm=sg.SnpNorm.EIGENSTRAT)
+    res = sg.fit_lfmm2(geno, sg.SubsetSpec.all(), geno, c.x, cfg, omega=omega, engine=engines[prec])
+    ref = O.fit_oracle64(c.raw, c.raw, c.x, k=30, norm=O.NORM_EIGENSTRAT, omega=omega)
+    assert res.tstat.shape == (c.p, 100) and res.gif_per_trait.shape == (100,)
     _check(res, ref.assoc, ref.u_hat)

@@ -29,6 +29,13 @@ def test_generate_omega_streams(engine, chacha_engine):
     import schnellfmm_gb300 as sg
     np.testing.assert_array_equal(chacha_engine.generate_omega(42, 500, 13), sg.reference_normal(42, 500, 13))
     np.testing.assert_array_equal(chacha_engine.generate_omega(42, 500, 13), O.chacha8_normal_matrix(42, 500, 13))
+    # the default engine draws the reference's stream; 2 000 x 40 draws take
+    # the parallel host path (outputs generated and tested on threads)
+    default = sg.Engine(precision=sg.Precision.SPLIT_FP8)
+    try:
+        np.testing.assert_array_equal(default.generate_omega(7, 2000, 40), O.chacha8_normal_matrix(7, 2000, 40))
+    finally:
+        default.close()
     # the counter stream: same draws, device log / cos against numpy's (ulps)
     np.testing.assert_allclose(engine.generate_omega(42, 500, 13), O.rng_normal_matrix(42, 500, 13),
                                rtol=0, atol=1e-13)

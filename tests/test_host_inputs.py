@@ -62,6 +62,9 @@ def test_intersect_samples(tmp_path):
     ("id\tv\nA\t1\nA\t2\n", "Duplicate sample ID 'A'"),
     ("id\tv\nA\t1\n\nB\t1\t2\n", "Line 4 has 3 fields"),
     ("id\tv\nA\tinf\n", "Infinite value"),
+    # the message shows the parsed value as Rust displays it (src/main.rs:436-443)
+    ("id\tv\nA\t1e999\n", r"Infinite value \(inf\) for covariate 'v' on line 2 \(sample 'A'\)"),
+    ("id\tv\nA\t-Infinity\n", r"Infinite value \(-inf\)"),
     ("id\tv\nA\t1_0\n", "Failed to parse value '1_0'"),
     ("id\tv\nA\tabc\n", "Failed to parse value 'abc' for covariate 'v' on line 2"),
 ])

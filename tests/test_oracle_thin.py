@@ -49,3 +49,22 @@ def test_fit_oracle_statistical_acceptance():
     assert np.mean(a.pvalue[c.causal, 0] < 0.05) > THRESH["power_min"]
     lo, hi = THRESH["gif_range"]
     assert lo < a.gif < hi
+
+
+def test_packed_streamed_oracle_equals_dense():
+    """The chunk-streamed oracle (used at n = 20 000) equals the dense one."""
+    c = simdata.simulate(90, 700, k_pop=3, fst=0.1, miss=0.03, d=3, n_causal=10, seed=6, monomorphic=2)
+    omega = O.rng_normal_matrix(2, c.n, 9)
+    est = O.subset_indices(c.p, rate=0.5)
+    dense = O.fit_oracle64(c.raw[:, est], c.raw, c.x, k=4, oversampling=5, norm=O.NORM_EIGENSTRAT, omega=omega)
+    packed = O.fit_oracle64_packed(c.packed, c.n, c.x, k=4, oversampling=5, norm=O.NORM_EIGENSTRAT, omega=omega,
+                                   est_snps=est, chunk=64)
+    assert O.principal_angles_sin_max(dense.u_hat, packed.u_hat) < 1e-10
+    np.testing.assert_allclose(packed.u_hat, dense.u_hat, atol=1e-10)
+    np.testing.assert_allclose(packed.assoc.tstat, dense.assoc.tstat, atol=1e-9)
+    np.testing.assert_allclose(packed.assoc.beta, dense.assoc.beta, atol=1e-10)
+    np.testing.assert_allclose(packed.assoc.r2, dense.assoc.r2, atol=1e-10)
+    assert packed.assoc.gif == dense.assoc.gif
+    y = O.PackedMatrix(c.packed, c.n, O.NORM_EIGENSTRAT)
+    st = O.snp_stats(c.raw, O.NORM_EIGENSTRAT)
+    assert (y.counts == st.counts).all() and (y.mean == st.mean).all() and (y.scale == st.scale).all()
