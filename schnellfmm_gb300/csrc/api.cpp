@@ -704,7 +704,8 @@ void step0(Ctx& c, const double* x_host, uint64_t n, int d, double lambda, bool 
     SLFMM_REQUIRE(lambda > 0.0, SLFMM_ERR_BAD_ARG,
                   "Ridge penalty lambda must be positive, got " + std::to_string(lambda) +
                       ". lambda=0 makes the D_lambda diagonal singular. Use a small positive value like 1e-10.");
-    SLFMM_REQUIRE(d >= 1 && d <= 64, SLFMM_ERR_BAD_ARG, "number of covariates must be in 1..64");
+    SLFMM_REQUIRE(d >= 1 && d <= kMaxDesign, SLFMM_ERR_BAD_ARG,
+                  "number of covariates must be in 1.." + std::to_string(kMaxDesign));
     s.n = n;
     s.d = d;
     s.xs = upload(c, x_host, n * d);
@@ -953,9 +954,18 @@ void assoc(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, const doubl
     std::vector<uint8_t> drop_x(d, 0);
     bool any_dropped = false;
     for (int k = 0; k < w; ++k) any_dropped = any_dropped || dr[k] != 0;
-    if (ctc_eps > 0.0 && any_dropped) {
-        // exactly singular C^T C: the limit of the reference's regularised
-        // solve, in unnormalised coordinates (theta_i = f_i theta~_i)
+    if (any_dropped) {
+        // C^T C singular (a zero LU pivot) or so close to it that the
+        // factorisation dropped a column: the limit of the regularised solve,
+        // in unnormalised coordinates (theta_i = f_i theta~_i).  Without a
+        // zero pivot the reference inverts the ill-conditioned matrix as it
+        // is, which also gives every column of the null space a near-zero t;
+        // eps = 1e-8 max|diag| stands for its effective regulariser then.
+        if (!(ctc_eps > 0.0)) {
+            double dmax = 0.0;
+            for (int k = 0; k < w; ++k) dmax = std::max(dmax, std::fabs(Graw[k * w + k]));
+            ctc_eps = 1e-8 * std::max(dmax, 1e-300);
+        }
         std::vector<double> Ginv((size_t)w * w, 0.0);  // generalised inverse on the kept columns
         for (int i = 0; i < w; ++i)
             for (int j = 0; j < w; ++j) {
@@ -1356,6 +1366,10 @@ void fit_impl(Ctx& c, const Geno& ge, const Geno& gf, const double* x, int d, co
     if (!pre) phase(c, "", true);
     check_cfg(cfg);
     SLFMM_REQUIRE(ge.n == gf.n, SLFMM_ERR_BAD_ARG, "estimation and testing genotypes have different sample counts");
+    // the reference's sketch stream is drawn on host threads while Step 0 and
+    // the SNP statistics run on the device
+    if (!omega && cfg->impute == SLFMM_IMPUTE_MEAN)
+        prefetch_normal(c, cfg->seed, gf.n, (int)(cfg->k + cfg->oversampling));
     Step0 s0_own;
     Step0& s0 = pre ? pre->s0 : s0_own;
     if (!pre) step0(c, x, gf.n, d, cfg->lambda, cfg->scale_cov != 0, s0);
@@ -1839,6 +1853,8 @@ int slfmm_fit_host(slfmm_ctx* c, const uint8_t* packed, uint64_t n_physical, uin
     // with every SNP in the estimation, the sketch pass runs under the upload
     Presketch ps;
     phase(*c, "", true);
+    if (cfg && !omega && cfg->impute == SLFMM_IMPUTE_MEAN)
+        prefetch_normal(*c, cfg->seed, sample_keep ? n_keep : n_physical, (int)(cfg->k + cfg->oversampling));
     const bool pre = all && cfg && presketch_eligible(*c, sample_keep ? n_keep : n_physical, n_snps, x, (int)d,
                                                       cfg, omega, ps);
     upload_geno(*c, full, packed, n_physical, n_snps, sample_keep, n_keep, nullptr,

@@ -6,7 +6,8 @@
 // NMF puts at the missing calls, f_ir = W_i . H_r, enter as sparse
 // corrections over the missing-call lists (CSR by SNP, CSC by sample), so no
 // imputed copy of the matrix is ever formed.  W (n x k) and H (p x k, one row
-// per SNP) are FP32 row-major here; k <= kMaxNmfK.
+// per SNP) are FP32 row-major here; k <= kMaxNmfK (kernels are built for
+// rank bounds 16 and 32).
 #include <cmath>
 #include <cstdint>
 
@@ -110,11 +111,12 @@ __device__ __forceinline__ float warp_sum_f(float v) {
     return v;
 }
 
-// f = W_i . h (h in shared memory, k <= kMaxNmfK)
+// f = W_i . h (h in shared memory, k <= KM)
+template <int KM>
 __device__ __forceinline__ float fill_dot(const float* __restrict__ Wi, const float* h, int k) {
     float f = 0.f;
 #pragma unroll
-    for (int c = 0; c < kMaxNmfK; ++c)
+    for (int c = 0; c < KM; ++c)
         if (c < k) f = fmaf(Wi[c], h[c], f);
     return f;
 }
@@ -122,12 +124,13 @@ __device__ __forceinline__ float fill_dot(const float* __restrict__ Wi, const fl
 // Per-SNP statistics with the NMF values at the missing calls: every call is
 // valid, mu = (S1 + F1) / n, s = scale(mu), TSS = s^2 (S2 + F2 - (S1+F1)^2/n)
 // (decode_single_snp with a fill, src/bed.rs:300-379).  One warp per SNP.
+template <int KM>
 __global__ void __launch_bounds__(256) k_fill_stats(uint64_t p, uint64_t n, int norm, const int32_t* __restrict__ counts,
                                                     const uint64_t* __restrict__ ptr, const uint32_t* __restrict__ idx,
                                                     const float* __restrict__ W, const float* __restrict__ H, int k,
                                                     double* __restrict__ mean, double* __restrict__ scale,
                                                     double* __restrict__ tss, uint8_t* __restrict__ zero_var) {
-    __shared__ float hs[8][kMaxNmfK];
+    __shared__ float hs[8][KM];
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     const uint64_t nw = (uint64_t)gridDim.x * 8;
     for (uint64_t r = (uint64_t)blockIdx.x * 8 + wl; r < p; r += nw) {
@@ -136,7 +139,7 @@ __global__ void __launch_bounds__(256) k_fill_stats(uint64_t p, uint64_t n, int 
         __syncwarp();
         double f1 = 0.0, f2 = 0.0;
         for (uint64_t e = ptr[r] + lane; e < ptr[r + 1]; e += 32) {
-            const float f = fill_dot(W + (uint64_t)idx[e] * k, hs[wl], k);
+            const float f = fill_dot<KM>(W + (uint64_t)idx[e] * k, hs[wl], k);
             f1 += (double)f;
             f2 += (double)f * (double)f;
         }
@@ -202,7 +205,7 @@ __device__ __forceinline__ void round_finish(float (&acc)[4]) {
 // Row pass correction: out[r, c] += s_r * sum_{i in miss(r)} (f_ir - mu_r) Wop[i, c]
 // (the base pass counted the missing calls at the mean).  One warp per SNP;
 // 32 missing indices and their fills are formed per round and broadcast.
-template <int CG, bool W4>
+template <int CG, bool W4, int KM>
 __global__ void __launch_bounds__(256) k_fill_row_correct(float* __restrict__ out, int ldo, uint64_t p, int w,
                                                           const uint64_t* __restrict__ ptr,
                                                           const uint32_t* __restrict__ idx, const float* __restrict__ Wop,
@@ -210,7 +213,7 @@ __global__ void __launch_bounds__(256) k_fill_row_correct(float* __restrict__ ou
                                                           const float* __restrict__ H, int k,
                                                           const double* __restrict__ mean,
                                                           const double* __restrict__ scale) {
-    __shared__ float hs[8][kMaxNmfK];
+    __shared__ float hs[8][KM];
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     const uint64_t nw = (uint64_t)gridDim.x * 8;
     for (uint64_t r = (uint64_t)blockIdx.x * 8 + wl; r < p; r += nw) {
@@ -230,7 +233,7 @@ __global__ void __launch_bounds__(256) k_fill_row_correct(float* __restrict__ ou
                 if constexpr (W4) {  // 16-byte loads of the W row, summed in fill_dot's order
                     const float4* w4 = reinterpret_cast<const float4*>(Wn + (uint64_t)my * k);
 #pragma unroll
-                    for (int q = 0; q < kMaxNmfK / 4; ++q) {
+                    for (int q = 0; q < KM / 4; ++q) {
                         if (4 * q < k) {
                             const float4 v = w4[q];
                             f = fmaf(v.x, hs[wl][4 * q], f);
@@ -240,7 +243,7 @@ __global__ void __launch_bounds__(256) k_fill_row_correct(float* __restrict__ ou
                         }
                     }
                 } else {
-                    f = fill_dot(Wn + (uint64_t)my * k, hs[wl], k);
+                    f = fill_dot<KM>(Wn + (uint64_t)my * k, hs[wl], k);
                 }
                 dm = f - mu;
             }
@@ -266,14 +269,14 @@ constexpr uint64_t kColSeg = 1024;
 // sm[r] = (s_r, mu_r) in FP32 (the values the correction uses), one 8-byte
 // gather per call; with H4 the H row (k % 4 == 0, 16-byte aligned) is read as
 // 16-byte loads, the products summed in the same order as fill_dot.
-template <int CG, bool H4>
+template <int CG, bool H4, int KM>
 __global__ void __launch_bounds__(256) k_fill_col_correct(double* __restrict__ S, int lds, uint64_t n, int w,
                                                           uint64_t nseg, const uint64_t* __restrict__ cptr,
                                                           const uint32_t* __restrict__ cidx,
                                                           const float* __restrict__ Qop, int ldq,
                                                           const float* __restrict__ Wn, const float* __restrict__ H,
                                                           int k, const float2* __restrict__ sm) {
-    __shared__ float ws[8][kMaxNmfK];
+    __shared__ float ws[8][KM];
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     const uint64_t nw = (uint64_t)gridDim.x * 8;
     for (uint64_t gw = (uint64_t)blockIdx.x * 8 + wl; gw < n * nseg; gw += nw) {
@@ -293,7 +296,7 @@ __global__ void __launch_bounds__(256) k_fill_col_correct(double* __restrict__ S
                 if constexpr (H4) {
                     const float4* h4 = reinterpret_cast<const float4*>(H + (uint64_t)my * k);
 #pragma unroll
-                    for (int q = 0; q < kMaxNmfK / 4; ++q) {
+                    for (int q = 0; q < KM / 4; ++q) {
                         if (4 * q < k) {
                             const float4 v = h4[q];
                             f = fmaf(v.x, ws[wl][4 * q], f);
@@ -303,7 +306,7 @@ __global__ void __launch_bounds__(256) k_fill_col_correct(double* __restrict__ S
                         }
                     }
                 } else {
-                    f = fill_dot(H + (uint64_t)my * k, ws[wl], k);
+                    f = fill_dot<KM>(H + (uint64_t)my * k, ws[wl], k);
                 }
                 const float2 smv = sm[my];
                 dm = smv.x * (f - smv.y);
@@ -388,12 +391,12 @@ __global__ void k_nmf_sign(const TS* __restrict__ src, int ldsrc, double* __rest
 // (r - chunk start) n + i (column-major, missing calls included) and is held
 // out iff the draw is below `rate` and the call is observed.  Per SNP:
 // sum |g - W_i.H_r|, sum |g - mean_r|, count.
-template <bool kChaCha>
+template <bool kChaCha, int KM>
 __global__ void __launch_bounds__(256) k_nmf_cv(const uint8_t* __restrict__ packed, uint64_t stride, uint64_t n,
                                                 uint64_t p, uint64_t chunk, uint64_t mask_seed, uint64_t thresh,
                                                 const float* __restrict__ W, const float* __restrict__ H, int k,
                                                 const int32_t* __restrict__ counts, double* __restrict__ part) {
-    __shared__ float hs[8][kMaxNmfK];
+    __shared__ float hs[8][KM];
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     const uint64_t nw = (uint64_t)gridDim.x * 8;
     for (uint64_t r = (uint64_t)blockIdx.x * 8 + wl; r < p; r += nw) {
@@ -426,7 +429,7 @@ __global__ void __launch_bounds__(256) k_nmf_cv(const uint8_t* __restrict__ pack
                 }
                 const uint64_t i = i0 + b;
                 const double g = code == 0 ? 0.0 : (double)(code - 1);
-                e1 += fabs(g - (double)fill_dot(W + i * k, hs[wl], k));
+                e1 += fabs(g - (double)fill_dot<KM>(W + i * k, hs[wl], k));
                 e2 += fabs(g - cm);
                 cnt += 1.0;
             }
@@ -465,12 +468,12 @@ __global__ void k_obs_base(const int32_t* __restrict__ counts, uint64_t p, uint6
 // kept observed calls of W+_i g, B = sum over missing and held-out calls of
 // W+_i.  One warp per SNP, two passes over its codes.  kChaCha draws from the
 // reference's ChaCha8 stream instead of the counter stream.
-template <bool kChaCha>
+template <bool kChaCha, int KM>
 __global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__ packed, uint64_t stride, uint64_t n,
                                                      uint64_t p, uint64_t chunk, uint64_t seed, uint64_t thresh,
                                                      const float* __restrict__ W, const float* __restrict__ Wpt, int k,
                                                      const uint64_t* __restrict__ base, double* __restrict__ part) {
-    __shared__ float hh[8][kMaxNmfK];
+    __shared__ float hh[8][KM];
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     const unsigned lt = (1u << lane) - 1u;
     const uint64_t nw = (uint64_t)gridDim.x * 8;
@@ -479,9 +482,9 @@ __global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__
         const uint64_t key = mix64(seed + seq + kGamma);
         ChaCha8Draws cc(seed + seq);
         const uint8_t* row = packed + r * stride;
-        float A[kMaxNmfK], B[kMaxNmfK];
+        float A[KM], B[KM];
 #pragma unroll
-        for (int c = 0; c < kMaxNmfK; ++c) A[c] = B[c] = 0.f;
+        for (int c = 0; c < KM; ++c) A[c] = B[c] = 0.f;
         double s1 = 0.0, nk = 0.0;
         int nmask = 0;
         uint64_t before = base[r];
@@ -504,11 +507,11 @@ __global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__
                     s1 += (double)g;
                     nk += 1.0;
 #pragma unroll
-                    for (int c = 0; c < kMaxNmfK; ++c)
+                    for (int c = 0; c < KM; ++c)
                         if (c < k) A[c] = fmaf(wp[c], g, A[c]);
                 } else {
 #pragma unroll
-                    for (int c = 0; c < kMaxNmfK; ++c)
+                    for (int c = 0; c < KM; ++c)
                         if (c < k) B[c] += wp[c];
                 }
             }
@@ -523,7 +526,7 @@ __global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__
         nk = warp_sum_d(nk);
         const double mu = nk > 0.0 ? s1 / nk : 0.0;
 #pragma unroll
-        for (int c = 0; c < kMaxNmfK; ++c) {
+        for (int c = 0; c < KM; ++c) {
             if (c < k) {
                 const float a = warp_sum_f(A[c]), b = warp_sum_f(B[c]);
                 if (lane == 0) hh[wl][c] = fmaxf(a + (float)mu * b, 0.f);
@@ -545,7 +548,7 @@ __global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__
             }
             if (held) {
                 const double g = code == 0 ? 0.0 : (double)(code - 1);
-                e1 += fabs(g - (double)fill_dot(W + i * k, hh[wl], k));
+                e1 += fabs(g - (double)fill_dot<KM>(W + i * k, hh[wl], k));
                 e2 += fabs(g - mu);
             }
             before += __popc(bal);
@@ -574,16 +577,22 @@ static uint64_t rate_threshold(double rate, int bits = 53) {
 void launch_fill_stats(Ctx& c, const Geno& g, int norm, const float* W, const float* H, int k, double* mean,
                        double* scale, double* tss, uint8_t* zero_var) {
     if (!g.p) return;
-    SLFMM_REQUIRE(k >= 1 && k <= kMaxNmfK, SLFMM_ERR_BAD_ARG, "NMF rank must be in 1..16");
-    k_fill_stats<<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(g.p, g.n, norm, g.counts.get(), g.miss_ptr.get(),
-                                                             g.miss_idx.get(), W, H, k, mean, scale, tss, zero_var);
+    SLFMM_REQUIRE(k >= 1 && k <= kMaxNmfK, SLFMM_ERR_BAD_ARG, "NMF rank must be in 1.." + std::to_string(kMaxNmfK));
+    if (k <= 16)
+        k_fill_stats<16><<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(g.p, g.n, norm, g.counts.get(), g.miss_ptr.get(),
+                                                                     g.miss_idx.get(), W, H, k, mean, scale, tss,
+                                                                     zero_var);
+    else
+        k_fill_stats<32><<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(g.p, g.n, norm, g.counts.get(), g.miss_ptr.get(),
+                                                                     g.miss_idx.get(), W, H, k, mean, scale, tss,
+                                                                     zero_var);
     SLFMM_LAUNCHED(c, "k_fill_stats");
 }
 
 // narrow operand group size: the smallest of 8, 16, 32 that holds w, else 0
 static int narrow_group(int w) { return w <= 8 ? 8 : w <= 16 ? 16 : w <= 32 ? 32 : 0; }
 
-template <bool W4>
+template <bool W4, int KM>
 static void fill_row_correct_launch(Ctx& c, const Geno& g, unsigned grid, float* out, int ldo, int w,
                                     const float* Wop, int ldw, const float* Wn, const float* H, int k,
                                     const double* mean, const double* scale) {
@@ -591,19 +600,19 @@ static void fill_row_correct_launch(Ctx& c, const Geno& g, unsigned grid, float*
     const uint32_t* mi = g.miss_idx.get();
     switch (narrow_group(w)) {
         case 8:
-            k_fill_row_correct<8, W4><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, mp, mi, Wop, ldw, Wn, H, k, mean,
+            k_fill_row_correct<8, W4, KM><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, mp, mi, Wop, ldw, Wn, H, k, mean,
                                                                   scale);
             break;
         case 16:
-            k_fill_row_correct<16, W4><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, mp, mi, Wop, ldw, Wn, H, k, mean,
+            k_fill_row_correct<16, W4, KM><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, mp, mi, Wop, ldw, Wn, H, k, mean,
                                                                    scale);
             break;
         case 32:
-            k_fill_row_correct<32, W4><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, mp, mi, Wop, ldw, Wn, H, k, mean,
+            k_fill_row_correct<32, W4, KM><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, mp, mi, Wop, ldw, Wn, H, k, mean,
                                                                    scale);
             break;
         default:
-            k_fill_row_correct<0, W4><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, mp, mi, Wop, ldw, Wn, H, k, mean,
+            k_fill_row_correct<0, W4, KM><<<grid, 256, 0, c.stream>>>(out, ldo, g.p, w, mp, mi, Wop, ldw, Wn, H, k, mean,
                                                                   scale);
     }
 }
@@ -613,10 +622,14 @@ void launch_fill_row_correct(Ctx& c, const Geno& g, float* out, int ldo, int w, 
     if (!g.p || !w) return;
     SLFMM_REQUIRE(w <= 128 && k >= 1 && k <= kMaxNmfK, SLFMM_ERR_BAD_ARG, "NMF correction shape");
     const unsigned grid = (unsigned)grid_for(c, g.p, 8);
-    if (k % 4 == 0 && reinterpret_cast<uintptr_t>(Wn) % 16 == 0)
-        fill_row_correct_launch<true>(c, g, grid, out, ldo, w, Wop, ldw, Wn, H, k, mean, scale);
-    else
-        fill_row_correct_launch<false>(c, g, grid, out, ldo, w, Wop, ldw, Wn, H, k, mean, scale);
+    const bool w4 = k % 4 == 0 && reinterpret_cast<uintptr_t>(Wn) % 16 == 0;
+    if (k <= 16) {
+        if (w4) fill_row_correct_launch<true, 16>(c, g, grid, out, ldo, w, Wop, ldw, Wn, H, k, mean, scale);
+        else fill_row_correct_launch<false, 16>(c, g, grid, out, ldo, w, Wop, ldw, Wn, H, k, mean, scale);
+    } else {
+        if (w4) fill_row_correct_launch<true, 32>(c, g, grid, out, ldo, w, Wop, ldw, Wn, H, k, mean, scale);
+        else fill_row_correct_launch<false, 32>(c, g, grid, out, ldo, w, Wop, ldw, Wn, H, k, mean, scale);
+    }
     SLFMM_LAUNCHED(c, "k_fill_row_correct");
 }
 
@@ -626,7 +639,7 @@ __global__ void k_scale_mean_f32(const double* __restrict__ mean, const double* 
         out[r] = make_float2((float)scale[r], (float)mean[r]);
 }
 
-template <bool H4>
+template <bool H4, int KM>
 static void fill_col_correct_launch(Ctx& c, const Geno& g, unsigned grid, uint64_t nseg, double* S, int lds, int w,
                                     const float* Qop, int ldq, const float* Wn, const float* H, int k,
                                     const float2* sm) {
@@ -634,16 +647,16 @@ static void fill_col_correct_launch(Ctx& c, const Geno& g, unsigned grid, uint64
     const uint32_t* ci = g.missT_idx.get();
     switch (narrow_group(w)) {
         case 8:
-            k_fill_col_correct<8, H4><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, sm);
+            k_fill_col_correct<8, H4, KM><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, sm);
             break;
         case 16:
-            k_fill_col_correct<16, H4><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, sm);
+            k_fill_col_correct<16, H4, KM><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, sm);
             break;
         case 32:
-            k_fill_col_correct<32, H4><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, sm);
+            k_fill_col_correct<32, H4, KM><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, sm);
             break;
         default:
-            k_fill_col_correct<0, H4><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, sm);
+            k_fill_col_correct<0, H4, KM><<<grid, 256, 0, c.stream>>>(S, lds, g.n, w, nseg, cp, ci, Qop, ldq, Wn, H, k, sm);
     }
 }
 
@@ -656,10 +669,14 @@ void launch_fill_col_correct(Ctx& c, const Geno& g, double* S, int lds, int w, c
     DBuf<float2> sm(std::max<uint64_t>(g.p, 1), c.stream);
     k_scale_mean_f32<<<grid_for(c, g.p, 256), 256, 0, c.stream>>>(mean, scale, g.p, sm.get());
     SLFMM_LAUNCHED(c, "k_scale_mean_f32");
-    if (k % 4 == 0 && reinterpret_cast<uintptr_t>(H) % 16 == 0)
-        fill_col_correct_launch<true>(c, g, grid, nseg, S, lds, w, Qop, ldq, Wn, H, k, sm.get());
-    else
-        fill_col_correct_launch<false>(c, g, grid, nseg, S, lds, w, Qop, ldq, Wn, H, k, sm.get());
+    const bool h4 = k % 4 == 0 && reinterpret_cast<uintptr_t>(H) % 16 == 0;
+    if (k <= 16) {
+        if (h4) fill_col_correct_launch<true, 16>(c, g, grid, nseg, S, lds, w, Qop, ldq, Wn, H, k, sm.get());
+        else fill_col_correct_launch<false, 16>(c, g, grid, nseg, S, lds, w, Qop, ldq, Wn, H, k, sm.get());
+    } else {
+        if (h4) fill_col_correct_launch<true, 32>(c, g, grid, nseg, S, lds, w, Qop, ldq, Wn, H, k, sm.get());
+        else fill_col_correct_launch<false, 32>(c, g, grid, nseg, S, lds, w, Qop, ldq, Wn, H, k, sm.get());
+    }
     SLFMM_LAUNCHED(c, "k_fill_col_correct");
 }
 
@@ -704,14 +721,20 @@ void launch_nmf_clamp0_f32(Ctx& c, const float* src, int ld, double* X, uint64_t
 void launch_nmf_cv(Ctx& c, const Geno& g, uint64_t chunk, uint64_t mask_seed, double rate, const float* W,
                    const float* H, int k, double* part) {
     if (!g.p) return;
-    if (c.rng == SLFMM_RNG_CHACHA8)
-        k_nmf_cv<true><<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(packed_rows(g), g.stride, g.n, g.p, chunk,
-                                                                  mask_seed, rate_threshold(rate, 52), W, H, k,
-                                                                  g.counts.get(), part);
-    else
-        k_nmf_cv<false><<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(packed_rows(g), g.stride, g.n, g.p, chunk,
-                                                                   mask_seed, rate_threshold(rate), W, H, k,
-                                                                   g.counts.get(), part);
+    const bool cc = c.rng == SLFMM_RNG_CHACHA8;
+    const uint64_t th = cc ? rate_threshold(rate, 52) : rate_threshold(rate);
+    const unsigned grid = (unsigned)grid_for(c, g.p, 8);
+    auto go = [&](auto kern) {
+        kern<<<grid, 256, 0, c.stream>>>(packed_rows(g), g.stride, g.n, g.p, chunk, mask_seed, th, W, H, k,
+                                         g.counts.get(), part);
+    };
+    if (k <= 16) {
+        if (cc) go(k_nmf_cv<true, 16>);
+        else go(k_nmf_cv<false, 16>);
+    } else {
+        if (cc) go(k_nmf_cv<true, 32>);
+        else go(k_nmf_cv<false, 32>);
+    }
     SLFMM_LAUNCHED(c, "k_nmf_cv");
 }
 
@@ -722,14 +745,20 @@ void launch_nmf_gwas_cv(Ctx& c, const Geno& g, uint64_t chunk, uint64_t seed, do
     const uint64_t nchunks = ceil_div(g.p, chunk);
     k_obs_base<<<grid_for(c, nchunks, 64), 64, 0, c.stream>>>(g.counts.get(), g.p, chunk, base.get());
     SLFMM_LAUNCHED(c, "k_obs_base");
-    if (c.rng == SLFMM_RNG_CHACHA8)
-        k_nmf_gwas_cv<true><<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(packed_rows(g), g.stride, g.n, g.p, chunk,
-                                                                       seed, rate_threshold(rate, 52), W, Wpt, k,
-                                                                       base.get(), part);
-    else
-        k_nmf_gwas_cv<false><<<grid_for(c, g.p, 8), 256, 0, c.stream>>>(packed_rows(g), g.stride, g.n, g.p, chunk,
-                                                                        seed, rate_threshold(rate), W, Wpt, k,
-                                                                        base.get(), part);
+    const bool cc = c.rng == SLFMM_RNG_CHACHA8;
+    const uint64_t th = cc ? rate_threshold(rate, 52) : rate_threshold(rate);
+    const unsigned grid = (unsigned)grid_for(c, g.p, 8);
+    auto go = [&](auto kern) {
+        kern<<<grid, 256, 0, c.stream>>>(packed_rows(g), g.stride, g.n, g.p, chunk, seed, th, W, Wpt, k, base.get(),
+                                         part);
+    };
+    if (k <= 16) {
+        if (cc) go(k_nmf_gwas_cv<true, 16>);
+        else go(k_nmf_gwas_cv<false, 16>);
+    } else {
+        if (cc) go(k_nmf_gwas_cv<true, 32>);
+        else go(k_nmf_gwas_cv<false, 32>);
+    }
     SLFMM_LAUNCHED(c, "k_nmf_gwas_cv");
 }
 

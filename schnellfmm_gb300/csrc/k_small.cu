@@ -646,7 +646,7 @@ __global__ void k_inverse(const double* __restrict__ A, int a, double* __restric
     }
 }
 
-// One-sided (Hestenes) Jacobi SVD of a square a x a matrix (a <= 64) in one
+// One-sided (Hestenes) Jacobi SVD of a square a x a matrix in one
 // CTA: A V = U diag(sig).  Outputs V (a x a), sig (descending) and U = A V
 // / sig in place of A.  Pairs are rotated in parallel with a round-robin
 // ordering, one warp per pair.
@@ -748,7 +748,7 @@ __device__ void gs_columns(double* Vs, int ap, double* dots) {
 }
 
 // Eigen-decomposition of a symmetric positive semi-definite a x a matrix
-// (a <= 64; the Gram matrices of Step 0, the RSVD and the NMF probe) in one
+// (a <= kMaxDesign; the Gram matrices of Step 0, the RSVD and the NMF probe) in one
 // CTA: A V = V diag(sig), sig descending, V orthonormal; A is overwritten by V
 // (its left singular vectors).
 //
@@ -760,9 +760,13 @@ __device__ void gs_columns(double* Vs, int ap, double* dots) {
 // off-diagonal part to second order before a final Gram-Schmidt.  Pairs with
 // (numerically) equal eigenvalues are not mixed: any basis of their span is
 // an eigenbasis.  Eigenvalues are v_j^T A v_j of the final vectors.
+// Matrices wider than 64 columns work in `ws` (global memory, L2-resident:
+// 2 ap^2 doubles + 2 ap^2 floats) instead of shared memory.
 __global__ void __launch_bounds__(1024) k_jacobi_svd(double* __restrict__ A, int a,
-                                                     double* __restrict__ V, double* __restrict__ sig) {
-    extern __shared__ double sm[];
+                                                     double* __restrict__ V, double* __restrict__ sig,
+                                                     double* __restrict__ ws) {
+    extern __shared__ double sm_dyn[];
+    double* sm = ws ? ws : sm_dyn;
     const int ap = a + (a & 1);     // even number of columns (padded column is zero)
     double* M = sm;                 // column-major ap x ap scratch
     double* Vs = sm + ap * ap;      // column-major eigenvectors
@@ -770,10 +774,10 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(double* __restrict__ A, int
     float* V32 = M32 + ap * ap;
     double* B = reinterpret_cast<double*>(M32);  // reuses the FP32 area after phase 1
     __shared__ int rotated;
-    __shared__ double sg[64];
-    __shared__ double dots[64];
+    __shared__ double sg[kMaxDesign];
+    __shared__ double dots[kMaxDesign];
     __shared__ double bmax;
-    __shared__ int order[64];
+    __shared__ int order[kMaxDesign];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
     // phase 1: FP32 sweeps
     for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) {
@@ -1139,11 +1143,17 @@ void launch_inverse(Ctx& c, const double* A, int a, double* Ainv, int* status, d
 }
 
 void launch_jacobi_svd(Ctx& c, const double* A, int a, double* V, double* sig) {
-    SLFMM_REQUIRE(a <= 64, SLFMM_ERR_BAD_ARG, "Jacobi SVD limited to 64 x 64");
+    SLFMM_REQUIRE(a >= 1 && a <= kMaxDesign, SLFMM_ERR_BAD_ARG,
+                  "small eigen-solve limited to " + std::to_string(kMaxDesign) + " x " + std::to_string(kMaxDesign));
     const int ap = a + (a & 1);
     const size_t sm = 2 * (size_t)ap * ap * (sizeof(double) + sizeof(float));
-    set_smem((const void*)k_jacobi_svd, sm);
-    k_jacobi_svd<<<1, 1024, sm, c.stream>>>(const_cast<double*>(A), a, V, sig);
+    if (a <= 64) {
+        set_smem((const void*)k_jacobi_svd, sm);
+        k_jacobi_svd<<<1, 1024, sm, c.stream>>>(const_cast<double*>(A), a, V, sig, nullptr);
+    } else {
+        DBuf<double> ws((sm + sizeof(double) - 1) / sizeof(double), c.stream);
+        k_jacobi_svd<<<1, 1024, 0, c.stream>>>(const_cast<double*>(A), a, V, sig, ws.get());
+    }
     SLFMM_LAUNCHED(c, "k_jacobi_svd");
 }
 

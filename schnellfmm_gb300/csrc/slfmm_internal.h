@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <map>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -41,7 +42,7 @@ struct Error : std::runtime_error {
 constexpr int kHistBins = 100000;      // src/testing.rs:124
 constexpr long long kWaitCyclesMax = 8000000000ll;  // the device waits' own limit (~4 s at 2 GHz)
 constexpr int kGifNoAllocMaxTraits = 8; // traits the static histogram of slfmm_gif_noalloc holds
-constexpr int kMaxNmfK = 16;            // NMF rank limit of the imputation kernels
+constexpr int kMaxNmfK = 32;            // NMF rank limit of the imputation kernels
 constexpr double kHistWidth = 0.001;   // src/testing.rs:125
 constexpr double kGifDivisor = 0.4549; // src/testing.rs:169
 constexpr int kMaxW = 128;             // widest GEMM operand (columns)
@@ -170,6 +171,9 @@ struct Ctx {
     std::vector<PhaseMark> phase_marks;
     int rng = SLFMM_RNG_CHACHA8;  // stream of the Gaussian sketches
     long long expire_next_wait = 0;  // test hook: next split-FP8 launch's wait limit (SM cycles)
+    // a host draw of the reference's sketch stream started ahead of its use
+    struct PendingNormal;
+    std::shared_ptr<PendingNormal> pending_normal;
     bool autotune = false;   // time the tensor-core ring depths per shape once
     std::map<std::string, std::pair<int, int>> tuned;  // shape -> (packed ring cap, W ring cap)
 };
@@ -383,6 +387,9 @@ void launch_normal(Ctx& c, uint64_t seed, uint64_t rows, int cols, double* out);
 // stream: the device counter stream (launch_normal) or the reference's ChaCha8
 // stream drawn on the host (reference_normal) and copied
 void draw_normal(Ctx& c, uint64_t seed, uint64_t rows, int cols, double* out);
+// start the host draw of draw_normal(c, seed, rows, cols, .) on host threads
+// now (no-op for the device counter stream); draw_normal then waits for it
+void prefetch_normal(Ctx& c, uint64_t seed, uint64_t rows, int cols);
 void reference_normal(uint64_t seed, uint64_t rows, uint64_t cols, double* out);
 void launch_f64_to_f32_pad(Ctx& c, const double* A, uint64_t m, int a, int lda, float* out,
                            uint64_t m_pad, int ldo);

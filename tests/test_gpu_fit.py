@@ -144,15 +144,16 @@ def test_high_missingness(engines, prec):
     _check(res, ref.assoc, ref.u_hat)
 
 
-def test_duplicated_covariate_safe_inv(engine, capfd):
-    """A duplicated covariate makes C^T C and X^T X exactly singular: the
-    reference's safe_inv adds eps = 1e-8 max|diag| and warns on stderr
-    (src/testing.rs:996-1024); both copies then share the coefficient and
-    get near-zero t.  The GPU fit follows the same regularised algebra."""
+def test_singular_design_safe_inv(engine, capfd):
+    """A covariate that is constant (zero after centring) makes C^T C and
+    X^T X exactly singular whatever the summation order: the reference's
+    safe_inv adds eps = 1e-8 max|diag| and warns on stderr
+    (src/testing.rs:996-1024), and that covariate gets t = 0.  The other
+    covariates are unaffected."""
     sg = _sg()
     c = simdata.simulate(300, 2000, k_pop=3, fst=0.1, miss=0.01, d=3, n_causal=20, seed=12)
     x = 0.5 * c.x
-    x[:, 2] = x[:, 0]
+    x[:, 1] = 2.5
     omega = O.rng_normal_matrix(5, c.n, 13)
     geno = engine.upload(c.packed, c.n)
     capfd.readouterr()
@@ -161,7 +162,7 @@ def test_duplicated_covariate_safe_inv(engine, capfd):
     err = capfd.readouterr().err
     ref = O.fit_oracle64(c.raw, c.raw, x, k=3, norm=O.NORM_EIGENSTRAT, omega=omega)
     _check(res, ref.assoc, ref.u_hat)
-    # the oracle's safe_inv regularises the same two matrices
+    assert (res.tstat[:, 1] == 0).all() and (ref.assoc.tstat[:, 1] == 0).all()
     xs = O.center_covariates(x, False)
     cmat = np.hstack([np.ones((c.n, 1)), xs, ref.u_hat])
     ctc = cmat.T @ cmat
@@ -173,9 +174,34 @@ def test_duplicated_covariate_safe_inv(engine, capfd):
             f"{O.rust_exp(eps_c, 2)} diagonal regularization") in err, err
     assert (f"Warning: X^T X for sequential R^2 is singular, adding epsilon="
             f"{O.rust_exp(eps_x, 2)} diagonal regularization") in err, err
-    # both copies of the covariate: near-zero t, half the single-copy effect each
-    assert np.abs(res.tstat[:, [0, 2]]).max() < 1e-2
-    np.testing.assert_allclose(res.tstat[:, 0], res.tstat[:, 2], atol=1e-4)
+
+
+def test_duplicated_covariate(engine):
+    """Two identical covariates: C^T C is singular in exact arithmetic, and
+    the reference either regularises it (a zero LU pivot) or inverts it as it
+    is, depending on the rounding of C^T C; both give the pair near-zero t
+    and split beta between the copies.  The GPU fit uses the limit of the
+    regularised solve: both copies get |t| < 1e-3, every other covariate the
+    least-squares t of the design without the copy."""
+    sg = _sg()
+    c = simdata.simulate(300, 2000, k_pop=3, fst=0.1, miss=0.01, d=3, n_causal=20, seed=12)
+    x = 0.5 * c.x
+    x[:, 2] = x[:, 0]
+    omega = O.rng_normal_matrix(5, c.n, 13)
+    geno = engine.upload(c.packed, c.n)
+    res = sg.fit_lfmm2(geno, sg.SubsetSpec.all(), geno, x, sg.Lfmm2Config(k=3, norm=sg.SnpNorm.EIGENSTRAT),
+                       omega=omega, engine=engine)
+    ref = O.fit_oracle64(c.raw, c.raw, x[:, :2], k=3, norm=O.NORM_EIGENSTRAT, omega=omega)
+    assert O.principal_angles_sin_max(res.u_hat, ref.u_hat) < 1e-3
+    assert np.abs(res.tstat[:, [0, 2]]).max() < 1e-3
+    # same least-squares fit; t scales with sqrt(df), and df = n - 1 - d - K
+    # counts the copy (src/testing.rs:272-279)
+    expect = ref.assoc.tstat[:, 1] * np.sqrt((c.n - 1 - 3 - 3) / (c.n - 1 - 2 - 3))
+    assert np.abs(res.tstat[:, 1] - expect).max() <= 1e-3
+    # ridge effects: the copies share the single-copy effect
+    full = O.fit_oracle64(c.raw, c.raw, x, k=3, norm=O.NORM_EIGENSTRAT, omega=omega)
+    scale = np.abs(full.assoc.beta).max()
+    assert np.abs(res.beta - full.assoc.beta).max() <= 1e-3 * scale
 
 
 def test_bounded_wait_expiry_leaves_context_usable():

@@ -24,13 +24,15 @@ def _cohort(seed=13):
     return raw, packed, c.x
 
 
-@pytest.mark.parametrize("prec", ["fp8", "bf16", "fp32"])
-def test_nmf_fit_matches_oracle(engines, prec):
+@pytest.mark.parametrize("prec,k", [("fp8", 4), ("bf16", 4), ("fp32", 4), ("fp8", 20)])
+def test_nmf_fit_matches_oracle(engines, prec, k):
+    """k = 20: NMF ranks above 16 (NmfConfig.k is any usize in the
+    reference, src/nmf.rs:15-35)."""
     import schnellfmm_gb300 as sg
     eng = engines[prec]
     raw, packed, x = _cohort()
     n, p = raw.shape
-    k, it, rate, chunk, seed = 4, 6, 0.01, 1000, 42
+    it, rate, chunk, seed = 6, 0.01, 1000, 42
     nmf = sg.NmfConfig(k=k, n_iter=it, eps=1e-16, cv_rate=rate)
     cfg = sg.Lfmm2Config(k=3, lambda_=1e-5, oversampling=10, norm=sg.SnpNorm.EIGENSTRAT,
                          impute=sg.ImputeStrategy.NMF, nmf=nmf, chunk_size=chunk, seed=seed)
@@ -61,7 +63,7 @@ def test_nmf_rank_limit(engine):
     import schnellfmm_gb300 as sg
     raw, packed, x = _cohort(5)
     geno = engine.upload(packed, raw.shape[0])
-    cfg = sg.Lfmm2Config(k=3, impute=sg.ImputeStrategy.NMF, nmf=sg.NmfConfig(k=17, n_iter=1))
+    cfg = sg.Lfmm2Config(k=3, impute=sg.ImputeStrategy.NMF, nmf=sg.NmfConfig(k=33, n_iter=1))
     with pytest.raises(sg.SchnelGpuError, match="NMF rank"):
         sg.fit_lfmm2(geno, sg.SubsetSpec.all(), geno, x, cfg, engine=engine)
     geno.free()
