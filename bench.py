@@ -642,10 +642,13 @@ def main():
             sg.fit_lfmm2_host(host_packed, n, x, cfg, est_subset=est, engine=eng, out=out)
         barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        calls = []
         t0 = time.perf_counter()
         e0.record(torch_stream)
         for _ in range(args.steps):
+            tc = time.perf_counter()
             sg.fit_lfmm2_host(host_packed, n, x, cfg, est_subset=est, engine=eng, out=out)
+            calls.append((time.perf_counter() - tc) * 1e3)
         e1.record(torch_stream)
         barrier()
         wall = (time.perf_counter() - t0) * 1e3 / args.steps
@@ -654,7 +657,7 @@ def main():
         d2h = sum(a.nbytes for a in out.values())
         e2e = {"value": job_rate(p, world, e2e_ms), "unit": "SNPs/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
-               "per_step_ms": [e0.elapsed_time(e1) / args.steps, wall]}
+               "per_step_ms": [e0.elapsed_time(e1) / args.steps, wall], "call_wall_ms": calls}
         # where one call's time goes (after the timed loop): device time per
         # phase from events on the engine's stream, host wall time per phase,
         # and this box's page-locked copy rates

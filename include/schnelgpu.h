@@ -179,6 +179,12 @@ int slfmm_contract_raw(slfmm_ctx* ctx, const slfmm_geno* g, int flags, const dou
 /* center_covariates (src/lib.rs:102-117). x, out: n x d row-major. */
 int slfmm_center_covariates(slfmm_ctx* ctx, const double* x, uint64_t n, uint32_t d,
                             int scale, double* out);
+/* Parity hook for the small symmetric eigen-solves (the X^T X of Step 0,
+ * src/precompute.rs:47, and the l x l Gram of the randomized SVD's final
+ * small SVD, src/rsvd.rs:162, both LAPACK in the reference): a (a x a,
+ * row-major, symmetric positive semi-definite, a <= 256) -> eigenvectors
+ * v_out (a x a, column j = vector j) and eigenvalues sig_out, descending. */
+int slfmm_small_eigh(slfmm_ctx* ctx, const double* a, uint32_t dim, double* v_out, double* sig_out);
 /* Random sketch Omega (n x l) the engine uses for a given seed. */
 int slfmm_generate_omega(slfmm_ctx* ctx, uint64_t seed, uint64_t n, uint32_t l,
                          double* out);

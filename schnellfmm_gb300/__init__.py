@@ -126,7 +126,7 @@ EXPORTED_SYMBOLS = (
     "slfmm_fit_host", "slfmm_write_tsv", "slfmm_format_exp6", "slfmm_simulate", "slfmm_geno_download",
     "slfmm_profile_enable", "slfmm_profile_read", "slfmm_host_alloc", "slfmm_host_free", "slfmm_contract_raw",
     "slfmm_gif_noalloc", "slfmm_fit_traits", "slfmm_fit_many", "slfmm_reference_normal", "slfmm_write_parquet",
-    "slfmm_phase_count", "slfmm_phase_read", "slfmm_debug_expire_next_wait",
+    "slfmm_phase_count", "slfmm_phase_read", "slfmm_debug_expire_next_wait", "slfmm_small_eigh",
 )
 
 _lib_handle = None
@@ -171,6 +171,7 @@ def load_library(path: Optional[os.PathLike] = None) -> C.CDLL:
         "slfmm_profile_enable": (i32, [vp, i32]),
         "slfmm_profile_read": (i32, [vp, C.c_char_p, _dp, C.POINTER(u64), _dp, _dp]),
         "slfmm_phase_count": (i32, [vp]),
+        "slfmm_small_eigh": (i32, [vp, vp, u32, vp, vp]),
         "slfmm_debug_expire_next_wait": (i32, [vp, u64]),
         "slfmm_phase_read": (i32, [vp, i32, C.c_char_p, C.c_size_t, _dp, _dp]),
         "slfmm_host_alloc": (i32, [C.c_size_t, C.POINTER(vp)]),
@@ -449,6 +450,17 @@ class Engine:
             self.check(self.lib.slfmm_phase_read(self.h, i, name, 96, C.byref(dev), C.byref(host)))
             out.append({"phase": name.value.decode(), "device_ms": dev.value, "host_ms": host.value})
         return out
+
+    def small_eigh(self, a: np.ndarray):
+        """Eigenvalues (descending) and eigenvectors (columns) of a small
+        symmetric PSD matrix by the engine's FP32-sweep / FP64-refined Jacobi
+        solve (the parity hook of the Step 0 and RSVD eigen-solves)."""
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        m = a.shape[0]
+        v = np.empty((m, m))
+        s = np.empty(m)
+        self.check(self.lib.slfmm_small_eigh(self.h, _ptr(a), m, _ptr(v), _ptr(s)))
+        return s, v
 
     def generate_omega(self, seed: int, n: int, l: int) -> np.ndarray:
         out = np.empty((n, l))

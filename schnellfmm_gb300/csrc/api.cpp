@@ -400,7 +400,7 @@ bool fp8_row_indicator_plan(int w, uint64_t tiles) {
     const int wp = pad16(w);
     const char* ind_env = std::getenv("SLFMM_TC8_ROW_IND");
     if (wp > kMaxW || (ind_env && ind_env[0] == '0')) return false;
-    const Fp8Plan pl = fp8_plan(wp, true, tiles);
+    const Fp8Plan pl = fp8_plan(wp, true, tiles, true);
     return pl.ok && pl.n_ind != 0;
 }
 
@@ -408,14 +408,18 @@ bool fp8_row_operand(Ctx& c, uint64_t n, uint64_t tiles, const double* W, int w,
     op.wp = pad16(w);
     op.n_pad = round_up(n, 256);  // whole split-FP8 stages (256 codes)
     if (!fp8_row_indicator_plan(w, tiles)) return false;
-    op.pl = fp8_plan(op.wp, true, tiles);
+    // genotype and indicator MMAs multiply the same W: the indicator's three
+    // terms are the leading three of the main four (ind_shared plan)
+    op.pl = fp8_plan(op.wp, true, tiles, true);
     op.cs.alloc(op.wp, c.stream);
     op.cs.zero();
     launch_colsums(c, W, n, w, ldw, op.cs.get());
     op.B.alloc((uint64_t)op.pl.n_total * op.n_pad, c.stream);
     op.isc.alloc(op.pl.n_total, c.stream);
     launch_fp8_terms_f64(c, W, ldw, n, w, op.wp, op.n_pad, nullptr, 4, 0, op.B.get(), op.isc.get());
-    launch_fp8_terms_f64(c, W, ldw, n, w, op.wp, op.n_pad, nullptr, 3, (int)op.pl.n_main, op.B.get(), op.isc.get());
+    if (!op.pl.ind_shared)
+        launch_fp8_terms_f64(c, W, ldw, n, w, op.wp, op.n_pad, nullptr, 3, (int)op.pl.n_main, op.B.get(),
+                             op.isc.get());
     op.ok = true;
     return true;
 }
@@ -425,7 +429,7 @@ bool fp8_row_operand(Ctx& c, uint64_t n, uint64_t tiles, const double* W, int w,
 void fp8_row_launch(Ctx& c, const Geno& g, const SnpStd& s, const Fp8RowOperand& op, uint64_t r0, uint64_t rows,
                     float* out, int* err_dev) {
     const uint64_t t0 = r0 / 128;
-    const TileView tv{g.tiles.get() + t0 * g.kbt * 4096, g.kbt, g.ntiles - t0};
+    const TileView tv{g.tiles.get() + t0 * g.kbt * 4096, g.kbt, g.ntiles - t0, t0};
     launch_tc8_rows(c, op.pl, tv, rows, g.n, op.B.get(), op.isc.get(), op.n_pad, 1, s.mean.get() + r0,
                     s.scale.get() + r0, op.cs.get(), out + r0 * op.wp, op.wp, 1, 0, err_dev);
 }
@@ -489,7 +493,7 @@ void fp8_row_run(Ctx& c, const Geno& g, const SnpStd& s, const Fp8RowPass& rp, u
         return;
     }
     const uint64_t t0 = r0 / 128;
-    const TileView tv{g.tiles.get() + t0 * g.kbt * 4096, g.kbt, g.ntiles - t0};
+    const TileView tv{g.tiles.get() + t0 * g.kbt * 4096, g.kbt, g.ntiles - t0, t0};
     for (size_t b = 0; b < rp.plans.size(); ++b) {
         const double share = (double)rp.plans[b].wpad / rp.wp;
         ProfScope ps(c, "row_contract", bytes * share, flops * share);
@@ -1794,6 +1798,20 @@ int slfmm_generate_omega(slfmm_ctx* c, uint64_t seed, uint64_t n, uint32_t l, do
     API_CATCH(c)
 }
 
+int slfmm_small_eigh(slfmm_ctx* c, const double* a_host, uint32_t a, double* v_out, double* sig_out) {
+    if (!c || !a_host || !v_out || !sig_out || a == 0) return SLFMM_ERR_BAD_ARG;
+    API_TRY
+    SLFMM_CUDA(cudaSetDevice(c->device));
+    SLFMM_REQUIRE(a <= (uint32_t)kMaxDesign, SLFMM_ERR_BAD_ARG,
+                  "matrix wider than " + std::to_string(kMaxDesign));
+    DBuf<double> A = upload(*c, a_host, (size_t)a * a), V((size_t)a * a, c->stream), sig(a, c->stream);
+    launch_jacobi_svd(*c, A.get(), (int)a, V.get(), sig.get());
+    d2h(*c, v_out, V.get(), (size_t)a * a);
+    d2h(*c, sig_out, sig.get(), a);
+    sync(*c);
+    API_CATCH(c)
+}
+
 int slfmm_estimate_factors(slfmm_ctx* c, const slfmm_geno* y_est, const double* x, uint32_t d,
                            const slfmm_config* cfg, const double* omega, double* u_hat) {
     if (!c || !y_est || !x || !u_hat) return SLFMM_ERR_BAD_ARG;
@@ -2140,7 +2158,7 @@ int slfmm_contract_raw(slfmm_ctx* c, const slfmm_geno* g, int flags, const doubl
     if (c->precision == SLFMM_PREC_SPLIT_FP8) {
         const TileView tv = build_tiles(*c, *g, transposed);
         const uint64_t tiles = ceil_div(rows, 128);
-        const Fp8Plan pl = fp8_plan(wp, with_ind, tiles);
+        const Fp8Plan pl = fp8_plan(wp, with_ind, tiles, true);
         SLFMM_REQUIRE(pl.ok || !with_ind, SLFMM_ERR_BAD_ARG, "indicator operand too wide for one launch");
         const int cb = pl.ok ? wp : 64;
         for (int c0 = 0; c0 < (int)w; c0 += cb) {
@@ -2149,7 +2167,7 @@ int slfmm_contract_raw(slfmm_ctx* c, const slfmm_geno* g, int flags, const doubl
             DBuf<uint8_t> B((uint64_t)pb.n_total * K_pad, c->stream);
             DBuf<float> isc(pb.n_total, c->stream);
             launch_fp8_terms_f64(*c, Wd.get() + c0, (int)w, K, wb, bp, K_pad, nullptr, 4, 0, B.get(), isc.get());
-            if (with_ind)
+            if (with_ind && !pb.ind_shared)
                 launch_fp8_terms_f64(*c, Wd.get() + c0, (int)w, K, wb, bp, K_pad, nullptr, 3, (int)pb.n_main, B.get(),
                                      isc.get());
             launch_tc8_rows(*c, pb, tv, rows, K, B.get(), isc.get(), K_pad, 0, nullptr, nullptr, nullptr,

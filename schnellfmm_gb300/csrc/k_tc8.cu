@@ -51,7 +51,8 @@ struct Tc8Args {
     uint32_t wpad;          // output columns
     uint32_t n_main;        // kMainTerms * wpad
     uint32_t n_ind;         // kIndTerms * wpad or 0
-    uint32_t n_total;       // B rows / D columns in use
+    uint32_t n_total;       // B rows (n_main + n_ind, or n_main when ind_shared)
+    uint32_t ind_shared;    // indicator MMAs read B rows [0, n_ind) of the main terms
     uint32_t d_cols;        // TMEM columns reserved for D
     uint32_t a_cols;        // TMEM columns per A stage (32, or 64 with the indicator)
     uint32_t stages, tmem_cols;  // stages: A operand ring depth (TMEM)
@@ -69,6 +70,8 @@ struct Tc8Args {
     const float* inv_scale; // n_total: 2^-(e0 + 4t) per B row
     int mode;               // 0: out = P + M; 1: out = s_r (P - mu_r (cs_c - M))
     long long expire_cycles;  // > 0: test hook, see below
+    uint32_t tile0;           // matrix index of the tile of blockIdx.x = 0
+    uint32_t rotate;          // stagger the K order of the tiles (see below)
     const double* row_mean;
     const double* row_scale;
     const double* cs;
@@ -138,7 +141,7 @@ __device__ __forceinline__ void tc8_mma_loop(const Tc8Args& a, uint32_t tmem, ui
     const uint64_t bdesc0 = smem_desc(bsm_addr);
     const uint64_t bstep = a.b_stage_bytes >> 4;          // descriptor address units per stage
     const uint64_t chstep = (uint64_t)chunk * (128 >> 4);  // per main chunk of B rows
-    const uint64_t indoff = (uint64_t)a.n_main * (128 >> 4);
+    const uint64_t indoff = a.ind_shared ? 0ull : (uint64_t)a.n_main * (128 >> 4);
     const uint64_t hstep = (uint64_t)a.n_total * (128 >> 4);  // next 128-sample half of the stage
     const uint32_t d_ind = tmem + a.n_main;
     const uint32_t a0 = tmem + a.a_base;
@@ -228,6 +231,13 @@ __global__ void __launch_bounds__(kThreads, 1)
     const uint32_t kb1 = min(a.kb_total, kb0 + a.kb_per_split);
     const uint32_t nkb = kb1 > kb0 ? kb1 - kb0 : 0;
     const bool ind = a.n_ind != 0;
+    // K order: the tiles of a launch all read the same W stages, and with
+    // every CTA at the same stage the L2 serves one 56 KB stage to ~150 SMs
+    // at once.  Each tile starts at its own stage (a rotation of the K loop,
+    // fixed by its index in the matrix, so the accumulation order and the
+    // bits do not depend on how rows are split into launches).
+    const uint32_t rot = (a.rotate && nkb > 1) ? (uint32_t)(((a.tile0 + blockIdx.x) * 37ull) % nkb) : 0u;
+    auto kstage = [&](uint32_t i) { return i + rot < nkb ? i + rot : i + rot - nkb; };
 
     if (threadIdx.x == 0) {
         for (uint32_t s = 0; s < SW; ++s) {
@@ -273,9 +283,10 @@ __global__ void __launch_bounds__(kThreads, 1)
             Ring pr{0, 0};
             uint32_t issued = 0;
             for (uint32_t i = 0; i < nkb; ++i) {
+                const uint32_t ks = kstage(i);
                 if (i >= P && !mbar_wait(p_empty + pr.slot, pr.phase ^ 1u, a.err, 21)) break;
                 mbar_arrive_tx(p_full + pr.slot, kStageBytes);
-                bulk_g2s(psm + pr.slot * kStageBytes, src + (uint64_t)i * kStageBytes, kStageBytes, p_full + pr.slot);
+                bulk_g2s(psm + pr.slot * kStageBytes, src + (uint64_t)ks * kStageBytes, kStageBytes, p_full + pr.slot);
                 issued = i + 1;
                 pr.advance(1, P);
             }
@@ -292,7 +303,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             for (uint32_t i = 0; i < nkb; ++i) {
                 if (i >= SW && !mbar_wait(b_empty + wr.slot, wr.phase ^ 1u, a.err, 23)) break;
                 mbar_arrive_tx(full_b + wr.slot, a.b_stage_bytes);
-                const int kb = (int)(kb0 + i);
+                const int kb = (int)(kb0 + kstage(i));
                 for (int h = 0; h < kHalves; ++h)
                     for (uint32_t l = 0; l < a.loads; ++l) {
                         const uint32_t y = l * a.box_rows;
@@ -461,10 +472,11 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (ind) {
                 for (int t = 0; t < kIndTerms; ++t) {
                     const uint32_t col = a.n_main + t * a.wpad + c0;
+                    const uint32_t scol = (a.ind_shared ? 0u : a.n_main) + t * a.wpad + c0;
                     tmem_ld_x16(lane_base + col, v);
                     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-                    for (int k = 0; k < 16; ++k) pi[k] = fmaf(scl[col + k], v[k], pi[k]);
+                    for (int k = 0; k < 16; ++k) pi[k] = fmaf(scl[scol + k], v[k], pi[k]);
                 }
             }
             if (live) {
@@ -793,13 +805,15 @@ static int env_int(const char* name, int dflt) {
 // The plan with explicit caps on the packed-code ring (pmax), the W ring
 // (smax) and the MMA wait group (gmax); fp8_plan takes them from the
 // environment (defaults 8, 8, 4).
-Fp8Plan fp8_plan_knobs(int wpad, bool ind, uint64_t tiles, int pmax_in, int smax, int gmax_in, int wmax) {
+Fp8Plan fp8_plan_knobs(int wpad, bool ind, uint64_t tiles, int pmax_in, int smax, int gmax_in, int wmax,
+                       bool ind_shared) {
     Fp8Plan p{};
     p.wpad = (uint32_t)wpad;
     p.n_main = kMainTerms * wpad;
     p.n_ind = ind ? kIndTerms * wpad : 0;
-    p.n_total = p.n_main + p.n_ind;
-    p.d_cols = (uint32_t)round_up(p.n_total, 32);
+    p.ind_shared = (ind && ind_shared) ? 1u : 0u;
+    p.n_total = p.ind_shared ? p.n_main : p.n_main + p.n_ind;      // B rows
+    p.d_cols = (uint32_t)round_up(p.n_main + p.n_ind, 32);       // accumulator columns
     p.a_cols = (ind ? 2 : 1) * (kStageK / 4);  // TMEM columns of one stage's A operand(s)
     p.b_stage_bytes = p.n_total * 128 * kHalves;
     // one CTA per SM: all of TMEM; the packed-code ring gives up depth (8, 4,
@@ -852,9 +866,10 @@ Fp8Plan fp8_plan_knobs(int wpad, bool ind, uint64_t tiles, int pmax_in, int smax
     return p;
 }
 
-Fp8Plan fp8_plan(int wpad, bool ind, uint64_t tiles) {
+Fp8Plan fp8_plan(int wpad, bool ind, uint64_t tiles, bool ind_shared) {
     return fp8_plan_knobs(wpad, ind, tiles, env_int("SLFMM_TC8_PSTAGES", 8), env_int("SLFMM_TC8_STAGES", 8),
-                          env_int("SLFMM_TC8_GROUP", 4), env_int("SLFMM_TC8_WSTAGES", 8));
+                          env_int("SLFMM_TC8_GROUP", 4), env_int("SLFMM_TC8_WSTAGES", 8),
+                          ind_shared && env_int("SLFMM_TC8_SHARED_IND", 1) != 0);
 }
 
 // row-major packed rows (rows x stride) -> tile-major copy; one thread per
@@ -1145,7 +1160,7 @@ static Fp8Plan tc8_tuned_plan(Ctx& c, const Fp8Plan& pl, const TileView& tv, uin
                             "/" + std::to_string(splits) + "/" + std::to_string(mode);
     auto rebuild = [&](int pmax, int smax) {
         return fp8_plan_knobs((int)pl.wpad, pl.n_ind != 0, ceil_div(rows, (uint64_t)kM), pmax, smax, (int)pl.group,
-                              env_int("SLFMM_TC8_WSTAGES", 8));
+                              env_int("SLFMM_TC8_WSTAGES", 8), pl.ind_shared != 0);
     };
     auto it = c.tuned.find(key);
     if (it != c.tuned.end()) return rebuild(it->second.first, it->second.second);
@@ -1234,6 +1249,7 @@ static int tc8_launch(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t ro
     a.n_main = pl.n_main;
     a.n_ind = pl.n_ind;
     a.n_total = pl.n_total;
+    a.ind_shared = pl.ind_shared;
     a.d_cols = pl.d_cols;
     a.a_cols = pl.a_cols;
     a.stages = pl.stages;
@@ -1250,6 +1266,8 @@ static int tc8_launch(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t ro
     a.loads = pl.loads;
     a.inv_scale = inv_scale;
     a.expire_cycles = c.expire_next_wait;
+    a.tile0 = (uint32_t)tv.tile0;
+    a.rotate = (uint32_t)env_int("SLFMM_TC8_ROTATE", 1);  // tuning override
     c.expire_next_wait = 0;
     a.mode = mode;
     a.row_mean = row_mean;

@@ -287,12 +287,17 @@ void launch_scale_product(Ctx& c, const double* a, const double* b, uint64_t n, 
 struct Fp8Plan {
     uint32_t wpad, n_main, n_ind, n_total, d_cols, a_cols, stages, wstages, pstages, group, tmem_cols, b_stage_bytes;
     uint32_t kcopies, nsplit, a_base;
+    uint32_t ind_shared;  // indicator MMAs read the leading main terms (B holds n_main rows)
     uint32_t box_rows, loads;
     size_t smem;
     bool ok;
 };
-Fp8Plan fp8_plan(int wpad, bool ind, uint64_t tiles);
-Fp8Plan fp8_plan_knobs(int wpad, bool ind, uint64_t tiles, int pmax, int smax, int gmax, int wmax);
+// ind_shared: the indicator operand's terms are the first kIndTerms terms of
+// the main operand's split (a row pass: both multiply the same W), so B holds
+// only the main terms and the indicator MMAs read their leading rows
+Fp8Plan fp8_plan(int wpad, bool ind, uint64_t tiles, bool ind_shared = false);
+Fp8Plan fp8_plan_knobs(int wpad, bool ind, uint64_t tiles, int pmax, int smax, int gmax, int wmax,
+                       bool ind_shared = false);
 // the row-major packed copy of a matrix (a sample subset built from the
 // tile-major copies has none: the passes that need it must not run on it)
 inline const uint8_t* packed_rows(const Geno& g) {
@@ -304,6 +309,7 @@ inline const uint8_t* packed_rows(const Geno& g) {
 struct TileView {
     const uint8_t* base;
     uint64_t kbt, ntiles;
+    uint64_t tile0 = 0;  // index of the first tile in the whole matrix
 };
 TileView build_tiles(Ctx& c, const Geno& g, bool transposed);
 // The samples keep_dev[0 .. n_keep) of a matrix as a new matrix holding only
