@@ -752,14 +752,17 @@ __device__ void gs_columns(double* Vs, int ap, double* dots) {
 // CTA: A V = V diag(sig), sig descending, V orthonormal; A is overwritten by V
 // (its left singular vectors).
 //
-// GB300 runs FP64 at a small fraction of its FP32 rate, so the rotations run
-// as FP32 one-sided Jacobi sweeps (pairs in parallel, round-robin order, one
-// warp per pair) to ~1e-6; V is re-orthonormalised in FP64 (Gram-Schmidt,
-// twice), B = V^T A V formed in FP64, and one first-order step
-// V <- V (I + E), E_ij = B_ij / (B_jj - B_ii), removes the remaining
-// off-diagonal part to second order before a final Gram-Schmidt.  Pairs with
-// (numerically) equal eigenvalues are not mixed: any basis of their span is
-// an eigenbasis.  Eigenvalues are v_j^T A v_j of the final vectors.
+// GB300 runs FP64 at a small fraction of its FP32 rate, so the bulk of the
+// rotation work runs as FP32 one-sided Jacobi sweeps (pairs in parallel,
+// round-robin order, one warp per pair) to ~1e-6; V is re-orthonormalised in
+// FP64 (Gram-Schmidt, twice) and B = V^T A V formed in FP64.  B is then
+// diagonal up to ~1e-6 of its norm, and two-sided cyclic Jacobi sweeps in
+// FP64 (Golub & Van Loan, Algorithm 8.5.2 with the parallel round-robin
+// ordering) finish it -- quadratic convergence, typically two sweeps --
+// accumulating their rotations into R; V <- V R and a final Gram-Schmidt.
+// Jacobi rotations are bounded (|tan| <= 1), so clusters of equal or nearly
+// equal eigenvalues need no special case.  Eigenvalues are v_j^T A v_j of the
+// final vectors.
 // Matrices wider than 64 columns work in `ws` (global memory, L2-resident:
 // 2 ap^2 doubles + 2 ap^2 floats) instead of shared memory.
 __global__ void __launch_bounds__(1024) k_jacobi_svd(double* __restrict__ A, int a,
@@ -778,6 +781,8 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(double* __restrict__ A, int
     __shared__ double dots[kMaxDesign];
     __shared__ double bmax;
     __shared__ int order[kMaxDesign];
+    __shared__ int jp[kMaxDesign / 2], jq[kMaxDesign / 2];
+    __shared__ double jc[kMaxDesign / 2], js[kMaxDesign / 2];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
     // phase 1: FP32 sweeps
     for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) {
@@ -813,21 +818,71 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(double* __restrict__ A, int
         bmax = m;
     }
     __syncthreads();
-    // phase 4: V <- V (I + E), into M
-    const double gap_tol = 1e-9 * bmax + 1e-300;
-    for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) {
-        const int col = e / ap, row = e % ap;   // new V[row, col]
-        double t = Vs[col * ap + row];
-        const double bjj = B[col * ap + col];
-        for (int i = 0; i < ap; ++i) {
-            if (i == col) continue;
-            const double gap = bjj - B[i * ap + i];
-            if (fabs(gap) > gap_tol) t += Vs[i * ap + row] * (B[col * ap + i] / gap);
+    // phase 4: FP64 two-sided Jacobi on B, rotations accumulated in R (in M)
+    double* R = M;
+    for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) R[e] = (e / ap == e % ap) ? 1.0 : 0.0;
+    const int npairs = ap / 2;
+    const double skip = 4e-16 * bmax;  // off-diagonals at the rounding level of B
+    for (int sweep = 0; sweep < 12; ++sweep) {
+        if (threadIdx.x == 0) rotated = 0;
+        __syncthreads();
+        for (int round = 0; round < ap - 1; ++round) {
+            auto pos = [&](int idx) { return idx == 0 ? 0 : 1 + ((idx - 1 + round) % (ap - 1)); };
+            for (int k = threadIdx.x; k < npairs; k += blockDim.x) {
+                int pc = pos(k), qc = pos(ap - 1 - k);
+                if (pc > qc) { const int t = pc; pc = qc; qc = t; }
+                const double app = B[pc * ap + pc], aqq = B[qc * ap + qc], apq = B[qc * ap + pc];
+                double cs = 1.0, sn = 0.0;
+                if (fabs(apq) > skip && apq != 0.0) {
+                    const double tau = (aqq - app) / (2.0 * apq);
+                    const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+                    cs = 1.0 / sqrt(1.0 + t * t);
+                    sn = t * cs;
+                    rotated = 1;
+                }
+                jp[k] = pc; jq[k] = qc; jc[k] = cs; js[k] = sn;
+            }
+            __syncthreads();
+            // B <- B J and R <- R J (columns p, q of each pair)
+            for (int e = threadIdx.x; e < npairs * ap; e += blockDim.x) {
+                const int k = e / ap, i = e % ap;
+                if (js[k] == 0.0) continue;
+                const double cs = jc[k], sn = js[k];
+                double* bp = B + jp[k] * ap;
+                double* bq = B + jq[k] * ap;
+                double x = bp[i], y = bq[i];
+                bp[i] = cs * x - sn * y;
+                bq[i] = sn * x + cs * y;
+                double* rp = R + jp[k] * ap;
+                double* rq = R + jq[k] * ap;
+                x = rp[i]; y = rq[i];
+                rp[i] = cs * x - sn * y;
+                rq[i] = sn * x + cs * y;
+            }
+            __syncthreads();
+            // B <- J^T B (rows p, q of each pair)
+            for (int e = threadIdx.x; e < npairs * ap; e += blockDim.x) {
+                const int k = e / ap, j = e % ap;
+                if (js[k] == 0.0) continue;
+                const double cs = jc[k], sn = js[k];
+                const int pr = jp[k], qr = jq[k];
+                const double x = B[j * ap + pr], y = B[j * ap + qr];
+                B[j * ap + pr] = cs * x - sn * y;
+                B[j * ap + qr] = sn * x + cs * y;
+            }
+            __syncthreads();
         }
-        M[e] = t;
+        if (!rotated) break;
+    }
+    // V <- V R (into B's area, no longer needed)
+    for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) {
+        const int col = e / ap, row = e % ap;
+        double t = 0.0;
+        for (int i = 0; i < ap; ++i) t += Vs[i * ap + row] * R[col * ap + i];
+        B[e] = t;
     }
     __syncthreads();
-    for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) Vs[e] = M[e];
+    for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) Vs[e] = B[e];
     __syncthreads();
     gs_columns(Vs, ap, dots);
     // phase 5: eigenvalues v_j^T A v_j, descending order

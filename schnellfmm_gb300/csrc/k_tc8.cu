@@ -1157,7 +1157,8 @@ static Fp8Plan tc8_tuned_plan(Ctx& c, const Fp8Plan& pl, const TileView& tv, uin
                               const double* row_mean, const double* row_scale, const double* cs, int ldo, int splits,
                               uint64_t split_stride) {
     const std::string key = std::to_string(pl.wpad) + "/" + std::to_string(pl.n_ind) + "/" + std::to_string(K) +
-                            "/" + std::to_string(splits) + "/" + std::to_string(mode);
+                            "/" + std::to_string(splits) + "/" + std::to_string(mode) + "/" +
+                            std::to_string(pl.ind_shared);
     auto rebuild = [&](int pmax, int smax) {
         return fp8_plan_knobs((int)pl.wpad, pl.n_ind != 0, ceil_div(rows, (uint64_t)kM), pmax, smax, (int)pl.group,
                               env_int("SLFMM_TC8_WSTAGES", 8), pl.ind_shared != 0);
