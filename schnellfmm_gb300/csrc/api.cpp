@@ -416,9 +416,10 @@ bool fp8_row_operand(Ctx& c, uint64_t n, uint64_t tiles, const double* W, int w,
     launch_colsums(c, W, n, w, ldw, op.cs.get());
     op.B.alloc((uint64_t)op.pl.n_total * op.n_pad, c.stream);
     op.isc.alloc(op.pl.n_total, c.stream);
-    launch_fp8_terms_f64(c, W, ldw, n, w, op.wp, op.n_pad, nullptr, 4, 0, op.B.get(), op.isc.get());
+    const int nr = (int)op.pl.n_total;
+    launch_fp8_terms_f64(c, W, ldw, n, w, op.wp, op.n_pad, nullptr, 4, 0, nr, op.B.get(), op.isc.get());
     if (!op.pl.ind_shared)
-        launch_fp8_terms_f64(c, W, ldw, n, w, op.wp, op.n_pad, nullptr, 3, (int)op.pl.n_main, op.B.get(),
+        launch_fp8_terms_f64(c, W, ldw, n, w, op.wp, op.n_pad, nullptr, 3, (int)op.pl.n_main, nr, op.B.get(),
                              op.isc.get());
     op.ok = true;
     return true;
@@ -471,7 +472,8 @@ void fp8_row_prepare(Ctx& c, const Geno& g, const double* W, int w, int ldw, Fp8
         const Fp8Plan pb = bp == rp.wp ? pl : fp8_plan(bp, false, tiles);
         DBuf<uint8_t> B((uint64_t)pb.n_total * rp.n_pad, c.stream);
         DBuf<float> isc(pb.n_total, c.stream);
-        launch_fp8_terms_f64(c, W + c0, ldw, g.n, wb, bp, rp.n_pad, nullptr, 4, 0, B.get(), isc.get());
+        launch_fp8_terms_f64(c, W + c0, ldw, g.n, wb, bp, rp.n_pad, nullptr, 4, 0, (int)pb.n_total, B.get(),
+                             isc.get());
         rp.plans.push_back(pb);
         rp.Bs.push_back(std::move(B));
         rp.iscs.push_back(std::move(isc));
@@ -578,7 +580,7 @@ void col_contract_base(Ctx& c, const Geno& g, const SnpStd& s, const float* Q, i
         DBuf<double> coef(std::max<uint64_t>(g.p, 1), c.stream), colterm(wp, c.stream);
         launch_scale_product(c, s.mean.get(), s.scale.get(), g.p, coef.get());
         launch_fp8_terms_f32_pair(c, Q, wp, g.p, w, wp, p_pad, s.scale.get(), ind ? coef.get() : nullptr,
-                                  (int)pl.n_main, B.get(), isc.get());
+                                  (int)pl.n_main, (int)pl.n_total, B.get(), isc.get());
         const int splits = tc_split_count(c, g.n, g.p);
         DBuf<float> part((uint64_t)splits * g.n * wp, c.stream);
         int used = 0;
@@ -2166,10 +2168,11 @@ int slfmm_contract_raw(slfmm_ctx* c, const slfmm_geno* g, int flags, const doubl
             const Fp8Plan pb = bp == wp ? pl : fp8_plan(bp, false, tiles);
             DBuf<uint8_t> B((uint64_t)pb.n_total * K_pad, c->stream);
             DBuf<float> isc(pb.n_total, c->stream);
-            launch_fp8_terms_f64(*c, Wd.get() + c0, (int)w, K, wb, bp, K_pad, nullptr, 4, 0, B.get(), isc.get());
+            launch_fp8_terms_f64(*c, Wd.get() + c0, (int)w, K, wb, bp, K_pad, nullptr, 4, 0, (int)pb.n_total,
+                                 B.get(), isc.get());
             if (with_ind && !pb.ind_shared)
-                launch_fp8_terms_f64(*c, Wd.get() + c0, (int)w, K, wb, bp, K_pad, nullptr, 3, (int)pb.n_main, B.get(),
-                                     isc.get());
+                launch_fp8_terms_f64(*c, Wd.get() + c0, (int)w, K, wb, bp, K_pad, nullptr, 3, (int)pb.n_main,
+                                     (int)pb.n_total, B.get(), isc.get());
             launch_tc8_rows(*c, pb, tv, rows, K, B.get(), isc.get(), K_pad, 0, nullptr, nullptr, nullptr,
                             o.get() + c0, wp, 1, 0);
         }

@@ -13,8 +13,14 @@
 // second set of terms, which makes the mean-imputation correction of missing
 // calls exact without any gather over the missing-call lists.
 //
-// Every CTA streams its own W stages with TMA; a stage is reloaded only after
-// the CTA's MMAs on it have completed (per-stage "B empty" barriers).
+// Every CTA streams its own W stages; a stage is reloaded only after the
+// CTA's MMAs on it have completed (per-stage "B empty" barriers).  The W
+// operand is stored stage-major in global memory -- each 256-sample stage one
+// contiguous blob [half][row][128 B] with the 128-byte swizzle already applied
+// -- so a stage lands with ONE bulk copy.  On GB300 the copies one thread
+// issues complete one after another at a near-constant ~500-750 cycles each
+// whatever their size (4 KB to 64 KB, L2 or HBM), so the number of copies per
+// stage, not their bytes, sets how fast a single producer can feed the MMAs.
 //
 // Replaces the reference's per-chunk FP64 dgemms (src/rsvd.rs:61-69, :88-97,
 // :117-125, :144-153; src/testing.rs:355-374) and, through the indicator
@@ -22,7 +28,6 @@
 // (src/bed.rs:349-378) inside them.
 #include <cuda.h>
 #include <cuda_fp8.h>
-#include <cudaTypedefs.h>
 
 #include <cstdlib>
 
@@ -64,10 +69,9 @@ struct Tc8Args {
     uint32_t a_base;        // first TMEM column of the A stages
     uint32_t usets;         // unpack sets in use: at most `stages`, so that a set never waits on a stage
                             // two uses ahead (an mbarrier parity wait cannot tell those apart)
-    uint32_t b_stage_bytes; // n_total * 128
-    uint32_t box_rows;      // rows per W TMA box
-    uint32_t loads;         // W boxes this CTA issues per stage
+    uint32_t b_stage_bytes; // n_total * 256: one stage of the stage-major W operand
     const float* inv_scale; // n_total: 2^-(e0 + 4t) per B row
+    const uint8_t* wop;     // stage-major, pre-swizzled W operand (wop_offset)
     int mode;               // 0: out = P + M; 1: out = s_r (P - mu_r (cs_c - M))
     long long expire_cycles;  // > 0: test hook, see below
     uint32_t tile0;           // matrix index of the tile of blockIdx.x = 0
@@ -206,8 +210,7 @@ __device__ __forceinline__ void tc8_mma_dispatch(const Tc8Args& a, uint32_t tmem
                                         len0, skip);
 }
 
-__global__ void __launch_bounds__(kThreads, 1)
-    k_tc8_rows(const __grid_constant__ CUtensorMap tm_b, Tc8Args a) {
+__global__ void __launch_bounds__(kThreads, 1) k_tc8_rows(const __grid_constant__ Tc8Args a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const uint32_t S = a.stages, SW = a.wstages, P = a.pstages;
@@ -297,20 +300,15 @@ __global__ void __launch_bounds__(kThreads, 1)
         // each spinning role has a warp of its own: lanes of one warp that
         // spin in different loops starve each other
         if (lane == 0) {
-            // W producer: every W stage in boxes of box_rows rows
+            // W producer: one bulk copy per stage
             Ring wr{0, 0};
             uint32_t issued = 0;
             for (uint32_t i = 0; i < nkb; ++i) {
                 if (i >= SW && !mbar_wait(b_empty + wr.slot, wr.phase ^ 1u, a.err, 23)) break;
                 mbar_arrive_tx(full_b + wr.slot, a.b_stage_bytes);
-                const int kb = (int)(kb0 + kstage(i));
-                for (int h = 0; h < kHalves; ++h)
-                    for (uint32_t l = 0; l < a.loads; ++l) {
-                        const uint32_t y = l * a.box_rows;
-                        uint8_t* dst = bsm + wr.slot * a.b_stage_bytes + (h * a.n_total + y) * 128;
-                        const int x = kb * kStageK + h * kTileK;
-                        tma_2d(dst, &tm_b, x, (int)y, full_b + wr.slot);
-                    }
+                const uint64_t kb = kb0 + kstage(i);
+                bulk_g2s(bsm + wr.slot * a.b_stage_bytes, a.wop + kb * a.b_stage_bytes, a.b_stage_bytes,
+                         full_b + wr.slot);
                 issued = i + 1;
                 wr.advance(1, SW);
             }
@@ -543,14 +541,28 @@ __device__ __forceinline__ float pow2f(int ex) {
     return (ex >= -126 && ex <= 127) ? __int_as_float((127 + ex) << 23) : ldexpf(1.f, ex);
 }
 
-// W (K x w) -> `terms` E4M3 rows per column at B rows row_off + t * wpad + c,
-// K contiguous, zero padded to K_pad; inv_scale[row] = 2^-(e0 + 4t).
+// Byte offset of element (row, k) of a stage-major W operand with n_rows rows:
+// stage kb = k / 256 is the contiguous blob [half][row][128 B] at
+// kb * n_rows * 256, and within each 128-byte row the 16-byte chunk j sits at
+// chunk j ^ (row & 7) -- the 128-byte swizzle the MMA descriptors expect of a
+// 1024-byte aligned shared-memory stage (n_rows % 8 == 0 keeps every half's
+// rows aligned to the 8-row swizzle period).
+__device__ __forceinline__ uint64_t wop_offset(uint32_t row, uint64_t k, uint32_t n_rows) {
+    const uint64_t kb = k >> 8;
+    const uint32_t h = (uint32_t)(k >> 7) & 1u, kk = (uint32_t)k & 127u;
+    return kb * (uint64_t)n_rows * 256 + (uint64_t)(h * n_rows + row) * 128 +
+           ((((kk >> 4) ^ (row & 7u)) << 4) | (kk & 15u));
+}
+
+// W (K x w) -> `terms` E4M3 rows per column at B rows row_off + t * wpad + c
+// of a stage-major operand with n_rows rows (wop_offset), zero padded to
+// K_pad; inv_scale[row] = 2^-(e0 + 4t).
 // Term t is round_e4m3((r - terms_<t) * 2^(e0 + 4t)); the power-of-two scales
 // are exact, so each step's residual is rounded once.
 template <typename T>
 __global__ void __launch_bounds__(256) k_fp8_terms(const T* __restrict__ src, int ld, uint64_t K, int w, int wpad,
                                                    uint64_t K_pad, const double* __restrict__ kscale, int terms,
-                                                   int row_off, const unsigned* __restrict__ colmax,
+                                                   int row_off, int n_rows, const unsigned* __restrict__ colmax,
                                                    uint8_t* __restrict__ B, float* __restrict__ inv_scale) {
     __shared__ __align__(16) uint8_t tile[kMainTerms][32][132];
     __shared__ float ks[128];
@@ -601,7 +613,8 @@ __global__ void __launch_bounds__(256) k_fp8_terms(const T* __restrict__ src, in
             const int kk = (kp & ~15) | ((kp & 7) << 1) | ((kp >> 3) & 1);
             word |= (uint32_t)tile[t][cc][kk] << (8 * b);
         }
-        *reinterpret_cast<uint32_t*>(B + (uint64_t)(row_off + t * wpad + c) * K_pad + k0 + kp0) = word;
+        *reinterpret_cast<uint32_t*>(B + wop_offset((uint32_t)(row_off + t * wpad + c), k0 + kp0, (uint32_t)n_rows)) =
+            word;
     }
 }
 
@@ -687,7 +700,7 @@ __global__ void __launch_bounds__(256) k_colmax_pair(const float* __restrict__ s
 // conversion rounds each value as the scalar one does, so the terms are the
 // same) and the power-of-two scales taken from per-column tables.
 __global__ void __launch_bounds__(256) k_fp8_terms_pair(const float* __restrict__ src, int ld, uint64_t K, int w,
-                                                        int wpad, uint64_t K_pad, TermSet sa, TermSet sb,
+                                                        int wpad, uint64_t K_pad, TermSet sa, TermSet sb, int n_rows,
                                                         uint8_t* __restrict__ B, float* __restrict__ inv_scale) {
     constexpr int kT = kMainTerms + kIndTerms;
     __shared__ __align__(16) uint8_t tile[kT][32][132];
@@ -754,7 +767,7 @@ __global__ void __launch_bounds__(256) k_fp8_terms_pair(const float* __restrict_
             const int kk = (kp & ~15) | ((kp & 7) << 1) | ((kp >> 3) & 1);
             word |= (uint32_t)tile[t][cc][kk] << (8 * b);
         }
-        *reinterpret_cast<uint32_t*>(B + (uint64_t)row * K_pad + k0 + kp0) = word;
+        *reinterpret_cast<uint32_t*>(B + wop_offset((uint32_t)row, k0 + kp0, (uint32_t)n_rows)) = word;
     }
 }
 
@@ -765,33 +778,6 @@ __global__ void k_sub_colterm(double* __restrict__ S, int lds, uint64_t n, int w
         const int c = (int)(t - i * w);
         S[i * lds + c] -= colterm[c];
     }
-}
-
-// thread-safe one-time lookup (contexts may run on several host threads)
-PFN_cuTensorMapEncodeTiled_v12000 encode_fn8() {
-    static const PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        SLFMM_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q));
-        SLFMM_REQUIRE(q == cudaDriverEntryPointSuccess && p, SLFMM_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
-        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }();
-    return fn;
-}
-
-CUtensorMap map2d_u8(const uint8_t* base, uint64_t inner, uint64_t rows, uint32_t box_inner, uint32_t box_rows,
-                     bool swizzle128) {
-    CUtensorMap m;
-    cuuint64_t dims[2] = {inner, rows};
-    cuuint64_t strides[1] = {inner};
-    cuuint32_t box[2] = {box_inner, box_rows};
-    cuuint32_t es[2] = {1, 1};
-    CUresult r = encode_fn8()(&m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 2, const_cast<uint8_t*>(base), dims, strides, box, es,
-                              CU_TENSOR_MAP_INTERLEAVE_NONE,
-                              swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
-                              CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    SLFMM_REQUIRE(r == CUDA_SUCCESS, SLFMM_ERR_CUDA, "tensor map encode failed: " + std::to_string((int)r));
-    return m;
 }
 
 }  // namespace
@@ -815,7 +801,7 @@ Fp8Plan fp8_plan_knobs(int wpad, bool ind, uint64_t tiles, int pmax_in, int smax
     p.n_total = p.ind_shared ? p.n_main : p.n_main + p.n_ind;      // B rows
     p.d_cols = (uint32_t)round_up(p.n_main + p.n_ind, 32);       // accumulator columns
     p.a_cols = (ind ? 2 : 1) * (kStageK / 4);  // TMEM columns of one stage's A operand(s)
-    p.b_stage_bytes = p.n_total * 128 * kHalves;
+    p.b_stage_bytes = p.n_total * 128 * kHalves;  // one bulk copy: 16-byte multiple, below the 1 MB tx limit
     // one CTA per SM: all of TMEM; the packed-code ring gives up depth (8, 4,
     // then 2 stages) until shared memory holds at least two W stages
     p.tmem_cols = 512;
@@ -857,11 +843,7 @@ Fp8Plan fp8_plan_knobs(int wpad, bool ind, uint64_t tiles, int pmax_in, int smax
     p.stages -= p.stages % p.group;
     p.smem = fixed + (size_t)p.pstages * kStageBytes + (size_t)p.wstages * p.b_stage_bytes;
     (void)tiles;
-    const uint32_t rows_mine = p.n_total;
-    p.loads = (uint32_t)ceil_div(rows_mine, 256);
-    while (rows_mine % p.loads != 0 || (rows_mine / p.loads) % 8 != 0) ++p.loads;
-    p.box_rows = rows_mine / p.loads;
-    p.ok = p.stages >= 2 && p.n_main % ceil_div(p.n_main, 256) == 0 && (p.n_main / ceil_div(p.n_main, 256)) % 16 == 0 &&
+    p.ok = p.n_total % 8 == 0 && p.stages >= 2 && p.n_main % ceil_div(p.n_main, 256) == 0 && (p.n_main / ceil_div(p.n_main, 256)) % 16 == 0 &&
            p.n_ind <= 256;
     return p;
 }
@@ -1083,22 +1065,27 @@ TileView build_tiles(Ctx& c, const Geno& g, bool transposed) {
 }
 
 void launch_fp8_terms_f64(Ctx& c, const double* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
-                          const double* kscale, int terms, int row_off, uint8_t* B, float* inv_scale) {
+                          const double* kscale, int terms, int row_off, int n_rows, uint8_t* B, float* inv_scale) {
     DBuf<unsigned> cm(wpad, c.stream);
     cm.zero();
     SLFMM_REQUIRE(w >= 1 && w <= 128 && wpad <= 128, SLFMM_ERR_BAD_ARG, "operand wider than 128 columns");
+    SLFMM_REQUIRE(n_rows % 8 == 0 && row_off + terms * wpad <= n_rows && K_pad % kStageK == 0, SLFMM_ERR_BAD_ARG,
+                  "bad stage-major operand shape");
     k_colmax_abs<double><<<grid_for(c, K, 8), 256, 0, c.stream>>>(src, ld, K, w, kscale, cm.get());
     SLFMM_LAUNCHED(c, "k_colmax_abs");
     dim3 grid((unsigned)ceil_div(K_pad, 128), (unsigned)ceil_div(wpad, 32));
-    k_fp8_terms<double><<<grid, 256, 0, c.stream>>>(src, ld, K, w, wpad, K_pad, kscale, terms, row_off, cm.get(), B,
-                                                    inv_scale);
+    k_fp8_terms<double><<<grid, 256, 0, c.stream>>>(src, ld, K, w, wpad, K_pad, kscale, terms, row_off, n_rows,
+                                                    cm.get(), B, inv_scale);
     SLFMM_LAUNCHED(c, "k_fp8_terms");
 }
 
 void launch_fp8_terms_f32_pair(Ctx& c, const float* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
-                               const double* ks_main, const double* ks_ind, int ind_row_off, uint8_t* B,
+                               const double* ks_main, const double* ks_ind, int ind_row_off, int n_rows, uint8_t* B,
                                float* inv_scale) {
     SLFMM_REQUIRE(w >= 1 && w <= 128 && wpad <= 128, SLFMM_ERR_BAD_ARG, "operand wider than 128 columns");
+    SLFMM_REQUIRE(n_rows % 8 == 0 && kMainTerms * wpad <= n_rows &&
+                      (!ks_ind || ind_row_off + kIndTerms * wpad <= n_rows) && K_pad % kStageK == 0,
+                  SLFMM_ERR_BAD_ARG, "bad stage-major operand shape");
     DBuf<unsigned> cm(2 * (uint64_t)wpad, c.stream);
     cm.zero();
     unsigned* cma = cm.get();
@@ -1120,21 +1107,8 @@ void launch_fp8_terms_f32_pair(Ctx& c, const float* src, int ld, uint64_t K, int
     const TermSet sa{ks_main, kMainTerms, 0, cma};
     const TermSet sb{ks_ind, ks_ind ? kIndTerms : 0, ind_row_off, cmb};
     dim3 grid((unsigned)ceil_div(K_pad, 128), (unsigned)ceil_div(wpad, 32));
-    k_fp8_terms_pair<<<grid, 256, 0, c.stream>>>(src, ld, K, w, wpad, K_pad, sa, sb, B, inv_scale);
+    k_fp8_terms_pair<<<grid, 256, 0, c.stream>>>(src, ld, K, w, wpad, K_pad, sa, sb, n_rows, B, inv_scale);
     SLFMM_LAUNCHED(c, "k_fp8_terms_pair");
-}
-
-void launch_fp8_terms_f32(Ctx& c, const float* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
-                          const double* kscale, int terms, int row_off, uint8_t* B, float* inv_scale) {
-    DBuf<unsigned> cm(wpad, c.stream);
-    cm.zero();
-    SLFMM_REQUIRE(w >= 1 && w <= 128 && wpad <= 128, SLFMM_ERR_BAD_ARG, "operand wider than 128 columns");
-    k_colmax_abs<float><<<grid_for(c, K, 8), 256, 0, c.stream>>>(src, ld, K, w, kscale, cm.get());
-    SLFMM_LAUNCHED(c, "k_colmax_abs");
-    dim3 grid((unsigned)ceil_div(K_pad, 128), (unsigned)ceil_div(wpad, 32));
-    k_fp8_terms<float><<<grid, 256, 0, c.stream>>>(src, ld, K, w, wpad, K_pad, kscale, terms, row_off, cm.get(), B,
-                                                   inv_scale);
-    SLFMM_LAUNCHED(c, "k_fp8_terms");
 }
 
 void throw_tc8_timeout(int site) {
@@ -1235,8 +1209,9 @@ static int tc8_launch(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t ro
     SLFMM_REQUIRE(tv.ntiles >= ceil_div(rows, kM), SLFMM_ERR_BAD_ARG,
                   "tile-major operand has too few tiles");
     SLFMM_REQUIRE(mode == 0 || pl.n_ind != 0, SLFMM_ERR_BAD_ARG, "row correction needs the indicator operand");
+    SLFMM_REQUIRE(reinterpret_cast<uintptr_t>(B) % 16 == 0 && pl.b_stage_bytes % 16 == 0, SLFMM_ERR_BAD_ARG,
+                  "W operand not 16-byte aligned");
     raise_dynamic_smem((const void*)k_tc8_rows, pl.smem);
-    const CUtensorMap tb = map2d_u8(B, K_pad, pl.n_total, 128, pl.box_rows, true);
     DBuf<int> err;
     if (!err_dev) {
         err.alloc(1, c.stream);
@@ -1263,9 +1238,8 @@ static int tc8_launch(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t ro
     a.usets = std::min<uint32_t>(kUnpackSets, std::min(pl.stages, pl.pstages));
     a.tmem_cols = pl.tmem_cols;
     a.b_stage_bytes = pl.b_stage_bytes;
-    a.box_rows = pl.box_rows;
-    a.loads = pl.loads;
     a.inv_scale = inv_scale;
+    a.wop = B;
     a.expire_cycles = c.expire_next_wait;
     a.tile0 = (uint32_t)tv.tile0;
     a.rotate = (uint32_t)env_int("SLFMM_TC8_ROTATE", 1);  // tuning override
@@ -1287,15 +1261,15 @@ static int tc8_launch(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t ro
     cfg.blockDim = dim3(kThreads, 1, 1);
     cfg.dynamicSmemBytes = pl.smem;
     cfg.stream = c.stream;
-    const cudaError_t le = cudaLaunchKernelEx(&cfg, k_tc8_rows, tb, a);
+    const cudaError_t le = cudaLaunchKernelEx(&cfg, k_tc8_rows, a);
     if (le != cudaSuccess) {
         cudaGetLastError();
         char buf[320];
         snprintf(buf, sizeof buf,
                  "split-FP8 contraction launch failed (%s): grid %u x %u, smem %zu, stages %u/%u, pstages %u, group %u, "
-                 "n_total %u, box %u x %u, rows %llu, K %llu",
-                 cudaGetErrorString(le), gx, gy, pl.smem, pl.stages, pl.wstages, pl.pstages, pl.group, pl.n_total, 128u,
-                 pl.box_rows, (unsigned long long)rows, (unsigned long long)K);
+                 "n_total %u, rows %llu, K %llu",
+                 cudaGetErrorString(le), gx, gy, pl.smem, pl.stages, pl.wstages, pl.pstages, pl.group, pl.n_total,
+                 (unsigned long long)rows, (unsigned long long)K);
         throw Error(SLFMM_ERR_CUDA, buf);
     }
     SLFMM_LAUNCHED(c, "k_tc8_rows");

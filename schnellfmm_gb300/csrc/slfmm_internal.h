@@ -288,7 +288,6 @@ struct Fp8Plan {
     uint32_t wpad, n_main, n_ind, n_total, d_cols, a_cols, stages, wstages, pstages, group, tmem_cols, b_stage_bytes;
     uint32_t kcopies, nsplit, a_base;
     uint32_t ind_shared;  // indicator MMAs read the leading main terms (B holds n_main rows)
-    uint32_t box_rows, loads;
     size_t smem;
     bool ok;
 };
@@ -317,16 +316,17 @@ TileView build_tiles(Ctx& c, const Geno& g, bool transposed);
 // the sample-major tiles, their 2-bit transpose, counts from the tiles.
 void tiles_subset_samples(Ctx& c, const Geno& full, const uint32_t* keep_dev, uint64_t n_keep, Geno& sub);
 void tile_chunk(Ctx& c, const Geno& g, uint64_t r0, uint64_t r1, bool last);
+// `terms` E4M3 terms of diag(kscale) src at rows row_off + t * wpad + c of a
+// stage-major W operand of n_rows rows (every 256-sample stage one contiguous,
+// pre-swizzled blob: one bulk copy per stage in k_tc8_rows)
 void launch_fp8_terms_f64(Ctx& c, const double* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
-                          const double* kscale, int terms, int row_off, uint8_t* B, float* inv_scale);
-void launch_fp8_terms_f32(Ctx& c, const float* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
-                          const double* kscale, int terms, int row_off, uint8_t* B, float* inv_scale);
+                          const double* kscale, int terms, int row_off, int n_rows, uint8_t* B, float* inv_scale);
 // both operands of a transposed pass in one pass over src: 4 terms of
 // diag(ks_main) src at B rows 0.., and (ks_ind non-null) 3 terms of
 // diag(ks_ind) src at B rows ind_row_off..; the same terms as two separate
-// launch_fp8_terms_f32 calls
+// term launches
 void launch_fp8_terms_f32_pair(Ctx& c, const float* src, int ld, uint64_t K, int w, int wpad, uint64_t K_pad,
-                               const double* ks_main, const double* ks_ind, int ind_row_off, uint8_t* B,
+                               const double* ks_main, const double* ks_ind, int ind_row_off, int n_rows, uint8_t* B,
                                float* inv_scale);
 // mode 0: out = P (+ M); mode 1: out = s_r (P - mu_r (cs_c - M)) (needs the indicator).
 // err_dev null: the launch waits and throws when a bounded device wait expired;
