@@ -452,41 +452,81 @@ struct Fp8RowPass {
     DBuf<double> cs;
 };
 
-void fp8_row_prepare(Ctx& c, const Geno& g, const double* W, int w, int ldw, Fp8RowPass& rp) {
+// Whether a row pass over g takes the missing-call indicator operand rather
+// than the sparse per-SNP fix over the missing-call lists.  The indicator adds
+// three E4M3 terms of tensor work and 96 + 64 TMEM columns that shorten the
+// operand ring; the fix gathers one W row per missing call from L2.  Measured
+// on GB300 at n = 20 000, w = 30, 0.5 % missing: the ring without the
+// indicator runs 4.6-5.5 ms per 2M-SNP pass and the fix about 2 ms, against
+// 8.2-15 ms for the indicator form (whose time also varied 2x between
+// otherwise equal runs).  So the indicator is taken only when
+// SLFMM_TC8_ROW_IND=1 forces it.  The rule looks neither at the data nor at
+// how the matrix is held (matrices kept only as tiles build their lists from
+// the tiles), so an upload that runs the sketch pass chunk by chunk, and a
+// per-trait sample subset, take the same form as the pass over a resident
+// upload of the same samples.
+bool fp8_row_indicator_forced() {
+    const char* env = std::getenv("SLFMM_TC8_ROW_IND");
+    return env && env[0] == '1';
+}
+
+bool fp8_row_take_indicator(const Geno&) { return fp8_row_indicator_forced(); }
+
+// The operand of a row pass over n samples and `tiles` row tiles: the
+// indicator form when `indicator` and it has a plan, else column blocks
+// without it (needs nothing of the matrix itself).
+void fp8_row_operand_prepare(Ctx& c, uint64_t n, uint64_t tiles, const double* W, int w, int ldw, bool indicator,
+                             Fp8RowPass& rp) {
     rp.w = w;
     rp.wp = pad16(w);
-    rp.n_pad = round_up(g.n, 256);  // whole split-FP8 stages (256 codes)
-    const uint64_t tiles = ceil_div(g.p, 128);
-    build_tiles(c, g, false);
-    if (fp8_row_operand(c, g.n, tiles, W, w, ldw, rp.op)) return;
+    rp.n_pad = round_up(n, 256);  // whole split-FP8 stages (256 codes)
+    if (indicator && fp8_row_operand(c, n, tiles, W, w, ldw, rp.op)) return;
     rp.W32.alloc(rp.n_pad * rp.wp, c.stream);
-    launch_f64_to_f32_pad(c, W, g.n, w, ldw, rp.W32.get(), rp.n_pad, rp.wp);
+    launch_f64_to_f32_pad(c, W, n, w, ldw, rp.W32.get(), rp.n_pad, rp.wp);
     const Fp8Plan pl = fp8_plan(rp.wp, false, tiles);
     const int cb = pl.ok ? rp.wp : 64;
     rp.cs.alloc(rp.wp, c.stream);
     rp.cs.zero();
-    launch_colsums(c, W, g.n, w, ldw, rp.cs.get());
+    launch_colsums(c, W, n, w, ldw, rp.cs.get());
     for (int c0 = 0; c0 < w; c0 += cb) {
         // the epilogue writes pb.wpad columns: the last block is padded only to 16
         const int wb = std::min(cb, w - c0), bp = std::min(cb, pad16(wb));
         const Fp8Plan pb = bp == rp.wp ? pl : fp8_plan(bp, false, tiles);
         DBuf<uint8_t> B((uint64_t)pb.n_total * rp.n_pad, c.stream);
         DBuf<float> isc(pb.n_total, c.stream);
-        launch_fp8_terms_f64(c, W + c0, ldw, g.n, wb, bp, rp.n_pad, nullptr, 4, 0, (int)pb.n_total, B.get(),
+        launch_fp8_terms_f64(c, W + c0, ldw, n, wb, bp, rp.n_pad, nullptr, 4, 0, (int)pb.n_total, B.get(),
                              isc.get());
         rp.plans.push_back(pb);
         rp.Bs.push_back(std::move(B));
         rp.iscs.push_back(std::move(isc));
         rp.c0s.push_back(c0);
     }
+}
+
+void fp8_row_prepare(Ctx& c, const Geno& g, const double* W, int w, int ldw, Fp8RowPass& rp) {
+    build_tiles(c, g, false);
+    const bool ind = fp8_row_take_indicator(g);
+    fp8_row_operand_prepare(c, g.n, ceil_div(g.p, 128), W, w, ldw, ind, rp);
+    if (!rp.op.ok) build_missing_lists(c, g);
+}
+
+// the per-SNP missing-call fix of rows [r0, r0 + rows) of a pass without
+// the indicator: out = s_j (P - mu_j (cs - sum over the SNP's missing calls of W))
+void fp8_row_fix(Ctx& c, const Geno& g, const SnpStd& s, const Fp8RowPass& rp, uint64_t r0, uint64_t rows,
+                 float* out) {
+    if (rp.op.ok) return;
     build_missing_lists(c, g);
+    launch_rowfix_mean(c, out + r0 * rp.wp, rp.wp, rows, rp.w, g.miss_ptr.get() + r0, g.miss_idx.get(),
+                       rp.W32.get(), rp.wp, rp.cs.get(), s.mean.get() + r0, s.scale.get() + r0);
 }
 
 // rows [r0, r0 + rows) of out (ld wp); err_dev as in launch_tc8_rows.  The
 // tensor-core launches are profiled as "row_contract" (algorithmic bytes:
-// the rows' packed codes, their outputs and the operand).
+// the rows' packed codes, their outputs and the operand).  Without the
+// indicator, `fix` false leaves the raw products P in out and the per-SNP fix
+// to fp8_row_fix (an upload that has not finished its missing-call lists).
 void fp8_row_run(Ctx& c, const Geno& g, const SnpStd& s, const Fp8RowPass& rp, uint64_t r0, uint64_t rows,
-                 float* out, int* err_dev) {
+                 float* out, int* err_dev, bool fix = true) {
     const double bytes = (double)rows * ceil_div(g.n, 4) + (double)rows * rp.w * 4 + (double)g.n * rp.w * 4;
     const double flops = 2.0 * g.n * rows * rp.w;
     if (rp.op.ok) {
@@ -503,8 +543,7 @@ void fp8_row_run(Ctx& c, const Geno& g, const SnpStd& s, const Fp8RowPass& rp, u
                         s.mean.get() + r0, s.scale.get() + r0, rp.cs.get(), out + r0 * rp.wp + rp.c0s[b], rp.wp, 1,
                         0, err_dev);
     }
-    launch_rowfix_mean(c, out + r0 * rp.wp, rp.wp, rows, rp.w, g.miss_ptr.get() + r0, g.miss_idx.get(),
-                       rp.W32.get(), rp.wp, rp.cs.get(), s.mean.get() + r0, s.scale.get() + r0);
+    if (fix) fp8_row_fix(c, g, s, rp, r0, rows, out);
 }
 
 // out (p x wp, FP32) = Y_hat^T W, W = n x w FP64 (leading dim ldw)
@@ -1319,7 +1358,7 @@ struct Presketch : ChunkHook {
     Step0 s0;
     SnpStd se;
     int norm = 0, l = 0;
-    Fp8RowOperand op;
+    Fp8RowPass rp;
     DBuf<float> Z;
     DBuf<int> err;
     // covariates (Step 0), P Omega and its split-FP8 operand, while the first
@@ -1328,26 +1367,31 @@ struct Presketch : ChunkHook {
         step0(c, x, n, d, cfg->lambda, cfg->scale_cov != 0, s0);
         DBuf<double> W;
         sketch_operand(c, s0, n, l, cfg->seed, omega, W);
-        SLFMM_REQUIRE(fp8_row_operand(c, n, ceil_div(p, 128), W.get(), l, l, op), SLFMM_ERR_CUDA,
-                      "sketch operand plan changed");
+        // the form the pass over the resident matrix takes (fp8_row_prepare)
+        fp8_row_operand_prepare(c, n, ceil_div(p, 128), W.get(), l, l, fp8_row_indicator_forced(), rp);
         se.mean.alloc(p, c.stream);
         se.scale.alloc(p, c.stream);
         se.tss.alloc(p, c.stream);
         se.zero_var.alloc(p, c.stream);
-        Z.alloc(p * op.wp, c.stream);
+        Z.alloc(p * rp.wp, c.stream);
         err.alloc(1, c.stream);
         err.zero();
     }
     void rows(Ctx& c, const Geno& g, uint64_t r0, uint64_t r1) override {
         launch_stats_mean_range(c, g, r0, r1 - r0, norm, se.mean.get(), se.scale.get(), se.tss.get(),
                                 se.zero_var.get());
-        fp8_row_launch(c, g, se, op, r0, r1 - r0, Z.get(), err.get());
+        fp8_row_run(c, g, se, rp, r0, r1 - r0, Z.get(), err.get(), false);
+    }
+    // after the upload, once the missing-call lists are complete: the per-SNP
+    // fix of the pass without the indicator, over every row at once
+    void finish(Ctx& c, const Geno& g) {
+        fp8_row_fix(c, g, se, rp, 0, g.p, Z.get());
     }
 };
 
 // true when the estimation and testing matrices are the same upload of p SNPs
-// with mean imputation and the sketch width has an indicator plan (host-side
-// checks only; the device setup runs in begin())
+// with mean imputation (host-side checks only; the device setup runs in
+// begin())
 bool presketch_eligible(Ctx& c, uint64_t n, uint64_t p, const double* x, int d, const slfmm_config* cfg,
                         const double* omega, Presketch& ps) {
     if (c.precision != SLFMM_PREC_SPLIT_FP8 || cfg->impute != SLFMM_IMPUTE_MEAN || p == 0) return false;
@@ -1356,7 +1400,6 @@ bool presketch_eligible(Ctx& c, uint64_t n, uint64_t p, const double* x, int d, 
     check_cfg(cfg);
     ps.l = (int)cfg->k + (int)cfg->oversampling;
     if (ps.l > 64 || p < (uint64_t)ps.l || n < (uint64_t)ps.l) return false;  // the fit reports these
-    if (!fp8_row_indicator_plan(ps.l, ceil_div(p, 128))) return false;
     ps.n = n;
     ps.p = p;
     ps.x = x;
@@ -1882,6 +1925,7 @@ int slfmm_fit_host(slfmm_ctx* c, const uint8_t* packed, uint64_t n_physical, uin
     if (pre) {
         const int e = fetch(*c, ps.err.get(), 1)[0];
         if (e) throw_tc8_timeout(e);
+        ps.finish(*c, full);
     }
     phase(*c, pre ? "covariates; upload with the sketch pass" : "upload");
     const Geno* ge = &full;
@@ -1944,6 +1988,7 @@ void fit_problem(Ctx& c, const slfmm_problem& pr) {
     if (pre) {
         const int e = fetch(c, ps.err.get(), 1)[0];
         if (e) throw_tc8_timeout(e);
+        ps.finish(c, full);
     }
     fit_impl(c, full, full, pr.x, (int)pr.d, pr.cfg, pr.omega, pr.res, pre ? &ps : nullptr);
 }

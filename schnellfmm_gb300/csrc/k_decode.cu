@@ -395,7 +395,10 @@ void build_missing_lists(Ctx& c, const Geno& g) {
     if (g.have_csr) return;
     DBuf<uint64_t> mc(g.p + 1, c.stream);
     SLFMM_CUDA(cudaMemsetAsync(mc.get() + g.p, 0, sizeof(uint64_t), c.stream));
-    launch_snp_counts(c, g, mc.get());
+    // a matrix held only as tiles (a per-trait sample subset) has its counts
+    const bool tiles_only = g.packed.get() == nullptr;
+    if (tiles_only) launch_miss_counts_of(c, g, mc.get());
+    else launch_snp_counts(c, g, mc.get());
     g.miss_ptr.alloc(g.p + 1, c.stream);
     size_t tmp_bytes = 0;
     SLFMM_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, mc.get(), g.miss_ptr.get(),
@@ -409,7 +412,9 @@ void build_missing_lists(Ctx& c, const Geno& g) {
     SLFMM_CUDA(cudaStreamSynchronize(c.stream));
     g.nnz = nnz;
     g.miss_idx.alloc(std::max<uint64_t>(nnz, 1), c.stream);
-    if (nnz && g.p) {
+    if (nnz && g.p && tiles_only) {
+        launch_miss_fill_tiles(c, g);
+    } else if (nnz && g.p) {
         const int block = 256;
         k_miss_fill<<<(unsigned)ceil_div(g.p * 32, block), block, 0, c.stream>>>(
             packed_rows(g), g.p, g.stride, g.n, g.miss_ptr.get(), g.miss_idx.get(), nullptr, ~0ull);

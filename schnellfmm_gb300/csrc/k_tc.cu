@@ -286,6 +286,59 @@ __global__ void k_rowfix_mean(float* __restrict__ P, int ldp, uint64_t rows, int
     }
 }
 
+// k_rowfix_mean with 16-byte W-row gathers: a group of L lanes (L = 8, 16
+// or 32, the column quads of W rounded up) covers one W row, lane q of the
+// group column quad q (w <= 128, W rows 16-byte aligned), and the 32 / L
+// groups of a warp take consecutive missing calls of the same SNP; their
+// partial sums are combined by shuffles at the end.
+template <int L>
+__global__ void k_rowfix_mean4(float* __restrict__ P, int ldp, uint64_t rows, int w,
+                               const uint64_t* __restrict__ ptr, const uint32_t* __restrict__ idx,
+                               const float* __restrict__ W, int ldw, const double* __restrict__ cs,
+                               const double* __restrict__ mean, const double* __restrict__ scale) {
+    constexpr int G = 32 / L;  // missing calls per warp step
+    const uint64_t j = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x & 31, q = lane % L, grp = lane / L;
+    if (j >= rows) return;
+    const bool act = 4 * q < w;
+    const uint64_t e0 = ptr[j], e1 = ptr[j + 1];
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (uint64_t b = e0; b < e1; b += 32) {
+        const uint32_t my = b + lane < e1 ? idx[b + lane] : 0u;
+        const int cnt = (int)(e1 - b < 32 ? e1 - b : 32);
+#pragma unroll 4
+        for (int t = 0; t < cnt; t += G) {
+            const int tt = t + grp;
+            const uint64_t i = __shfl_sync(0xffffffffu, my, tt & 31);
+            if (act && tt < cnt) {
+                const float4 v = reinterpret_cast<const float4*>(W + i * ldw)[q];
+                acc.x += v.x;
+                acc.y += v.y;
+                acc.z += v.z;
+                acc.w += v.w;
+            }
+        }
+    }
+#pragma unroll
+    for (int o = L; o < 32; o <<= 1) {
+        acc.x += __shfl_xor_sync(0xffffffffu, acc.x, o);
+        acc.y += __shfl_xor_sync(0xffffffffu, acc.y, o);
+        acc.z += __shfl_xor_sync(0xffffffffu, acc.z, o);
+        acc.w += __shfl_xor_sync(0xffffffffu, acc.w, o);
+    }
+    if (!act || grp != 0) return;
+    const double mu = mean[j], sc = scale[j];
+    const float a4[4] = {acc.x, acc.y, acc.z, acc.w};
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int c = 4 * q + u;
+        if (c < w) {
+            const double v = (double)P[j * ldp + c] - mu * (cs[c] - (double)a4[u]);
+            P[j * ldp + c] = (float)(sc * v);
+        }
+    }
+}
+
 // per-sample fix of a forward pass on the transposed matrix (mean imputation):
 //   S[i, c] += sum_{j in missT_i} coef_j Q[j, c] - colterm_c,  coef_j = mu_j s_j
 __global__ void k_colfix_mean(double* __restrict__ S, int lds, uint64_t n, int w,
@@ -582,6 +635,21 @@ void launch_rowfix_mean(Ctx& c, float* P, int ldp, uint64_t rows, int w, const u
     if (!rows) return;
     // a warp covers 128 columns (4 per lane): wider operands in column blocks
     for (int c0 = 0; c0 < w; c0 += 128) {
+        if (ldw % 4 == 0 && reinterpret_cast<uintptr_t>(W + c0) % 16 == 0) {
+            const int wb = std::min(128, w - c0);
+            const unsigned grid = (unsigned)ceil_div(rows * 32, 256);
+            if (wb <= 32)
+                k_rowfix_mean4<8><<<grid, 256, 0, c.stream>>>(P + c0, ldp, rows, wb, ptr, idx, W + c0, ldw, cs + c0,
+                                                              mean, scale);
+            else if (wb <= 64)
+                k_rowfix_mean4<16><<<grid, 256, 0, c.stream>>>(P + c0, ldp, rows, wb, ptr, idx, W + c0, ldw, cs + c0,
+                                                               mean, scale);
+            else
+                k_rowfix_mean4<32><<<grid, 256, 0, c.stream>>>(P + c0, ldp, rows, wb, ptr, idx, W + c0, ldw, cs + c0,
+                                                               mean, scale);
+            SLFMM_LAUNCHED(c, "k_rowfix_mean4");
+            continue;
+        }
         k_rowfix_mean<<<(unsigned)ceil_div(rows * 32, 256), 256, 0, c.stream>>>(
             P + c0, ldp, rows, std::min(128, w - c0), ptr, idx, W + c0, ldw, cs + c0, mean, scale);
         SLFMM_LAUNCHED(c, "k_rowfix_mean");

@@ -968,6 +968,73 @@ __global__ void k_snp_counts_tiles(const uint8_t* __restrict__ tiles, uint64_t k
     }
 }
 
+// Missing-call lists (CSR by SNP, ascending sample indices) of a matrix held
+// only as SNP-major tiles: one warp per SNP, lanes over 32 K blocks at a
+// time; a lane's missing calls (code 01) are placed after those of the lower
+// lanes by a warp scan of the per-lane counts.
+__global__ void k_miss_fill_tiles(const uint8_t* __restrict__ tiles, uint64_t kbt, uint64_t p,
+                                  const uint64_t* __restrict__ ptr, uint32_t* __restrict__ idx) {
+    constexpr uint32_t kLo2 = 0x55555555u;
+    const uint64_t j = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / 32;
+    const int lane = threadIdx.x & 31;
+    if (j >= p) return;
+    const uint64_t t = j / kM, r = j % kM;
+    uint64_t base = ptr[j];
+    for (uint64_t kb0 = 0; kb0 < kbt; kb0 += 32) {
+        const uint64_t kb = kb0 + lane;
+        uint32_t m[8];
+        int cnt = 0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) m[k] = 0u;
+        if (kb < kbt) {
+            const uint4* q = reinterpret_cast<const uint4*>(tiles + (t * kbt + kb) * kTileBytes + r * 32);
+            const uint4 a = q[0], b = q[1];
+            const uint32_t ws[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                m[k] = ws[k] & kLo2 & ~((ws[k] >> 1) & kLo2);
+                cnt += __popc(m[k]);
+            }
+        }
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        uint64_t pos = base + (uint64_t)(incl - cnt);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+            uint32_t mm = m[k];
+            while (mm) {
+                const int bit = __ffs(mm) - 1;
+                idx[pos++] = (uint32_t)(kb * 128 + k * 16 + bit / 2);
+                mm &= mm - 1;
+            }
+        }
+        base += (uint64_t)__shfl_sync(0xffffffffu, incl, 31);
+    }
+}
+
+__global__ void k_miss_counts_of(const int32_t* __restrict__ counts, uint64_t p, uint64_t* __restrict__ mc) {
+    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < p; j += (uint64_t)gridDim.x * blockDim.x)
+        mc[j] = (uint64_t)counts[j * 4 + 3];
+}
+
+void launch_miss_counts_of(Ctx& c, const Geno& g, uint64_t* mc) {
+    if (!g.p) return;
+    k_miss_counts_of<<<grid_for(c, g.p, 256), 256, 0, c.stream>>>(g.counts.get(), g.p, mc);
+    SLFMM_LAUNCHED(c, "k_miss_counts_of");
+}
+
+void launch_miss_fill_tiles(Ctx& c, const Geno& g) {
+    SLFMM_REQUIRE(g.have_tiles, SLFMM_ERR_BAD_ARG, "this matrix has neither a row-major copy nor SNP-major tiles");
+    if (!g.p) return;
+    k_miss_fill_tiles<<<(unsigned)ceil_div(g.p * 32, 256), 256, 0, c.stream>>>(g.tiles.get(), g.kbt, g.p,
+                                                                               g.miss_ptr.get(), g.miss_idx.get());
+    SLFMM_LAUNCHED(c, "k_miss_fill_tiles");
+}
+
 static void tile_rows(Ctx& c, const uint8_t* in, uint64_t rows, uint64_t stride, DBuf<uint8_t>& out, uint64_t& kbt,
                       uint64_t& ntiles) {
     SLFMM_REQUIRE(stride % 32 == 0, SLFMM_ERR_BAD_ARG, "packed stride must be a multiple of 32 bytes");

@@ -233,6 +233,10 @@ void launch_snp_counts(Ctx& c, const Geno& g, uint64_t* miss_count_out);
 void launch_snp_counts_range(Ctx& c, const Geno& g, uint64_t r0, uint64_t rows);
 void build_missing_lists(Ctx& c, const Geno& g);
 void build_missing_csc(Ctx& c, const Geno& g);
+// missing counts p (from g.counts) and the CSR fill from the SNP-major tiles,
+// for matrices without a row-major copy
+void launch_miss_counts_of(Ctx& c, const Geno& g, uint64_t* mc);
+void launch_miss_fill_tiles(Ctx& c, const Geno& g);
 // missing-call lists of an upload chunk [r0, r0 + rows): offsets continue
 // g.miss_ptr[r0] (needs the chunk's counts); the fill writes below cap only
 void csr_chunk_offsets(Ctx& c, const Geno& g, uint64_t r0, uint64_t rows);
