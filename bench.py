@@ -669,7 +669,7 @@ def main():
         barrier()
     ms_total = maxover(ev0.elapsed_time(ev1))
     launches = eng.launches - launches0
-    prof = {kname: eng.profile_read(kname) for kname in ("row_contract", "col_contract", "assoc_epilogue")}
+    prof = {kname: eng.profile_read(kname) for kname in ("row_contract", "col_contract", "assoc_epilogue", "row_fix", "cholqr2", "small_eigh", "small_inverse")}
     eng.profile(False)
     ms_step = ms_total / args.steps
     value = job_rate(p, world, ms_step)

@@ -448,7 +448,7 @@ struct Fp8RowPass {
     std::vector<DBuf<uint8_t>> Bs;
     std::vector<DBuf<float>> iscs;
     std::vector<int> c0s;
-    DBuf<float> W32;
+    DBuf<float> W32;  // the fix's W rows (FP32)
     DBuf<double> cs;
 };
 
@@ -516,6 +516,9 @@ void fp8_row_fix(Ctx& c, const Geno& g, const SnpStd& s, const Fp8RowPass& rp, u
                  float* out) {
     if (rp.op.ok) return;
     build_missing_lists(c, g);
+    // algorithmic bytes: the lists' indices and one W row per missing call
+    const uint64_t nnz_rows = rows == g.p ? g.nnz : (uint64_t)((double)g.nnz * rows / std::max<uint64_t>(g.p, 1));
+    ProfScope ps(c, "row_fix", (double)nnz_rows * (4.0 + 4.0 * rp.w) + (double)rows * rp.w * 8, 1.0 * nnz_rows * rp.w);
     launch_rowfix_mean(c, out + r0 * rp.wp, rp.wp, rows, rp.w, g.miss_ptr.get() + r0, g.miss_idx.get(),
                        rp.W32.get(), rp.wp, rp.cs.get(), s.mean.get() + r0, s.scale.get() + r0);
 }
@@ -820,6 +823,7 @@ void center_columns(Ctx& c, double* A, uint64_t m, int b, int lda) {
 // orthonormalisation (Cholesky-QR2, FP64 Gram + Cholesky)
 // ---------------------------------------------------------------------------
 void cholqr2_f32(Ctx& c, float* Z, uint64_t m, int a, int ld) {
+    ProfScope ps(c, "cholqr2", 2.0 * m * a * 4, 4.0 * m * a * a);
     DBuf<double> G(a * a, c.stream), Linv(a * a, c.stream);
     DBuf<int> st(1, c.stream);
     for (int round = 0; round < 2; ++round) {
@@ -831,6 +835,7 @@ void cholqr2_f32(Ctx& c, float* Z, uint64_t m, int a, int ld) {
 }
 
 void cholqr2_f64(Ctx& c, double* A, uint64_t m, int a, int ld) {
+    ProfScope ps(c, "cholqr2", 2.0 * m * a * 8, 4.0 * m * a * a);
     DBuf<double> G(a * a, c.stream), Linv(a * a, c.stream), LinvT(a * a, c.stream), tmp(m * a, c.stream);
     DBuf<int> st(1, c.stream);
     for (int round = 0; round < 2; ++round) {
@@ -1109,14 +1114,14 @@ void assoc(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, const doubl
     phase(c, "association design");
     // u = Q_C[:, 1:]^T y for every SNP, then the statistics.  With page-locked
     // host outputs the split-FP8 pass runs in chunks of SNPs: each chunk's
-    // beta and r2 are final after its epilogue and copy out on the copy
-    // stream while later chunks compute (t and p wait for the GIF).
+    // beta, r2 and t are final after its epilogue and copy out on the copy
+    // stream while later chunks compute (only the p-values wait for the GIF).
     DBuf<float> U;
     int wp = 0;
     const uint64_t chunk = round_up(ceil_div(p, 8), 128);
     const bool chunked = c.precision == SLFMM_PREC_SPLIT_FP8 && st.fill.k == 0 && p >= 2 * chunk &&
-                         (out.beta || out.r2) && (!out.beta || is_pinned(out.beta)) &&
-                         (!out.r2 || is_pinned(out.r2));
+                         (out.beta || out.r2 || out.tstat) && (!out.beta || is_pinned(out.beta)) &&
+                         (!out.r2 || is_pinned(out.r2)) && (!out.tstat || is_pinned(out.tstat));
     bool copied = false;
     if (chunked) {
         Fp8RowPass rp;
@@ -1141,8 +1146,14 @@ void assoc(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, const doubl
                 launch_assoc_epilogue(c, rows, U.get() + r0 * wp, wp, st.tss.get() + r0, kc, beta.get() + r0 * d,
                                       t32.get() + r0 * d, r2.get() + r0 * 3, hist.get());
             }
+            // t reaches the host as the widened FP32 statistic (what the
+            // calibration writes), so it is final here too
+            if (out.tstat) launch_f32_to_f64(c, t32.get() + r0 * d, rows, d, d, t64.get() + r0 * d, d);
             SLFMM_CUDA(cudaEventRecord(ev, c.stream));
             SLFMM_CUDA(cudaStreamWaitEvent(c.copy_stream, ev, 0));
+            if (out.tstat)
+                SLFMM_CUDA(cudaMemcpyAsync(out.tstat + r0 * d, t64.get() + r0 * d, rows * d * sizeof(double),
+                                           cudaMemcpyDeviceToHost, c.copy_stream));
             if (out.beta)
                 SLFMM_CUDA(cudaMemcpyAsync(out.beta + r0 * d, beta.get() + r0 * d, rows * d * sizeof(double),
                                            cudaMemcpyDeviceToHost, c.copy_stream));
@@ -1175,10 +1186,11 @@ void assoc(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, const doubl
     out.gif = gsum / d;
     if (out.gif_per_trait) std::copy(gpt.begin(), gpt.end(), out.gif_per_trait);
     DBuf<double> gptd = upload(c, gpt.data(), gpt.size());
-    launch_calibrate(c, p, d, t32.get(), gptd.get(), t64.get(), pv.get());
+    // t64 is already widened (and being copied out) when the pass ran in chunks
+    launch_calibrate(c, p, d, t32.get(), gptd.get(), copied && out.tstat ? nullptr : t64.get(), pv.get());
     phase(c, "association statistics, GIF");
     if (out.beta && !copied) d2h(c, out.beta, beta.get(), p * d);
-    if (out.tstat) d2h(c, out.tstat, t64.get(), p * d);
+    if (out.tstat && !copied) d2h(c, out.tstat, t64.get(), p * d);
     if (out.pvalue) d2h(c, out.pvalue, pv.get(), p * d);
     if (out.r2 && !copied) d2h(c, out.r2, r2.get(), p * 3);
     sync(c);
@@ -1963,17 +1975,47 @@ void geno_subset_samples(Ctx& c, const Geno& src, const std::vector<uint64_t>& k
 }
 
 // Whether a split-FP8 mean-imputation fit of an n x p matrix with one
-// covariate runs on the tile-major copies alone: every row and column pass
-// (the RSVD sketch width and the test-pass width 1 + K) has an indicator plan,
-// so no pass needs the missing-call lists or the row-major copy.
+// covariate runs on the tile-major copies alone: every column pass (the RSVD
+// sketch width) has an indicator plan, and the row passes take their
+// missing-call lists from the SNP-major tiles, so no pass needs the
+// row-major copy.
 bool tiles_only_fit(const Ctx& c, const slfmm_config* cfg, uint64_t n, uint64_t p) {
     if (c.precision != SLFMM_PREC_SPLIT_FP8 || cfg->impute != SLFMM_IMPUTE_MEAN) return false;
     const int l = (int)cfg->k + (int)cfg->oversampling;
     if (l > 64) return false;
-    const uint64_t tp = ceil_div(p, 128), tn = ceil_div(n, 128);
-    if (!fp8_row_indicator_plan(l, tp)) return false;
-    const Fp8Plan col = fp8_plan(pad16(l), true, tn);
-    return col.ok && col.n_ind != 0 && fp8_row_indicator_plan((int)cfg->k + 1, tp);
+    (void)p;
+    const Fp8Plan col = fp8_plan(pad16(l), true, ceil_div(n, 128));
+    return col.ok && col.n_ind != 0;
+}
+
+// One trait of slfmm_fit_traits on context c: its sample subset taken from
+// the resident matrix g on the device, then a d = 1 fit.
+void fit_trait(Ctx& c, const Geno& g, const double* y, const uint8_t* masks, uint32_t n_traits, uint32_t t,
+               const slfmm_config* cfg, slfmm_results* res) {
+    std::vector<uint64_t> keep;
+    std::vector<double> xt;
+    for (uint64_t i = 0; i < g.n; ++i)
+        if (masks[i * n_traits + t]) {
+            keep.push_back(i);
+            xt.push_back(y[i * n_traits + t]);
+        }
+    try {
+        SLFMM_REQUIRE(!keep.empty(), SLFMM_ERR_BAD_ARG, "no samples");
+        Geno sub;
+        phase(c, "", true);
+        if (tiles_only_fit(c, cfg, keep.size(), g.p)) {
+            std::vector<uint32_t> k32(keep.begin(), keep.end());
+            DBuf<uint32_t> keep_d = upload(c, k32.data(), k32.size());
+            tiles_subset_samples(c, g, keep_d.get(), keep.size(), sub);
+            sync(c);
+        } else {
+            geno_subset_samples(c, g, keep, sub);
+        }
+        phase(c, "trait sample subset");
+        fit_impl(c, sub, sub, xt.data(), 1, cfg, nullptr, &res[t]);
+    } catch (const Error& e) {
+        throw Error(e.code, "trait " + std::to_string(t) + ": " + e.what());
+    }
 }
 
 // one problem of slfmm_fit_many on a worker's context (the body of
@@ -2001,33 +2043,7 @@ int slfmm_fit_traits(slfmm_ctx* c, const slfmm_geno* g, const double* y, const u
     API_TRY
     SLFMM_CUDA(cudaSetDevice(c->device));
     SLFMM_REQUIRE(n_traits >= 1, SLFMM_ERR_BAD_ARG, "no traits");
-    const uint64_t n = g->n;
-    for (uint32_t t = 0; t < n_traits; ++t) {
-        std::vector<uint64_t> keep;
-        std::vector<double> xt;
-        for (uint64_t i = 0; i < n; ++i)
-            if (masks[i * n_traits + t]) {
-                keep.push_back(i);
-                xt.push_back(y[i * n_traits + t]);
-            }
-        try {
-            SLFMM_REQUIRE(!keep.empty(), SLFMM_ERR_BAD_ARG, "no samples");
-            Geno sub;
-            phase(*c, "", true);
-            if (tiles_only_fit(*c, cfg, keep.size(), g->p)) {
-                std::vector<uint32_t> k32(keep.begin(), keep.end());
-                DBuf<uint32_t> keep_d = upload(*c, k32.data(), k32.size());
-                tiles_subset_samples(*c, *g, keep_d.get(), keep.size(), sub);
-                sync(*c);
-            } else {
-                geno_subset_samples(*c, *g, keep, sub);
-            }
-            phase(*c, "trait sample subset");
-            fit_impl(*c, sub, sub, xt.data(), 1, cfg, nullptr, &res[t]);
-        } catch (const Error& e) {
-            throw Error(e.code, "trait " + std::to_string(t) + ": " + e.what());
-        }
-    }
+    for (uint32_t t = 0; t < n_traits; ++t) fit_trait(*c, *g, y, masks, n_traits, t, cfg, res);
     API_CATCH(c)
 }
 

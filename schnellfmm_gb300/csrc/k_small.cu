@@ -646,16 +646,102 @@ __global__ void k_inverse(const double* __restrict__ A, int a, double* __restric
     }
 }
 
+// safe_inv by Gauss-Jordan elimination on [A + eps I | I] in shared memory
+// (a <= kMaxGaussJordan), every thread of the CTA on each pivot step.  The
+// pivot search (first largest |value| in the column, from the diagonal down)
+// and the updates of the rows below the pivot are those of lu_smem, so the
+// pivots, and the exact-zero test that triggers the eps retry, are the same
+// as the LU's; the rows above the pivot are eliminated in the same sweep, so
+// the inverse needs no triangular solves.
+constexpr int kMaxGaussJordan = 112;  // 16 a^2 bytes of shared memory
+__global__ void __launch_bounds__(1024) k_inverse_gj(const double* __restrict__ A, int a, double* __restrict__ X,
+                                                     int* __restrict__ status, double* __restrict__ eps_used) {
+    extern __shared__ double S[];  // a rows x 2a columns
+    __shared__ double f[kMaxGaussJordan];
+    __shared__ double eps;
+    __shared__ int p_sh, ok;
+    const int ld = 2 * a, warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        if (threadIdx.x == 0) {
+            double dmax = 0.0;
+            for (int k = 0; k < a; ++k) dmax = fmax(dmax, fabs(A[k * a + k]));
+            dmax = fmax(dmax, 1e-300);
+            eps = attempt == 0 ? 0.0 : 1e-8 * dmax;
+            ok = 1;
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < a * ld; e += blockDim.x) {
+            const int i = e / ld, j = e % ld;
+            S[e] = j < a ? A[i * a + j] + (i == j ? eps : 0.0) : (j - a == i ? 1.0 : 0.0);
+        }
+        __syncthreads();
+        for (int k = 0; k < a; ++k) {
+            if (warp == 0) {
+                int p = -1;
+                double best = -1.0;
+                for (int i = k + lane; i < a; i += 32) {
+                    const double v = fabs(S[i * ld + k]);
+                    if (v > best) { best = v; p = i; }
+                }
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+                    const int op = __shfl_xor_sync(0xffffffffu, p, o);
+                    if (ob > best || (ob == best && op >= 0 && (p < 0 || op < p))) { best = ob; p = op; }
+                }
+                if (lane == 0) {
+                    p_sh = p;
+                    if (best == 0.0) ok = 0;
+                }
+            }
+            __syncthreads();
+            if (!ok) break;
+            const int p = p_sh;
+            if (p != k)
+                for (int j = k + threadIdx.x; j < ld; j += blockDim.x) {
+                    const double t = S[k * ld + j];
+                    S[k * ld + j] = S[p * ld + j];
+                    S[p * ld + j] = t;
+                }
+            __syncthreads();
+            const double d = S[k * ld + k];
+            for (int i = threadIdx.x; i < a; i += blockDim.x) f[i] = i == k ? 0.0 : S[i * ld + k] / d;
+            __syncthreads();
+            const int span = ld - k - 1;
+            for (int e = threadIdx.x; e < a * span; e += blockDim.x) {
+                const int i = e / span, j = k + 1 + e % span;
+                if (i != k) S[i * ld + j] -= f[i] * S[k * ld + j];
+            }
+            __syncthreads();
+            for (int j = k + 1 + threadIdx.x; j < ld; j += blockDim.x) S[k * ld + j] /= d;
+            __syncthreads();
+        }
+        if (ok) {
+            for (int e = threadIdx.x; e < a * a; e += blockDim.x) X[e] = S[(e / a) * ld + a + e % a];
+            if (threadIdx.x == 0) {
+                if (status) status[0] = attempt;
+                if (eps_used) eps_used[0] = eps;
+            }
+            return;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        if (status) status[0] = 2;
+        if (eps_used) eps_used[0] = eps;
+    }
+}
+
 // One-sided (Hestenes) Jacobi SVD of a square a x a matrix in one
 // CTA: A V = U diag(sig).  Outputs V (a x a), sig (descending) and U = A V
 // / sig in place of A.  Pairs are rotated in parallel with a round-robin
 // ordering, one warp per pair.
 //
 // GB300 runs FP64 at a small fraction of its FP32 rate, so the sweeps run in
-// FP32 first (to ~1e-6 relative orthogonality); V is then re-orthonormalised
-// in FP64 (classical Gram-Schmidt, twice), M = A V formed in FP64, and FP64
-// sweeps polish to the FP64 tolerance -- typically two, against the ~10 a
-// cold FP64 start needs.
+// FP32 first (to ~1e-5 relative orthogonality, at most 12 sweeps); V is then
+// re-orthonormalised in FP64 (classical Gram-Schmidt, twice), M = A V formed
+// in FP64, and FP64 sweeps polish to the FP64 tolerance -- typically two or
+// three, against the ~10 a cold FP64 start needs.
 __device__ __forceinline__ float warp_sumf(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -665,7 +751,7 @@ __device__ __forceinline__ float warp_sumf(float v) {
 // one Jacobi sweep-set on column-major M (ap x ap, rows a used) with
 // accumulated V; returns after convergence or max_sweeps
 template <typename F>
-__device__ void jacobi_sweeps(F* M, F* Vs, int a, int ap, F tol, int max_sweeps, int* rotated) {
+__device__ void jacobi_sweeps(F* M, F* Vs, int a, int ap, F tol, int max_sweeps, int* rotated, F abs_tol = 0) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
     const int npairs = ap / 2;
     for (int sweep = 0; sweep < max_sweeps; ++sweep) {
@@ -691,7 +777,7 @@ __device__ void jacobi_sweeps(F* M, F* Vs, int a, int ap, F tol, int max_sweeps,
                     al = warp_sumf(al); be = warp_sumf(be); ga = warp_sumf(ga);
                 }
                 const F tiny = sizeof(F) == 8 ? (F)1e-300 : (F)1e-37;
-                if (fabs(ga) > tol * sqrt(al * be) && fabs(ga) > tiny) {
+                if (fabs(ga) > tol * sqrt(al * be) && fabs(ga) > tiny && fabs(ga) > abs_tol) {
                     const F zeta = (be - al) / (2 * ga);
                     const F t = (zeta >= 0 ? (F)1 : (F)-1) / (fabs(zeta) + sqrt((F)1 + zeta * zeta));
                     const F cs = (F)1 / sqrt((F)1 + t * t), sn = cs * t;
@@ -754,9 +840,12 @@ __device__ void gs_columns(double* Vs, int ap, double* dots) {
 //
 // GB300 runs FP64 at a small fraction of its FP32 rate, so the bulk of the
 // rotation work runs as FP32 one-sided Jacobi sweeps (pairs in parallel,
-// round-robin order, one warp per pair) to ~1e-6; V is re-orthonormalised in
-// FP64 (Gram-Schmidt, twice) and B = V^T A V formed in FP64.  B is then
-// diagonal up to ~1e-6 of its norm, and two-sided cyclic Jacobi sweeps in
+// round-robin order, one warp per pair) to ~1e-5 (at most 12 sweeps: with
+// Gram matrices of condition 1e6 and more, FP32 rounding keeps rotating the
+// small columns, and the FP64 phase converges quadratically from there
+// anyway); V is re-orthonormalised in FP64 (Gram-Schmidt, twice) and
+// B = V^T A V formed in FP64.  B is then diagonal up to ~1e-5 of its norm,
+// and two-sided cyclic Jacobi sweeps in
 // FP64 (Golub & Van Loan, Algorithm 8.5.2 with the parallel round-robin
 // ordering) finish it -- quadratic convergence, typically two sweeps --
 // accumulating their rotations into R; V <- V R and a final Gram-Schmidt.
@@ -790,8 +879,23 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(double* __restrict__ A, int
         M32[e] = (row < a && col < a) ? (float)A[row * a + col] : 0.f;
         V32[e] = (row == col) ? 1.f : 0.f;
     }
+    // FP32 resolution of the whole matrix: couplings below 1e-7 of the largest
+    // squared column norm are left to the FP64 sweeps (columns of a rank-deficient
+    // Gram that are zero up to FP32 rounding would otherwise keep rotating
+    // until the sweep limit)
+    __shared__ float colmax2;
+    if (threadIdx.x == 0) colmax2 = 0.f;
     __syncthreads();
-    jacobi_sweeps<float>(M32, V32, a, ap, 2.0e-6f, 30, &rotated);
+    if (warp < ap) {
+        for (int cc = warp; cc < ap; cc += nwarps) {
+            float t = 0.f;
+            for (int r = lane; r < a; r += 32) t += M32[cc * ap + r] * M32[cc * ap + r];
+            t = warp_sumf(t);
+            if (lane == 0) atomicMax(reinterpret_cast<int*>(&colmax2), __float_as_int(t));
+        }
+    }
+    __syncthreads();
+    jacobi_sweeps<float>(M32, V32, a, ap, 1.0e-5f, 12, &rotated, 1e-7f * colmax2);
     // phase 2: FP64 orthonormal V
     for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) Vs[e] = (double)V32[e];
     __syncthreads();
@@ -1187,7 +1291,11 @@ void launch_tri_inv_lower(Ctx& c, const double* L, int a, double* Linv) {
 
 void launch_inverse(Ctx& c, const double* A, int a, double* Ainv, int* status, double* eps_used) {
     SLFMM_REQUIRE(a <= kMaxDesign, SLFMM_ERR_BAD_ARG, "matrix too large for the small inverse");
-    if (a <= kMaxSmall) {
+    ProfScope ps(c, "small_inverse", 16.0 * a * a, 2.0 * a * a * a);
+    if (a <= kMaxGaussJordan) {
+        set_smem((const void*)k_inverse_gj, 2 * smem_sq(a));
+        k_inverse_gj<<<1, 1024, 2 * smem_sq(a), c.stream>>>(A, a, Ainv, status, eps_used);
+    } else if (a <= kMaxSmall) {
         set_smem((const void*)k_inverse, smem_sq(a));
         k_inverse<<<1, 256, smem_sq(a), c.stream>>>(A, a, Ainv, status, eps_used, nullptr);
     } else {
@@ -1202,6 +1310,7 @@ void launch_jacobi_svd(Ctx& c, const double* A, int a, double* V, double* sig) {
                   "small eigen-solve limited to " + std::to_string(kMaxDesign) + " x " + std::to_string(kMaxDesign));
     const int ap = a + (a & 1);
     const size_t sm = 2 * (size_t)ap * ap * (sizeof(double) + sizeof(float));
+    ProfScope ps(c, "small_eigh", 16.0 * a * a, 0.0);
     if (a <= 64) {
         set_smem((const void*)k_jacobi_svd, sm);
         k_jacobi_svd<<<1, 1024, sm, c.stream>>>(const_cast<double*>(A), a, V, sig, nullptr);
