@@ -455,22 +455,30 @@ struct Fp8RowPass {
 // Whether a row pass over g takes the missing-call indicator operand rather
 // than the sparse per-SNP fix over the missing-call lists.  The indicator adds
 // three E4M3 terms of tensor work and 96 + 64 TMEM columns that shorten the
-// operand ring; the fix gathers one W row per missing call from L2.  Measured
-// on GB300 at n = 20 000, w = 30, 0.5 % missing: the ring without the
-// indicator runs 4.6-5.5 ms per 2M-SNP pass and the fix about 2 ms, against
-// 8.2-15 ms for the indicator form (whose time also varied 2x between
-// otherwise equal runs).  So the indicator is taken only when
-// SLFMM_TC8_ROW_IND=1 forces it.  The rule looks neither at the data nor at
-// how the matrix is held (matrices kept only as tiles build their lists from
-// the tiles), so an upload that runs the sketch pass chunk by chunk, and a
-// per-trait sample subset, take the same form as the pass over a resident
-// upload of the same samples.
+// operand ring; the fix gathers one W row per missing call from L2, so its
+// cost grows with the missing calls.  Measured on GB300 (n = 20 000, w = 30,
+// 0.5 % missing): 4.18 ms for the ring without the indicator plus 3.43 ms for
+// the fix, against 8.2 ms with the indicator (which also measured 15 ms on
+// some boxes, where the other forms did not change); at 7 % missing (n =
+// 5 000) the fix costs more than the indicator.  So the fix is taken when at
+// most 1 % of the calls are missing, and always for the sketch pass of the
+// randomized SVD (`sketch`): that pass also runs chunk by chunk under an
+// upload, before the missing-call count is known, and both must take the
+// same form.  SLFMM_TC8_ROW_IND=1 / =0 force the indicator on / off.
 bool fp8_row_indicator_forced() {
     const char* env = std::getenv("SLFMM_TC8_ROW_IND");
     return env && env[0] == '1';
 }
 
-bool fp8_row_take_indicator(const Geno&) { return fp8_row_indicator_forced(); }
+bool fp8_row_take_indicator(Ctx& c, const Geno& g, bool sketch) {
+    if (fp8_row_indicator_forced()) return true;
+    if (sketch) return false;
+    const char* env = std::getenv("SLFMM_TC8_ROW_IND");
+    if (env && env[0] == '0') return false;
+    build_missing_lists(c, g);
+    const double cells = (double)g.n * (double)g.p;
+    return cells > 0 && (double)g.nnz > 0.01 * cells;
+}
 
 // The operand of a row pass over n samples and `tiles` row tiles: the
 // indicator form when `indicator` and it has a plan, else column blocks
@@ -503,9 +511,9 @@ void fp8_row_operand_prepare(Ctx& c, uint64_t n, uint64_t tiles, const double* W
     }
 }
 
-void fp8_row_prepare(Ctx& c, const Geno& g, const double* W, int w, int ldw, Fp8RowPass& rp) {
+void fp8_row_prepare(Ctx& c, const Geno& g, const double* W, int w, int ldw, Fp8RowPass& rp, bool sketch = false) {
     build_tiles(c, g, false);
-    const bool ind = fp8_row_take_indicator(g);
+    const bool ind = fp8_row_take_indicator(c, g, sketch);
     fp8_row_operand_prepare(c, g.n, ceil_div(g.p, 128), W, w, ldw, ind, rp);
     if (!rp.op.ok) build_missing_lists(c, g);
 }
@@ -551,7 +559,7 @@ void fp8_row_run(Ctx& c, const Geno& g, const SnpStd& s, const Fp8RowPass& rp, u
 
 // out (p x wp, FP32) = Y_hat^T W, W = n x w FP64 (leading dim ldw)
 void row_contract_base(Ctx& c, const Geno& g, const SnpStd& s, const double* W, int w, int ldw,
-                       DBuf<float>& out, int& wp) {
+                       DBuf<float>& out, int& wp, bool sketch = false) {
     wp = pad16(w);
     if (wp > kMaxW) {
         // wider operands (association designs with many covariates): blocks
@@ -561,7 +569,7 @@ void row_contract_base(Ctx& c, const Geno& g, const SnpStd& s, const double* W, 
             const int wb = std::min(kMaxW, w - c0);
             DBuf<float> part;
             int wpb = 0;
-            row_contract_base(c, g, s, W + c0, wb, ldw, part, wpb);
+            row_contract_base(c, g, s, W + c0, wb, ldw, part, wpb, sketch);
             if (g.p)
                 SLFMM_CUDA(cudaMemcpy2DAsync(out.get() + c0, (size_t)wp * sizeof(float), part.get(),
                                              (size_t)wpb * sizeof(float), (size_t)wpb * sizeof(float), g.p,
@@ -576,7 +584,7 @@ void row_contract_base(Ctx& c, const Geno& g, const SnpStd& s, const double* W, 
         // exact E4M3 genotypes x 4 scaled E4M3 terms of W; with the missing-call
         // indicator operand the epilogue applies out = s_j (P - mu_j (cs - M))
         Fp8RowPass rp;
-        fp8_row_prepare(c, g, W, w, ldw, rp);
+        fp8_row_prepare(c, g, W, w, ldw, rp, sketch);
         fp8_row_run(c, g, s, rp, 0, g.p, out.get(), nullptr);
         return;
     }
@@ -677,8 +685,8 @@ void col_contract_base(Ctx& c, const Geno& g, const SnpStd& s, const float* Q, i
 // missing call at the SNP mean (standardised 0); the correction adds
 // s_r (f_ir - mu_r) times the operand row.
 void row_contract(Ctx& c, const Geno& g, const SnpStd& s, const double* W, int w, int ldw, DBuf<float>& out,
-                  int& wp) {
-    row_contract_base(c, g, s, W, w, ldw, out, wp);
+                  int& wp, bool sketch = false) {
+    row_contract_base(c, g, s, W, w, ldw, out, wp, sketch);
     if (s.fill.k) {
         build_missing_lists(c, g);
         DBuf<float> W32(std::max<uint64_t>(g.n, 1) * wp, c.stream);
@@ -882,7 +890,7 @@ void rsvd(Ctx& c, const Geno& g, const SnpStd& st, const Step0& s0, int K, int l
     } else {
         DBuf<double> W;
         sketch_operand(c, s0, n, l, seed, omega_host, W);
-        row_contract(c, g, st, W.get(), l, l, Z, wp);       // sketch (:56-72)
+        row_contract(c, g, st, W.get(), l, l, Z, wp, true);  // sketch (:56-72)
     }
     cholqr2_f32(c, Z.get(), g.p, l, wp);                     // QR (:75)
     for (int it = 0; it < q; ++it) {

@@ -83,7 +83,10 @@ struct ChaCha8Draws {
             blk = ctr >> 3;
             refill();
         }
-        const int j = (int)(ctr & 7);
+        return word((int)(ctr & 7));
+    }
+    // output j (0..7) of the block in registers
+    __device__ uint64_t word(int j) const {
         uint32_t lo = x[0], hi = x[1];
 #pragma unroll
         for (int w = 1; w < 8; ++w)
@@ -414,24 +417,39 @@ __global__ void __launch_bounds__(256) k_nmf_cv(const uint8_t* __restrict__ pack
         const uint32_t* row = reinterpret_cast<const uint32_t*>(packed + r * stride);
         const uint64_t nwords = (n + 15) / 16;
         double e1 = 0.0, e2 = 0.0, cnt = 0.0;
+        auto held_out = [&](uint64_t i, uint32_t code) {
+            const double g = code == 0 ? 0.0 : (double)(code - 1);
+            e1 += fabs(g - (double)fill_dot<KM>(W + i * k, hs[wl], k));
+            e2 += fabs(g - cm);
+            cnt += 1.0;
+        };
         for (uint64_t wd = lane; wd < nwords; wd += 32) {
             const uint32_t v = row[wd];
             const uint64_t i0 = wd * 16;
-            uint64_t z = key + (col * n + i0 + 1) * kGamma;
             const int nb = n - i0 < 16 ? (int)(n - i0) : 16;
-            for (int b = 0; b < nb; ++b, z += kGamma) {
-                const uint32_t code = (v >> (2 * b)) & 3u;
-                if (code == 1u) continue;
-                if constexpr (kChaCha) {
-                    if ((cc.at(col * n + i0 + b) >> 12) >= thresh) continue;
-                } else {
-                    if ((mix64(z) >> 11) >= thresh) continue;
+            if constexpr (kChaCha) {
+                // the word's entries use the blocks e0 / 8 .. (e0 + nb - 1) / 8;
+                // every lane refills at the same points (e0 is the same modulo
+                // 8 for all lanes of the SNP), so the refills do not diverge
+                const uint64_t e0 = col * n + i0, last = (e0 + nb - 1) >> 3;
+                for (uint64_t bk = e0 >> 3; bk <= last; ++bk) {
+                    cc.blk = bk;
+                    cc.refill();
+                    const int lo = bk * 8 > e0 ? (int)(bk * 8 - e0) : 0;
+                    const int hi = min(nb, (int)((bk + 1) * 8 - e0));
+                    for (int b = lo; b < hi; ++b) {
+                        const uint32_t code = (v >> (2 * b)) & 3u;
+                        if (code == 1u || (cc.word((int)((e0 + b) & 7)) >> 12) >= thresh) continue;
+                        held_out(i0 + b, code);
+                    }
                 }
-                const uint64_t i = i0 + b;
-                const double g = code == 0 ? 0.0 : (double)(code - 1);
-                e1 += fabs(g - (double)fill_dot<KM>(W + i * k, hs[wl], k));
-                e2 += fabs(g - cm);
-                cnt += 1.0;
+            } else {
+                uint64_t z = key + (col * n + i0 + 1) * kGamma;
+                for (int b = 0; b < nb; ++b, z += kGamma) {
+                    const uint32_t code = (v >> (2 * b)) & 3u;
+                    if (code == 1u || (mix64(z) >> 11) >= thresh) continue;
+                    held_out(i0 + b, code);
+                }
             }
         }
         e1 = warp_sum_d(e1);
@@ -460,14 +478,72 @@ __global__ void k_obs_base(const int32_t* __restrict__ counts, uint64_t p, uint6
     }
 }
 
+// Hold-out draws of the warp's 256 samples i0 .. i0 + 255 with the draws
+// laid out so that one ChaCha8 block (eight outputs) serves up to eight of
+// them: lane l takes samples i0 + 8 l .. i0 + 8 l + 7, whose observed calls
+// (code != 01) have consecutive counters -- `before` (observed calls of the
+// SNP's chunk before i0) plus those of the lower lanes, by a warp scan.
+// Returns the lane's held-out bits (bit b: sample i0 + 8 l + b) and its 16
+// code bits in `codes`; `before` advances past the 256 samples.  The callers
+// move the bits back to one sample per lane with shuffles, so their W-row
+// loads stay coalesced.
+template <bool kChaCha>
+__device__ __forceinline__ uint32_t lane_held8(const uint8_t* row, uint64_t n, uint64_t i0, uint64_t& before,
+                                               uint64_t key, ChaCha8Draws& cc, uint64_t thresh, uint32_t& codes) {
+    const uint64_t ib = i0 + 8 * (uint64_t)(threadIdx.x & 31);
+    uint32_t obs = 0;
+    codes = 0x5555u;  // past n: "missing", neither observed nor drawn
+    if (ib < n) {
+        codes = *reinterpret_cast<const uint16_t*>(row + ib / 4);
+#pragma unroll
+        for (int b = 0; b < 8; ++b)
+            if (ib + b < n && ((codes >> (2 * b)) & 3u) != 1u) obs |= 1u << b;
+    }
+    const int cnt = __popc(obs);
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((int)(threadIdx.x & 31) >= o) incl += v;
+    }
+    const uint64_t c0 = before + (uint64_t)(incl - cnt);
+    before += (uint64_t)__shfl_sync(0xffffffffu, incl, 31);
+    uint32_t held = 0;
+    if constexpr (kChaCha) {
+        // at most eight consecutive counters: blocks c0 / 8 and c0 / 8 + 1,
+        // computed by every lane together (no divergent refills)
+#pragma unroll
+        for (int half = 0; half < 2; ++half) {
+            cc.blk = (c0 >> 3) + (uint64_t)half;
+            cc.refill();
+            uint64_t ctr = c0;
+#pragma unroll
+            for (int b = 0; b < 8; ++b) {
+                if (!((obs >> b) & 1u)) continue;
+                if ((ctr >> 3) == cc.blk && (cc.word((int)(ctr & 7)) >> 12) < thresh) held |= 1u << b;
+                ++ctr;
+            }
+        }
+    } else {
+        uint64_t ctr = c0;
+        for (int b = 0; b < 8; ++b) {
+            if (!((obs >> b) & 1u)) continue;
+            if (draw_below(key, ctr, thresh)) held |= 1u << b;
+            ++ctr;
+        }
+    }
+    return held;
+}
+
 // GWAS-phase CV (src/testing.rs:423-487): per chunk the stream seed + seq,
 // one draw per OBSERVED call (counter = its column-major rank in the chunk),
 // held out iff the draw is below `rate`; the held-out column is refilled with
 // its leave-out mean mu', H = max(0, W+ y~) and the MAE of W_i.H and of mu'
 // over the held-out calls accumulate.  W+ y~ = A + mu' B with A = sum over
 // kept observed calls of W+_i g, B = sum over missing and held-out calls of
-// W+_i.  One warp per SNP, two passes over its codes.  kChaCha draws from the
-// reference's ChaCha8 stream instead of the counter stream.
+// W+_i.  One warp per SNP, two passes over its codes; the hold-out draws of
+// each 256 samples come from lane_held8.  kChaCha draws from the reference's
+// ChaCha8 stream instead of the counter stream.
 template <bool kChaCha, int KM>
 __global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__ packed, uint64_t stride, uint64_t n,
                                                      uint64_t p, uint64_t chunk, uint64_t seed, uint64_t thresh,
@@ -475,7 +551,6 @@ __global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__
                                                      const uint64_t* __restrict__ base, double* __restrict__ part) {
     __shared__ float hh[8][KM];
     const int lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    const unsigned lt = (1u << lane) - 1u;
     const uint64_t nw = (uint64_t)gridDim.x * 8;
     for (uint64_t r = (uint64_t)blockIdx.x * 8 + wl; r < p; r += nw) {
         const uint64_t seq = r / chunk;
@@ -488,21 +563,20 @@ __global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__
         double s1 = 0.0, nk = 0.0;
         int nmask = 0;
         uint64_t before = base[r];
-        for (uint64_t i0 = 0; i0 < n; i0 += 32) {
-            const uint64_t i = i0 + lane;
-            const uint32_t code = i < n ? code_at(row, i) : 1u;
-            const bool obs = i < n && code != 1u;
-            const unsigned bal = __ballot_sync(0xffffffffu, obs);
-            bool held = false;
-            if (obs) {
-                const uint64_t ctr = before + __popc(bal & lt);
-                if constexpr (kChaCha) held = (cc.at(ctr) >> 12) < thresh;
-                else held = draw_below(key, ctr, thresh);
-            }
-            before += __popc(bal);
-            if (i < n) {
+        for (uint64_t i0 = 0; i0 < n; i0 += 256) {
+            uint32_t codes;
+            const uint32_t held8 = lane_held8<kChaCha>(row, n, i0, before, key, cc, thresh, codes);
+            // the warp's 256 samples in the coalesced layout: sample i0 + 32 j + lane
+            for (int j = 0; j < 8; ++j) {
+                const uint64_t i = i0 + 32 * (uint64_t)j + lane;
+                const int src = 4 * j + (lane >> 3), bit = lane & 7;
+                const uint32_t hm = __shfl_sync(0xffffffffu, held8, src);
+                const uint32_t cw = __shfl_sync(0xffffffffu, codes, src);
+                if (i >= n) continue;
+                const uint32_t code = (cw >> (2 * bit)) & 3u;
+                const bool held = (hm >> bit) & 1u;
                 const float* wp = Wpt + i * k;
-                if (obs && !held) {
+                if (code != 1u && !held) {
                     const float g = code == 0 ? 0.f : (float)(code - 1);
                     s1 += (double)g;
                     nk += 1.0;
@@ -514,8 +588,8 @@ __global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__
                     for (int c = 0; c < KM; ++c)
                         if (c < k) B[c] += wp[c];
                 }
+                nmask += held ? 1 : 0;
             }
-            nmask += held ? 1 : 0;
         }
         nmask = __reduce_add_sync(0xffffffffu, nmask);
         if (nmask == 0) {
@@ -535,23 +609,20 @@ __global__ void __launch_bounds__(256) k_nmf_gwas_cv(const uint8_t* __restrict__
         __syncwarp();
         double e1 = 0.0, e2 = 0.0;
         before = base[r];
-        for (uint64_t i0 = 0; i0 < n; i0 += 32) {
-            const uint64_t i = i0 + lane;
-            const uint32_t code = i < n ? code_at(row, i) : 1u;
-            const bool obs = i < n && code != 1u;
-            const unsigned bal = __ballot_sync(0xffffffffu, obs);
-            bool held = false;
-            if (obs) {
-                const uint64_t ctr = before + __popc(bal & lt);
-                if constexpr (kChaCha) held = (cc.at(ctr) >> 12) < thresh;
-                else held = draw_below(key, ctr, thresh);
-            }
-            if (held) {
+        for (uint64_t i0 = 0; i0 < n; i0 += 256) {
+            uint32_t codes;
+            const uint32_t held8 = lane_held8<kChaCha>(row, n, i0, before, key, cc, thresh, codes);
+            for (int j = 0; j < 8; ++j) {
+                const uint64_t i = i0 + 32 * (uint64_t)j + lane;
+                const int src = 4 * j + (lane >> 3), bit = lane & 7;
+                const uint32_t hm = __shfl_sync(0xffffffffu, held8, src);
+                const uint32_t cw = __shfl_sync(0xffffffffu, codes, src);
+                if (i >= n || !((hm >> bit) & 1u)) continue;
+                const uint32_t code = (cw >> (2 * bit)) & 3u;
                 const double g = code == 0 ? 0.0 : (double)(code - 1);
                 e1 += fabs(g - (double)fill_dot<KM>(W + i * k, hh[wl], k));
                 e2 += fabs(g - mu);
             }
-            before += __popc(bal);
         }
         e1 = warp_sum_d(e1);
         e2 = warp_sum_d(e2);
