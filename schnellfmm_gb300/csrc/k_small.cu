@@ -1165,8 +1165,10 @@ void launch_scale_cols_sd(Ctx& c, double* A, uint64_t m, int a, int lda) {
 template <typename T>
 static void atb_impl(Ctx& c, const T* A, int lda, const T* B, int ldb, uint64_t m, int a, int b,
                      double* out) {
+    // FP64-bound (GB300 runs FP64 at a small fraction of FP32): enough row
+    // splits that every SM holds a few CTAs (64 rows each at least)
     const int ta = (int)ceil_div(a, 32), tb = (int)ceil_div(b, 32);
-    uint64_t splits = std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(m, 256),
+    uint64_t splits = std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(m, 64),
                                           ceil_div((uint64_t)c.sm_count * 8, (uint64_t)ta * tb)));
     splits = std::min<uint64_t>(splits, 65535);
     const uint64_t per = round_up(ceil_div(std::max<uint64_t>(m, 1), splits), 32);
