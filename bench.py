@@ -703,7 +703,8 @@ def main():
         d2h = sum(a.nbytes for a in out.values())
         e2e = {"value": job_rate(p, world, e2e_ms), "unit": "SNPs/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h), "ms_per_step": e2e_ms,
-               "per_step_ms": [e0.elapsed_time(e1) / args.steps, wall], "call_wall_ms": calls}
+               "per_step_ms": [e0.elapsed_time(e1) / args.steps, wall], "call_wall_ms": calls,
+               "call_wall_median_ms": statistics.median(calls)}
         # where one call's time goes (after the timed loop): device time per
         # phase from events on the engine's stream, host wall time per phase,
         # and this box's page-locked copy rates

@@ -460,19 +460,35 @@ struct Fp8RowPass {
 // 0.5 % missing): 4.18 ms for the ring without the indicator plus 3.43 ms for
 // the fix, against 8.2 ms with the indicator (which also measured 15 ms on
 // some boxes, where the other forms did not change); at 7 % missing (n =
-// 5 000) the fix costs more than the indicator.  So the fix is taken when at
-// most 1 % of the calls are missing, and always for the sketch pass of the
-// randomized SVD (`sketch`): that pass also runs chunk by chunk under an
-// upload, before the missing-call count is known, and both must take the
-// same form.  SLFMM_TC8_ROW_IND=1 / =0 force the indicator on / off.
+// 5 000) the fix costs more than the indicator, and below a few thousand
+// samples (a few stages per tile, n = 100-3 000 measured) the indicator ring
+// is not the limiter while the fix is one more launch per pass.  So the fix
+// is taken for n >= 8192 samples when at most 1 % of the calls are missing,
+// and for the sketch pass of the randomized SVD (`sketch`) whenever
+// n >= 8192: that pass also runs chunk by chunk under an upload, before the
+// missing-call count is known, and both must take the same form.
+// SLFMM_TC8_ROW_IND=1 / =0 force the indicator on / off.
+constexpr uint64_t kSparseFixMinSamples = 8192;
+
 bool fp8_row_indicator_forced() {
     const char* env = std::getenv("SLFMM_TC8_ROW_IND");
     return env && env[0] == '1';
 }
 
+// the form of a sketch pass over n samples, known before any data lands
+bool fp8_sketch_takes_indicator(uint64_t n) {
+    const char* env = std::getenv("SLFMM_TC8_ROW_IND");
+    if (env && env[0] == '0') return false;
+    return fp8_row_indicator_forced() || n < kSparseFixMinSamples;
+}
+
 bool fp8_row_take_indicator(Ctx& c, const Geno& g, bool sketch) {
+    if (sketch) return fp8_sketch_takes_indicator(g.n);
     if (fp8_row_indicator_forced()) return true;
-    if (sketch) return false;
+    if (g.n < kSparseFixMinSamples) {
+        const char* env = std::getenv("SLFMM_TC8_ROW_IND");
+        return !(env && env[0] == '0');
+    }
     const char* env = std::getenv("SLFMM_TC8_ROW_IND");
     if (env && env[0] == '0') return false;
     build_missing_lists(c, g);
@@ -1388,7 +1404,7 @@ struct Presketch : ChunkHook {
         DBuf<double> W;
         sketch_operand(c, s0, n, l, cfg->seed, omega, W);
         // the form the pass over the resident matrix takes (fp8_row_prepare)
-        fp8_row_operand_prepare(c, n, ceil_div(p, 128), W.get(), l, l, fp8_row_indicator_forced(), rp);
+        fp8_row_operand_prepare(c, n, ceil_div(p, 128), W.get(), l, l, fp8_sketch_takes_indicator(n), rp);
         se.mean.alloc(p, c.stream);
         se.scale.alloc(p, c.stream);
         se.tss.alloc(p, c.stream);
