@@ -74,7 +74,8 @@ struct Tc8Args {
     const uint8_t* wop;     // stage-major, pre-swizzled W operand (wop_offset)
     int mode;               // 0: out = P + M; 1: out = s_r (P - mu_r (cs_c - M))
     long long expire_cycles;  // > 0: test hook, see below
-    uint32_t tile0;           // matrix index of the tile of blockIdx.x = 0
+    uint32_t tile0;           // matrix index of the tile of unit 0
+    uint32_t units, gx;       // work units (row tiles x K splits) and row tiles
     uint32_t rotate;          // stagger the K order of the tiles (see below)
     const double* row_mean;
     const double* row_scale;
@@ -131,12 +132,18 @@ struct Ring {
 // in the epilogue); with it one issues the genotype MMAs and the other the
 // indicator MMAs of every K block, their group boundaries G/2 apart.
 //
-// This warp's K blocks: [start, start + len0), then groups of G, each
-// followed by `skip` K blocks that belong to the other warp.
+// This warp's K blocks of one work unit: [start, start + len0), then groups
+// of G, each followed by `skip` K blocks that belong to the other warp.  The
+// unit's first K block is stage g0 of the CTA's stage sequence (the rings run
+// on across the CTA's units: stage g sits in A slot g % S, W slot g % SW).
+__device__ __forceinline__ Ring ring_at(uint64_t g, uint32_t n) {
+    return Ring{(uint32_t)(g % n), (uint32_t)((g / n) & 1u)};
+}
+
 template <int NCH, bool MAIN, bool IND, int G>
-__device__ __forceinline__ void tc8_mma_loop(const Tc8Args& a, uint32_t tmem, uint32_t d_main, uint32_t bsm_addr,
+__device__ __forceinline__ bool tc8_mma_loop(const Tc8Args& a, uint32_t tmem, uint32_t d_main, uint32_t bsm_addr,
                                              uint64_t* full_b, uint64_t* full_a, uint64_t* a_empty,
-                                             uint64_t* b_empty, uint32_t nkb, uint32_t start,
+                                             uint64_t* b_empty, uint64_t g0, uint32_t nkb, uint32_t start,
                                              uint32_t len0, uint32_t skip) {
     const uint32_t S = a.stages, SW = a.wstages;
     const uint32_t chunk = a.n_main / NCH;
@@ -149,9 +156,7 @@ __device__ __forceinline__ void tc8_mma_loop(const Tc8Args& a, uint32_t tmem, ui
     const uint64_t hstep = (uint64_t)a.n_total * (128 >> 4);  // next 128-sample half of the stage
     const uint32_t d_ind = tmem + a.n_main;
     const uint32_t a0 = tmem + a.a_base;
-    Ring st{0, 0}, sw{0, 0};  // A ring (TMEM) and W ring (shared memory) positions
-    st.advance(start, S);
-    sw.advance(start, SW);
+    Ring st = ring_at(g0 + start, S), sw = ring_at(g0 + start, SW);  // A ring (TMEM), W ring (shared memory)
     uint32_t i = start, len = len0;
     while (i < nkb) {
         const uint32_t g = min(len, nkb - i);
@@ -162,7 +167,7 @@ __device__ __forceinline__ void tc8_mma_loop(const Tc8Args& a, uint32_t tmem, ui
             w.advance(1, S);
             wb.advance(1, SW);
         }
-        if (!ok) break;
+        if (!ok) return false;
         fence_after();
 #pragma unroll
         for (int j = 0; j < G; ++j) {
@@ -192,24 +197,32 @@ __device__ __forceinline__ void tc8_mma_loop(const Tc8Args& a, uint32_t tmem, ui
         sw.advance(skip, SW);
         len = G;
     }
+    return true;
 }
 
 template <int NCH, bool MAIN, bool IND>
-__device__ __forceinline__ void tc8_mma_dispatch(const Tc8Args& a, uint32_t tmem, uint32_t d_main, uint32_t bsm_addr,
+__device__ __forceinline__ bool tc8_mma_dispatch(const Tc8Args& a, uint32_t tmem, uint32_t d_main, uint32_t bsm_addr,
                                                  uint64_t* full_b, uint64_t* full_a, uint64_t* a_empty,
-                                                 uint64_t* b_empty, uint32_t nkb, uint32_t start,
+                                                 uint64_t* b_empty, uint64_t g0, uint32_t nkb, uint32_t start,
                                                  uint32_t len0, uint32_t skip) {
     if (a.group == 4)
-        tc8_mma_loop<NCH, MAIN, IND, 4>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty, nkb,start,
-                                        len0, skip);
-    else if (a.group == 2)
-        tc8_mma_loop<NCH, MAIN, IND, 2>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty, nkb,start,
-                                        len0, skip);
-    else
-        tc8_mma_loop<NCH, MAIN, IND, 1>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty, nkb,start,
-                                        len0, skip);
+        return tc8_mma_loop<NCH, MAIN, IND, 4>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty, g0, nkb,
+                                               start, len0, skip);
+    if (a.group == 2)
+        return tc8_mma_loop<NCH, MAIN, IND, 2>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty, g0, nkb,
+                                               start, len0, skip);
+    return tc8_mma_loop<NCH, MAIN, IND, 1>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty, g0, nkb,
+                                           start, len0, skip);
 }
 
+// One CTA per SM runs work units u = blockIdx.x, blockIdx.x + gridDim.x, ...
+// (unit u: row tile u % gx, K split u / gx); a launch with one CTA per unit
+// is the same code with one unit each.  The copy and MMA rings run on across
+// a CTA's units (stage g of the CTA's sequence sits in slot g % depth), so the
+// producers prefetch the next unit's operands while the current unit's last
+// stages and epilogue run; D is reused once the epilogue has read it
+// (d_empty).  A unit's accumulation order depends only on its tile and
+// split, so every grid gives the same bits.
 __global__ void __launch_bounds__(kThreads, 1) k_tc8_rows(const __grid_constant__ Tc8Args a) {
     extern __shared__ uint8_t smem_raw[];
     uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -224,23 +237,26 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc8_rows(const __grid_constant_
     uint64_t* a_empty = full_a + S;          // [S] the MMAs reading the A stage done
     uint64_t* p_full = a_empty + S;          // [P] packed codes landed (TMA tx)
     uint64_t* p_empty = p_full + P;          // [P] packed codes consumed (4 warp arrivals)
-    uint64_t* tmem_full = p_empty + P;
-    uint64_t* never = tmem_full + 1;         // test hook: a barrier nothing arrives at
+    uint64_t* tmem_full = p_empty + P;       // a unit's MMAs done (both MMA warps commit)
+    uint64_t* d_empty = tmem_full + 1;       // a unit's epilogue has read D (8 unpack warps)
+    uint64_t* never = d_empty + 1;           // test hook: a barrier nothing arrives at
     uint32_t* tmem_holder = reinterpret_cast<uint32_t*>(never + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const uint32_t row0 = blockIdx.x * kM;
-    const uint32_t kb0 = blockIdx.y * a.kb_per_split;
-    const uint32_t kb1 = min(a.kb_total, kb0 + a.kb_per_split);
-    const uint32_t nkb = kb1 > kb0 ? kb1 - kb0 : 0;
     const bool ind = a.n_ind != 0;
+    auto unit_kb0 = [&](uint32_t u) { return (u / a.gx) * a.kb_per_split; };
+    auto unit_nkb = [&](uint32_t u) {
+        const uint32_t kb0 = unit_kb0(u), kb1 = min(a.kb_total, kb0 + a.kb_per_split);
+        return kb1 > kb0 ? kb1 - kb0 : 0u;
+    };
     // K order: the tiles of a launch all read the same W stages, and with
     // every CTA at the same stage the L2 serves one 56 KB stage to ~150 SMs
     // at once.  Each tile starts at its own stage (a rotation of the K loop,
     // fixed by its index in the matrix, so the accumulation order and the
     // bits do not depend on how rows are split into launches).
-    const uint32_t rot = (a.rotate && nkb > 1) ? (uint32_t)(((a.tile0 + blockIdx.x) * 37ull) % nkb) : 0u;
-    auto kstage = [&](uint32_t i) { return i + rot < nkb ? i + rot : i + rot - nkb; };
+    auto unit_rot = [&](uint32_t u, uint32_t nkb) {
+        return (a.rotate && nkb > 1) ? (uint32_t)(((a.tile0 + u % a.gx) * 37ull) % nkb) : 0u;
+    };
 
     if (threadIdx.x == 0) {
         for (uint32_t s = 0; s < SW; ++s) {
@@ -256,6 +272,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc8_rows(const __grid_constant_
             mbar_init(p_empty + p, 4);
         }
         mbar_init(tmem_full, 2);
+        mbar_init(d_empty, 4 * kUnpackSets);
         mbar_init(never, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -280,40 +297,59 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc8_rows(const __grid_constant_
         if (threadIdx.x == 0) mbar_wait_for(never, 0, a.err, 30, a.expire_cycles);
     } else if (warp == 0) {
         if (lane == 0) {
-            // packed-code producer: runs up to P stages ahead of the unpackers;
-            // each (tile, stage) operand is one contiguous bulk copy
-            const uint8_t* src = a.tiles + (uint64_t)blockIdx.x * a.tile_bytes + (uint64_t)kb0 * kStageBytes;
-            Ring pr{0, 0};
-            uint32_t issued = 0;
-            for (uint32_t i = 0; i < nkb; ++i) {
-                const uint32_t ks = kstage(i);
-                if (i >= P && !mbar_wait(p_empty + pr.slot, pr.phase ^ 1u, a.err, 21)) break;
-                mbar_arrive_tx(p_full + pr.slot, kStageBytes);
-                bulk_g2s(psm + pr.slot * kStageBytes, src + (uint64_t)ks * kStageBytes, kStageBytes, p_full + pr.slot);
-                issued = i + 1;
-                pr.advance(1, P);
+            // packed-code producer: runs up to P stages ahead of the unpackers,
+            // across units; each (tile, stage) operand is one contiguous bulk copy
+            uint64_t g = 0, issued = 0;
+            bool ok = true;
+            for (uint32_t u = blockIdx.x; u < a.units && ok; u += gridDim.x) {
+                const uint32_t nkb = unit_nkb(u), rot = unit_rot(u, nkb);
+                const uint8_t* src =
+                    a.tiles + (uint64_t)(u % a.gx) * a.tile_bytes + (uint64_t)unit_kb0(u) * kStageBytes;
+                for (uint32_t i = 0; i < nkb; ++i, ++g) {
+                    const uint32_t ks = i + rot < nkb ? i + rot : i + rot - nkb;
+                    const Ring pr = ring_at(g, P);
+                    if (g >= P && !mbar_wait(p_empty + pr.slot, pr.phase ^ 1u, a.err, 21)) {
+                        ok = false;
+                        break;
+                    }
+                    mbar_arrive_tx(p_full + pr.slot, kStageBytes);
+                    bulk_g2s(psm + pr.slot * kStageBytes, src + (uint64_t)ks * kStageBytes, kStageBytes,
+                             p_full + pr.slot);
+                    issued = g + 1;
+                }
             }
-            for (uint32_t i = issued > P ? issued - P : 0; i < issued; ++i)
-                mbar_wait(p_full + i % P, (i / P) & 1, a.err, 22);
+            // never leave with copies in flight into this CTA's shared memory
+            for (uint64_t q = issued > P ? issued - P : 0; q < issued; ++q) {
+                const Ring pr = ring_at(q, P);
+                mbar_wait(p_full + pr.slot, pr.phase, a.err, 22);
+            }
         }
     } else if (warp == 2) {
         // each spinning role has a warp of its own: lanes of one warp that
         // spin in different loops starve each other
         if (lane == 0) {
-            // W producer: one bulk copy per stage
-            Ring wr{0, 0};
-            uint32_t issued = 0;
-            for (uint32_t i = 0; i < nkb; ++i) {
-                if (i >= SW && !mbar_wait(b_empty + wr.slot, wr.phase ^ 1u, a.err, 23)) break;
-                mbar_arrive_tx(full_b + wr.slot, a.b_stage_bytes);
-                const uint64_t kb = kb0 + kstage(i);
-                bulk_g2s(bsm + wr.slot * a.b_stage_bytes, a.wop + kb * a.b_stage_bytes, a.b_stage_bytes,
-                         full_b + wr.slot);
-                issued = i + 1;
-                wr.advance(1, SW);
+            // W producer: one bulk copy per stage, across units
+            uint64_t g = 0, issued = 0;
+            bool ok = true;
+            for (uint32_t u = blockIdx.x; u < a.units && ok; u += gridDim.x) {
+                const uint32_t nkb = unit_nkb(u), rot = unit_rot(u, nkb), kb0 = unit_kb0(u);
+                for (uint32_t i = 0; i < nkb; ++i, ++g) {
+                    const uint32_t ks = i + rot < nkb ? i + rot : i + rot - nkb;
+                    const Ring wr = ring_at(g, SW);
+                    if (g >= SW && !mbar_wait(b_empty + wr.slot, wr.phase ^ 1u, a.err, 23)) {
+                        ok = false;
+                        break;
+                    }
+                    mbar_arrive_tx(full_b + wr.slot, a.b_stage_bytes);
+                    bulk_g2s(bsm + wr.slot * a.b_stage_bytes, a.wop + (uint64_t)(kb0 + ks) * a.b_stage_bytes,
+                             a.b_stage_bytes, full_b + wr.slot);
+                    issued = g + 1;
+                }
             }
-            for (uint32_t i = issued > SW ? issued - SW : 0; i < issued; ++i)
-                mbar_wait(full_b + i % SW, (i / SW) & 1, a.err, 24);
+            for (uint64_t q = issued > SW ? issued - SW : 0; q < issued; ++q) {
+                const Ring wr = ring_at(q, SW);
+                mbar_wait(full_b + wr.slot, wr.phase, a.err, 24);
+            }
         }
     } else if (warp == 1 || warp == 3) {
         if (lane == 0) {
@@ -321,174 +357,202 @@ __global__ void __launch_bounds__(kThreads, 1) k_tc8_rows(const __grid_constant_
             const uint32_t bsm_addr = smem_u32(bsm);
             const uint32_t G = a.group;
             const int nch = a.n_main > 256 ? 2 : 1;  // host guarantees an even split into <= 256-wide MMAs
-            if (a.nsplit) {
-                // genotype MMAs on warp 0, indicator MMAs on warp 1, boundaries G/2 apart
-                if (m == 0) {
+            uint64_t g0 = 0;
+            uint32_t k = 0;  // this CTA's units so far
+            bool ok = true;
+            for (uint32_t u = blockIdx.x; u < a.units && ok; u += gridDim.x, ++k) {
+                const uint32_t nkb = unit_nkb(u);
+                // D is free once the previous unit's epilogue has read it
+                if (k > 0) {
+                    ok = mbar_wait(d_empty, (k - 1) & 1u, a.err, 31);
+                    fence_after();
+                }
+                if (ok && a.nsplit) {
+                    // genotype MMAs on warp 0, indicator MMAs on warp 1, boundaries G/2 apart
+                    if (m == 0) {
+                        if (nch == 1)
+                            ok = tc8_mma_dispatch<1, true, false>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty,
+                                                                  b_empty, g0, nkb, 0, G, 0);
+                        else
+                            ok = tc8_mma_dispatch<2, true, false>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty,
+                                                                  b_empty, g0, nkb, 0, G, 0);
+                    } else {
+                        ok = tc8_mma_dispatch<1, false, true>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty,
+                                                              b_empty, g0, nkb, 0, G > 1 ? G / 2 : 1, 0);
+                    }
+                } else if (ok && a.kcopies == 2) {
+                    // alternate groups of G K blocks into accumulator copies m
+                    const uint32_t d_main = tmem + m * a.d_cols;
                     if (nch == 1)
-                        tc8_mma_dispatch<1, true, false>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty,
-                                                         nkb,0, G, 0);
+                        ok = tc8_mma_dispatch<1, true, false>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty,
+                                                              b_empty, g0, nkb, m * G, G, G);
                     else
-                        tc8_mma_dispatch<2, true, false>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty,
-                                                         nkb,0, G, 0);
-                } else {
-                    tc8_mma_dispatch<1, false, true>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty, nkb,
-                                                     0, G > 1 ? G / 2 : 1, 0);
+                        ok = tc8_mma_dispatch<2, true, false>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty,
+                                                              b_empty, g0, nkb, m * G, G, G);
+                } else if (ok && m == 0) {
+                    // one MMA warp does everything
+                    if (nch == 1) {
+                        if (ind)
+                            ok = tc8_mma_dispatch<1, true, true>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty,
+                                                                 b_empty, g0, nkb, 0, G, 0);
+                        else
+                            ok = tc8_mma_dispatch<1, true, false>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty,
+                                                                  b_empty, g0, nkb, 0, G, 0);
+                    } else {
+                        if (ind)
+                            ok = tc8_mma_dispatch<2, true, true>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty,
+                                                                 b_empty, g0, nkb, 0, G, 0);
+                        else
+                            ok = tc8_mma_dispatch<2, true, false>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty,
+                                                                  b_empty, g0, nkb, 0, G, 0);
+                    }
                 }
-            } else if (a.kcopies == 2) {
-                // alternate groups of G K blocks into accumulator copies m
-                const uint32_t d_main = tmem + m * a.d_cols;
-                if (nch == 1)
-                    tc8_mma_dispatch<1, true, false>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty,
-                                                     nkb,m * G, G, G);
-                else
-                    tc8_mma_dispatch<2, true, false>(a, tmem, d_main, bsm_addr, full_b, full_a, a_empty, b_empty,
-                                                     nkb,m * G, G, G);
-            } else if (m == 0) {
-                // one MMA warp does everything
-                if (nch == 1) {
-                    if (ind)
-                        tc8_mma_dispatch<1, true, true>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty,
-                                                        nkb,0, G, 0);
-                    else
-                        tc8_mma_dispatch<1, true, false>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty,
-                                                         nkb,0, G, 0);
-                } else {
-                    if (ind)
-                        tc8_mma_dispatch<2, true, true>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty,
-                                                        nkb,0, G, 0);
-                    else
-                        tc8_mma_dispatch<2, true, false>(a, tmem, tmem, bsm_addr, full_b, full_a, a_empty, b_empty,
-                                                         nkb,0, G, 0);
-                }
+                mma_commit(tmem_full);  // both MMA warps arrive per unit (an idle one at once)
+                g0 += nkb;
             }
-            mma_commit(tmem_full);  // both MMA warps arrive (an idle one at once)
         }
     } else {
-        // kUnpackSets sets of four unpack warps take K blocks round robin;
-        // warp % 4 is the TMEM lane quarter a warp may access
+        // kUnpackSets sets of four unpack warps take the stages of the CTA's
+        // sequence round robin; warp % 4 is the TMEM lane quarter a warp may access
         const uint32_t set = (uint32_t)(warp - 4) >> 2;
         const uint32_t q = (uint32_t)warp & 3u;
         const uint32_t row = q * 32 + lane;
         const uint32_t lane_base = tmem + ((q * 32) << 16);
-        Ring pr{0, 0}, st{0, 0};
-        pr.advance(set, P);
-        st.advance(set, S);
         const uint32_t nsets = a.usets;
-        for (uint32_t i = set; i < nkb && set < nsets; i += nsets) {
-            // one lane polls each barrier and the warp follows it (the warp
-            // barrier orders the other lanes after its observation)
-            if (!warp_wait(p_full + pr.slot, pr.phase, a.err, 27)) break;
-            // this row's 256 codes: 32 B in each of the stage's two tile blocks
-            const uint8_t* rp = psm + pr.slot * kStageBytes + row * (kTileK / 4);
-            const uint4 p0 = reinterpret_cast<const uint4*>(rp)[0], p1 = reinterpret_cast<const uint4*>(rp)[1];
-            const uint4 p2 = reinterpret_cast<const uint4*>(rp + kTileBytes)[0];
-            const uint4 p3 = reinterpret_cast<const uint4*>(rp + kTileBytes)[1];
-            __syncwarp();
-            if (lane == 0) mbar_arrive(p_empty + pr.slot);   // codes are in registers: release the slot
-            pr.advance(nsets, P);
-            // a 32-bit word holds 16 two-bit codes; masking the even / odd codes
-            // into nibbles gives PRMT selectors directly (4 codes per PRMT), and
-            // the B operand stores K in the matching even-then-odd order
-            const uint32_t w16[16] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w,
-                                      p2.x, p2.y, p2.z, p2.w, p3.x, p3.y, p3.z, p3.w};
-            uint32_t ev[16], od[16];
+        uint64_t g0 = 0;
+        uint32_t k = 0;
+        bool ok = true;
+        for (uint32_t u = blockIdx.x; u < a.units && ok; u += gridDim.x, ++k) {
+            const uint32_t nkb = unit_nkb(u);
+            for (uint32_t i = 0; i < nkb && set < nsets; ++i) {
+                const uint64_t g = g0 + i;
+                if (g % nsets != set) continue;
+                const Ring pr = ring_at(g, P), st = ring_at(g, S);
+                // one lane polls each barrier and the warp follows it (the warp
+                // barrier orders the other lanes after its observation)
+                if (!warp_wait(p_full + pr.slot, pr.phase, a.err, 27)) {
+                    ok = false;
+                    break;
+                }
+                // this row's 256 codes: 32 B in each of the stage's two tile blocks
+                const uint8_t* rp = psm + pr.slot * kStageBytes + row * (kTileK / 4);
+                const uint4 p0 = reinterpret_cast<const uint4*>(rp)[0], p1 = reinterpret_cast<const uint4*>(rp)[1];
+                const uint4 p2 = reinterpret_cast<const uint4*>(rp + kTileBytes)[0];
+                const uint4 p3 = reinterpret_cast<const uint4*>(rp + kTileBytes)[1];
+                __syncwarp();
+                if (lane == 0) mbar_arrive(p_empty + pr.slot);   // codes are in registers: release the slot
+                // a 32-bit word holds 16 two-bit codes; masking the even / odd codes
+                // into nibbles gives PRMT selectors directly (4 codes per PRMT), and
+                // the B operand stores K in the matching even-then-odd order
+                const uint32_t w16[16] = {p0.x, p0.y, p0.z, p0.w, p1.x, p1.y, p1.z, p1.w,
+                                          p2.x, p2.y, p2.z, p2.w, p3.x, p3.y, p3.z, p3.w};
+                uint32_t ev[16], od[16];
 #pragma unroll
-            for (int t = 0; t < 16; ++t) {
-                ev[t] = w16[t] & 0x33333333u;
-                od[t] = (w16[t] >> 2) & 0x33333333u;
-            }
-            uint32_t g[32], h[32];
-#pragma unroll
-            for (int t = 0; t < 8; ++t) {
-                g[4 * t] = __byte_perm(kTabGeno, 0u, ev[t]);
-                g[4 * t + 1] = __byte_perm(kTabGeno, 0u, ev[t] >> 16);
-                g[4 * t + 2] = __byte_perm(kTabGeno, 0u, od[t]);
-                g[4 * t + 3] = __byte_perm(kTabGeno, 0u, od[t] >> 16);
-                h[4 * t] = __byte_perm(kTabGeno, 0u, ev[8 + t]);
-                h[4 * t + 1] = __byte_perm(kTabGeno, 0u, ev[8 + t] >> 16);
-                h[4 * t + 2] = __byte_perm(kTabGeno, 0u, od[8 + t]);
-                h[4 * t + 3] = __byte_perm(kTabGeno, 0u, od[8 + t] >> 16);
-            }
-            keep32(g);  // expanded before the stage wait: only the stores follow it
-            keep32(h);
-            if (i >= S && !warp_wait(a_empty + st.slot, st.phase ^ 1u, a.err, 28)) break;
-            const uint32_t a_col = lane_base + a.a_base + st.slot * a.a_cols;
-            tmem_st_x32(a_col, g);
-            tmem_st_x32(a_col + 32, h);
-            if (ind) {
+                for (int t = 0; t < 16; ++t) {
+                    ev[t] = w16[t] & 0x33333333u;
+                    od[t] = (w16[t] >> 2) & 0x33333333u;
+                }
+                uint32_t gv[32], h[32];
 #pragma unroll
                 for (int t = 0; t < 8; ++t) {
-                    g[4 * t] = __byte_perm(kTabMiss, 0u, ev[t]);
-                    g[4 * t + 1] = __byte_perm(kTabMiss, 0u, ev[t] >> 16);
-                    g[4 * t + 2] = __byte_perm(kTabMiss, 0u, od[t]);
-                    g[4 * t + 3] = __byte_perm(kTabMiss, 0u, od[t] >> 16);
-                    h[4 * t] = __byte_perm(kTabMiss, 0u, ev[8 + t]);
-                    h[4 * t + 1] = __byte_perm(kTabMiss, 0u, ev[8 + t] >> 16);
-                    h[4 * t + 2] = __byte_perm(kTabMiss, 0u, od[8 + t]);
-                    h[4 * t + 3] = __byte_perm(kTabMiss, 0u, od[8 + t] >> 16);
+                    gv[4 * t] = __byte_perm(kTabGeno, 0u, ev[t]);
+                    gv[4 * t + 1] = __byte_perm(kTabGeno, 0u, ev[t] >> 16);
+                    gv[4 * t + 2] = __byte_perm(kTabGeno, 0u, od[t]);
+                    gv[4 * t + 3] = __byte_perm(kTabGeno, 0u, od[t] >> 16);
+                    h[4 * t] = __byte_perm(kTabGeno, 0u, ev[8 + t]);
+                    h[4 * t + 1] = __byte_perm(kTabGeno, 0u, ev[8 + t] >> 16);
+                    h[4 * t + 2] = __byte_perm(kTabGeno, 0u, od[8 + t]);
+                    h[4 * t + 3] = __byte_perm(kTabGeno, 0u, od[8 + t] >> 16);
                 }
-                tmem_st_x32(a_col + 64, g);
-                tmem_st_x32(a_col + 96, h);
-            }
-            asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-            fence_before();
-            __syncwarp();
-            if (lane == 0) mbar_arrive(full_a + st.slot);
-            st.advance(nsets, S);
-        }
-        // epilogue: the sets take 16-column groups round robin
-        const bool ok = warp_wait(tmem_full, 0, a.err, 29);
-        // the second accumulator copy holds data only if its first group exists
-        const bool second_copy = a.kcopies == 2 && nkb > a.group;
-        fence_after();
-        const uint32_t grow = row0 + row;
-        const bool live = ok && grow < a.rows;
-        double rm = 0.0, rs = 0.0;
-        if (a.mode == 1 && live) {
-            rm = a.row_mean[grow];
-            rs = a.row_scale[grow];
-        }
-        float* dst = a.out + (uint64_t)blockIdx.y * a.split_stride + (uint64_t)grow * a.ldo;
-        for (uint32_t c0 = set * 16; c0 < a.wpad; c0 += 16 * kUnpackSets) {
-            float pm[16], pi[16], v[16];
-#pragma unroll
-            for (int k = 0; k < 16; ++k) pm[k] = pi[k] = 0.f;
-            for (int t = 0; t < kMainTerms; ++t) {
-                const uint32_t col = t * a.wpad + c0;
-                tmem_ld_x16(lane_base + col, v);
-                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-                if (second_copy) {
-                    float v2[16];
-                    tmem_ld_x16(lane_base + a.d_cols + col, v2);
-                    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-                    for (int k = 0; k < 16; ++k) v[k] += v2[k];
+                keep32(gv);  // expanded before the stage wait: only the stores follow it
+                keep32(h);
+                if (g >= S && !warp_wait(a_empty + st.slot, st.phase ^ 1u, a.err, 28)) {
+                    ok = false;
+                    break;
                 }
+                const uint32_t a_col = lane_base + a.a_base + st.slot * a.a_cols;
+                tmem_st_x32(a_col, gv);
+                tmem_st_x32(a_col + 32, h);
+                if (ind) {
 #pragma unroll
-                for (int k = 0; k < 16; ++k) pm[k] = fmaf(scl[col + k], v[k], pm[k]);
+                    for (int t = 0; t < 8; ++t) {
+                        gv[4 * t] = __byte_perm(kTabMiss, 0u, ev[t]);
+                        gv[4 * t + 1] = __byte_perm(kTabMiss, 0u, ev[t] >> 16);
+                        gv[4 * t + 2] = __byte_perm(kTabMiss, 0u, od[t]);
+                        gv[4 * t + 3] = __byte_perm(kTabMiss, 0u, od[t] >> 16);
+                        h[4 * t] = __byte_perm(kTabMiss, 0u, ev[8 + t]);
+                        h[4 * t + 1] = __byte_perm(kTabMiss, 0u, ev[8 + t] >> 16);
+                        h[4 * t + 2] = __byte_perm(kTabMiss, 0u, od[8 + t]);
+                        h[4 * t + 3] = __byte_perm(kTabMiss, 0u, od[8 + t] >> 16);
+                    }
+                    tmem_st_x32(a_col + 64, gv);
+                    tmem_st_x32(a_col + 96, h);
+                }
+                asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+                fence_before();
+                __syncwarp();
+                if (lane == 0) mbar_arrive(full_a + st.slot);
             }
-            if (ind) {
-                for (int t = 0; t < kIndTerms; ++t) {
-                    const uint32_t col = a.n_main + t * a.wpad + c0;
-                    const uint32_t scol = (a.ind_shared ? 0u : a.n_main) + t * a.wpad + c0;
+            if (!ok) break;
+            // epilogue of unit u: the sets take 16-column groups round robin
+            ok = warp_wait(tmem_full, k & 1u, a.err, 29);
+            // the second accumulator copy holds data only if its first group exists
+            const bool second_copy = a.kcopies == 2 && nkb > a.group;
+            fence_after();
+            const uint32_t grow = (u % a.gx) * kM + row;
+            const bool live = ok && grow < a.rows;
+            double rm = 0.0, rs = 0.0;
+            if (a.mode == 1 && live) {
+                rm = a.row_mean[grow];
+                rs = a.row_scale[grow];
+            }
+            float* dst = a.out + (uint64_t)(u / a.gx) * a.split_stride + (uint64_t)grow * a.ldo;
+            for (uint32_t c0 = set * 16; c0 < a.wpad && ok; c0 += 16 * kUnpackSets) {
+                float pm[16], pi[16], v[16];
+#pragma unroll
+                for (int kk = 0; kk < 16; ++kk) pm[kk] = pi[kk] = 0.f;
+                for (int t = 0; t < kMainTerms; ++t) {
+                    const uint32_t col = t * a.wpad + c0;
                     tmem_ld_x16(lane_base + col, v);
                     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                    if (second_copy) {
+                        float v2[16];
+                        tmem_ld_x16(lane_base + a.d_cols + col, v2);
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-                    for (int k = 0; k < 16; ++k) pi[k] = fmaf(scl[scol + k], v[k], pi[k]);
+                        for (int kk = 0; kk < 16; ++kk) v[kk] += v2[kk];
+                    }
+#pragma unroll
+                    for (int kk = 0; kk < 16; ++kk) pm[kk] = fmaf(scl[col + kk], v[kk], pm[kk]);
+                }
+                if (ind) {
+                    for (int t = 0; t < kIndTerms; ++t) {
+                        const uint32_t col = a.n_main + t * a.wpad + c0;
+                        const uint32_t scol = (a.ind_shared ? 0u : a.n_main) + t * a.wpad + c0;
+                        tmem_ld_x16(lane_base + col, v);
+                        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+                        for (int kk = 0; kk < 16; ++kk) pi[kk] = fmaf(scl[scol + kk], v[kk], pi[kk]);
+                    }
+                }
+                if (live) {
+#pragma unroll
+                    for (int kk = 0; kk < 16; ++kk) {
+                        if (a.mode == 1)
+                            v[kk] = (float)(rs * ((double)pm[kk] - rm * (a.cs[c0 + kk] - (double)pi[kk])));
+                        else
+                            v[kk] = pm[kk] + pi[kk];
+                    }
+                    float4* d4 = reinterpret_cast<float4*>(dst + c0);
+#pragma unroll
+                    for (int t = 0; t < 4; ++t) d4[t] = make_float4(v[4 * t], v[4 * t + 1], v[4 * t + 2], v[4 * t + 3]);
                 }
             }
-            if (live) {
-#pragma unroll
-                for (int k = 0; k < 16; ++k) {
-                    if (a.mode == 1)
-                        v[k] = (float)(rs * ((double)pm[k] - rm * (a.cs[c0 + k] - (double)pi[k])));
-                    else
-                        v[k] = pm[k] + pi[k];
-                }
-                float4* d4 = reinterpret_cast<float4*>(dst + c0);
-#pragma unroll
-                for (int t = 0; t < 4; ++t) d4[t] = make_float4(v[4 * t], v[4 * t + 1], v[4 * t + 2], v[4 * t + 3]);
-            }
+            // D may be overwritten by the next unit's MMAs
+            fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(d_empty);
+            g0 += nkb;
         }
     }
     fence_before();
@@ -1323,8 +1387,15 @@ static int tc8_launch(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t ro
     a.err = err_dev ? err_dev : err.get();
     const unsigned gy = (unsigned)ceil_div(a.kb_total, a.kb_per_split);
     const unsigned gx = (unsigned)ceil_div(rows, kM);
+    a.gx = gx;
+    a.units = gx * gy;
+    // one CTA per SM working through the units (SLFMM_TC8_PERSIST=0: one CTA
+    // per unit; the same code and bits either way)
+    const unsigned ctas = env_int("SLFMM_TC8_PERSIST", 1) != 0
+                              ? std::min<unsigned>(a.units, (unsigned)std::max(c.sm_count, 1))
+                              : a.units;
     cudaLaunchConfig_t cfg{};
-    cfg.gridDim = dim3(gx, gy, 1);
+    cfg.gridDim = dim3(std::max(ctas, 1u), 1, 1);
     cfg.blockDim = dim3(kThreads, 1, 1);
     cfg.dynamicSmemBytes = pl.smem;
     cfg.stream = c.stream;
@@ -1333,8 +1404,8 @@ static int tc8_launch(Ctx& c, const Fp8Plan& pl, const TileView& tv, uint64_t ro
         cudaGetLastError();
         char buf[320];
         snprintf(buf, sizeof buf,
-                 "split-FP8 contraction launch failed (%s): grid %u x %u, smem %zu, stages %u/%u, pstages %u, group %u, "
-                 "n_total %u, rows %llu, K %llu",
+                 "split-FP8 contraction launch failed (%s): units %u x %u, smem %zu, stages %u/%u, pstages %u, "
+                 "group %u, n_total %u, rows %llu, K %llu",
                  cudaGetErrorString(le), gx, gy, pl.smem, pl.stages, pl.wstages, pl.pstages, pl.group, pl.n_total,
                  (unsigned long long)rows, (unsigned long long)K);
         throw Error(SLFMM_ERR_CUDA, buf);
