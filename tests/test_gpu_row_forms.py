@@ -6,7 +6,9 @@ would all take it); SLFMM_TC8_ROW_IND forces either form, and both must
 match the FP64 oracle.  The paths that have to give the same bits as the
 resident fit -- the sketch pass under the upload and the per-trait subsets
 built from the tiles, whose missing-call lists then come from the tiles --
-must do so in the sparse form too."""
+must do so in the sparse form too.  The sparse form is also checked on
+ragged sample and SNP counts, on SNPs with most or all of their calls
+missing, and on the split-BF16 engine, whose row passes take the same fix."""
 import numpy as np
 import pytest
 
@@ -36,6 +38,37 @@ def test_row_forms_match_oracle(engine, monkeypatch, form):
     ref = O.fit_oracle64(c.raw, c.raw, c.x, k=4, oversampling=6, norm=O.NORM_EIGENSTRAT, omega=omega)
     _check(res, ref.assoc, ref.u_hat)
     geno.free()
+
+
+def _heavy(c, rows, frac, seed):
+    """Packed codes and raw values of cohort c with a share `frac` of the
+    calls of SNPs `rows` made missing."""
+    rng = np.random.default_rng(seed)
+    codes = c.codes.copy()
+    for j in rows:
+        codes[j, rng.random(c.n) < frac] = 1
+    return O.pack_codes(codes), O.DECODE_TABLE[codes].T.copy()
+
+
+@pytest.mark.parametrize("shape", [(700, 3001), (2000, 2500), (1537, 1800)])
+def test_sparse_fix_edges_match_oracle(engines, monkeypatch, shape):
+    sg = _sg()
+    monkeypatch.setenv("SLFMM_TC8_ROW_IND", "0")
+    n, p = shape
+    c = simdata.simulate(n, p, k_pop=3, fst=0.08, miss=0.02, d=2, n_causal=15, seed=64)
+    # SNPs with 60 % of their calls missing, and one with all of them
+    packed, raw = _heavy(c, [0, 5, 767, 768, p - 1], 0.6, 65)
+    packed[3] = O.pack_codes(np.ones((1, n), np.uint8))[0]
+    raw[:, 3] = np.nan
+    cfg = sg.Lfmm2Config(k=3, oversampling=5, norm=sg.SnpNorm.EIGENSTRAT)
+    omega = O.rng_normal_matrix(11, n, 8)
+    ref = O.fit_oracle64(raw, raw, c.x, k=3, oversampling=5, norm=O.NORM_EIGENSTRAT, omega=omega)
+    for prec in ("fp8", "bf16"):
+        eng = engines[prec]
+        geno = eng.upload(packed, n)
+        res = sg.fit_lfmm2(geno, sg.SubsetSpec.all(), geno, c.x, cfg, omega=omega, engine=eng)
+        _check(res, ref.assoc, ref.u_hat)
+        geno.free()
 
 
 def test_sparse_form_fit_host_equals_resident(engine, monkeypatch):
