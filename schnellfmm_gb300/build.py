@@ -53,7 +53,8 @@ def up_to_date() -> bool:
     if not LIB.exists():
         return False
     t = LIB.stat().st_mtime
-    deps = sources() + list(CSRC.glob("*.h")) + list((HERE.parent / "include").glob("*.h")) + [Path(__file__)]
+    deps = (sources() + list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + list((HERE.parent / "include").glob("*.h")) +
+            [Path(__file__)])
     return all(p.stat().st_mtime <= t for p in deps)
 
 

@@ -16,6 +16,7 @@
 #include <mutex>
 #include <string>
 
+#include "fp_convert.cuh"
 #include "slfmm_internal.h"
 
 namespace slfmm {
@@ -48,12 +49,13 @@ __device__ __forceinline__ int tsq_bin(float t) {
 }
 constexpr int kUsStride = kTileSnps + 4;  // 16-byte rows, staggered banks
 
+
 // One block of up to 64 traits per launch: traits [t0, t0 + d) of a model
 // with d_model covariates (the first d_model coordinates of u are the
 // covariate ones, so SS_cov always sums over d_model); beta and t32 rows
 // have d_model entries and point at trait t0; r2 may be null (written by the
 // launch of the first block).
-__global__ void __launch_bounds__(256) k_assoc_epilogue(
+__global__ void __launch_bounds__(256, 3) k_assoc_epilogue(
     uint64_t p, const float* __restrict__ u, int ldu, const double* __restrict__ tss,
     const uint8_t* __restrict__ zero_var, int d, int d_model, int w, double df,
     const float* __restrict__ theta_rows, const float* __restrict__ beta_rows,
@@ -66,6 +68,8 @@ __global__ void __launch_bounds__(256) k_assoc_epilogue(
     float* us = btT + w * kTraitPad;          // [w][68]
     float* s2s = us + w * kUsStride;          // [64] sigma^2 per SNP of the tile
     int* zvs = reinterpret_cast<int*>(s2s + kTileSnps);
+    float* sss = s2s + 2 * kTileSnps;         // [64] ||u||^2 per SNP of the tile
+    float* scs = sss + kTileSnps;             // [64] its covariate part
     __shared__ float cj[kTraitPad];
     __shared__ int dr[kTraitPad];
     const int tid = threadIdx.x;
@@ -103,31 +107,39 @@ __global__ void __launch_bounds__(256) k_assoc_epilogue(
                 sc += __shfl_xor_sync(0xffffffffu, sc, o);
             }
             if (l8 == 0) {
-                const uint64_t j = j0 + sn;
-                float s2f = 0.f;
-                int zv = 1;
-                if (j < p) {
-                    zv = zero_var && zero_var[j];
-                    const double T = tss[j];
-                    double rss = T - (double)ss;
-                    if (rss < 0.0 || zv) rss = 0.0;
-                    s2f = (float)(rss / df);
-                    double a = 0.0, b = 0.0, c = 0.0;
-                    if (T > 1e-300 && !zv) {                        // src/testing.rs:394-404
-                        const double ssc = (double)sc;
-                        a = ssc / T;
-                        b = fmax(T - rss - ssc, 0.0) / T;
-                        c = rss / T;
-                    }
-                    if (r2) {
-                        r2[j * 3 + 0] = a;
-                        r2[j * 3 + 1] = b;
-                        r2[j * 3 + 2] = c;
-                    }
-                }
-                s2s[sn] = s2f;
-                zvs[sn] = zv;
+                sss[sn] = ss;
+                scs[sn] = sc;
             }
+        }
+        __syncthreads();
+        // the FP64 part per SNP on one lane each (two full warps): this part's
+        // FP64 pipe is a small fraction of the FP32 one
+        if (tid < kTileSnps) {
+            const int sn = tid;
+            const uint64_t j = j0 + sn;
+            float s2f = 0.f;
+            int zv = 1;
+            if (j < p) {
+                zv = zero_var && zero_var[j];
+                const double T = tss[j];
+                double rss = T - (double)sss[sn];
+                if (rss < 0.0 || zv) rss = 0.0;
+                s2f = (float)(rss / df);
+                double a = 0.0, b = 0.0, c = 0.0;
+                if (T > 1e-300 && !zv) {                        // src/testing.rs:394-404
+                    const double ssc = (double)scs[sn];
+                    a = ssc / T;
+                    b = fmax(T - rss - ssc, 0.0) / T;
+                    c = rss / T;
+                }
+                if (r2) {
+                    r2[j * 3 + 0] = a;
+                    r2[j * 3 + 1] = b;
+                    r2[j * 3 + 2] = c;
+                }
+            }
+            s2s[sn] = s2f;
+            zvs[sn] = zv;
         }
         __syncthreads();
         float th[4][4], bb[4][4];
@@ -174,7 +186,7 @@ __global__ void __launch_bounds__(256) k_assoc_epilogue(
                     t = th[a][b] * rsqrtf(var);
                     if (!isfinite(t)) t = 0.f;
                 }
-                beta[j * d_model + jj] = zv ? 0.0 : (double)bb[a][b];
+                beta[j * d_model + jj] = zv ? 0.0 : f64_of_f32(bb[a][b]);
                 t32[j * d_model + jj] = t;
                 const int bin = tsq_bin(t);
                 if (bin >= 0) atomicAdd(&hist[(uint64_t)jj * kHistBins + bin], 1u);
@@ -244,7 +256,8 @@ constexpr int kMaxCalibTraits = 1024;
 
 // The per-trait factors 1/sqrt(2 GIF) (FP32) and 1/sqrt(GIF) (FP64) are
 // formed once per block: FP64 square roots and divisions per element would
-// dominate on this part, whose FP64 rate is a small fraction of FP32.
+// dominate on this part, whose FP64 rate is a small fraction of FP32; the
+// widening of t and p to FP64 moves bits with integer operations.
 __global__ void k_calibrate(uint64_t p, int d, const float* __restrict__ t32,
                             const double* __restrict__ gif, double* __restrict__ t64,
                             double* __restrict__ pval) {
@@ -261,11 +274,11 @@ __global__ void k_calibrate(uint64_t p, int d, const float* __restrict__ t32,
          e += (uint64_t)gridDim.x * blockDim.x) {
         const int jj = (int)(e % d);
         const float tf = t32[e];
-        if (t64) t64[e] = (double)tf;
+        if (t64) t64[e] = f64_of_f32(tf);
         if (pval) {
             const float zf = fabsf(tf) * zs[jj];
             double pv;
-            if (zf < 8.0f) pv = (double)erfcf(zf);
+            if (zf < 8.0f) pv = f64_of_f32(erfcf(zf));
             else pv = erfc(fabs((double)tf) * rs[jj] * 0.7071067811865476);
             pval[e] = pv;
         }
@@ -345,11 +358,15 @@ void launch_assoc_epilogue(Ctx& c, uint64_t p, const float* u, int ldu, const do
                            const AssocConsts& k, double* beta, float* t32, double* r2,
                            uint32_t* hist) {
     if (p == 0) return;
-    const size_t smem = (size_t)(2 * k.w * kTraitPad + k.w * kUsStride + 2 * kTileSnps) * sizeof(float);
+    const size_t smem = (size_t)(2 * k.w * kTraitPad + k.w * kUsStride + 4 * kTileSnps) * sizeof(float);
     SLFMM_REQUIRE(smem <= 227 * 1024, SLFMM_ERR_BAD_ARG, "association design too wide for the epilogue");
     raise_dynamic_smem((const void*)k_assoc_epilogue, smem);
     const uint64_t tiles = ceil_div(p, (uint64_t)kTileSnps);
-    const unsigned grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)c.sm_count * 3);
+    // one wave of persistent CTAs: as many per SM as fit (registers and
+    // shared memory), so no CTA starts its share of tiles after the others
+    int per_sm = 0;
+    SLFMM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_assoc_epilogue, 256, smem));
+    const unsigned grid = (unsigned)std::min<uint64_t>(tiles, (uint64_t)c.sm_count * std::max(per_sm, 1));
     // traits in blocks of 64 (the coefficient tables of one block stay in
     // shared memory); every block reads the same u rows
     for (int t0 = 0; t0 < k.d; t0 += kTraitPad) {
@@ -372,7 +389,9 @@ void launch_calibrate(Ctx& c, uint64_t p, int d, const float* t32, const double*
                       double* pval) {
     if (p == 0 || d == 0) return;
     SLFMM_REQUIRE(d <= kMaxCalibTraits, SLFMM_ERR_BAD_ARG, "too many traits for the calibration kernel");
-    k_calibrate<<<grid_for(c, p * d, 256), 256, 0, c.stream>>>(p, d, t32, gif, t64, pval);
+    // few blocks: each forms the d per-trait factors in FP64 before its loop
+    const unsigned grid = (unsigned)std::min<int>(grid_for(c, p * d, 256), c.sm_count * 8);
+    k_calibrate<<<grid, 256, 0, c.stream>>>(p, d, t32, gif, t64, pval);
     SLFMM_LAUNCHED(c, "k_calibrate");
 }
 

@@ -1104,10 +1104,38 @@ void set_smem(const void* fn, size_t bytes) { raise_dynamic_smem(fn, bytes); }
 
 }  // namespace
 
+// column means of a tall matrix: rows in ranges of kColRows per block, then
+// the partials summed in order and divided by m (one block per column left
+// too few blocks on the GPU: 30 blocks each walking 20 000 rows)
+constexpr uint64_t kColRows = 2048;
+
+__global__ void k_colsum_split(const double* __restrict__ A, uint64_t m, int a, int lda, uint64_t per,
+                               double* __restrict__ part);
+
+__global__ void k_mean_partials(const double* __restrict__ part, int splits, int a, uint64_t m,
+                                double* __restrict__ out) {
+    const int col = blockIdx.x * blockDim.x + threadIdx.x;
+    if (col >= a) return;
+    double s = 0.0;
+    for (int k = 0; k < splits; ++k) s += part[(uint64_t)k * a + col];
+    out[col] = m ? s / (double)m : 0.0;
+}
+
 void launch_colmeans(Ctx& c, const double* A, uint64_t m, int a, int lda, double* out) {
     if (a == 0) return;
-    k_colmeans<<<a, 256, 0, c.stream>>>(A, m, lda, out, 1);
-    SLFMM_LAUNCHED(c, "k_colmeans");
+    if (m <= 2 * kColRows) {
+        k_colmeans<<<a, 256, 0, c.stream>>>(A, m, lda, out, 1);
+        SLFMM_LAUNCHED(c, "k_colmeans");
+        return;
+    }
+    const uint64_t splits = std::min<uint64_t>(ceil_div(m, kColRows), 512);
+    const uint64_t per = ceil_div(m, splits);
+    DBuf<double> part(splits * a, c.stream);
+    k_colsum_split<<<dim3(a, (unsigned)splits), 256, 0, c.stream>>>(A, m, a, lda, per, part.get());
+    SLFMM_LAUNCHED(c, "k_colsum_split");
+    k_mean_partials<<<(unsigned)ceil_div((uint64_t)a, 128), 128, 0, c.stream>>>(part.get(), (int)splits, a, m,
+                                                                                 out);
+    SLFMM_LAUNCHED(c, "k_mean_partials");
 }
 
 // column sums of a tall matrix: row ranges of `per` rows in parallel, then
@@ -1125,12 +1153,12 @@ __global__ void k_colsum_split(const double* __restrict__ A, uint64_t m, int a, 
 
 void launch_colsums(Ctx& c, const double* A, uint64_t m, int a, int lda, double* out) {
     if (a == 0) return;
-    if (m <= 65536) {
+    if (m <= 2 * kColRows) {
         k_colmeans<<<a, 256, 0, c.stream>>>(A, m, lda, out, 0);
         SLFMM_LAUNCHED(c, "k_colsums");
         return;
     }
-    const uint64_t splits = std::min<uint64_t>(ceil_div(m, 16384), 512);
+    const uint64_t splits = std::min<uint64_t>(ceil_div(m, m <= 65536 ? kColRows : 16384), 512);
     const uint64_t per = ceil_div(m, splits);
     DBuf<double> part(splits * a, c.stream);
     k_colsum_split<<<dim3(a, (unsigned)splits), 256, 0, c.stream>>>(A, m, a, lda, per, part.get());

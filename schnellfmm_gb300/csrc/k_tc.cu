@@ -23,6 +23,7 @@
 #include <cuda.h>
 #include <cudaTypedefs.h>
 
+#include "fp_convert.cuh"
 #include "slfmm_internal.h"
 #include "tc_common.cuh"
 
@@ -329,14 +330,18 @@ __global__ void __launch_bounds__(256, 8) k_rowfix_mean4(float* __restrict__ P, 
         acc.w += __shfl_xor_sync(0xffffffffu, acc.w, o);
     }
     if (!act || grp != 0) return;
-    const double mu = mean[j], sc = scale[j];
+    // FP32 arithmetic, with the FP64 inputs narrowed by integer operations:
+    // P carries the FP32 rounding of its contraction, which the FP64 form of
+    // this update did not remove, and FP64 arithmetic here ran the FP64 pipe
+    // at 69 % of its peak for the whole kernel
+    const float mu = f32_of_f64(mean[j]), sc = f32_of_f64(scale[j]);
     const float a4[4] = {acc.x, acc.y, acc.z, acc.w};
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
         const int c = 4 * q + u;
         if (c < w) {
-            const double v = (double)P[j * ldp + c] - mu * (cs[c] - (double)a4[u]);
-            P[j * ldp + c] = (float)(sc * v);
+            const float t = f32_of_f64(cs[c]) - a4[u];
+            P[j * ldp + c] = sc * fmaf(-mu, t, P[j * ldp + c]);
         }
     }
 }
