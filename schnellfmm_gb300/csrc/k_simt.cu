@@ -7,6 +7,7 @@
 // missing call under mean imputation) and multiplied in FP32.  It serves as
 // the "plain FP32 GPU path" the tensor-core path is measured against and as
 // an independent second implementation for parity checks.
+#include "fp_convert.cuh"
 #include "slfmm_internal.h"
 
 namespace slfmm {
@@ -157,7 +158,7 @@ __global__ void k_reduce_splits(const float* __restrict__ part, int splits, uint
     for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < total;
          t += (uint64_t)gridDim.x * blockDim.x) {
         double acc = 0.0;
-        for (int s = 0; s < splits; ++s) acc += (double)part[(uint64_t)s * n_pad * wp + t];
+        for (int s = 0; s < splits; ++s) acc += f64_of_f32(part[(uint64_t)s * n_pad * wp + t]);
         S[t] = acc;
     }
 }

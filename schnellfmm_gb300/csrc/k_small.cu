@@ -114,6 +114,63 @@ __global__ void __launch_bounds__(256) k_atb(const T* __restrict__ A, int lda, c
         }
 }
 
+// A^T B over a row range with the a x b outputs laid flat: thread t of the
+// CTA owns outputs o0 + t + 256 k (k < R), rows of A and B are staged 32 at
+// a time in shared memory, and every FMA issued is one of the a x b (the
+// 32 x 32 output tiles of k_atb spend 39-61 % of their FP64 FMAs on padding
+// at the widths used here: 20, 50, 71).  FP64 accumulation in row order
+// within the range; partial[split] written, reduced by k_sum_partials.
+template <typename T, int R>
+__global__ void __launch_bounds__(256) k_atb_flat(const T* __restrict__ A, int lda, const T* __restrict__ B,
+                                                  int ldb, uint64_t m, int a, int b, uint64_t rows_per_split,
+                                                  double* __restrict__ part) {
+    extern __shared__ double stage[];
+    double* As = stage;             // [32][a]
+    double* Bs = stage + 32 * a;    // [32][b]
+    const int tid = threadIdx.x;
+    const int ab = a * b;
+    const int o0 = blockIdx.x * 256 * R;
+    const uint64_t i0 = (uint64_t)blockIdx.y * rows_per_split;
+    const uint64_t i1 = min(m, i0 + rows_per_split);
+    int ra[R], cb[R];
+    double acc[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int o = o0 + tid + 256 * k;
+        ra[k] = o < ab ? o / b : 0;
+        cb[k] = o < ab ? o % b : 0;
+        acc[k] = 0.0;
+    }
+    // warp-uniform: the last k with an output in this warp
+    const int wfirst = o0 + (tid & ~31);
+    for (uint64_t ib = i0; ib < i1; ib += 32) {
+        __syncthreads();
+        for (int e = tid; e < 32 * a; e += 256) {
+            const int ii = e / a, cc = e % a;
+            const uint64_t i = ib + ii;
+            As[e] = i < i1 ? (double)A[i * lda + cc] : 0.0;
+        }
+        for (int e = tid; e < 32 * b; e += 256) {
+            const int ii = e / b, cc = e % b;
+            const uint64_t i = ib + ii;
+            Bs[e] = i < i1 ? (double)B[i * ldb + cc] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            if (wfirst + 256 * k >= ab) break;
+#pragma unroll 8
+            for (int ii = 0; ii < 32; ++ii) acc[k] = fma(As[ii * a + ra[k]], Bs[ii * b + cb[k]], acc[k]);
+        }
+    }
+    double* dst = part + (uint64_t)blockIdx.y * ab;
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        const int o = o0 + tid + 256 * k;
+        if (o < ab) dst[o] = acc[k];
+    }
+}
+
 // FP32 Gram with FP32 products summed over 32-row tiles and FP64 across
 // tiles (used for the p x l sketches, whose FP64 Gram would dominate).
 __global__ void __launch_bounds__(256) k_gram_f32(const float* __restrict__ A, int lda, uint64_t m, int a,
@@ -1195,6 +1252,35 @@ static void atb_impl(Ctx& c, const T* A, int lda, const T* B, int ldb, uint64_t 
                      double* out) {
     // FP64-bound (GB300 runs FP64 at a small fraction of FP32): enough row
     // splits that every SM holds a few CTAs (64 rows each at least)
+    if (a > 0 && b > 0 && a * b <= 256 * 16 * 4 && a <= 128 && b <= 128) {
+        const int ab = a * b;
+        const int R = ab <= 256 ? 1 : ab <= 512 ? 2 : ab <= 1024 ? 4 : ab <= 2048 ? 8 : 16;
+        const int blocks_o = (int)ceil_div((uint64_t)ab, (uint64_t)256 * R);
+        uint64_t splits = std::max<uint64_t>(
+            1, std::min<uint64_t>(ceil_div(m, 64), ceil_div((uint64_t)c.sm_count * 8, (uint64_t)blocks_o)));
+        splits = std::min<uint64_t>(splits, 65535);
+        const uint64_t per = round_up(ceil_div(std::max<uint64_t>(m, 1), splits), 32);
+        splits = std::max<uint64_t>(1, ceil_div(m, per));
+        DBuf<double> part(splits * ab, c.stream);
+        const size_t smem = (size_t)32 * (a + b) * sizeof(double);
+        dim3 grid(blocks_o, (unsigned)splits);
+#define SLFMM_ATB_FLAT(RR)                                                                        \
+    do {                                                                                          \
+        raise_dynamic_smem((const void*)k_atb_flat<T, RR>, smem);                                 \
+        k_atb_flat<T, RR><<<grid, 256, smem, c.stream>>>(A, lda, B, ldb, m, a, b, per, part.get()); \
+    } while (0)
+        switch (R) {
+            case 1: SLFMM_ATB_FLAT(1); break;
+            case 2: SLFMM_ATB_FLAT(2); break;
+            case 4: SLFMM_ATB_FLAT(4); break;
+            case 8: SLFMM_ATB_FLAT(8); break;
+            default: SLFMM_ATB_FLAT(16); break;
+        }
+#undef SLFMM_ATB_FLAT
+        SLFMM_LAUNCHED(c, "k_atb_flat");
+        launch_sum_partials(c, part.get(), (int)splits, (uint64_t)ab, out);
+        return;
+    }
     const int ta = (int)ceil_div(a, 32), tb = (int)ceil_div(b, 32);
     uint64_t splits = std::max<uint64_t>(1, std::min<uint64_t>(ceil_div(m, 64),
                                           ceil_div((uint64_t)c.sm_count * 8, (uint64_t)ta * tb)));
