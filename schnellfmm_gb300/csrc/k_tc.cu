@@ -287,9 +287,9 @@ __global__ void k_rowfix_mean(float* __restrict__ P, int ldp, uint64_t rows, int
     }
 }
 
-// k_rowfix_mean with 16-byte W-row gathers: a group of L lanes (L = 8, 16
-// or 32, the column quads of W rounded up) covers one W row, lane q of the
-// group column quad q (w <= 128, W rows 16-byte aligned), and the 32 / L
+// k_rowfix_mean with 16-byte W-row gathers: a group of L lanes (L = 1, 2,
+// 4, 8 or 16, the column quads of the block rounded up) covers one W row,
+// lane q of the group column quad q (W rows 16-byte aligned), and the 32 / L
 // groups of a warp take consecutive missing calls of the same SNP; their
 // partial sums are combined by shuffles at the end.  The gathers are bound by
 // L2 latency, so the register cap keeps all 64 warps of an SM resident
@@ -640,26 +640,38 @@ int tc_split_count(Ctx& c, uint64_t rows, uint64_t K) {
 void launch_rowfix_mean(Ctx& c, float* P, int ldp, uint64_t rows, int w, const uint64_t* ptr, const uint32_t* idx,
                         const float* W, int ldw, const double* cs, const double* mean, const double* scale) {
     if (!rows) return;
-    // a warp covers 128 columns (4 per lane): wider operands in column blocks
-    for (int c0 = 0; c0 < w; c0 += 128) {
-        if (ldw % 4 == 0 && reinterpret_cast<uintptr_t>(W + c0) % 16 == 0) {
-            const int wb = std::min(128, w - c0);
+    const bool quads = ldw % 4 == 0 && reinterpret_cast<uintptr_t>(W) % 16 == 0;
+    for (int c0 = 0; c0 < w;) {
+        if (quads) {
+            // Column blocks that keep the lanes of a group busy: 64 columns
+            // (16 lanes), 32 (8 lanes), then the rest in the fewest lanes
+            // that hold it.  A warp step gathers 32 / L missing calls, so a
+            // block of 32 lanes for w = 71 (18 of them busy) took one call
+            // per step and 2.5 times as long as the w = 30 fix; as 64 + 7
+            // columns in 16 + 2 lanes the lists are read twice.  Every
+            // column's fix is separate.
+            const int rem = w - c0;
+            const int wb = rem >= 64 ? 64 : (rem > 32 ? 32 : rem);
+            const int nq = (wb + 3) / 4;
             const unsigned grid = (unsigned)ceil_div(rows * 32, 256);
-            if (wb <= 32)
-                k_rowfix_mean4<8><<<grid, 256, 0, c.stream>>>(P + c0, ldp, rows, wb, ptr, idx, W + c0, ldw, cs + c0,
-                                                              mean, scale);
-            else if (wb <= 64)
-                k_rowfix_mean4<16><<<grid, 256, 0, c.stream>>>(P + c0, ldp, rows, wb, ptr, idx, W + c0, ldw, cs + c0,
-                                                               mean, scale);
-            else
-                k_rowfix_mean4<32><<<grid, 256, 0, c.stream>>>(P + c0, ldp, rows, wb, ptr, idx, W + c0, ldw, cs + c0,
-                                                               mean, scale);
+#define SLFMM_ROWFIX4(LL)                                                                                     \
+    k_rowfix_mean4<LL><<<grid, 256, 0, c.stream>>>(P + c0, ldp, rows, wb, ptr, idx, W + c0, ldw, cs + c0, mean, \
+                                                   scale)
+            if (nq <= 1) SLFMM_ROWFIX4(1);
+            else if (nq <= 2) SLFMM_ROWFIX4(2);
+            else if (nq <= 4) SLFMM_ROWFIX4(4);
+            else if (nq <= 8) SLFMM_ROWFIX4(8);
+            else SLFMM_ROWFIX4(16);
+#undef SLFMM_ROWFIX4
             SLFMM_LAUNCHED(c, "k_rowfix_mean4");
+            c0 += wb;
             continue;
         }
+        // a warp covers 128 columns (4 per lane): wider operands in column blocks
         k_rowfix_mean<<<(unsigned)ceil_div(rows * 32, 256), 256, 0, c.stream>>>(
             P + c0, ldp, rows, std::min(128, w - c0), ptr, idx, W + c0, ldw, cs + c0, mean, scale);
         SLFMM_LAUNCHED(c, "k_rowfix_mean");
+        c0 += 128;
     }
 }
 
