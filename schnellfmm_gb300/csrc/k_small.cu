@@ -979,27 +979,64 @@ __global__ void __launch_bounds__(1024) k_jacobi_svd(double* __restrict__ A, int
         bmax = m;
     }
     __syncthreads();
-    // phase 4: FP64 two-sided Jacobi on B, rotations accumulated in R (in M)
+    // phase 4: FP64 two-sided Jacobi on B, rotations accumulated in R (in M).
+    // Each sweep pairs only the active columns, those with an off-diagonal
+    // entry above the skip level, in the round-robin order over them: a
+    // column whose couplings are all at that level stays there while the
+    // others rotate (a rotation of p and q mixes B_ip and B_iq and keeps
+    // their norm), and the sweeps after the first usually have a few
+    // columns left, the ones of the small eigenvalues the FP32 phase could
+    // not resolve -- a sweep over all columns costs ap - 1 rounds of block
+    // barriers and FP64 rotation angles whatever the number rotated.
     double* R = M;
     for (int e = threadIdx.x; e < ap * ap; e += blockDim.x) R[e] = (e / ap == e % ap) ? 1.0 : 0.0;
-    const int npairs = ap / 2;
     const double skip = 4e-16 * bmax;  // off-diagonals at the rounding level of B
+    __shared__ int act[kMaxDesign];
+    __shared__ int actflag[kMaxDesign];
+    __shared__ int nact;
     for (int sweep = 0; sweep < 12; ++sweep) {
         if (threadIdx.x == 0) rotated = 0;
         __syncthreads();
-        for (int round = 0; round < ap - 1; ++round) {
-            auto pos = [&](int idx) { return idx == 0 ? 0 : 1 + ((idx - 1 + round) % (ap - 1)); };
+        for (int cc = warp; cc < ap; cc += nwarps) {
+            bool any = false;
+            for (int r = lane; r < ap; r += 32) any |= r != cc && fabs(B[cc * ap + r]) > skip;
+            any = __any_sync(0xffffffffu, any);
+            if (lane == 0) actflag[cc] = any ? 1 : 0;
+        }
+        __syncthreads();
+        if (warp == 0) {  // the active columns in ascending order
+            int run = 0;
+            for (int base = 0; base < ap; base += 32) {
+                const bool f = base + lane < ap && actflag[base + lane];
+                const unsigned m = __ballot_sync(0xffffffffu, f);
+                if (f) act[run + __popc(m & ((1u << lane) - 1u))] = base + lane;
+                run += __popc(m);
+            }
+            if (lane == 0) nact = run;
+        }
+        __syncthreads();
+        const int na = nact;
+        if (na < 2) break;
+        const int nap = na + (na & 1);  // even; position na (odd na) pairs with no column
+        const int npairs = nap / 2;
+        for (int round = 0; round < nap - 1; ++round) {
+            auto pos = [&](int idx) { return idx == 0 ? 0 : 1 + ((idx - 1 + round) % (nap - 1)); };
             for (int k = threadIdx.x; k < npairs; k += blockDim.x) {
-                int pc = pos(k), qc = pos(ap - 1 - k);
-                if (pc > qc) { const int t = pc; pc = qc; qc = t; }
-                const double app = B[pc * ap + pc], aqq = B[qc * ap + qc], apq = B[qc * ap + pc];
+                const int x = pos(k), y = pos(nap - 1 - k);
                 double cs = 1.0, sn = 0.0;
-                if (fabs(apq) > skip && apq != 0.0) {
-                    const double tau = (aqq - app) / (2.0 * apq);
-                    const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-                    cs = 1.0 / sqrt(1.0 + t * t);
-                    sn = t * cs;
-                    rotated = 1;
+                int pc = 0, qc = 0;
+                if (x < na && y < na) {
+                    pc = act[x];
+                    qc = act[y];
+                    if (pc > qc) { const int t = pc; pc = qc; qc = t; }
+                    const double app = B[pc * ap + pc], aqq = B[qc * ap + qc], apq = B[qc * ap + pc];
+                    if (fabs(apq) > skip && apq != 0.0) {
+                        const double tau = (aqq - app) / (2.0 * apq);
+                        const double t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
+                        cs = 1.0 / sqrt(1.0 + t * t);
+                        sn = t * cs;
+                        rotated = 1;
+                    }
                 }
                 jp[k] = pc; jq[k] = qc; jc[k] = cs; js[k] = sn;
             }
