@@ -330,18 +330,6 @@ __global__ void k_lut_std(uint64_t p, const double* __restrict__ mean,
     }
 }
 
-__global__ void k_lut_raw(uint64_t p, const double* __restrict__ fill, float* __restrict__ lut) {
-    for (uint64_t j = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; j < p;
-         j += (uint64_t)gridDim.x * blockDim.x) {
-        float4 v;
-        v.x = 0.0f;
-        v.y = fill ? (float)fill[j] : 0.0f;
-        v.z = 1.0f;
-        v.w = 2.0f;
-        reinterpret_cast<float4*>(lut)[j] = v;
-    }
-}
-
 }  // namespace
 
 void launch_repack(Ctx& c, const uint8_t* in, uint64_t rows, uint64_t in_bps, uint64_t /*n_phys*/,
@@ -512,12 +500,6 @@ void launch_lut_std(Ctx& c, uint64_t p, const double* mean, const double* scale,
     if (p == 0) return;
     k_lut_std<<<grid_for(c, p, 256), 256, 0, c.stream>>>(p, mean, scale, lut);
     SLFMM_LAUNCHED(c, "k_lut_std");
-}
-
-void launch_lut_raw(Ctx& c, uint64_t p, const double* fill, float* lut) {
-    if (p == 0) return;
-    k_lut_raw<<<grid_for(c, p, 256), 256, 0, c.stream>>>(p, fill, lut);
-    SLFMM_LAUNCHED(c, "k_lut_raw");
 }
 
 }  // namespace slfmm

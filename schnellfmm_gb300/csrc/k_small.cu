@@ -1386,16 +1386,6 @@ void launch_gemm_small(Ctx& c, const double* A, int lda, uint64_t m, int a, cons
     }
 }
 
-void launch_gemm_small_f32out(Ctx& c, const double* A, int lda, uint64_t m, int a, const double* B,
-                              int ldb, int b, float* C, int ldc) {
-    if (m == 0 || b == 0) return;
-    const size_t sm = (size_t)a * b * sizeof(double);
-    set_smem((const void*)k_gemm_small<float>, sm);
-    k_gemm_small<float><<<grid_for(c, m * b, 256), 256, sm, c.stream>>>(A, lda, m, a, B, ldb, b, 1.0,
-                                                                        0.0, C, ldc);
-    SLFMM_LAUNCHED(c, "k_gemm_small");
-}
-
 void launch_trmul_f32(Ctx& c, float* A, int lda, uint64_t m, int a, const double* Linv) {
     SLFMM_REQUIRE(a <= 64, SLFMM_ERR_BAD_ARG, "sketch width must be <= 64");
     if (m == 0) return;

@@ -249,7 +249,6 @@ void launch_decode_chunk(Ctx& c, const Geno& g, uint64_t snp0, uint64_t ncols,
                          const double* mean, const double* scale, double* out);
 // per-SNP 4-entry lookup tables (value of code 0,1,2,3)
 void launch_lut_std(Ctx& c, uint64_t p, const double* mean, const double* scale, float* lut);
-void launch_lut_raw(Ctx& c, uint64_t p, const double* fill_missing, float* lut);
 
 // k_sim.cu : synthetic structured cohort written into a device packed matrix
 void launch_simulate(Ctx& c, uint64_t n, uint64_t p, int n_pop, const float* admix_dev, double fst,
@@ -375,8 +374,6 @@ void launch_atb(Ctx& c, const double* A, int lda, const double* B, int ldb, uint
 void launch_gram_f32(Ctx& c, const float* A, int lda, uint64_t m, int a, double* out);
 void launch_gemm_small(Ctx& c, const double* A, int lda, uint64_t m, int a, const double* B,
                        int ldb, int b, double alpha, double beta, double* C, int ldc);
-void launch_gemm_small_f32out(Ctx& c, const double* A, int lda, uint64_t m, int a,
-                              const double* B, int ldb, int b, float* C, int ldc);
 // A <- A * Linv^T (Linv lower-triangular a x a, a <= 64)
 void launch_trmul_f32(Ctx& c, float* A, int lda, uint64_t m, int a, const double* Linv);
 // in place lower Cholesky; drop_tol < 0: replace non-positive pivots by a
