@@ -52,7 +52,7 @@ BATCHED = {
     # 64 independent problems: n ~ U[100, 3000], p ~ U[50k, 400k], K ~ U[2, 16],
     # 1-8 covariates, 2-6 populations with Fst ~ U(0.02, 0.2), 1 % MCAR
     "many": dict(problems=64, n_lo=100, n_hi=3000, p_lo=50_000, p_hi=400_000, k_lo=2, k_hi=16, d_lo=1, d_hi=8,
-                 pop_lo=2, pop_hi=6, fst_lo=0.02, fst_hi=0.2, miss=0.01, streams=4),
+                 pop_lo=2, pop_hi=6, fst_lo=0.02, fst_hi=0.2, miss=0.01, streams=8),
 }
 
 WORKLOADS = {

@@ -245,7 +245,7 @@ typedef struct slfmm_problem {
 
 /* Many independent problems of uneven n, p, K and d (the reference runs them
  * one CLI invocation at a time): they run concurrently on n_streams internal
- * streams of the context's device (0: 4), each problem's kernels in order on
+ * streams of the context's device (0: 8), each problem's kernels in order on
  * one stream.  status[i] (may be NULL) receives problem i's status; returns
  * the first nonzero status, or SLFMM_OK. */
 int slfmm_fit_many(slfmm_ctx* ctx, const slfmm_problem* problems, uint32_t n_problems,

@@ -996,7 +996,7 @@ def fit_lfmm2_many(problems: Sequence[Tuple[np.ndarray, int, np.ndarray, Lfmm2Co
                    engine: Optional[Engine] = None, n_streams: int = 0,
                    outs: Optional[Sequence[dict]] = None) -> List[TestResults]:
     """Independent problems (packed payload, n_physical, x, config), run
-    concurrently on n_streams streams of the engine's device (0: 4).
+    concurrently on n_streams streams of the engine's device (0: 8).
     ``outs`` may hold preallocated (e.g. pinned) result arrays per problem."""
     eng = engine or default_engine()
     keep = []
