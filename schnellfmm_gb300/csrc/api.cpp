@@ -544,7 +544,7 @@ void fp8_row_fix(Ctx& c, const Geno& g, const SnpStd& s, const Fp8RowPass& rp, u
     const uint64_t nnz_rows = rows == g.p ? g.nnz : (uint64_t)((double)g.nnz * rows / std::max<uint64_t>(g.p, 1));
     ProfScope ps(c, "row_fix", (double)nnz_rows * (4.0 + 4.0 * rp.w) + (double)rows * rp.w * 8, 1.0 * nnz_rows * rp.w);
     launch_rowfix_mean(c, out + r0 * rp.wp, rp.wp, rows, rp.w, g.miss_ptr.get() + r0, g.miss_idx.get(),
-                       rp.W32.get(), rp.wp, rp.cs.get(), s.mean.get() + r0, s.scale.get() + r0);
+                       rp.W32.get(), rp.wp, g.n, rp.cs.get(), s.mean.get() + r0, s.scale.get() + r0);
 }
 
 // rows [r0, r0 + rows) of out (ld wp); err_dev as in launch_tc8_rows.  The
@@ -619,8 +619,8 @@ void row_contract_base(Ctx& c, const Geno& g, const SnpStd& s, const double* W, 
             ProfScope ps(c, "row_contract", bytes, 2.0 * g.n * g.p * w);
             launch_tc_rows(c, packed_rows(g), g.stride, g.p, g.n, bs.get(), n_pad, wp, out.get(), wp, 1, 0);
         }
-        launch_rowfix_mean(c, out.get(), wp, g.p, w, g.miss_ptr.get(), g.miss_idx.get(), W32.get(), wp, cs.get(),
-                           s.mean.get(), s.scale.get());
+        launch_rowfix_mean(c, out.get(), wp, g.p, w, g.miss_ptr.get(), g.miss_idx.get(), W32.get(), wp, g.n,
+                           cs.get(), s.mean.get(), s.scale.get());
         return;
     }
     ProfScope ps(c, "row_contract", bytes, 2.0 * g.n * g.p * w);

@@ -305,16 +305,21 @@ __global__ void __launch_bounds__(256, 8) k_rowfix_mean4(float* __restrict__ P, 
     if (j >= rows) return;
     const bool act = 4 * q < w;
     const uint64_t e0 = ptr[j], e1 = ptr[j + 1];
+    // each lane's own column quad of W; a missing call's row offset (in
+    // 16-byte units, 32 bits: the launcher checks n x ldw / 4 < 2^32) is
+    // formed once per batch by the lane that loaded the call
+    const float4* Wq = reinterpret_cast<const float4*>(W) + q;
+    const uint32_t q4 = (uint32_t)ldw >> 2;
     float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
     for (uint64_t b = e0; b < e1; b += 32) {
-        const uint32_t my = b + lane < e1 ? idx[b + lane] : 0u;
+        const uint32_t my = b + lane < e1 ? idx[b + lane] * q4 : 0u;
         const int cnt = (int)(e1 - b < 32 ? e1 - b : 32);
 #pragma unroll 4
         for (int t = 0; t < cnt; t += G) {
             const int tt = t + grp;
-            const uint64_t i = __shfl_sync(0xffffffffu, my, tt & 31);
+            const uint32_t off = __shfl_sync(0xffffffffu, my, tt & 31);
             if (act && tt < cnt) {
-                const float4 v = reinterpret_cast<const float4*>(W + i * ldw)[q];
+                const float4 v = Wq[off];
                 acc.x += v.x;
                 acc.y += v.y;
                 acc.z += v.z;
@@ -638,9 +643,11 @@ int tc_split_count(Ctx& c, uint64_t rows, uint64_t K) {
 }
 
 void launch_rowfix_mean(Ctx& c, float* P, int ldp, uint64_t rows, int w, const uint64_t* ptr, const uint32_t* idx,
-                        const float* W, int ldw, const double* cs, const double* mean, const double* scale) {
+                        const float* W, int ldw, uint64_t n, const double* cs, const double* mean,
+                        const double* scale) {
     if (!rows) return;
-    const bool quads = ldw % 4 == 0 && reinterpret_cast<uintptr_t>(W) % 16 == 0;
+    const bool quads = ldw % 4 == 0 && reinterpret_cast<uintptr_t>(W) % 16 == 0 &&
+                       n * (uint64_t)(ldw / 4) <= 0xffffffffull;
     for (int c0 = 0; c0 < w;) {
         if (quads) {
             // Column blocks that keep the lanes of a group busy: 64 columns

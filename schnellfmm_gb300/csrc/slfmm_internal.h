@@ -278,8 +278,10 @@ int launch_tc_rows(Ctx& c, const uint8_t* packed, uint64_t stride, uint64_t rows
                     const __nv_bfloat16* bsplit, uint64_t K_pad, int wpad, float* out, int ldo, int splits,
                     uint64_t split_stride);
 int tc_split_count(Ctx& c, uint64_t rows, uint64_t K);
+// (W has n rows of ldw floats)
 void launch_rowfix_mean(Ctx& c, float* P, int ldp, uint64_t rows, int w, const uint64_t* ptr, const uint32_t* idx,
-                        const float* W, int ldw, const double* cs, const double* mean, const double* scale);
+                        const float* W, int ldw, uint64_t n, const double* cs, const double* mean,
+                        const double* scale);
 void launch_colfix_mean(Ctx& c, double* S, int lds, uint64_t n, int w, const uint64_t* ptr, const uint32_t* idx,
                         const float* Q, int ldq, const double* coef, const double* colterm);
 void launch_weighted_colsum(Ctx& c, const float* Q, int ldq, uint64_t p, int w, const double* coef, double* out);
