@@ -1,8 +1,9 @@
 """The small symmetric eigen-solve (Step 0's X^T X, src/precompute.rs:47; the
 randomized SVD's l x l Gram, src/rsvd.rs:162) against numpy's LAPACK eigh:
-FP32 Jacobi sweeps, then FP64 re-orthonormalisation and a first-order FP64
-correction.  Eigenvalues to 1e-10 of the largest, eigenvectors by the
-projector onto each cluster of (numerically) equal eigenvalues."""
+FP32 one-sided Jacobi sweeps, then FP64 re-orthonormalisation and FP64
+two-sided sweeps over the columns still coupled above the rounding level.
+Eigenvalues to 1e-10 of the largest, eigenvectors by the projector onto
+each cluster of (numerically) equal eigenvalues."""
 import numpy as np
 import pytest
 
@@ -53,3 +54,12 @@ def test_near_degenerate_and_rank_deficient(engine):
     _check(engine, _spd(rng, 12, eig))
     eig = np.concatenate([np.full(20, 3.0), np.linspace(2.0, 1.0, 20), np.zeros(10)])
     _check(engine, _spd(rng, 50, eig))
+
+
+def test_wide_spectrum(engine):
+    """Eigenvalues over twelve decades, as in a Gram of nearly collinear
+    covariates: the FP32 sweeps leave the small ones to the FP64 sweeps,
+    which then run on those columns alone."""
+    rng = np.random.default_rng(2)
+    _check(engine, _spd(rng, 50, np.logspace(0, -12, 50)))
+    _check(engine, _spd(rng, 30, np.concatenate([np.logspace(2, -1, 20), np.full(10, 1e-9)])))
